@@ -1,0 +1,124 @@
+/*
+ * macsav.h -- C ABI of the GB300 (sm_103a) MAC mr-SAV stage library.
+ *
+ * Drop-in boundary for the no-slip MAC hot path of HaifengWang1031/MAC-mr-SAV-RK.
+ * Every entry point names the reference interface it replaces (paths are
+ * relative to that project's root).  Conventions:
+ *   - All array arguments are DEVICE pointers to float64 data unless stated.
+ *   - A "packed velocity" is the reference's free vector
+ *     [u[:,1:-1].ravel(), v[1:-1,:].ravel()] of length size=(nx-1)ny+nx(ny-1)
+ *     (solver/mac/grid.py:52-65); cells are (ny, nx) row-major, length np=nx*ny.
+ *   - Multi-column data is column-blocked: column k starts at k*size (or k*np).
+ *     (The reference stores (size, c) row-major; the Python layer transposes.)
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *     stream-ordered; entry points that return scalars synchronise the stream.
+ *   - Return value: MACSAV_OK or an error code; macsav_plan_error() gives the
+ *     message.  Codes map to the reference's exception types (see below).
+ *   - No entry point falls back to the CPU.
+ */
+#ifndef MACSAV_H
+#define MACSAV_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MACSAV_OK 0
+#define MACSAV_ERR_VALUE 1        /* ValueError: invalid argument / RHS / shifts */
+#define MACSAV_ERR_CUDA 2         /* CUDA runtime failure */
+#define MACSAV_ERR_CG 3           /* RuntimeError("Pressure Schur CG failed with info=N") */
+#define MACSAV_ERR_STOKES_GATE 4  /* RuntimeError("Stokes residual=..., divergence=...") */
+#define MACSAV_ERR_STAGE_GATE 5   /* RuntimeError("SAV stage residuals ...") */
+#define MACSAV_ERR_NEG_ENERGY 6   /* RuntimeError("Negative Stokes response energy") */
+#define MACSAV_ERR_SCALAR 7       /* RuntimeError from the frozen SAV scalar map */
+#define MACSAV_ERR_UNSUPPORTED 8  /* grid size outside what the plan supports */
+
+/* precision of the Stokes solve */
+#define MACSAV_FP64 0        /* FP64 throughout (parity path) */
+#define MACSAV_FP32_MIXED 1  /* FP32 transforms/stencils, FP64 reductions + FP64 defect correction */
+
+/* transform kinds for macsav_transform */
+#define MACSAV_DCT2 0
+#define MACSAV_DST2 1
+#define MACSAV_DST1 2
+
+#define MACSAV_MAX_COLUMNS 4
+
+typedef struct macsav_plan macsav_plan;
+
+/* Result of one Stokes solve (StokesResult, solver/mac/stokes.py:32-37, plus
+ * the TensorStokes counters of solver/mac/tensor_stokes.py:169-174,340-344). */
+typedef struct {
+  double residual;        /* max|defect| / (1 + max|f|) */
+  double divergence_inf;  /* max|D u| */
+  double max_velocity;    /* max|u| (gate scale) */
+  int iterations[MACSAV_MAX_COLUMNS];
+  int refinements;        /* defect-correction sweeps (FP32_MIXED), 0 for FP64 */
+} macsav_stokes_info;
+
+/* Replaces TensorStokes.__init__ (solver/mac/tensor_stokes.py:128-174) and the
+ * MACGrid/MACOperators set-up it relies on (solver/mac/grid.py:9-34,
+ * solver/mac/operators.py:11-31): builds eigenvalue/twiddle tables and owns
+ * the device work buffers for up to max_columns right-hand sides. */
+int macsav_plan_create(macsav_plan** plan, int nx, int ny, double lx, double ly, int precision,
+                       double tolerance, double krylov_tolerance, int max_iterations, int max_columns);
+void macsav_plan_destroy(macsav_plan* plan);
+/* Message of the last failing call on this plan (or of a failed create when plan==NULL). */
+const char* macsav_plan_error(const macsav_plan* plan);
+/* Kernel launches issued through this plan so far. */
+long long macsav_plan_launches(const macsav_plan* plan);
+
+/* y = K x (MACOperators.K, solver/mac/operators.py:16-18; MACNavierStokes.apply_K,
+ * solver/mac_ns.py:47-48).  x, y: packed velocities, `columns` columns. */
+int macsav_apply_K(macsav_plan* plan, const double* x, double* y, int columns, void* stream);
+/* p = D x (MACOperators.D, operators.py:19-29; packed_divergence[_vector],
+ * solver/mac/kernels.py:46-87). */
+int macsav_apply_D(macsav_plan* plan, const double* x, double* p, int columns, void* stream);
+/* x = D^T p = -G p (packed_divergence_transpose[_vector], kernels.py:89-132;
+ * MACNavierStokes.apply_G is the negative, solver/mac_ns.py:50-51). */
+int macsav_apply_Dt(macsav_plan* plan, const double* p, double* x, int columns, void* stream);
+/* n = N(x): skew-symmetric dual-cell convection on the packed vector
+ * (kernels.convection, solver/mac/kernels.py:6-35, via MACNavierStokes.nonlinear,
+ * solver/mac_ns.py:22-25). */
+int macsav_convection(macsav_plan* plan, const double* x, double* n, int columns, void* stream);
+
+/* Orthonormal DCT-II / DST-II / DST-I (or inverse) along each row of a
+ * (rows, n) row-major array (_transform_axis, solver/mac/tensor_stokes.py:58-82,
+ * scipy.fft norm="ortho").  Runs the same FFT machinery as the solver. */
+int macsav_transform(macsav_plan* plan, int kind, int inverse, int rows, int n, const double* in,
+                     double* out, void* stream);
+
+/* Shifted Stokes solve (mass I + viscosity K) u - D^T p = f, D u = 0 by
+ * DST/DCT velocity inverses inside a pressure Schur PCG
+ * (TensorStokes.solve, solver/mac/tensor_stokes.py:245-364).
+ * rhs, velocity: packed, `columns` columns; pressure: cells, mean-zero per column.
+ * Returns MACSAV_ERR_VALUE for invalid shifts or a non-finite RHS,
+ * MACSAV_ERR_CG when PCG does not converge in max_iterations, and
+ * MACSAV_ERR_STOKES_GATE when residual > tolerance or
+ * divergence > tolerance*(1+max|u|); info is filled in every case. */
+int macsav_stokes_solve(macsav_plan* plan, const double* rhs, int columns, double mass, double viscosity,
+                        double* velocity, double* pressure, macsav_stokes_info* info, void* stream);
+
+/* out = sum_k coeffs[k] * fields[k] accumulated in the order given
+ * (MACNavierStokes.combine, solver/mac_ns.py:40-45).  coeffs is a HOST array,
+ * fields a HOST array of device pointers, n elements each. */
+int macsav_combine(macsav_plan* plan, int nterms, const double* coeffs, const double* const* fields, double* out,
+                   long long n, void* stream);
+/* Host scalar results (synchronising):
+ * inner = hx*hy*dot(a,b) (MACGrid.inner, solver/mac/grid.py:67-68);
+ * max_abs = max|a| with NaN propagation (MACNavierStokes.max_abs, solver/mac_ns.py:66-67). */
+int macsav_inner(macsav_plan* plan, const double* a, const double* b, long long n, double* result, void* stream);
+int macsav_max_abs(macsav_plan* plan, const double* a, long long n, double* result, void* stream);
+
+/* MACNavierStokes.diagnostics (solver/mac_ns.py:95-107) of a packed velocity x
+ * with scalar r: out[0..7] = kinetic, modified_energy, divergence_inf,
+ * h1_seminorm_squared, r, angular_momentum, power, dissipation.  force may be
+ * NULL (zero body force). */
+int macsav_diagnostics(macsav_plan* plan, const double* x, double r, double nu, const double* force,
+                       double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MACSAV_H */

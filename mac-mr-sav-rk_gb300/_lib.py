@@ -1,0 +1,93 @@
+"""ctypes binding of ``libmacsav.so`` (the C ABI in include/macsav.h).
+
+Loading fails loudly when the library is missing: there is no CPU fallback.
+Error codes are turned into the reference's exception types and messages.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+import re
+
+LIB_PATH = pathlib.Path(__file__).resolve().parent / "libmacsav.so"
+HEADER = pathlib.Path(__file__).resolve().parent.parent / "include" / "macsav.h"
+
+OK, ERR_VALUE, ERR_CUDA, ERR_CG, ERR_STOKES_GATE, ERR_STAGE_GATE, ERR_NEG_ENERGY, ERR_SCALAR, ERR_UNSUPPORTED = range(9)
+FP64, FP32_MIXED = 0, 1
+DCT2, DST2, DST1 = 0, 1, 2
+MAX_COLUMNS = 4
+
+
+class MacsavError(RuntimeError):
+    """CUDA-side failure that has no counterpart in the reference."""
+
+
+class StokesInfo(C.Structure):
+    _fields_ = [("residual", C.c_double), ("divergence_inf", C.c_double), ("max_velocity", C.c_double),
+                ("iterations", C.c_int * MAX_COLUMNS), ("refinements", C.c_int)]
+
+
+_P = C.c_void_p
+_D = C.c_double
+_I = C.c_int
+_LL = C.c_longlong
+_SIGNATURES = {
+    "macsav_plan_create": (_I, [C.POINTER(_P), _I, _I, _D, _D, _I, _D, _D, _I, _I]),
+    "macsav_plan_destroy": (None, [_P]),
+    "macsav_plan_error": (C.c_char_p, [_P]),
+    "macsav_plan_launches": (_LL, [_P]),
+    "macsav_apply_K": (_I, [_P, _P, _P, _I, _P]),
+    "macsav_apply_D": (_I, [_P, _P, _P, _I, _P]),
+    "macsav_apply_Dt": (_I, [_P, _P, _P, _I, _P]),
+    "macsav_convection": (_I, [_P, _P, _P, _I, _P]),
+    "macsav_transform": (_I, [_P, _I, _I, _I, _I, _P, _P, _P]),
+    "macsav_stokes_solve": (_I, [_P, _P, _I, _D, _D, _P, _P, C.POINTER(StokesInfo), _P]),
+    "macsav_combine": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_P), _P, _LL, _P]),
+    "macsav_inner": (_I, [_P, _P, _P, _LL, C.POINTER(_D), _P]),
+    "macsav_max_abs": (_I, [_P, _P, _LL, C.POINTER(_D), _P]),
+    "macsav_diagnostics": (_I, [_P, _P, _D, _D, _P, C.POINTER(_D), _P]),
+}
+
+_lib = None
+
+
+def header_symbols() -> list[str]:
+    """Function names declared in include/macsav.h."""
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"\b(macsav_[a-z0-9_]+)\s*\(", text)))
+
+
+def load(path: pathlib.Path | None = None):
+    """Load (once) and return the library; raises ImportError if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = pathlib.Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(f"{p.name} is not built: run __graft_entry__.build() (no CPU fallback exists)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def error_message(plan) -> str:
+    msg = load().macsav_plan_error(plan)
+    return msg.decode() if msg else ""
+
+
+def check(code: int, plan) -> None:
+    """Raise the reference's exception for a non-zero status code."""
+    if code == OK:
+        return
+    msg = error_message(plan)
+    if code in (ERR_VALUE,):
+        raise ValueError(msg)
+    if code in (ERR_CG, ERR_STOKES_GATE, ERR_STAGE_GATE, ERR_NEG_ENERGY, ERR_SCALAR):
+        raise RuntimeError(msg)
+    if code == ERR_UNSUPPORTED:
+        raise ValueError(f"unsupported by the GB300 library: {msg}")
+    raise MacsavError(msg or f"macsav error code {code}")

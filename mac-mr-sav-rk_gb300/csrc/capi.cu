@@ -1,0 +1,223 @@
+// extern "C" entry points (declared in include/macsav.h).
+#include <cmath>
+#include <cstdio>
+#include <string>
+
+#include "plan.cuh"
+
+struct macsav_plan {
+  macsav::Plan p;
+};
+
+namespace macsav {
+int solve_fp64(Plan* P, const double* f, int cols, double mass, double visc, double* vel, double* pres,
+               cudaStream_t s);
+int solve_mixed(Plan* P, const double* f, int cols, double mass, double visc, double* vel, double* pres,
+                cudaStream_t s, int* sweeps);
+int op_apply(Plan* P, int which, const double* in, double* out, int cols, cudaStream_t s);
+int op_combine(Plan* P, int nterms, const double* coeffs, const double* const* fields, double* out, long long n,
+               cudaStream_t s);
+int op_dot_max(Plan* P, const double* a, const double* b, long long n, double* result, cudaStream_t s);
+int op_diagnostics(Plan* P, const double* x, double r, double nu, const double* force, double* out,
+                   cudaStream_t s);
+int op_transform(Plan* P, int kind, int inverse, int rows, int n, const double* in, double* out, cudaStream_t s);
+}  // namespace macsav
+
+using macsav::Plan;
+
+static thread_local std::string g_create_error;
+
+static int fail(Plan* P, int code, const std::string& msg) {
+  P->err = msg;
+  return code;
+}
+
+static int cuda_status(Plan* P) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(P, MACSAV_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+  return MACSAV_OK;
+}
+
+extern "C" {
+
+int macsav_plan_create(macsav_plan** out, int nx, int ny, double lx, double ly, int precision, double tolerance,
+                       double krylov_tolerance, int max_iterations, int max_columns) {
+  if (!out) return MACSAV_ERR_VALUE;
+  *out = nullptr;
+  // solver/mac/grid.py:15-19 and solver/mac/tensor_stokes.py:137-143
+  if (nx < 3 || ny < 3 || !std::isfinite(lx) || !std::isfinite(ly) || lx <= 0 || ly <= 0) {
+    g_create_error = "Require nx,ny >= 3 and positive finite domain lengths";
+    return MACSAV_ERR_VALUE;
+  }
+  if (!(tolerance > 0) || !(krylov_tolerance > 0) || !std::isfinite(tolerance) || !std::isfinite(krylov_tolerance) ||
+      max_iterations < 1) {
+    g_create_error = "Invalid solver controls";
+    return MACSAV_ERR_VALUE;
+  }
+  if (precision != MACSAV_FP64 && precision != MACSAV_FP32_MIXED) {
+    g_create_error = "precision must be MACSAV_FP64 or MACSAV_FP32_MIXED";
+    return MACSAV_ERR_VALUE;
+  }
+  if (max_columns < 1 || max_columns > MACSAV_MAX_COLUMNS) {
+    g_create_error = "max_columns must be in 1..4";
+    return MACSAV_ERR_VALUE;
+  }
+  macsav_plan* h = new macsav_plan();
+  Plan& p = h->p;
+  macsav::GridDev& g = p.g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nu = (nx - 1) * ny;
+  g.nv = nx * (ny - 1);
+  g.size = g.nu + g.nv;
+  g.np = nx * ny;
+  g.hx = lx / nx;
+  g.hy = ly / ny;
+  g.ihx = 1.0 / g.hx;
+  g.ihy = 1.0 / g.hy;
+  g.ihx2 = 1.0 / (g.hx * g.hx);
+  g.ihy2 = 1.0 / (g.hy * g.hy);
+  p.lx = lx;
+  p.ly = ly;
+  p.precision = precision;
+  p.tol = tolerance;
+  p.ktol = krylov_tolerance;
+  p.maxit = max_iterations;
+  p.maxcols = max_columns;
+  const int rc = macsav::plan_build(&p);
+  if (rc != MACSAV_OK) {
+    g_create_error = p.err;
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return MACSAV_OK;
+}
+
+void macsav_plan_destroy(macsav_plan* plan) {
+  if (!plan) return;
+  macsav::plan_free(&plan->p);
+  delete plan;
+}
+
+const char* macsav_plan_error(const macsav_plan* plan) {
+  return plan ? plan->p.err.c_str() : g_create_error.c_str();
+}
+
+long long macsav_plan_launches(const macsav_plan* plan) { return plan ? plan->p.launches : 0; }
+
+static int apply(macsav_plan* plan, int which, const double* in, double* out, int columns, void* stream) {
+  if (!plan || !in || !out) return MACSAV_ERR_VALUE;
+  if (columns < 1) return fail(&plan->p, MACSAV_ERR_VALUE, "columns must be >= 1");
+  const int rc = macsav::op_apply(&plan->p, which, in, out, columns, static_cast<cudaStream_t>(stream));
+  return rc != MACSAV_OK ? cuda_status(&plan->p) : MACSAV_OK;
+}
+int macsav_apply_K(macsav_plan* plan, const double* x, double* y, int columns, void* stream) {
+  return apply(plan, 0, x, y, columns, stream);
+}
+int macsav_apply_D(macsav_plan* plan, const double* x, double* p, int columns, void* stream) {
+  return apply(plan, 1, x, p, columns, stream);
+}
+int macsav_apply_Dt(macsav_plan* plan, const double* p, double* x, int columns, void* stream) {
+  return apply(plan, 2, p, x, columns, stream);
+}
+int macsav_convection(macsav_plan* plan, const double* x, double* n, int columns, void* stream) {
+  return apply(plan, 3, x, n, columns, stream);
+}
+
+int macsav_transform(macsav_plan* plan, int kind, int inverse, int rows, int n, const double* in, double* out,
+                     void* stream) {
+  if (!plan || !in || !out) return MACSAV_ERR_VALUE;
+  return macsav::op_transform(&plan->p, kind, inverse, rows, n, in, out, static_cast<cudaStream_t>(stream));
+}
+
+int macsav_stokes_solve(macsav_plan* plan, const double* rhs, int columns, double mass, double viscosity,
+                        double* velocity, double* pressure, macsav_stokes_info* info, void* stream) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (info) *info = macsav_stokes_info{};
+  // tensor_stokes.py:246-251
+  if (!std::isfinite(mass) || !std::isfinite(viscosity) || std::fmin(mass, viscosity) < 0 || mass + viscosity <= 0)
+    return fail(P, MACSAV_ERR_VALUE, "Require mass,viscosity >= 0 and nonzero total");
+  if (!rhs || !velocity || !pressure || columns < 1 || columns > P->maxcols)
+    return fail(P, MACSAV_ERR_VALUE, "Invalid Stokes RHS");
+  double shift[2 * MACSAV_MAX_COLUMNS];
+  for (int c = 0; c < columns; ++c) {
+    shift[2 * c] = mass;
+    shift[2 * c + 1] = viscosity;
+  }
+  cudaMemcpyAsync(P->shift, shift, sizeof(double) * 2 * columns, cudaMemcpyHostToDevice, s);
+  int sweeps = 0;
+  int rc = P->precision == MACSAV_FP64
+               ? macsav::solve_fp64(P, rhs, columns, mass, viscosity, velocity, pressure, s)
+               : macsav::solve_mixed(P, rhs, columns, mass, viscosity, velocity, pressure, s, &sweeps);
+  if (rc != MACSAV_OK) return rc;
+  cudaMemcpyAsync(P->h_cg, P->cg, sizeof(macsav::CGScalars) * columns, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(P->h_checks, P->checks, sizeof(macsav::SolveChecks) * columns, cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status(P);
+  if ((rc = cuda_status(P)) != MACSAV_OK) return rc;
+  double maxdef = 0, maxf = 0, maxu = 0, maxdiv = 0;
+  bool bad_rhs = false, bad_sol = false;
+  for (int c = 0; c < columns; ++c) {
+    const macsav::SolveChecks& k = P->h_checks[c];
+    auto mx = [](double a, double b) { return (a != a || b != b) ? NAN : (a > b ? a : b); };
+    maxdef = mx(maxdef, k.max_defect);
+    maxf = mx(maxf, k.max_force);
+    maxu = mx(maxu, k.max_velocity);
+    maxdiv = mx(maxdiv, k.max_div);
+    bad_rhs |= k.nonfinite_force != 0;
+    bad_sol |= k.nonfinite_solution != 0;
+  }
+  const double residual = maxdef / (1.0 + maxf);
+  if (info) {
+    info->residual = residual;
+    info->divergence_inf = maxdiv;
+    info->max_velocity = maxu;
+    info->refinements = sweeps;
+    for (int c = 0; c < columns; ++c) info->iterations[c] = P->h_cg[c].iters;
+  }
+  if (bad_rhs) return fail(P, MACSAV_ERR_VALUE, "Invalid Stokes RHS");
+  for (int c = 0; c < columns; ++c)
+    if (P->h_cg[c].info != 0) {
+      char buf[96];
+      std::snprintf(buf, sizeof buf, "Pressure Schur CG failed with info=%d", P->h_cg[c].info);
+      return fail(P, MACSAV_ERR_CG, buf);
+    }
+  if (bad_sol || residual > P->tol || maxdiv > P->tol * (1.0 + maxu)) {
+    char buf[128];
+    std::snprintf(buf, sizeof buf, "Stokes residual=%.3e, divergence=%.3e", residual, maxdiv);
+    return fail(P, MACSAV_ERR_STOKES_GATE, buf);
+  }
+  return MACSAV_OK;
+}
+
+int macsav_combine(macsav_plan* plan, int nterms, const double* coeffs, const double* const* fields, double* out,
+                   long long n, void* stream) {
+  if (!plan || !coeffs || !fields || !out) return MACSAV_ERR_VALUE;
+  return macsav::op_combine(&plan->p, nterms, coeffs, fields, out, n, static_cast<cudaStream_t>(stream));
+}
+
+int macsav_inner(macsav_plan* plan, const double* a, const double* b, long long n, double* result, void* stream) {
+  if (!plan || !a || !b || !result) return MACSAV_ERR_VALUE;
+  double r[2];
+  const int rc = macsav::op_dot_max(&plan->p, a, b, n, r, static_cast<cudaStream_t>(stream));
+  *result = plan->p.g.hx * plan->p.g.hy * r[0];
+  return rc;
+}
+
+int macsav_max_abs(macsav_plan* plan, const double* a, long long n, double* result, void* stream) {
+  if (!plan || !a || !result) return MACSAV_ERR_VALUE;
+  double r[2];
+  const int rc = macsav::op_dot_max(&plan->p, a, nullptr, n, r, static_cast<cudaStream_t>(stream));
+  *result = r[1];
+  return rc;
+}
+
+int macsav_diagnostics(macsav_plan* plan, const double* x, double r, double nu, const double* force, double* out,
+                       void* stream) {
+  if (!plan || !x || !out) return MACSAV_ERR_VALUE;
+  return macsav::op_diagnostics(&plan->p, x, r, nu, force, out, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

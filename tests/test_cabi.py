@@ -1,0 +1,35 @@
+"""The C-ABI library builds for sm_103a and exports every declared symbol
+(no GPU needed: nothing here launches a kernel)."""
+import ctypes
+
+from helpers import load_package
+
+
+def _lib_module():
+    import __graft_entry__
+    __graft_entry__.build()
+    pkg = load_package()
+    from importlib import import_module
+    return import_module(pkg.__name__ + "._lib")
+
+
+def test_library_exports_every_header_symbol():
+    lib = _lib_module()
+    names = lib.header_symbols()
+    assert "macsav_stokes_solve" in names and "macsav_plan_create" in names
+    so = ctypes.CDLL(str(lib.LIB_PATH))
+    missing = [n for n in names if not hasattr(so, n)]
+    assert not missing, missing
+    # every declared symbol also has a ctypes signature in the binding
+    assert set(names) <= set(lib._SIGNATURES), set(names) - set(lib._SIGNATURES)
+
+
+def test_plan_create_rejects_bad_arguments_without_gpu():
+    lib = _lib_module()
+    so = lib.load()
+    h = ctypes.c_void_p()
+    assert so.macsav_plan_create(ctypes.byref(h), 2, 5, 1.0, 1.0, 0, 1e-9, 1e-12, 100, 2) == lib.ERR_VALUE
+    assert b"nx,ny >= 3" in so.macsav_plan_error(None)
+    assert so.macsav_plan_create(ctypes.byref(h), 8, 8, 1.0, 1.0, 0, -1.0, 1e-12, 100, 2) == lib.ERR_VALUE
+    assert b"Invalid solver controls" in so.macsav_plan_error(None)
+    assert not h.value
