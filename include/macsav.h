@@ -118,6 +118,56 @@ int macsav_max_abs(macsav_plan* plan, const double* a, long long n, double* resu
 int macsav_diagnostics(macsav_plan* plan, const double* x, double r, double nu, const double* force,
                        double* out, void* stream);
 
+/* time schemes for macsav_step (make_scheme names, solver/schemes/registry.py:24-41) */
+#define MACSAV_SDIRK2_MRSAV 0
+#define MACSAV_SDIRK3_MRSAV 1
+#define MACSAV_IMEX_EULER_MRSAV 2
+#define MACSAV_SDIRK2 3
+#define MACSAV_SDIRK3 4
+#define MACSAV_IMEX_EULER 5
+
+/* stage status codes (records[i].status) */
+#define MACSAV_STAGE_OK 0
+#define MACSAV_STAGE_STOKES_RHS 1    /* ValueError("Invalid Stokes RHS") */
+#define MACSAV_STAGE_CG 2            /* RuntimeError("Pressure Schur CG failed with info=N") */
+#define MACSAV_STAGE_STOKES_GATE 3   /* RuntimeError("Stokes residual=..., divergence=...") */
+#define MACSAV_STAGE_NEG_ENERGY 4    /* RuntimeError("Negative Stokes response energy") */
+#define MACSAV_STAGE_SAV_INPUT 5     /* ValueError("Invalid frozen SAV scalar inputs") */
+#define MACSAV_STAGE_SAV_DENOM 6     /* RuntimeError("Invalid frozen SAV scalar denominator") */
+#define MACSAV_STAGE_SAV_NONFINITE 7 /* RuntimeError("Nonfinite frozen SAV correction") */
+#define MACSAV_STAGE_GATE 8          /* RuntimeError("SAV stage residuals ..., divergence ...") */
+
+/* One stage record: the fields of solver/core.py:15-26 (Stage) that are
+ * scalars, plus the Stokes solve's own outcome and CG iterations. */
+typedef struct {
+  double r, residual, scalar_residual, divergence_inf, continuity_residual;
+  double correction_predictor, frozen_factor, corrections[2];
+  double stokes_residual, stokes_divergence, max_velocity, max_pressure;
+  int n_corrections, iterations[2], cg_info, status;
+} macsav_stage_record;
+
+/* One whole time step of `scheme` on the device: replaces Scheme.step for
+ * SDIRK2MRSAV (solver/schemes/sdirk2_mrsav.py:61-75), SDIRK3MRSAV
+ * (sdirk3_mrsav.py:18-65), IMEXEulerMRSAV (imex_euler_mrsav.py:20-52) and the
+ * plain SDIRK2 / SDIRK3 / IMEXEuler (sdirk2.py:20-43, sdirk3.py:34-57,
+ * imex_euler.py:13-32) over MACNavierStokes (solver/mac_ns.py:12-107).
+ *   x0: packed velocity at t; r0: SAV scalar; forces: NULL for zero body
+ *   force, else n_nodes packed vectors f(t + c_j dt) back to back (nodes: SDIRK3
+ *   c = 0, 1/4, 4/5, 1; SDIRK2 c = 0, 1-1/sqrt(2); Euler c = 0).
+ *   x1: packed velocity at t+dt; embedded (NULL = skip): the embedded velocity;
+ *   pressures (NULL = skip): the stage pressures pi_i, n_stages x np;
+ *   records: HOST array of n_stages; r1: HOST scalar.
+ * Returns MACSAV_OK, or the code of the first failing stage (records[i].status
+ * tells which check failed; MACSAV_ERR_VALUE / _CG / _STOKES_GATE /
+ * _NEG_ENERGY / _SCALAR / _STAGE_GATE).  Synchronises the stream. */
+int macsav_step(macsav_plan* plan, int scheme, double t, double dt, double nu, double gamma, const double* x0,
+                double r0, const double* forces, double* x1, double* embedded, double* pressures,
+                macsav_stage_record* records, double* r1, void* stream);
+
+/* Run macsav_step as one captured CUDA graph per (scheme, force, embedded)
+ * (the pressure CG loop becomes a conditional WHILE node).  Default: off. */
+int macsav_plan_set_graph(macsav_plan* plan, int enable);
+
 #ifdef __cplusplus
 }
 #endif

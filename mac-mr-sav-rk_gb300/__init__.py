@@ -10,12 +10,20 @@ built library raises.
 from .grid import MACGrid, grid_of  # noqa: F401
 from . import fields  # noqa: F401
 
-__all__ = ["MACGrid", "grid_of", "fields", "TensorStokes", "StokesResult", "Plan"]
+from .core import DeviceArray, Stage, State, Trial, stage_diagnostics  # noqa: F401
+from .integrate import Result, integrate, nearest_node_indices, schedule_nodes, step_sizes  # noqa: F401
+
+__all__ = ["MACGrid", "grid_of", "fields", "State", "Stage", "Trial", "DeviceArray", "stage_diagnostics",
+           "Result", "integrate", "step_sizes", "schedule_nodes", "nearest_node_indices",
+           "TensorStokes", "StokesResult", "Plan", "MACNavierStokes", "make_scheme", "scheme_info", "SCHEMES"]
+
+_LAZY = {"TensorStokes": "stokes", "StokesResult": "stokes", "Plan": "stokes", "MACNavierStokes": "model",
+         "make_scheme": "schemes", "scheme_info": "schemes", "SCHEMES": "schemes", "FusedScheme": "schemes"}
 
 
 def __getattr__(name):
     # GPU-facing modules import torch and the CUDA library lazily.
-    if name in ("TensorStokes", "StokesResult", "Plan"):
-        from . import stokes
-        return getattr(stokes, name)
+    if name in _LAZY:
+        from importlib import import_module
+        return getattr(import_module(f"{__name__}.{_LAZY[name]}"), name)
     raise AttributeError(name)

@@ -27,6 +27,16 @@ class StokesInfo(C.Structure):
                 ("iterations", C.c_int * MAX_COLUMNS), ("refinements", C.c_int)]
 
 
+class StageRecord(C.Structure):
+    """``macsav_stage_record``."""
+    _fields_ = [("r", C.c_double), ("residual", C.c_double), ("scalar_residual", C.c_double),
+                ("divergence_inf", C.c_double), ("continuity_residual", C.c_double),
+                ("correction_predictor", C.c_double), ("frozen_factor", C.c_double),
+                ("corrections", C.c_double * 2), ("stokes_residual", C.c_double),
+                ("stokes_divergence", C.c_double), ("max_velocity", C.c_double), ("max_pressure", C.c_double),
+                ("n_corrections", C.c_int), ("iterations", C.c_int * 2), ("cg_info", C.c_int), ("status", C.c_int)]
+
+
 _P = C.c_void_p
 _D = C.c_double
 _I = C.c_int
@@ -46,6 +56,8 @@ _SIGNATURES = {
     "macsav_inner": (_I, [_P, _P, _P, _LL, C.POINTER(_D), _P]),
     "macsav_max_abs": (_I, [_P, _P, _LL, C.POINTER(_D), _P]),
     "macsav_diagnostics": (_I, [_P, _P, _D, _D, _P, C.POINTER(_D), _P]),
+    "macsav_step": (_I, [_P, _I, _D, _D, _D, _D, _P, _D, _P, _P, _P, _P, C.POINTER(StageRecord), C.POINTER(_D), _P]),
+    "macsav_plan_set_graph": (_I, [_P, _I]),
 }
 
 _lib = None

@@ -3,7 +3,7 @@
 #include <cstdio>
 #include <string>
 
-#include "plan.cuh"
+#include "step.cuh"
 
 struct macsav_plan {
   macsav::Plan p;
@@ -218,6 +218,38 @@ int macsav_diagnostics(macsav_plan* plan, const double* x, double r, double nu, 
                        void* stream) {
   if (!plan || !x || !out) return MACSAV_ERR_VALUE;
   return macsav::op_diagnostics(&plan->p, x, r, nu, force, out, static_cast<cudaStream_t>(stream));
+}
+
+int macsav_step(macsav_plan* plan, int scheme, double t, double dt, double nu, double gamma, const double* x0,
+                double r0, const double* forces, double* x1, double* embedded, double* pressures,
+                macsav_stage_record* records, double* r1, void* stream) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  if (scheme < 0 || scheme > MACSAV_IMEX_EULER) return fail(P, MACSAV_ERR_VALUE, "Unknown scheme");
+  if (!std::isfinite(dt) || dt <= 0) return fail(P, MACSAV_ERR_VALUE, "Invalid step size");
+  if (!std::isfinite(nu) || nu <= 0) return fail(P, MACSAV_ERR_VALUE, "nu must be positive and finite");
+  if (!std::isfinite(gamma) || gamma < 0) return fail(P, MACSAV_ERR_VALUE, "gamma must be finite and nonnegative");
+  if (!x0 || !records || P->maxcols < 2) return fail(P, MACSAV_ERR_VALUE, "invalid step buffers");
+  const int st = macsav::run_step(P, scheme, t, dt, nu, gamma, x0, r0, forces, x1, embedded, pressures, records, r1,
+                                  static_cast<cudaStream_t>(stream));
+  switch (st) {
+    case macsav::ST_OK: return MACSAV_OK;
+    case macsav::ST_STOKES_RHS: return fail(P, MACSAV_ERR_VALUE, "Invalid Stokes RHS");
+    case macsav::ST_CG: return fail(P, MACSAV_ERR_CG, "Pressure Schur CG failed");
+    case macsav::ST_STOKES_GATE: return fail(P, MACSAV_ERR_STOKES_GATE, "Stokes gate");
+    case macsav::ST_NEG_ENERGY: return fail(P, MACSAV_ERR_NEG_ENERGY, "Negative Stokes response energy");
+    case macsav::ST_SAV_INPUT: return fail(P, MACSAV_ERR_VALUE, "Invalid frozen SAV scalar inputs");
+    case macsav::ST_SAV_DENOM: return fail(P, MACSAV_ERR_SCALAR, "Invalid frozen SAV scalar denominator");
+    case macsav::ST_SAV_NONFINITE: return fail(P, MACSAV_ERR_SCALAR, "Nonfinite frozen SAV correction");
+    case macsav::ST_STAGE_GATE: return fail(P, MACSAV_ERR_STAGE_GATE, "stage gate");
+    default: return st == MACSAV_ERR_CUDA ? cuda_status(P) : st;
+  }
+}
+
+int macsav_plan_set_graph(macsav_plan* plan, int enable) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  plan->p.use_graph = enable ? 1 : 0;
+  return MACSAV_OK;
 }
 
 }  // extern "C"

@@ -184,6 +184,11 @@ int op_apply(Plan* P, int which, const double* in, double* out, int cols, cudaSt
   return cudaGetLastError() == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
 }
 
+void launch_convection(Plan* P, const double* x, double* out, cudaStream_t s) {
+  k_convection<<<dim3(op_blocks(P->g.size), 1), kThreads, 0, s>>>(P->g, x, out);
+  ++P->launches;
+}
+
 int op_combine(Plan* P, int nterms, const double* coeffs, const double* const* fields, double* out, long long n,
                cudaStream_t s) {
   if (nterms < 1 || nterms > kMaxTerms) {

@@ -204,7 +204,10 @@ fail:
   return MACSAV_ERR_CUDA;
 }
 
+void step_free(Plan* P);
+
 void plan_free(Plan* p) {
+  step_free(p);
   free_transforms(p->t64);
   free_transforms(p->t32);
   cudaFree(p->w); cudaFree(p->vel); cudaFree(p->cells); cudaFree(p->cells32); cudaFree(p->w32);

@@ -20,6 +20,45 @@ struct SolveChecks {
   int nonfinite_force, nonfinite_solution, pad0, pad1;
 };
 
+// Detailed status of one device stage (mapped to exceptions by the host).
+enum StageStatus : int {
+  ST_OK = 0,
+  ST_STOKES_RHS = 1,     // ValueError("Invalid Stokes RHS")
+  ST_CG = 2,             // RuntimeError("Pressure Schur CG failed with info=N")
+  ST_STOKES_GATE = 3,    // RuntimeError("Stokes residual=..., divergence=...")
+  ST_NEG_ENERGY = 4,     // RuntimeError("Negative Stokes response energy")
+  ST_SAV_INPUT = 5,      // ValueError("Invalid frozen SAV scalar inputs")
+  ST_SAV_DENOM = 6,      // RuntimeError("Invalid frozen SAV scalar denominator")
+  ST_SAV_NONFINITE = 7,  // RuntimeError("Nonfinite frozen SAV correction")
+  ST_STAGE_GATE = 8,     // RuntimeError("SAV stage residuals ...")
+};
+
+// Device record of one stage (folded into macsav_stage_record).
+struct StageRec {
+  double r, residual, scalar_residual, divergence, predictor, factor, corr[2];
+  double stokes_residual, stokes_divergence, alpha, beta, coupling, scalar_rhs;
+  double max_rhs, max_conv, nn, max_velocity, max_pressure;
+  int n_corr, status, iters[2], cg_info, pad;
+};
+
+struct GraphEntry {
+  int key;
+  cudaGraphExec_t exec;
+};
+
+// Buffers of the device time step, allocated at the first step call.
+struct StepBuffers {
+  void* base = nullptr;
+  double *X = nullptr, *KU = nullptr, *NN = nullptr, *F = nullptr, *VW = nullptr, *FORCE = nullptr,
+         *EMB = nullptr, *PI = nullptr, *PS = nullptr, *coef = nullptr;
+  StageRec* recs = nullptr;
+  StageRec* h_recs = nullptr;
+  double* h_coef = nullptr;
+  cudaStream_t stream = nullptr, side = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  std::vector<GraphEntry> graphs;
+};
+
 template <typename T>
 struct Transforms {
   TBlockDev<T> u, v, p;
@@ -60,8 +99,22 @@ struct Plan {
   int* h_err = nullptr;
   cudaEvent_t done = nullptr;
 
+  // device time step
+  StepBuffers st;
+  int use_graph = 0;
+
   // counters of kernel launches issued by this plan (for reporting)
   long long launches = 0;
+};
+
+// Execution context of one enqueue: eager (the host drives the CG loop on the
+// device flags) or graph capture (the CG loop becomes a conditional WHILE
+// node whose body is one iteration).
+struct Exec {
+  cudaStream_t s;
+  bool graph;
+  cudaStream_t side;  // body capture stream (graph mode)
+  cudaGraphConditionalHandle cond;
 };
 
 int plan_build(Plan* p);

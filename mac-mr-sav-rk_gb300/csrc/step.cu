@@ -1,0 +1,644 @@
+// Whole mr-SAV / plain IMEX-SDIRK time step on the device.
+//
+// Restates SDIRK2MRSAV (solver/schemes/sdirk2_mrsav.py:15-75), SDIRK3MRSAV
+// (solver/schemes/sdirk3_mrsav.py:11-65), IMEXEulerMRSAV
+// (solver/schemes/imex_euler_mrsav.py:11-53) and the plain SDIRK2 / SDIRK3 /
+// IMEXEuler schemes (sdirk2.py:17-43, sdirk3.py:31-57, imex_euler.py:10-32)
+// over the MAC model seam (solver/mac_ns.py:12-107).  Every scalar of a stage
+// (alpha, beta, the frozen-factor map Phi, the residuals and gates) is
+// computed on the device, so a whole step is one stream of launches (or one
+// CUDA graph) with a single read-back of the stage records at the end.
+//
+// Coefficients that depend on dt, nu and gamma are written by the host into a
+// device table before each step; kernels read them by index, so a captured
+// graph stays valid when dt changes.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "step.cuh"
+
+namespace macsav {
+
+int enqueue_solve_fp64(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres);
+int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres);
+
+namespace {
+
+constexpr double kEta = 1.0 - 0.70710678118654752440;    // sdirk2.py:14, 1 - 1/sqrt(2)
+constexpr double kDelta = -0.70710678118654752440;       // sdirk2.py:15, -1/sqrt(2)
+const double kD3[4][4] = {{1. / 4, 0, 0, 0}, {3. / 10, 1. / 4, 0, 0}, {-31. / 220, 1. / 11, 1. / 4, 0},
+                          {31. / 198, 5. / 132, -4. / 9, 1. / 4}};                       // sdirk3.py:8-9
+const double kDH3[4][4] = {{1. / 4, 0, 0, 0}, {-33. / 50, 121. / 100, 0, 0}, {239. / 400, -71. / 100, 5. / 16, 0},
+                           {-1. / 48, -17. / 66, 235. / 528, -1. / 6}};                  // sdirk3.py:10-12
+const double kC3[5] = {0., 1. / 4, 4. / 5, 1., 1.};                                      // sdirk3.py:13
+
+// ------------------------------------------------------------- kernels ---
+// out[k] = sum_t coef[idx[k][t]] * src[k][t]  for two outputs (rhs and the
+// convection combination); partial slots: max|out0|, max|out1|, sum out1^2.
+__global__ void __launch_bounds__(kThreads) k_combine2(CombineArgs a, const double* coef, long long n,
+                                                       double* partial) {
+  __shared__ double red[6 * 32];
+  double m[2] = {0.0, 0.0}, s[1] = {0.0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    for (int o = 0; o < a.nout; ++o) {
+      double acc = 0.0;
+      for (int t = 0; t < a.nterm[o]; ++t) {
+        const double* src = a.src[o][t];
+        if (src) acc += coef[a.idx[o][t]] * src[i];
+      }
+      a.out[o][i] = acc;
+      m[o] = nanmax(m[o], fabs(acc));
+      if (o == 1) s[0] += acc * acc;
+    }
+  }
+  block_max<2>(m, red);
+  block_sum<1>(s, red);
+  if (threadIdx.x == 0) {
+    double* o = partial + blockIdx.x * 3;
+    o[0] = m[0];
+    o[1] = m[1];
+    o[2] = s[0];
+  }
+}
+
+// Partial sums of <N,V>, <N,W>, <W,W> with V, W the two Stokes columns.
+__global__ void __launch_bounds__(kThreads) k_dots3(const double* N, const double* V, const double* W, long long n,
+                                                    double* partial) {
+  __shared__ double red[6 * 32];
+  double s[3] = {0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double nv = N[i], w = W[i];
+    s[0] += nv * V[i];
+    s[1] += nv * w;
+    s[2] += w * w;
+  }
+  block_sum<3>(s, red);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 3; ++k) partial[blockIdx.x * 3 + k] = s[k];
+}
+
+// U = V - dt*coupling*W ; pi = piV/dt - coupling*piW ; partial <N,U>.
+// Plain schemes (sav == 0): U = V, pi = piV/dt.
+__global__ void __launch_bounds__(kThreads) k_recombine(GridDev g, const double* VW, const double* PI,
+                                                        const double* N, double* U, double* pi,
+                                                        const StageRec* rec, const double* coef, int dt_idx, int sav,
+                                                        double* partial) {
+  __shared__ double red[64];
+  const double dt = coef[dt_idx];
+  const double cpl = sav ? rec->coupling : 0.0;
+  const double resp = dt * cpl;
+  double s[1] = {0.0};
+  const int n = g.size > g.np ? g.size : g.np;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (i < g.size) {
+      const double u = sav ? VW[i] - resp * VW[g.size + i] : VW[i];
+      U[i] = u;
+      if (sav) s[0] += N[i] * u;
+    }
+    if (i < g.np) pi[i] = sav ? PI[i] / dt - cpl * PI[g.np + i] : PI[i] / dt;
+  }
+  block_sum<1>(s, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
+}
+
+// KU and the stage momentum defect (sdirk3_mrsav.py:107-110):
+// defect = U + kappa K U + dt G pi - rhs + dt*coupling*N,  G = -D^T.
+// Partial slots: max|defect|, max|U|, max|D U|, max|pi|.
+__global__ void __launch_bounds__(kThreads) k_stage_defect(GridDev g, const double* U, const double* pi,
+                                                           const double* rhs, const double* N, double* KU,
+                                                           const StageRec* rec, const double* coef, int dt_idx,
+                                                           int kappa_idx, int sav, double* partial) {
+  __shared__ double red[6 * 32];
+  const double dt = coef[dt_idx], kappa = coef[kappa_idx];
+  const double dtc = sav ? dt * rec->coupling : 0.0;
+  double m[4] = {0, 0, 0, 0};
+  const int n = g.size > g.np ? g.size : g.np;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (i < g.size) {
+      const double u = U[i];
+      const double ku = K_at(U, g, i);
+      if (KU) KU[i] = ku;
+      double d = u + kappa * ku;
+      d = d - dt * Dt_at(pi, g, i);
+      d = d - rhs[i];
+      if (sav) d = d + dtc * N[i];
+      m[0] = nanmax(m[0], fabs(d));
+      m[1] = nanmax(m[1], fabs(u));
+    }
+    if (i < g.np) {
+      const int j = i / g.nx, k = i - j * g.nx;
+      m[2] = nanmax(m[2], fabs(D_at(U, g, j, k)));
+      m[3] = nanmax(m[3], fabs(pi[i]));
+    }
+  }
+  block_max<4>(m, red);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 4; ++k) partial[blockIdx.x * 4 + k] = m[k];
+}
+
+__device__ double fold_sum(const double* partial, int nb, int K, int k, double* red) {
+  double s[1] = {0.0};
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) s[0] += partial[b * K + k];
+  block_sum<1>(s, red);
+  return s[0];
+}
+__device__ double fold_max(const double* partial, int nb, int K, int k, double* red) {
+  double m[1] = {0.0};
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) m[0] = nanmax(m[0], partial[b * K + k]);
+  block_max<1>(m, red);
+  return m[0];
+}
+
+// Stokes outcome of the stage: residual / divergence over both columns
+// (tensor_stokes.py:338-351) and the iteration counts.
+__global__ void k_stage_stokes(const SolveChecks* checks, const CGScalars* cg, int cols, double tol,
+                               StageRec* rec) {
+  if (threadIdx.x != 0) return;
+  double md = 0, mf = 0, mu = 0, mdiv = 0;
+  int bad_rhs = 0, bad_sol = 0, info = 0;
+  for (int c = 0; c < cols; ++c) {
+    md = nanmax(md, checks[c].max_defect);
+    mf = nanmax(mf, checks[c].max_force);
+    mu = nanmax(mu, checks[c].max_velocity);
+    mdiv = nanmax(mdiv, checks[c].max_div);
+    bad_rhs |= checks[c].nonfinite_force;
+    bad_sol |= checks[c].nonfinite_solution;
+    rec->iters[c] = cg[c].iters;
+    if (!info && cg[c].info) info = cg[c].info;
+  }
+  const double res = md / (1.0 + mf);
+  rec->stokes_residual = res;
+  rec->stokes_divergence = mdiv;
+  rec->cg_info = info;
+  if (rec->status) return;
+  if (bad_rhs) rec->status = ST_STOKES_RHS;
+  else if (info) rec->status = ST_CG;
+  else if (bad_sol || res > tol || mdiv > tol * (1.0 + mu)) rec->status = ST_STOKES_GATE;
+}
+
+// The frozen SAV scalar map for one stage (scalar_correction.py:29-52 and the
+// alpha/beta guard of sdirk3_mrsav.py:92-100).
+__global__ void __launch_bounds__(kThreads) k_stage_sav(const double* partial, int nb, StageRec* recs, int stage,
+                                                        const double* coef, SavIdx ix, double area) {
+  __shared__ double red[64];
+  const double nv = fold_sum(partial, nb, 3, 0, red);
+  const double nw = fold_sum(partial, nb, 3, 1, red);
+  const double ww = fold_sum(partial, nb, 3, 2, red);
+  if (threadIdx.x != 0) return;
+  StageRec& R = recs[stage];
+  const double dt = coef[ix.dt], d = coef[ix.d], r0 = coef[ix.r0];
+  // predictor and scalar right-hand side from earlier stages' r (r_0 = r0)
+  auto rval = [&](int k) { return k == 0 ? r0 : recs[k - 1].r; };
+  const double predictor = rval(ix.pred);
+  double srhs = 0.0;
+  for (int t = 0; t < ix.nsr; ++t) srhs += coef[ix.sr_coef[t]] * rval(ix.sr_r[t]);
+  R.scalar_rhs = srhs;
+  R.predictor = predictor;
+  const double alpha = area * nv;  // + lifting work, zero for MAC
+  double beta = area * nw;
+  R.alpha = alpha;
+  if (R.status) return;
+  if (beta < 0.0) {
+    const double scale = sqrt(area * R.nn * area * ww);  // Momentum.cauchy_scale
+    if (beta < -1e-12 * (1.0 + scale)) {
+      R.status = ST_NEG_ENERGY;
+      return;
+    }
+  }
+  beta = beta > 0.0 ? beta : 0.0;
+  R.beta = beta;
+  const int order = ix.order;
+  if (!isfinite(predictor) || !isfinite(dt) || !isfinite(d) || !isfinite(srhs) || !isfinite(alpha) ||
+      !isfinite(beta) || dt <= 0 || d <= 0) {
+    R.status = ST_SAV_INPUT;
+    return;
+  }
+  double z = predictor, c = 1.0;
+  const int count = order == 3 ? 2 : 1;
+  for (int it = 0; it < count; ++it) {
+    c = order == 1 ? 1.0 : (order == 2 ? 1.0 + z : 1.0 + z + z * z);
+    const double resp = dt * dt * c * c * beta;
+    const double den = d + resp;
+    if (!isfinite(den) || den <= 0) {
+      R.status = ST_SAV_DENOM;
+      return;
+    }
+    z = (srhs - dt * c * alpha + resp) / den;
+    if (!isfinite(z)) {
+      R.status = ST_SAV_NONFINITE;
+      return;
+    }
+    R.corr[it] = z;
+  }
+  R.n_corr = count;
+  R.factor = c;
+  R.r = z;
+  R.coupling = c * (1.0 - z);
+}
+
+// Closing scalar checks of the stage (sdirk3_mrsav.py:105-114).
+// gate: 1 = the stage defect gate (mr-SAV schemes, IMEX Euler); 0 = none
+// (plain SDIRK2/3 report the Stokes residual, sdirk3.py:52-55).
+__global__ void __launch_bounds__(kThreads) k_stage_close(const double* pdefect, int nbd, const double* pnu, int nbn,
+                                                          StageRec* recs, int stage, const double* coef, SavIdx ix,
+                                                          double area, int sav, int gate) {
+  __shared__ double red[64];
+  const double maxdef = fold_max(pdefect, nbd, 4, 0, red);
+  const double maxu = fold_max(pdefect, nbd, 4, 1, red);
+  const double maxdiv = fold_max(pdefect, nbd, 4, 2, red);
+  const double maxpi = fold_max(pdefect, nbd, 4, 3, red);
+  const double nu_dot = sav ? fold_sum(pnu, nbn, 1, 0, red) : 0.0;
+  if (threadIdx.x != 0) return;
+  StageRec& R = recs[stage];
+  const double dt = coef[ix.dt];
+  R.max_velocity = maxu;
+  R.divergence = maxdiv;
+  R.max_pressure = maxpi;
+  double denom = 1.0 + R.max_rhs;
+  if (sav) {
+    const double scalar = coef[ix.d] * R.r - R.scalar_rhs + dt * R.factor * (area * nu_dot);
+    R.scalar_residual = fabs(scalar) / (1.0 + fabs(R.scalar_rhs) + fabs(R.r));
+    denom += dt * fabs(R.coupling) * R.max_conv;
+  } else {
+    R.scalar_residual = 0.0;
+  }
+  R.residual = gate ? maxdef / denom : R.stokes_residual;
+  if (R.status || !gate) return;
+  const bool finite = isfinite(R.residual) && isfinite(R.scalar_residual) && isfinite(maxdiv) && isfinite(maxu) &&
+                      isfinite(maxpi);
+  if (!finite || R.residual > 1e-8 || R.scalar_residual > 1e-8 || maxdiv > 1e-8 * (1.0 + maxu))
+    R.status = ST_STAGE_GATE;
+}
+
+__global__ void k_fold_combine(const double* partial, int nb, StageRec* rec) {
+  __shared__ double red[64];
+  const double m0 = fold_max(partial, nb, 3, 0, red);
+  const double m1 = fold_max(partial, nb, 3, 1, red);
+  const double s2 = fold_sum(partial, nb, 3, 2, red);
+  if (threadIdx.x == 0) {
+    rec->max_rhs = m0;
+    rec->max_conv = m1;
+    rec->nn = s2;
+  }
+}
+
+__global__ void k_set_shift(double* shift, const double* coef, int kappa_idx, int cols) {
+  if (threadIdx.x < cols) {
+    shift[2 * threadIdx.x] = 1.0;
+    shift[2 * threadIdx.x + 1] = coef[kappa_idx];
+  }
+}
+
+__global__ void k_clear_recs(StageRec* recs, int n) {
+  if (threadIdx.x < n) {
+    StageRec z;
+    memset(&z, 0, sizeof(z));
+    recs[threadIdx.x] = z;
+  }
+}
+
+}  // namespace
+
+// --------------------------------------------------------------- host side ---
+static int red_nb(long long n) {
+  long long b = (n + kThreads - 1) / kThreads;
+  return int(b < 1 ? 1 : (b > 1024 ? 1024 : b));
+}
+
+int step_buffers(Plan* P) {
+  if (P->st.X) return MACSAV_OK;
+  const size_t sz = P->g.size, np = P->g.np;
+  StepBuffers& B = P->st;
+  const size_t total = sizeof(double) * (sz * (5 + 4 + 4 + 2 + 2 + 4 + 1) + np * (2 + 4)) + 256 * sizeof(double);
+  void* d = nullptr;
+  if (cudaMalloc(&d, total) != cudaSuccess) return MACSAV_ERR_CUDA;
+  B.base = d;
+  double* p = static_cast<double*>(d);
+  B.X = p; p += 5 * sz;
+  B.KU = p; p += 4 * sz;
+  B.NN = p; p += 4 * sz;
+  B.F = p; p += 2 * sz;
+  B.VW = p; p += 2 * sz;
+  B.FORCE = p; p += 4 * sz;
+  B.EMB = p; p += sz;
+  B.PI = p; p += 2 * np;
+  B.PS = p; p += 4 * np;
+  B.coef = p;
+  if (cudaMalloc(&B.recs, sizeof(StageRec) * 4) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaMallocHost(&B.h_recs, sizeof(StageRec) * 4) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaMallocHost(&B.h_coef, sizeof(double) * 256) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaStreamCreateWithFlags(&B.side, cudaStreamNonBlocking) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaEventCreateWithFlags(&B.ev_in, cudaEventDisableTiming) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaEventCreateWithFlags(&B.ev_out, cudaEventDisableTiming) != cudaSuccess) return MACSAV_ERR_CUDA;
+  return MACSAV_OK;
+}
+
+void step_free(Plan* P) {
+  StepBuffers& B = P->st;
+  for (auto& kv : B.graphs) cudaGraphExecDestroy(kv.exec);
+  B.graphs.clear();
+  cudaFree(B.base);
+  cudaFree(B.recs);
+  cudaFreeHost(B.h_recs);
+  cudaFreeHost(B.h_coef);
+  if (B.stream) cudaStreamDestroy(B.stream);
+  if (B.side) cudaStreamDestroy(B.side);
+  if (B.ev_in) cudaEventDestroy(B.ev_in);
+  if (B.ev_out) cudaEventDestroy(B.ev_out);
+  B = StepBuffers{};
+}
+
+int scheme_stages(int scheme) {
+  switch (scheme) {
+    case MACSAV_SDIRK2_MRSAV: case MACSAV_SDIRK2: return 2;
+    case MACSAV_SDIRK3_MRSAV: case MACSAV_SDIRK3: return 4;
+    case MACSAV_IMEX_EULER_MRSAV: case MACSAV_IMEX_EULER: return 1;
+  }
+  return 0;
+}
+static bool scheme_sav(int scheme) {
+  return scheme == MACSAV_SDIRK2_MRSAV || scheme == MACSAV_SDIRK3_MRSAV || scheme == MACSAV_IMEX_EULER_MRSAV;
+}
+
+// Host-built stage program: which vectors each combine reads, with which
+// coefficient slots, plus the slot values for the current (dt, nu, gamma).
+struct StageProgram {
+  CombineArgs comb[4];
+  SavIdx sav[4];
+  int kappa[4];
+  int dt_idx, r0_idx;
+  int need_conv[5];    // convection at node j needed
+  int emb_terms;
+  int emb_idx[4];
+  int emb_node[4];
+  int nstages;
+};
+
+static void build_program(Plan* P, int scheme, bool has_force, double dt, double nu, double gamma, double r0,
+                          StageProgram& G, double* coef) {
+  StepBuffers& B = P->st;
+  const long long sz = P->g.size;
+  int nc = 0;
+  auto slot = [&](double v) { coef[nc] = v; return nc++; };
+  std::memset(&G, 0, sizeof(G));
+  G.nstages = scheme_stages(scheme);
+  G.dt_idx = slot(dt);
+  G.r0_idx = slot(r0);
+  auto U = [&](int k) { return B.X + k * sz; };
+  auto KU = [&](int k) { return B.KU + k * sz; };
+  auto NN = [&](int k) { return B.NN + k * sz; };
+  auto FF = [&](int k) { return has_force ? B.FORCE + k * sz : (const double*)nullptr; };
+  const bool sav = scheme_sav(scheme);
+  for (int i = 0; i < G.nstages; ++i) {
+    CombineArgs& c = G.comb[i];
+    c.nout = 2;
+    c.out[0] = B.F;
+    c.out[1] = B.F + sz;
+    auto add = [&](int o, const double* src, double v) {
+      const int t = c.nterm[o]++;
+      c.src[o][t] = src;
+      c.idx[o][t] = slot(v);
+    };
+    SavIdx& s = G.sav[i];
+    if (scheme == MACSAV_SDIRK3_MRSAV || scheme == MACSAV_SDIRK3) {
+      // rhs = U_i + dt*sum_j DHAT[i,j] f_j - nu*dt*sum_{j<i} D[i,j] K U_{j+1}   (sdirk3_mrsav.py:85-88)
+      add(0, U(i), 1.0);
+      for (int j = 0; j <= i; ++j) add(0, FF(j), dt * kDH3[i][j]);
+      for (int j = 0; j < i; ++j) add(0, KU(j), -nu * dt * kD3[i][j]);
+      for (int j = 0; j <= i; ++j) add(1, NN(j), kDH3[i][j]);
+      if (scheme == MACSAV_SDIRK3) {  // plain: convection moves into the rhs (sdirk3.py:44-46)
+        for (int j = 0; j <= i; ++j) add(0, NN(j), -dt * kDH3[i][j]);
+      }
+      G.kappa[i] = slot(nu * dt * kD3[i][i]);
+      s.d = slot(1.0 + gamma * dt * kD3[i][i]);
+      s.order = 3;
+      s.pred = i;  // scalars[-1]
+      s.nsr = 0;
+      s.sr_r[s.nsr] = i;
+      s.sr_coef[s.nsr++] = slot(1.0);
+      for (int j = 0; j < i; ++j) {
+        s.sr_r[s.nsr] = j + 1;
+        s.sr_coef[s.nsr++] = slot(-gamma * dt * kD3[i][j]);
+      }
+    } else if (scheme == MACSAV_SDIRK2_MRSAV || scheme == MACSAV_SDIRK2) {
+      const bool plain = scheme == MACSAV_SDIRK2;
+      if (i == 0) {  // sdirk2_mrsav.py:215-216
+        add(0, U(0), 1.0);
+        add(0, FF(0), kEta * dt);
+        add(1, NN(0), kEta);
+        if (plain) add(0, NN(0), -kEta * dt);  // sdirk2.py:32
+        s.pred = 0;
+        s.nsr = 1;
+        s.sr_r[0] = 0;
+        s.sr_coef[0] = slot(1.0);
+      } else {  // sdirk2_mrsav.py:218-221
+        add(0, U(1), 1.0);
+        add(0, KU(0), -nu * dt * (1 - 2 * kEta));
+        add(0, FF(0), -dt);
+        add(0, FF(1), dt * (1 - kDelta));
+        add(1, NN(0), -1.0);
+        add(1, NN(1), 1 - kDelta);
+        if (plain) {  // sdirk2.py:36-37
+          add(0, NN(0), dt);
+          add(0, NN(1), -dt * (1 - kDelta));
+        }
+        s.pred = 1;
+        s.nsr = 1;
+        s.sr_r[0] = 1;
+        s.sr_coef[0] = slot(1 - gamma * dt * (1 - 2 * kEta));
+      }
+      G.kappa[i] = slot(nu * kEta * dt);
+      s.d = slot(1.0 + gamma * kEta * dt);
+      s.order = 2;
+    } else {  // IMEX Euler (imex_euler_mrsav.py:57-58, imex_euler.py:19)
+      add(0, U(0), 1.0);
+      add(0, FF(0), dt);
+      add(1, NN(0), 1.0);
+      if (scheme == MACSAV_IMEX_EULER) add(0, NN(0), -dt);
+      G.kappa[i] = slot(nu * dt);
+      s.d = slot(1.0 + gamma * dt);
+      s.order = 1;
+      s.pred = 0;
+      s.nsr = 1;
+      s.sr_r[0] = 0;
+      s.sr_coef[0] = slot(1.0);
+    }
+    s.dt = G.dt_idx;
+    s.r0 = G.r0_idx;
+    (void)sav;
+  }
+  // convection needed at nodes 0..nstages-1
+  for (int j = 0; j < G.nstages; ++j) G.need_conv[j] = 1;
+  // embedded velocity (sdirk3.py:16-19; sdirk2_mrsav.py:222)
+  if (G.nstages == 4) {
+    const double w[4] = {2. / 3, -128. / 99, 50. / 33, 1. / 9};
+    G.emb_terms = 4;
+    for (int k = 0; k < 4; ++k) {
+      G.emb_idx[k] = slot(w[k]);
+      G.emb_node[k] = k;
+    }
+  } else if (G.nstages == 2) {
+    G.emb_terms = 2;
+    G.emb_idx[0] = slot(1.0 - 1.0 / kEta);
+    G.emb_node[0] = 0;
+    G.emb_idx[1] = slot(1.0 / kEta);
+    G.emb_node[1] = 1;
+  }
+}
+
+// Enqueue one whole step on X.s reading U_0 from B.X (and forces from B.FORCE),
+// writing U_n to B.X + n*size, stage pressures to B.PS, records to B.recs.
+static int enqueue_step(Plan* P, Exec& X, int scheme, const StageProgram& G, bool want_emb) {
+  StepBuffers& B = P->st;
+  const GridDev& g = P->g;
+  const long long sz = g.size, np = g.np;
+  const cudaStream_t s = X.s;
+  const int nbs = red_nb(sz), nbn = red_nb(sz > np ? sz : np);
+  const bool sav = scheme_sav(scheme);
+  const int cols = sav ? 2 : 1;
+  const double area = g.hx * g.hy;
+  (void)np;
+  k_clear_recs<<<1, 32, 0, s>>>(B.recs, 4);
+  ++P->launches;
+  // N(U_0)
+  launch_convection(P, B.X, B.NN, s);
+  for (int i = 0; i < G.nstages; ++i) {
+    StageRec* rec = B.recs + i;
+    double* U = B.X + (i + 1) * sz;
+    CombineArgs ca = G.comb[i];
+    if (!sav) ca.nout = 1;
+    k_combine2<<<nbs, kThreads, 0, s>>>(ca, B.coef, sz, P->partial);
+    k_fold_combine<<<1, kThreads, 0, s>>>(P->partial, nbs, rec);
+    k_set_shift<<<1, 32, 0, s>>>(P->shift, B.coef, G.kappa[i], cols);
+    P->launches += 3;
+    int rc = P->precision == MACSAV_FP64 ? enqueue_solve_fp64(P, X, B.F, cols, B.VW, B.PI)
+                                         : enqueue_solve_mixed(P, X, B.F, cols, B.VW, B.PI);
+    if (rc != MACSAV_OK) return rc;
+    k_stage_stokes<<<1, 32, 0, s>>>(P->checks, P->cg, cols, P->tol, rec);
+    ++P->launches;
+    if (sav) {
+      k_dots3<<<nbs, kThreads, 0, s>>>(B.F + sz, B.VW, B.VW + sz, sz, P->partial);
+      k_stage_sav<<<1, kThreads, 0, s>>>(P->partial, nbs, B.recs, i, B.coef, G.sav[i], area);
+      P->launches += 2;
+    }
+    double* pi = B.PS + i * np;
+    double* pnu = P->partial + 8192;
+    k_recombine<<<nbn, kThreads, 0, s>>>(g, B.VW, B.PI, B.F + sz, U, pi, rec, B.coef, G.dt_idx, sav ? 1 : 0, pnu);
+    k_stage_defect<<<nbn, kThreads, 0, s>>>(g, U, pi, B.F, B.F + sz, B.KU + i * sz, rec, B.coef, G.dt_idx,
+                                            G.kappa[i], sav ? 1 : 0, P->partial);
+    const int gate = (scheme == MACSAV_SDIRK2 || scheme == MACSAV_SDIRK3) ? 0 : 1;
+    k_stage_close<<<1, kThreads, 0, s>>>(P->partial, nbn, pnu, nbn, B.recs, i, B.coef, G.sav[i], area,
+                                         sav ? 1 : 0, gate);
+    P->launches += 3;
+    if (i + 1 < G.nstages) launch_convection(P, U, B.NN + (i + 1) * sz, s);
+  }
+  if (want_emb && G.emb_terms) {
+    CombineArgs e;
+    std::memset(&e, 0, sizeof(e));
+    e.nout = 1;
+    e.out[0] = B.EMB;
+    e.nterm[0] = G.emb_terms;
+    for (int k = 0; k < G.emb_terms; ++k) {
+      e.src[0][k] = B.X + G.emb_node[k] * sz;
+      e.idx[0][k] = G.emb_idx[k];
+    }
+    k_combine2<<<nbs, kThreads, 0, s>>>(e, B.coef, sz, P->partial);
+    ++P->launches;
+  }
+  return MACSAV_OK;
+}
+
+int run_step(Plan* P, int scheme, double t, double dt, double nu, double gamma, const double* x0, double r0,
+             const double* forces, double* x1, double* embedded, double* pressures, macsav_stage_record* records,
+             double* r1, cudaStream_t user) {
+  (void)t;
+  int rc = step_buffers(P);
+  if (rc != MACSAV_OK) return rc;
+  StepBuffers& B = P->st;
+  const long long sz = P->g.size, np = P->g.np;
+  StageProgram G;
+  double* coef = B.h_coef;
+  build_program(P, scheme, forces != nullptr, dt, nu, gamma, r0, G, coef);
+  const int n = G.nstages;
+  // inputs onto the plan's stream
+  cudaEventRecord(B.ev_in, user);
+  cudaStreamWaitEvent(B.stream, B.ev_in, 0);
+  const cudaStream_t s = B.stream;
+  cudaMemcpyAsync(B.coef, coef, sizeof(double) * 256, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(B.X, x0, sizeof(double) * sz, cudaMemcpyDeviceToDevice, s);
+  if (forces) cudaMemcpyAsync(B.FORCE, forces, sizeof(double) * sz * n, cudaMemcpyDeviceToDevice, s);
+  const bool want_emb = embedded != nullptr;
+  if (!P->use_graph) {
+    Exec X{s, false, nullptr, 0};
+    rc = enqueue_step(P, X, scheme, G, want_emb);
+    if (rc != MACSAV_OK) return rc;
+  } else {
+    const int key = scheme * 4 + (forces ? 1 : 0) + (want_emb ? 2 : 0);
+    cudaGraphExec_t exec = nullptr;
+    for (auto& kv : B.graphs)
+      if (kv.key == key) exec = kv.exec;
+    if (!exec) {
+      Exec X{s, true, B.side, 0};
+      if (cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed) != cudaSuccess) return MACSAV_ERR_CUDA;
+      rc = enqueue_step(P, X, scheme, G, want_emb);
+      cudaGraph_t graph = nullptr;
+      cudaError_t e = cudaStreamEndCapture(s, &graph);
+      if (rc != MACSAV_OK || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        P->err = std::string("graph capture failed: ") + cudaGetErrorString(e);
+        return MACSAV_ERR_CUDA;
+      }
+      e = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) {
+        P->err = std::string("graph instantiate failed: ") + cudaGetErrorString(e);
+        return MACSAV_ERR_CUDA;
+      }
+      B.graphs.push_back(GraphEntry{key, exec});
+    }
+    if (cudaGraphLaunch(exec, s) != cudaSuccess) return MACSAV_ERR_CUDA;
+  }
+  if (x1) cudaMemcpyAsync(x1, B.X + n * sz, sizeof(double) * sz, cudaMemcpyDeviceToDevice, s);
+  if (want_emb && G.emb_terms) cudaMemcpyAsync(embedded, B.EMB, sizeof(double) * sz, cudaMemcpyDeviceToDevice, s);
+  if (pressures) cudaMemcpyAsync(pressures, B.PS, sizeof(double) * np * n, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(B.h_recs, B.recs, sizeof(StageRec) * n, cudaMemcpyDeviceToHost, s);
+  cudaEventRecord(B.ev_out, s);
+  cudaStreamWaitEvent(user, B.ev_out, 0);
+  if (cudaEventSynchronize(B.ev_out) != cudaSuccess) return MACSAV_ERR_CUDA;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    P->err = std::string("CUDA: ") + cudaGetErrorString(e);
+    return MACSAV_ERR_CUDA;
+  }
+  int status = MACSAV_OK;
+  for (int i = 0; i < n; ++i) {
+    const StageRec& R = B.h_recs[i];
+    macsav_stage_record& o = records[i];
+    std::memset(&o, 0, sizeof(o));
+    o.r = R.r;
+    o.residual = R.residual;
+    o.scalar_residual = R.scalar_residual;
+    o.divergence_inf = R.divergence;
+    o.continuity_residual = R.divergence;
+    o.correction_predictor = scheme_sav(scheme) ? R.predictor : NAN;
+    o.frozen_factor = scheme_sav(scheme) ? R.factor : NAN;
+    o.n_corrections = scheme_sav(scheme) ? R.n_corr : 0;
+    o.corrections[0] = R.corr[0];
+    o.corrections[1] = R.corr[1];
+    o.iterations[0] = R.iters[0];
+    o.iterations[1] = R.iters[1];
+    o.stokes_residual = R.stokes_residual;
+    o.stokes_divergence = R.stokes_divergence;
+    o.max_velocity = R.max_velocity;
+    o.max_pressure = R.max_pressure;
+    o.cg_info = R.cg_info;
+    o.status = R.status;
+    if (status == MACSAV_OK && R.status) status = R.status;
+  }
+  if (r1) *r1 = scheme_sav(scheme) ? B.h_recs[n - 1].r : 0.0;
+  return status;
+}
+
+}  // namespace macsav

@@ -1,0 +1,32 @@
+// Internal declarations of the device time step (step.cu).
+#pragma once
+#include "plan.cuh"
+
+namespace macsav {
+
+constexpr int kMaxCombine = 12;
+
+// Two outputs, each a sum of coef[idx] * src (null src = zero term).
+struct CombineArgs {
+  int nout;
+  int nterm[2];
+  double* out[2];
+  const double* src[2][kMaxCombine];
+  int idx[2][kMaxCombine];
+};
+
+// Coefficient-table slots of one stage's scalar update.
+struct SavIdx {
+  int dt, d, order, pred, nsr, r0;
+  int sr_r[4];      // which r_k enters the scalar rhs (0 = the step's r0)
+  int sr_coef[4];   // coefficient slots
+};
+
+void launch_convection(Plan* P, const double* x, double* out, cudaStream_t s);
+int run_step(Plan* P, int scheme, double t, double dt, double nu, double gamma, const double* x0, double r0,
+             const double* forces, double* x1, double* embedded, double* pressures, macsav_stage_record* records,
+             double* r1, cudaStream_t user);
+int scheme_stages(int scheme);
+void step_free(Plan* P);
+
+}  // namespace macsav
