@@ -1,0 +1,308 @@
+"""Benchmark of the MAC mr-SAV stage hot path on one or more GB300s.
+
+Metric (cell-stage updates/s): nx*ny*(stages completed)/second for the
+512^2 sdirk3_mrsav cavity (nu=1e-3, dt=2.5e-4, psi modes k,l<=16, seeded
+synthetic field), the single-case precision configuration.  ``value`` is the
+FP32-bulk form (FP32 transforms/stencils/Krylov vectors, FP64 reductions,
+FP64 defect correction so the reference's 1e-9 Stokes and 1e-8 stage gates
+hold) with the state resident in HBM; the plain FP64 path is timed beside it
+(``fp64``) and the relative L2 difference of the two trajectories is reported.
+``e2e`` is the same metric through the public API (``scheme.step(model,
+state, dt)`` with a host ``State``: the velocity goes host->device and the new
+state device->host every step).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU: independent replicas of the cavity, one per rank (a single cavity
+does not shard; the reference has no distributed path), ``scaling: weak``.
+``--impl reference`` times the CPU oracle (a NumPy/SciPy restatement of the
+reference's own path, all host threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = {"workload": "cavity512_sdirk3_mrsav", "nx": 512, "ny": 512, "lx": 1.0, "ly": 1.0, "nu": 1e-3,
+            "dt": 2.5e-4, "scheme": "sdirk3_mrsav", "psi_modes": 16, "seed": 20261203, "stages_per_step": 4}
+METRIC = "cell-stage updates/s"
+L2_BYTES = 129 * 2 ** 20
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int) -> None:
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def initial_state(pkg):
+    w = WORKLOAD
+    return pkg.fields.packed_curl_velocity(w["nx"], w["ny"], w["lx"], w["ly"], w["psi_modes"], w["seed"])
+
+
+def cpu_baseline(steps: int = 2, threads: int = 1) -> dict:
+    """The CPU oracle (restatement of the reference path) on a bounded sample."""
+    import __graft_entry__
+    pkg = __graft_entry__.load_package()
+    import oracle
+    w = WORKLOAD
+    g = oracle.Grid(w["nx"], w["ny"], w["lx"], w["ly"])
+    model = oracle.OracleModel(g, w["nu"], backend=oracle.TensorStokesOracle(g, 1e-9, 1e-12, workers=threads))
+    scheme = oracle.make_scheme(w["scheme"])
+    state = model.state(0.0, initial_state(pkg), 0.0)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        state = scheme.step(model, state, w["dt"]).state
+    sec = time.perf_counter() - t0
+    cells = w["nx"] * w["ny"] * w["stages_per_step"] * steps
+    return {"value": cells / sec, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{steps} steps of the {w['workload']} workload (NumPy/SciPy oracle, {threads} thread(s))",
+            "seconds": sec}
+
+
+def run_reference(args) -> None:
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    w = WORKLOAD
+    base = cpu_baseline(steps=max(1, args.steps), threads=threads)
+    value = base["value"]
+    sec_per_step = base["seconds"] / max(1, args.steps)
+    line = {"metric": METRIC, "value": value, "unit": "cell-stage/s", "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sec_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded stream-function curl field)",
+            "config": {"workload": w["workload"], **{k: w[k] for k in ("nx", "ny", "nu", "dt", "scheme",
+                                                                       "psi_modes")}},
+            "cpu_baseline": {"value": value, "unit": "cell-stage/s", "cores": threads, "kind": "port",
+                             "sample": base["sample"]},
+            "e2e": {"value": value, "unit": "cell-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    if args.warmup < 3:
+        args.warmup = 3
+
+    import torch
+    import torch.distributed as dist
+    import __graft_entry__
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    __graft_entry__.build()
+    pkg = __graft_entry__.load_package()
+    from importlib import import_module
+    lib = import_module(pkg.__name__ + "._lib")
+    stokes = import_module(pkg.__name__ + ".stokes")
+    w = WORKLOAD
+    g = pkg.MACGrid(w["nx"], w["ny"], w["lx"], w["ly"])
+    x0_host = initial_state(pkg)
+    dev = torch.device("cuda", local)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed_device_run(precision: str):
+        """W warm-up + K timed steps on device-resident state; per-step events,
+        L2 flushed (256 MiB write) between timed steps outside the events."""
+        model = pkg.MACNavierStokes(g, w["nu"], precision=precision, use_graph=True)
+        scheme = pkg.make_scheme(w["scheme"])
+        x = torch.from_numpy(x0_host.copy()).to(dev)
+        y = torch.empty_like(x)
+        pres = torch.empty((4, g.np), dtype=torch.float64, device=dev)
+        t, r = 0.0, 0.0
+        iters = []
+        for _ in range(args.warmup):
+            y, r, recs, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
+            x, y, t = y, x, t + w["dt"]
+        # kernels per step: one eager step on a copy (same CG iteration counts)
+        eager = pkg.MACNavierStokes(g, w["nu"], precision=precision, use_graph=False)
+        before = eager.plan.launches
+        scheme.step_device(eager, x, t, r, w["dt"], pres=pres, want_embedded=False)
+        launches_per_step = eager.plan.launches - before
+        del eager
+        barrier()
+        times = []
+        with ClockSampler(local) as clk:
+            for _ in range(args.steps):
+                flush.fill_(1.0)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                y, r, recs, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres,
+                                                      want_embedded=False)
+                b.record(stream)
+                x, y, t = y, x, t + w["dt"]
+                iters.append([tuple(rc.iterations[:2]) for rc in recs])
+                times.append((a, b))
+            torch.cuda.synchronize()
+        ms = [a.elapsed_time(b) for a, b in times]
+        return model, scheme, x, r, sum(ms), ms, iters, launches_per_step, clk.summary()
+
+    barrier()
+    m32, s32, x32, r32, ms32, per32, it32, l32, clk32 = timed_device_run("fp32")
+    barrier()
+    m64, s64, x64, r64, ms64, per64, it64, l64, clk64 = timed_device_run("fp64")
+    barrier()
+    # both trajectories start from the same field and take the same steps
+    diff = float(torch.linalg.vector_norm(x32 - x64) / torch.linalg.vector_norm(x64))
+
+    # max over ranks of the timed totals
+    tot = torch.tensor([ms32, ms64], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(tot, op=dist.ReduceOp.MAX)
+    ms32, ms64 = float(tot[0]), float(tot[1])
+    cells = w["nx"] * w["ny"] * w["stages_per_step"] * args.steps * world
+    value = cells / (ms32 / 1e3)
+    value64 = cells / (ms64 / 1e3)
+
+    # end to end through the public API with host state (H2D + D2H each step)
+    scheme = pkg.make_scheme(w["scheme"])
+    st_host = pkg.State(0.0, *g.unpack(x0_host), 0.0)
+    for _ in range(args.warmup):
+        st_host = scheme.step(m32, pkg.State(st_host.t, np.array(st_host.u), np.array(st_host.v), st_host.r),
+                              w["dt"]).state
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fresh = pkg.State(st_host.t, np.array(st_host.u), np.array(st_host.v), st_host.r)  # no device copy
+        st_host = scheme.step(m32, fresh, w["dt"]).state
+    torch.cuda.synchronize()
+    e2e_sec = time.perf_counter() - t0
+    et = torch.tensor([e2e_sec], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(et, op=dist.ReduceOp.MAX)
+    e2e_value = cells / float(et[0])
+
+    # dominant kernel (FP32 column pass of the velocity blocks) timed alone
+    import ctypes as C
+    ms_k, bytes_k = C.c_double(), C.c_double()
+    m32.plan.check(lib.load().macsav_time_pass(m32.plan.handle, 0, 50, C.byref(ms_k), C.byref(bytes_k),
+                                               stokes.stream_handle()))
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = bytes_k.value / (ms_k.value * 1e-3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "column_pass_traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("traffic_bytes_per_launch")
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    base = None if args.no_cpu_baseline else cpu_baseline(steps=2, threads=1)
+    mean_iters = float(np.mean([[a, b] for stage in it32 for (a, b) in stage]))
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-stage/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic (seeded stream-function curl field)",
+        "config": {"workload": w["workload"], "nx": w["nx"], "ny": w["ny"], "nu": w["nu"], "dt": w["dt"],
+                   "scheme": w["scheme"], "psi_modes": w["psi_modes"], "parallelism": f"replicas{world}",
+                   "form": "fp32 transforms/stencils/Krylov + fp64 reductions + fp64 defect correction",
+                   "preconditioner": "spectral m(DD^T)^+ + kI (learned preconditioner not built)",
+                   "l2": "flushed (256 MiB write) before every timed step", "graph": "one CUDA graph per step"},
+        "fp64": {"value": value64, "ms_per_step": ms64 / args.steps, "unit": "cell-stage/s"},
+        "speedup_vs_fp64": value / value64,
+        "error_vs_fp64": {"rel_l2_velocity": diff, "after_steps": args.warmup + args.steps},
+        "cg_iterations_mean": mean_iters,
+        "clocks": clk32,
+        "e2e": {"value": e2e_value, "unit": "cell-stage/s", "h2d_bytes_per_step": g.size * 8,
+                "d2h_bytes_per_step": g.size * 8 + 4 * 160},
+        "gpu_launches": int(l32 * args.steps),
+        "roofline": {"kernel": "k_column<float> (velocity blocks, 2 RHS)", "bound": "hbm",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_source": "measured" if pk.exists() else "fallback",
+                     "traffic": traffic, "bytes_per_launch": bytes_k.value, "ms_per_launch": ms_k.value},
+    }
+    if base is not None:
+        line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -164,6 +164,14 @@ int macsav_step(macsav_plan* plan, int scheme, double t, double dt, double nu, d
                 double r0, const double* forces, double* x1, double* embedded, double* pressures,
                 macsav_stage_record* records, double* r1, void* stream);
 
+/* Measurement helper (no reference counterpart: it times this library's own
+ * kernels for the roofline): average device milliseconds of `reps`
+ * back-to-back launches of one transform pass over the velocity blocks with two
+ * right-hand sides, and the pass's algorithmic bytes per launch.
+ * pass 0: FP32 column pass, 1: FP32 forward row pass, 2: FP32 inverse row pass
+ * (these need a MACSAV_FP32_MIXED plan), 3: FP64 column pass.  Synchronises. */
+int macsav_time_pass(macsav_plan* plan, int pass, int reps, double* ms, double* bytes, void* stream);
+
 /* Run macsav_step as one captured CUDA graph per (scheme, force, embedded)
  * (the pressure CG loop becomes a conditional WHILE node).  Default: off. */
 int macsav_plan_set_graph(macsav_plan* plan, int enable);

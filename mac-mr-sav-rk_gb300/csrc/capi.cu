@@ -21,6 +21,7 @@ int op_dot_max(Plan* P, const double* a, const double* b, long long n, double* r
 int op_diagnostics(Plan* P, const double* x, double r, double nu, const double* force, double* out,
                    cudaStream_t s);
 int op_transform(Plan* P, int kind, int inverse, int rows, int n, const double* in, double* out, cudaStream_t s);
+int time_pass(Plan* P, int pass, int reps, cudaStream_t s, double* ms, double* bytes);
 }  // namespace macsav
 
 using macsav::Plan;
@@ -244,6 +245,12 @@ int macsav_step(macsav_plan* plan, int scheme, double t, double dt, double nu, d
     case macsav::ST_STAGE_GATE: return fail(P, MACSAV_ERR_STAGE_GATE, "stage gate");
     default: return st == MACSAV_ERR_CUDA ? cuda_status(P) : st;
   }
+}
+
+int macsav_time_pass(macsav_plan* plan, int pass, int reps, double* ms, double* bytes, void* stream) {
+  if (!plan || !ms || !bytes) return MACSAV_ERR_VALUE;
+  const int rc = macsav::time_pass(&plan->p, pass, reps, static_cast<cudaStream_t>(stream), ms, bytes);
+  return rc == MACSAV_ERR_CUDA ? cuda_status(&plan->p) : rc;
 }
 
 int macsav_plan_set_graph(macsav_plan* plan, int enable) {

@@ -44,7 +44,49 @@ enum ErrorBits : int {
   ERR_SCALAR = 1 << 5,
 };
 
-constexpr int kThreads = 256;
+// Division by a runtime-constant divisor d >= 1 for 0 <= n < 2^31 with one
+// multiply-high (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", 1994): q = (umulhi(n, m) + n) >> s, m = floor(2^32 (2^s - d) / d) + 1.
+struct FastDiv {
+  unsigned int d, m, s;
+  FastDiv() : d(1), m(1), s(0) {}
+  explicit FastDiv(unsigned int div) : d(div) {
+    s = 0;
+    while ((1ull << s) < d) ++s;
+    m = (unsigned int)((((1ull << s) - d) << 32) / d + 1);
+  }
+  __device__ __forceinline__ int div(int n) const {
+    return int((__umulhi((unsigned int)n, m) + (unsigned int)n) >> s);
+  }
+  __device__ __forceinline__ int mod(int n, int q) const { return n - q * int(d); }
+};
+
+constexpr int kThreads = 256;     // element-wise and reduction kernels
+constexpr int kFFTThreads = 512;  // transform passes (shared-memory FFTs)
+
+// Element type of a 16-byte vector of T.
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
+template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
+
+// Per-thread accumulator for inner products: plain double for FP64 data;
+// for FP32 data the products are summed in float with Neumaier compensation
+// (error independent of the number of terms), and the block and grid sums
+// are then formed in double.
+template <typename T> struct Acc {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct Acc<float> {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = s + x;
+    c += (fabsf(s) >= fabsf(x)) ? (s - t) + x : (x - t) + s;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return double(s) + double(c); }
+};
 
 // ---- deterministic block reductions in double --------------------------------
 __device__ __forceinline__ double warp_sum(double v) {
@@ -105,5 +147,29 @@ __device__ __forceinline__ void block_max(double (&v)[NV], double* scratch) {
   __syncthreads();
 }
 
+
+// Grid-wide "last block finishes" step: every block calls this once after
+// writing its partials; the block that arrives last (all partials visible)
+// runs fin() with all its threads and resets the counter for the next kernel.
+template <class Fin>
+__device__ __forceinline__ void last_block_finish(const Fin& fin, unsigned int* counter) {
+  __shared__ int is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int total = gridDim.x * gridDim.y * gridDim.z;
+    is_last = (atomicAdd(counter, 1u) == total - 1) ? 1 : 0;
+  }
+  __syncthreads();
+  if (is_last) {
+    __threadfence();
+    fin();
+    if (threadIdx.x == 0) *counter = 0u;
+  }
+}
+
+struct NoFin {
+  __device__ void operator()() const {}
+};
 
 }  // namespace macsav

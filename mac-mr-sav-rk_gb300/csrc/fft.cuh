@@ -14,13 +14,16 @@
 
 namespace macsav {
 
-constexpr int kMaxStages = 24;
+constexpr int kMaxStages = 14;
 
-// Radix plan of one FFT length (host fills, passed by value to kernels).
+// Radix plan of one FFT length (host fills, passed by value to kernels),
+// with the stage divisors pre-inverted (FastDiv) so no butterfly divides.
 struct FFTPlan {
   int L;
   int nstages;       // 0 => direct DFT
   int radix[kMaxStages];
+  FastDiv ns[kMaxStages];   // Ns, the product of the earlier radices
+  FastDiv nbf[kMaxStages];  // L / radix
 };
 
 template <typename T>
@@ -58,8 +61,8 @@ __device__ __forceinline__ void dft_small(cplx<T> (&v)[R], int sign) {
 // One Stockham stage of radix R over all lines, in place.  MAXB bounds the
 // butterflies a thread owns (host guarantees nl*L/R <= MAXB*blockDim.x).
 template <typename T, int R, int MAXB>
-__device__ __forceinline__ void stockham_stage(cplx<T>* buf, int L, int LS, int nl, int Ns,
-                                               const cplx<T>* __restrict__ tw, int sign) {
+__device__ __forceinline__ void stockham_stage(cplx<T>* buf, int L, int LS, int nl, int Ns, const FastDiv& fns,
+                                               const FastDiv& fnbf, const cplx<T>* __restrict__ tw, int sign) {
   const int nbf = L / R;
   const int total = nl * nbf;
   const int step = L / (Ns * R);
@@ -70,15 +73,16 @@ __device__ __forceinline__ void stockham_stage(cplx<T>* buf, int L, int LS, int 
     const int b = threadIdx.x + q * blockDim.x;
     dst[q] = -1;
     if (b < total) {
-      const int line = b / nbf;
+      const int line = fnbf.div(b);
       const int j = b - line * nbf;
       const cplx<T>* in = buf + line * LS;
-      const int k = j % Ns;
+      const int jq = fns.div(j);
+      const int k = j - jq * Ns;
       v[q][0] = in[j];
 #pragma unroll
       for (int r = 1; r < R; ++r) v[q][r] = cmul(in[j + r * nbf], twiddle(tw, r * k * step, sign));
       dft_small<T, R>(v[q], sign);
-      dst[q] = line * LS + (j / Ns) * Ns * R + k;
+      dst[q] = line * LS + jq * Ns * R + k;
     }
   }
   __syncthreads();
@@ -130,9 +134,9 @@ __device__ void fft_lines(cplx<T>* buf, cplx<T>* tmp, const FFTPlan& plan, int L
   int Ns = 1;
   for (int s = 0; s < plan.nstages; ++s) {
     const int R = plan.radix[s];
-    if (R == 4) stockham_stage<T, 4, (VMAX + 3) / 4>(buf, L, LS, nl, Ns, tw, sign);
-    else if (R == 2) stockham_stage<T, 2, (VMAX + 1) / 2>(buf, L, LS, nl, Ns, tw, sign);
-    else stockham_stage<T, 3, (VMAX + 2) / 3>(buf, L, LS, nl, Ns, tw, sign);
+    if (R == 4) stockham_stage<T, 4, (VMAX + 3) / 4>(buf, L, LS, nl, Ns, plan.ns[s], plan.nbf[s], tw, sign);
+    else if (R == 2) stockham_stage<T, 2, (VMAX + 1) / 2>(buf, L, LS, nl, Ns, plan.ns[s], plan.nbf[s], tw, sign);
+    else stockham_stage<T, 3, (VMAX + 2) / 3>(buf, L, LS, nl, Ns, plan.ns[s], plan.nbf[s], tw, sign);
     Ns *= R;
   }
 }

@@ -249,13 +249,14 @@ int op_transform(Plan* P, int kind, int inverse, int rows, int n, const double* 
     if (!inverse) {
       auto k = k_row_forward<double, kVmax, SrcCells<double, double>>;
       set_smem(k, sm);
-      k<<<dim3(total_groups(a), 1), kThreads, sm, s>>>(a, SrcCells<double, double>{in, 0, n});
+      k<<<dim3(total_groups(a), 1), kFFTThreads, sm, s>>>(a, SrcCells<double, double>{in, 0, n});
       k_ortho_out<<<og, kThreads, 0, s>>>(H, B.pitch, out, rows, n, kind);
     } else {
       k_ortho_in<<<og, kThreads, 0, s>>>(in, H, B.pitch, rows, n, kind);
-      auto k = k_row_inverse<double, kVmax, DstCells<double, double>>;
+      auto k = k_row_inverse<double, kVmax, DstCells<double, double>, NoFin>;
       set_smem(k, sm);
-      k<<<dim3(total_groups(a), 1), kThreads, sm, s>>>(a, DstCells<double, double>{out, 0, n}, nullptr);
+      k<<<dim3(total_groups(a), 1), kFFTThreads, sm, s>>>(a, DstCells<double, double>{out, 0, n}, nullptr, NoFin{},
+                                                          nullptr);
     }
     P->launches += 2;
     e = cudaStreamSynchronize(s);

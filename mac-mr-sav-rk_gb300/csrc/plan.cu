@@ -20,6 +20,12 @@ FFTPlan make_fft_plan(int L) {
   while (m % 2 == 0 && ns < kMaxStages) { f.radix[ns++] = 2; m /= 2; }
   while (m % 3 == 0 && ns < kMaxStages) { f.radix[ns++] = 3; m /= 3; }
   f.nstages = (m == 1) ? ns : 0;  // 0: direct DFT
+  int prod = 1;
+  for (int s = 0; s < f.nstages; ++s) {
+    f.ns[s] = FastDiv(prod);
+    f.nbf[s] = FastDiv(L / f.radix[s]);
+    prod *= f.radix[s];
+  }
   return f;
 }
 
@@ -45,13 +51,15 @@ static int pick_pairs(int L, int rows, int sms) {
   return P;
 }
 
-// Columns per CTA of the column pass: at most 4096 complex values in shared
-// memory, and at least 32 bytes of each row per CTA (one full DRAM sector)
-// when that fits, then narrower only while there are too few CTAs.
+// Columns per CTA of the column pass (a power of two): at most 4096 complex
+// values in shared memory, and at least 32 bytes of each row per CTA (one
+// full DRAM sector) when that fits, then narrower only while there are too
+// few CTAs.
 static int pick_strip(int L, int cols, int sms, int elem_bytes) {
-  int W = std::min(32, 2 * std::max(1, 4096 / L));
+  int W = 2;
+  while (W < 32 && (W * 2 / 2) * L <= 4096 && W * 2 * L / 2 <= 4096) W *= 2;
   const int wmin = std::min(W, std::max(2, 32 / elem_bytes));
-  while (W > wmin && (cols + W - 1) / W < 2 * sms) W -= 2;
+  while (W > wmin && (cols + W - 1) / W < 2 * sms) W /= 2;
   return W;
 }
 
@@ -70,6 +78,11 @@ static cudaError_t build_block(TBlockDev<T>& B, int rows, int cols, int kx, int 
   B.pitch = (cols + 31) / 32 * 32;
   B.px = pick_pairs(Lx, rows, sms);
   B.wy = pick_strip(Ly, cols, sms, int(sizeof(T)));
+  B.fcols = FastDiv(cols);
+  B.frows = FastDiv(rows);
+  B.fw = FastDiv(B.wy);
+  B.fvpr = FastDiv(std::max(1, B.wy / int(16 / sizeof(T))));
+  B.fhalf = FastDiv(rows / 2 + 1);
   // host tables
   std::vector<cplx<T>> twx(Lx), twy(Ly), qx(cols), qy(rows);
   for (int m = 0; m < Lx; ++m) twx[m] = mk(T(std::cos(2 * kPi * m / Lx)), T(-std::sin(2 * kPi * m / Lx)));
@@ -131,6 +144,7 @@ static cudaError_t build_transforms(Transforms<T>& t, const Plan& pl) {
   void* d = nullptr;
   if ((e = cudaMalloc(&d, sizeof(T) * per_col * pl.maxcols))) return e;
   t.allocations.push_back(d);
+  if ((e = cudaMemset(d, 0, sizeof(T) * per_col * pl.maxcols))) return e;  // padding stays zero
   t.H = static_cast<T*>(d);
   t.u.H = t.H;
   t.v.H = t.H + hu;
@@ -183,6 +197,8 @@ int plan_build(Plan* p) {
     if ((e = cudaMalloc(&p->active, sizeof(int) * C))) goto fail;
     if ((e = cudaMalloc(&p->shift, sizeof(double) * 2 * C))) goto fail;
     if ((e = cudaMalloc(&p->errword, sizeof(int)))) goto fail;
+    if ((e = cudaMalloc(&p->done_counter, sizeof(unsigned int) * 16))) goto fail;
+    if ((e = cudaMemset(p->done_counter, 0, sizeof(unsigned int) * 16))) goto fail;
     if ((e = cudaMallocHost(&p->h_cg, sizeof(CGScalars) * C))) goto fail;
     if ((e = cudaMallocHost(&p->h_checks, sizeof(SolveChecks) * C))) goto fail;
     if ((e = cudaMallocHost(&p->h_active, sizeof(int) * C))) goto fail;
@@ -213,6 +229,8 @@ void plan_free(Plan* p) {
   cudaFree(p->w); cudaFree(p->vel); cudaFree(p->cells); cudaFree(p->cells32); cudaFree(p->w32);
   cudaFree(p->partial); cudaFree(p->cg); cudaFree(p->checks); cudaFree(p->active); cudaFree(p->shift);
   cudaFree(p->errword);
+  cudaFree(p->done_counter);
+  p->done_counter = nullptr;
   cudaFreeHost(p->h_cg); cudaFreeHost(p->h_checks); cudaFreeHost(p->h_active); cudaFreeHost(p->h_err);
   if (p->done) cudaEventDestroy(p->done);
   p->w = p->vel = p->cells = p->partial = p->shift = nullptr;

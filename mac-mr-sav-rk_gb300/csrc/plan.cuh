@@ -73,6 +73,9 @@ struct Plan {
   int precision;  // MACSAV_FP64 or MACSAV_FP32_MIXED
   double tol, ktol;
   int maxit, maxcols;
+  // FP32_MIXED: inner FP32 Krylov tolerance and defect-correction sweeps
+  double inner_ktol = 1e-5;
+  int corrections = 2;
   int num_sms;
   std::string err;
   Transforms<double> t64;
@@ -92,6 +95,7 @@ struct Plan {
   int* active = nullptr;
   double* shift = nullptr;
   int* errword = nullptr;
+  unsigned int* done_counter = nullptr;  // last-block counter of reductions
   // pinned host mirrors
   CGScalars* h_cg = nullptr;
   SolveChecks* h_checks = nullptr;
@@ -115,6 +119,7 @@ struct Exec {
   bool graph;
   cudaStream_t side;  // body capture stream (graph mode)
   cudaGraphConditionalHandle cond;
+  double ktol;        // Krylov tolerance of the solve being enqueued (0: the plan's)
 };
 
 int plan_build(Plan* p);

@@ -1,4 +1,4 @@
-// Device functors, CG kernels and the templated Stokes solve core.
+// Device functors, the Krylov scalar logic and the transform launchers.
 #pragma once
 #include "plan.cuh"
 
@@ -37,39 +37,33 @@ struct SrcLift {
   long long pstride;
   int nx, nu;
   T ihx, ihy;
-  __device__ T P(const PIn* a, const PIn* b, T beta, long long i) const {
-    return b ? T(a[i]) + beta * T(b[i]) : T(a[i]);
-  }
   __device__ T operator()(int bk, int c, int row, int n) const {
     const PIn* a = p1 + c * pstride;
-    const PIn* b = nullptr;
-    T beta = T(0);
-    if (p2 && cg[c].iters > 0) {
-      b = p2 + c * pstride;
-      beta = T(cg[c].beta);
-    }
     const long long l = (long long)row * nx + n;
-    T v;
-    long long fi;
-    if (bk == 0) {
-      v = (P(a, b, beta, l) - P(a, b, beta, l + 1)) * ihx;
-      fi = (long long)row * (nx - 1) + n;
-    } else {
-      v = (P(a, b, beta, l) - P(a, b, beta, l + nx)) * ihy;
-      fi = nu + l;
+    const long long l2 = bk == 0 ? l + 1 : l + nx;
+    T v0 = T(a[l]), v1 = T(a[l2]);
+    if (p2 && cg[c].iters > 0) {
+      const PIn* b = p2 + c * pstride;
+      const T beta = T(cg[c].beta);
+      v0 = v0 + beta * T(b[l]);
+      v1 = v1 + beta * T(b[l2]);
     }
-    if (f) v += T(f[c * fstride + fi]);
+    T v = (v0 - v1) * (bk == 0 ? ihx : ihy);
+    if (f) v += T(f[c * fstride + (bk == 0 ? (long long)row * (nx - 1) + n : nu + l)]);
     return v;
   }
 };
 
 // --------------------------------------------------------------- row sinks ---
+// Two-phase sinks: aux = load(...) is issued for a batch, then store(...).
 template <typename T, typename Out>
 struct DstPacked {
+  using aux_t = int;
   Out* x;
   long long cstride;
   int off1, n0, n1;
-  __device__ void operator()(int b, int c, int row, int n, T v, double (&)[2]) const {
+  __device__ aux_t load(int, int, int, int) const { return 0; }
+  __device__ void store(int b, int c, int row, int n, T v, aux_t, Acc<T> (&)[2]) const {
     Out* base = x + c * cstride;
     if (b == 0) base[(long long)row * n0 + n] = Out(v);
     else base[off1 + (long long)row * n1 + n] = Out(v);
@@ -78,10 +72,12 @@ struct DstPacked {
 
 template <typename T, typename Out>
 struct DstCells {
+  using aux_t = int;
   Out* x;
   long long cstride;
   int nx;
-  __device__ void operator()(int, int c, int row, int n, T v, double (&)[2]) const {
+  __device__ aux_t load(int, int, int, int) const { return 0; }
+  __device__ void store(int, int c, int row, int n, T v, aux_t, Acc<T> (&)[2]) const {
     x[c * cstride + (long long)row * nx + n] = Out(v);
   }
 };
@@ -89,38 +85,126 @@ struct DstCells {
 // z = value; acc[0] += r . z
 template <typename T>
 struct DstCellsDot {
+  using aux_t = T;
   T* z;
   const T* r;
   long long cstride;
   int nx;
-  __device__ void operator()(int, int c, int row, int n, T v, double (&acc)[2]) const {
-    const long long i = c * cstride + (long long)row * nx + n;
-    z[i] = v;
-    acc[0] += double(r[i]) * double(v);
+  __device__ aux_t load(int, int c, int row, int n) const { return r[c * cstride + (long long)row * nx + n]; }
+  __device__ void store(int, int c, int row, int n, T v, aux_t rv, Acc<T> (&acc)[2]) const {
+    z[c * cstride + (long long)row * nx + n] = v;
+    acc[0].add(rv * v);
   }
 };
 
-// ------------------------------------------------------------- launching ---
-template <typename T>
-struct Launcher {
-  const Transforms<T>& t;
-  cudaStream_t s;
-  long long* counter;
+// ------------------------------------------------------- Krylov scalars ---
+enum ScalarOp : int { OP_MEAN_B, OP_START, OP_RHO, OP_ALPHA, OP_CHECK, OP_MEAN_X, OP_CHECKS };
 
-  template <class Src>
-  void row_forward_uv(Src src, int cols, const int* active) const;
-  template <class Dst>
-  void row_inverse_uv(Dst dst, int cols, const int* active, double* partial) const;
-  void column_uv(int cols, const int* active, const double* shift) const;
-  template <class Src>
-  void row_forward_p(Src src, int cols, const int* active) const;
-  template <class Dst>
-  void row_inverse_p(Dst dst, int cols, const int* active, double* partial) const;
-  void column_p(int cols, const int* active, const double* shift, T thr) const;
-  int groups_row_p() const { return (t.p.rows + 2 * t.p.px - 1) / (2 * t.p.px); }
+// Block-wide fold of the K-slot partials of `nb` blocks per column (fixed
+// order; sums, and maxima for OP_START slot 1 and every OP_CHECKS slot), then
+// thread 0 updates each column's scalars.  Under graph capture OP_START and
+// OP_CHECK also set the CG while-loop condition to "some column active".
+struct CGFin {
+  int op;
+  const double* partial;
+  int nb, K, cols;
+  CGScalars* cg;
+  int* active;
+  int np;
+  double ktol;
+  int maxit;
+  SolveChecks* checks;
+  int use_cond;
+  cudaGraphConditionalHandle cond;
+
+  __device__ void operator()() const {
+    __shared__ double red[6 * 32];
+    const bool gated = op == OP_RHO || op == OP_ALPHA || op == OP_CHECK;
+    for (int c = 0; c < cols; ++c) {
+      if (gated && !active[c]) continue;  // uniform across the block
+      double s[6] = {0, 0, 0, 0, 0, 0}, m[6] = {0, 0, 0, 0, 0, 0};
+      for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        const double* o = partial + (size_t(c) * nb + b) * K;
+        for (int k = 0; k < K && k < 6; ++k) {
+          const double v = __ldcg(o + k);
+          s[k] += v;
+          m[k] = nanmax(m[k], v);
+        }
+      }
+      block_sum<6>(s, red);
+      block_max<6>(m, red);
+      if (threadIdx.x == 0) update(c, s, m);
+      __syncthreads();
+    }
+    if (use_cond && threadIdx.x == 0 && (op == OP_START || op == OP_CHECK)) {
+      int a = 0;
+      for (int c = 0; c < cols; ++c) a |= active[c];
+      cudaGraphSetConditional(cond, a ? 1u : 0u);
+    }
+  }
+
+  __device__ void update(int c, const double (&s)[6], const double (&m)[6]) const {
+    CGScalars& g = cg[c];
+    switch (op) {
+      case OP_MEAN_B:
+        g.mean_b = s[0] / np;
+        break;
+      case OP_START: {
+        g.bnorm = sqrt(s[0]);
+        g.max_b = m[1];
+        g.atol = ktol * g.bnorm;  // _get_atol_rtol: max(atol=0, rtol*||b||)
+        g.iters = 0;
+        g.info = 0;
+        g.rho_prev = 0;
+        g.beta = 0;
+        g.rr = s[0];
+        // zero RHS (tensor_stokes.py:309-311) or already converged: no update
+        const bool go = (g.max_b != 0.0) && !(sqrt(g.rr) < g.atol) && (g.bnorm == g.bnorm);
+        active[c] = go ? 1 : 0;
+        break;
+      }
+      case OP_RHO:
+        g.rho = s[0];
+        g.beta = g.iters > 0 ? g.rho / g.rho_prev : 0.0;
+        break;
+      case OP_ALPHA:
+        g.mean_q = s[1] / np;
+        g.pq = s[0] - s[1] * s[2] / np;  // p . (q - mean(q))
+        g.alpha = g.rho / g.pq;
+        break;
+      case OP_CHECK:
+        g.rr = s[0];
+        g.iters += 1;
+        g.rho_prev = g.rho;
+        if (sqrt(g.rr) < g.atol) {
+          active[c] = 0;
+        } else if (g.iters >= maxit || !(g.rr == g.rr)) {
+          active[c] = 0;
+          g.info = maxit;
+        }
+        break;
+      case OP_MEAN_X:
+        g.mean_q = s[0] / np;
+        break;
+      case OP_CHECKS:
+        checks[c].max_defect = m[0];
+        checks[c].max_force = m[1];
+        checks[c].max_velocity = m[2];
+        checks[c].max_div = m[3];
+        checks[c].nonfinite_force = m[4] != 0.0;
+        checks[c].nonfinite_solution = m[5] != 0.0;
+        break;
+    }
+  }
 };
 
-constexpr int kVmax = 16;
+inline CGFin make_fin(const Plan* P, const Exec& X, int op, int nb, int K, int cols) {
+  return CGFin{op, P->partial, nb, K, cols, P->cg, P->active, P->g.np, X.ktol > 0 ? X.ktol : P->ktol, P->maxit,
+               P->checks, X.graph ? 1 : 0, X.cond};
+}
+
+// ------------------------------------------------------------- launching ---
+constexpr int kVmax = 8;
 
 template <typename T>
 inline RowArgs<T> row_args(const TBlockDev<T>& a, const TBlockDev<T>* b, const int* active) {
@@ -167,56 +251,61 @@ inline void set_smem(K kernel, size_t bytes) {
 }
 
 template <typename T>
-template <class Src>
-void Launcher<T>::row_forward_uv(Src src, int cols, const int* active) const {
-  RowArgs<T> a = row_args(t.u, &t.v, active);
-  auto k = k_row_forward<T, kVmax, Src>;
-  set_smem(k, t.smem_row_uv);
-  k<<<dim3(total_groups(a), cols), kThreads, t.smem_row_uv, s>>>(a, src);
-  ++*counter;
-}
-template <typename T>
-template <class Dst>
-void Launcher<T>::row_inverse_uv(Dst dst, int cols, const int* active, double* partial) const {
-  RowArgs<T> a = row_args(t.u, &t.v, active);
-  auto k = k_row_inverse<T, kVmax, Dst>;
-  set_smem(k, t.smem_row_uv);
-  k<<<dim3(total_groups(a), cols), kThreads, t.smem_row_uv, s>>>(a, dst, partial);
-  ++*counter;
-}
-template <typename T>
-void Launcher<T>::column_uv(int cols, const int* active, const double* shift) const {
-  ColArgs<T> a = col_args(t.u, &t.v, active, W_HELMHOLTZ, shift, T(0));
-  auto k = k_column<T, kVmax>;
-  set_smem(k, t.smem_col_uv);
-  k<<<dim3(total_groups(a), cols), kThreads, t.smem_col_uv, s>>>(a);
-  ++*counter;
-}
-template <typename T>
-template <class Src>
-void Launcher<T>::row_forward_p(Src src, int cols, const int* active) const {
-  RowArgs<T> a = row_args(t.p, (const TBlockDev<T>*)nullptr, active);
-  auto k = k_row_forward<T, kVmax, Src>;
-  set_smem(k, t.smem_row_p);
-  k<<<dim3(total_groups(a), cols), kThreads, t.smem_row_p, s>>>(a, src);
-  ++*counter;
-}
-template <typename T>
-template <class Dst>
-void Launcher<T>::row_inverse_p(Dst dst, int cols, const int* active, double* partial) const {
-  RowArgs<T> a = row_args(t.p, (const TBlockDev<T>*)nullptr, active);
-  auto k = k_row_inverse<T, kVmax, Dst>;
-  set_smem(k, t.smem_row_p);
-  k<<<dim3(total_groups(a), cols), kThreads, t.smem_row_p, s>>>(a, dst, partial);
-  ++*counter;
-}
-template <typename T>
-void Launcher<T>::column_p(int cols, const int* active, const double* shift, T thr) const {
-  ColArgs<T> a = col_args(t.p, (const TBlockDev<T>*)nullptr, active, W_POISSON, shift, thr);
-  auto k = k_column<T, kVmax>;
-  set_smem(k, t.smem_col_p);
-  k<<<dim3(total_groups(a), cols), kThreads, t.smem_col_p, s>>>(a);
-  ++*counter;
-}
+struct Launcher {
+  const Transforms<T>& t;
+  cudaStream_t s;
+  long long* counter;
+
+  template <class Src>
+  void row_forward(const TBlockDev<T>& a, const TBlockDev<T>* b, size_t smem, Src src, int cols,
+                   const int* active) const {
+    RowArgs<T> r = row_args(a, b, active);
+    auto k = k_row_forward<T, kVmax, Src>;
+    set_smem(k, smem);
+    k<<<dim3(total_groups(r), cols), kFFTThreads, smem, s>>>(r, src);
+    ++*counter;
+  }
+  template <class Dst, class Fin>
+  void row_inverse(const TBlockDev<T>& a, const TBlockDev<T>* b, size_t smem, Dst dst, int cols, const int* active,
+                   double* partial, Fin fin, unsigned int* done) const {
+    RowArgs<T> r = row_args(a, b, active);
+    auto k = k_row_inverse<T, kVmax, Dst, Fin>;
+    set_smem(k, smem);
+    k<<<dim3(total_groups(r), cols), kFFTThreads, smem, s>>>(r, dst, partial, fin, done);
+    ++*counter;
+  }
+  void column(const TBlockDev<T>& a, const TBlockDev<T>* b, size_t smem, int cols, const int* active, int mode,
+              const double* shift, T thr) const {
+    ColArgs<T> r = col_args(a, b, active, mode, shift, thr);
+    auto k = k_column<T, kVmax>;
+    set_smem(k, smem);
+    k<<<dim3(total_groups(r), cols), kFFTThreads, smem, s>>>(r);
+    ++*counter;
+  }
+
+  template <class Src>
+  void row_forward_uv(Src src, int cols, const int* active) const {
+    row_forward(t.u, &t.v, t.smem_row_uv, src, cols, active);
+  }
+  template <class Dst>
+  void row_inverse_uv(Dst dst, int cols, const int* active) const {
+    row_inverse(t.u, &t.v, t.smem_row_uv, dst, cols, active, nullptr, NoFin{}, nullptr);
+  }
+  void column_uv(int cols, const int* active, const double* shift) const {
+    column(t.u, &t.v, t.smem_col_uv, cols, active, W_HELMHOLTZ, shift, T(0));
+  }
+  template <class Src>
+  void row_forward_p(Src src, int cols, const int* active) const {
+    row_forward(t.p, nullptr, t.smem_row_p, src, cols, active);
+  }
+  template <class Dst, class Fin>
+  void row_inverse_p(Dst dst, int cols, const int* active, double* partial, Fin fin, unsigned int* done) const {
+    row_inverse(t.p, nullptr, t.smem_row_p, dst, cols, active, partial, fin, done);
+  }
+  void column_p(int cols, const int* active, const double* shift, T thr) const {
+    column(t.p, nullptr, t.smem_col_p, cols, active, W_POISSON, shift, thr);
+  }
+  int groups_row_p() const { return (t.p.rows + 2 * t.p.px - 1) / (2 * t.p.px); }
+};
 
 }  // namespace macsav

@@ -53,6 +53,17 @@ __device__ __forceinline__ double D_at(const In* x, const GridDev& g, int j, int
   return v;
 }
 
+// (D x) at cell (j, i) computed in T (the FP32 path stays off the FP64 units).
+template <typename T, typename In>
+__device__ __forceinline__ T D_atT(const In* x, const GridDev& g, int j, int i, T ihx, T ihy) {
+  T v = T(0);
+  if (i < g.nx - 1) v += T(x[j * (g.nx - 1) + i]) * ihx;
+  if (i > 0) v -= T(x[j * (g.nx - 1) + i - 1]) * ihx;
+  if (j < g.ny - 1) v += T(x[g.nu + j * g.nx + i]) * ihy;
+  if (j > 0) v -= T(x[g.nu + (j - 1) * g.nx + i]) * ihy;
+  return v;
+}
+
 // (D^T p) at packed face e (kernels.py:89-132).
 template <typename In>
 __device__ __forceinline__ double Dt_at(const In* p, const GridDev& g, int e) {

@@ -571,7 +571,7 @@ int run_step(Plan* P, int scheme, double t, double dt, double nu, double gamma, 
   if (forces) cudaMemcpyAsync(B.FORCE, forces, sizeof(double) * sz * n, cudaMemcpyDeviceToDevice, s);
   const bool want_emb = embedded != nullptr;
   if (!P->use_graph) {
-    Exec X{s, false, nullptr, 0};
+    Exec X{s, false, nullptr, 0, 0.0};
     rc = enqueue_step(P, X, scheme, G, want_emb);
     if (rc != MACSAV_OK) return rc;
   } else {
@@ -580,7 +580,7 @@ int run_step(Plan* P, int scheme, double t, double dt, double nu, double gamma, 
     for (auto& kv : B.graphs)
       if (kv.key == key) exec = kv.exec;
     if (!exec) {
-      Exec X{s, true, B.side, 0};
+      Exec X{s, true, B.side, 0, 0.0};
       if (cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed) != cudaSuccess) return MACSAV_ERR_CUDA;
       rc = enqueue_step(P, X, scheme, G, want_emb);
       cudaGraph_t graph = nullptr;

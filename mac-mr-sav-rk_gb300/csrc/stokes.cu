@@ -7,11 +7,14 @@
 //
 // Device data per right-hand-side column c: b (pressure RHS), x (pressure),
 // r (residual), z (preconditioned residual), p (search direction), q (S p).
-// Every Krylov scalar lives on the device (CGScalars); each kernel of the
-// loop is predicated on the column's `active` flag, so the host only needs the
-// flags to know when to stop launching.
+// Every Krylov scalar lives on the device (CGScalars).  Each reduction kernel
+// writes per-block partials and its last block folds them in a fixed order
+// and updates the scalars (no separate scalar launches).  Each kernel of the
+// loop is predicated on the column's `active` flag, so the host (or a CUDA
+// graph conditional node) only needs the flags to know when to stop.
 #include <cmath>
 #include <cstdio>
+#include <type_traits>
 
 #include "solver.cuh"
 
@@ -25,66 +28,82 @@ inline int red_blocks(long long n) {
 }
 
 // ------------------------------------------------------------ CG kernels ---
+// b = rd - D w (rd: continuity defect of a correction solve, may be null);
+// last block: mean of b (OP_MEAN_B).
 template <typename T, typename WIn>
 __global__ void __launch_bounds__(kThreads) k_pressure_rhs(GridDev g, const WIn* w, long long ws, T* b, long long cs,
-                                                           double* partial) {
+                                                           const double* rd, double* partial, CGFin fin,
+                                                           unsigned int* done) {
   __shared__ double red[64];
   const int c = blockIdx.y;
-  double acc[1] = {0.0};
+  const T ihx = T(g.ihx), ihy = T(g.ihy);
+  Acc<T> acc;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < g.np; idx += gridDim.x * blockDim.x) {
     const int j = idx / g.nx, i = idx - j * g.nx;
-    const T v = T(-D_at(w + c * ws, g, j, i));
+    T v = -D_atT<T>(w + c * ws, g, j, i, ihx, ihy);
+    if (rd) v += T(rd[c * (long long)g.np + idx]);
     b[c * cs + idx] = v;
-    acc[0] += double(v);
+    acc.add(v);
   }
-  block_sum<1>(acc, red);
-  if (threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = acc[0];
+  double s[1] = {acc.value()};
+  block_sum<1>(s, red);
+  if (threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = s[0];
+  last_block_finish(fin, done);
 }
 
+// b -= mean; x = 0; r = b; last block: ||b||, max|b| and the start (OP_START).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_cg_start(int np, T* b, T* x, T* r, long long cs, const CGScalars* cg,
-                                                       double* partial) {
+                                                       double* partial, CGFin fin, unsigned int* done) {
   __shared__ double red[64];
   const int c = blockIdx.y;
-  const double mean = cg[c].mean_b;
-  double s[1] = {0.0}, m[1] = {0.0};
+  const T mean = T(cg[c].mean_b);
+  Acc<T> s;
+  T mt = T(0);
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
     const long long i = c * cs + idx;
-    const T v = T(double(b[i]) - mean);
+    const T v = b[i] - mean;
     b[i] = v;
     r[i] = v;
     x[i] = T(0);
-    s[0] += double(v) * double(v);
-    m[0] = nanmax(m[0], fabs(double(v)));
+    s.add(v * v);
+    const T av = v < T(0) ? -v : v;
+    mt = (av != av || mt != mt) ? av + mt : (av > mt ? av : mt);
   }
-  block_sum<1>(s, red);
+  double ss[1] = {s.value()}, m[1] = {double(mt)};
+  block_sum<1>(ss, red);
   block_max<1>(m, red);
   if (threadIdx.x == 0) {
-    partial[(c * gridDim.x + blockIdx.x) * 2] = s[0];
+    partial[(c * gridDim.x + blockIdx.x) * 2] = ss[0];
     partial[(c * gridDim.x + blockIdx.x) * 2 + 1] = m[0];
   }
+  last_block_finish(fin, done);
 }
 
+// q = D w; last block: alpha from p.q, sum q, sum p (OP_ALPHA), p = z + beta p.
 template <typename T, typename WIn>
 __global__ void __launch_bounds__(kThreads) k_div_q(GridDev g, const WIn* w, long long ws, T* q, const T* z, const T* p,
                                                     long long cs, const CGScalars* cg, const int* active,
-                                                    double* partial) {
-  const int c = blockIdx.y;
-  if (!active[c]) return;
+                                                    double* partial, CGFin fin, unsigned int* done) {
   __shared__ double red[96];
-  const bool first = cg[c].iters == 0;
-  const T beta = T(cg[c].beta);
-  double acc[3] = {0.0, 0.0, 0.0};
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < g.np; idx += gridDim.x * blockDim.x) {
-    const int j = idx / g.nx, i = idx - j * g.nx;
-    const long long k = c * cs + idx;
-    const T qv = T(D_at(w + c * ws, g, j, i));
-    q[k] = qv;
-    const T pd = first ? z[k] : T(z[k] + beta * p[k]);
-    acc[0] += double(pd) * double(qv);
-    acc[1] += double(qv);
-    acc[2] += double(pd);
+  const int c = blockIdx.y;
+  Acc<T> a0, a1, a2;
+  if (active[c]) {
+    const bool first = cg[c].iters == 0;
+    const T beta = T(cg[c].beta);
+    const T ihx = T(g.ihx), ihy = T(g.ihy);
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < g.np; idx += gridDim.x * blockDim.x) {
+      const int j = idx / g.nx, i = idx - j * g.nx;
+      const long long k = c * cs + idx;
+      const T qv = D_atT<T>(w + c * ws, g, j, i, ihx, ihy);
+      q[k] = qv;
+      const T pd = first ? z[k] : T(z[k] + beta * p[k]);
+      a0.add(pd * qv);
+      a1.add(qv);
+      a2.add(pd);
+    }
   }
+  double acc[3] = {a0.value(), a1.value(), a2.value()};
   block_sum<3>(acc, red);
   if (threadIdx.x == 0) {
     double* o = partial + (c * gridDim.x + blockIdx.x) * 3;
@@ -92,64 +111,70 @@ __global__ void __launch_bounds__(kThreads) k_div_q(GridDev g, const WIn* w, lon
     o[1] = acc[1];
     o[2] = acc[2];
   }
+  last_block_finish(fin, done);
 }
 
+// p = z + beta p; x += alpha p; r -= alpha (q - mean q); last block: ||r||
+// and the convergence test (OP_CHECK).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_cg_update(int np, T* x, T* r, T* p, const T* z, const T* q,
                                                         long long cs, const CGScalars* cg, const int* active,
-                                                        double* partial) {
-  const int c = blockIdx.y;
-  if (!active[c]) return;
+                                                        double* partial, CGFin fin, unsigned int* done) {
   __shared__ double red[64];
-  const bool first = cg[c].iters == 0;
-  const T beta = T(cg[c].beta), alpha = T(cg[c].alpha), mq = T(cg[c].mean_q);
-  double acc[1] = {0.0};
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
-    const long long k = c * cs + idx;
-    const T pd = first ? z[k] : T(z[k] + beta * p[k]);
-    p[k] = pd;
-    x[k] = x[k] + alpha * pd;
-    const T rv = r[k] - alpha * (q[k] - mq);
-    r[k] = rv;
-    acc[0] += double(rv) * double(rv);
+  const int c = blockIdx.y;
+  Acc<T> acc;
+  if (active[c]) {
+    const bool first = cg[c].iters == 0;
+    const T beta = T(cg[c].beta), alpha = T(cg[c].alpha), mq = T(cg[c].mean_q);
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
+      const long long k = c * cs + idx;
+      const T pd = first ? z[k] : T(z[k] + beta * p[k]);
+      p[k] = pd;
+      x[k] = x[k] + alpha * pd;
+      const T rv = r[k] - alpha * (q[k] - mq);
+      r[k] = rv;
+      acc.add(rv * rv);
+    }
   }
-  block_sum<1>(acc, red);
-  if (threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = acc[0];
+  double s[1] = {acc.value()};
+  block_sum<1>(s, red);
+  if (threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = s[0];
+  last_block_finish(fin, done);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_sum_cells(int np, const T* x, long long cs, double* partial) {
-  __shared__ double red[64];
-  const int c = blockIdx.y;
-  double acc[1] = {0.0};
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x)
-    acc[0] += double(x[c * cs + idx]);
-  block_sum<1>(acc, red);
-  if (threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = acc[0];
-}
-
-// out = x - mean (mean kept in cg[c].mean_q after the loop); partial sum of out.
+// out = x - mean (the mean held in cg[c].mean_q when `center`); partial sum
+// of out; last block: the new mean (OP_MEAN_X).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_center_cells(int np, const T* x, long long xs, double* out,
-                                                           long long os, const CGScalars* cg, double* partial) {
+                                                           long long os, const CGScalars* cg, int center,
+                                                           double* partial, CGFin fin, unsigned int* done) {
   __shared__ double red[64];
   const int c = blockIdx.y;
-  const double mean = cg[c].mean_q;
+  const double mean = center ? cg[c].mean_q : 0.0;
   double acc[1] = {0.0};
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
     const double v = double(x[c * xs + idx]) - mean;
-    out[c * os + idx] = v;
+    if (out) out[c * os + idx] = v;
     acc[0] += v;
   }
   block_sum<1>(acc, red);
-  if (partial && threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = acc[0];
+  if (threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = acc[0];
+  last_block_finish(fin, done);
+}
+
+__global__ void __launch_bounds__(kThreads) k_shift_cells(int np, double* out, long long os, const CGScalars* cg) {
+  const int c = blockIdx.y;
+  const double mean = cg[c].mean_q;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x)
+    out[c * os + idx] -= mean;
 }
 
 // Closing checks (tensor_stokes.py:329-351): defect = m u + k K u - D^T p - f.
 // Partial slots: max|defect|, max|f|, max|u|, max|D u|, nonfinite f, nonfinite u/p.
 __global__ void __launch_bounds__(kThreads) k_stokes_check(GridDev g, const double* vel, const double* pres,
                                                            const double* f, long long vs, long long ps,
-                                                           const double* shift, double* partial) {
+                                                           const double* shift, double* partial, CGFin fin,
+                                                           unsigned int* done) {
   __shared__ double red[6 * 32];
   const int c = blockIdx.y;
   const double mass = shift[2 * c], visc = shift[2 * c + 1];
@@ -177,102 +202,7 @@ __global__ void __launch_bounds__(kThreads) k_stokes_check(GridDev g, const doub
   block_max<6>(m, red);
   if (threadIdx.x == 0)
     for (int k = 0; k < 6; ++k) partial[(c * gridDim.x + blockIdx.x) * 6 + k] = m[k];
-}
-
-// ----------------------------------------------------------- scalar logic ---
-enum ScalarOp : int { OP_MEAN_B, OP_START, OP_RHO, OP_ALPHA, OP_CHECK, OP_MEAN_X, OP_CHECKS };
-
-// One block for all columns: reduce the K-slot partials of `nb` blocks per
-// column in a fixed order (sums, and maxima for OP_START slot 1 and every
-// OP_CHECKS slot), then thread 0 updates the column's scalars.  Under graph
-// capture (cond != 0) OP_START and OP_CHECK also set the CG while-loop
-// condition to "some column still active".
-__global__ void __launch_bounds__(kThreads) k_scalar(int op, const double* partial, int nb, int K, int cols,
-                                                     CGScalars* cgs, int* active, int np, double ktol, int maxit,
-                                                     SolveChecks* checks, int use_cond,
-                                                     cudaGraphConditionalHandle cond) {
-  __shared__ double red[6 * 32];
-  const bool gated = op == OP_RHO || op == OP_ALPHA || op == OP_CHECK;
-  int any = 0;
-  for (int c = 0; c < cols; ++c) {
-    CGScalars& cg = cgs[c];
-    if (gated && !active[c]) continue;  // uniform across the block
-    double s[6] = {0, 0, 0, 0, 0, 0}, m[6] = {0, 0, 0, 0, 0, 0};
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-      const double* o = partial + (size_t(c) * nb + b) * K;
-      for (int k = 0; k < K && k < 6; ++k) {
-        s[k] += o[k];
-        m[k] = nanmax(m[k], o[k]);
-      }
-    }
-    block_sum<6>(s, red);
-    block_max<6>(m, red);
-    if (threadIdx.x == 0) {
-      switch (op) {
-        case OP_MEAN_B:
-          cg.mean_b = s[0] / np;
-          break;
-        case OP_START: {
-          cg.bnorm = sqrt(s[0]);
-          cg.max_b = m[1];
-          cg.atol = ktol * cg.bnorm;  // _get_atol_rtol: max(atol=0, rtol*||b||)
-          cg.iters = 0;
-          cg.info = 0;
-          cg.rho_prev = 0;
-          cg.beta = 0;
-          cg.rr = s[0];
-          // zero RHS (tensor_stokes.py:309-311) or already converged: no update
-          const bool go = (cg.max_b != 0.0) && !(sqrt(cg.rr) < cg.atol) && (cg.bnorm == cg.bnorm);
-          active[c] = go ? 1 : 0;
-          break;
-        }
-        case OP_RHO:
-          cg.rho = s[0];
-          cg.beta = cg.iters > 0 ? cg.rho / cg.rho_prev : 0.0;
-          break;
-        case OP_ALPHA:
-          cg.mean_q = s[1] / np;
-          cg.pq = s[0] - s[1] * s[2] / np;  // p . (q - mean(q))
-          cg.alpha = cg.rho / cg.pq;
-          break;
-        case OP_CHECK:
-          cg.rr = s[0];
-          cg.iters += 1;
-          cg.rho_prev = cg.rho;
-          if (sqrt(cg.rr) < cg.atol) {
-            active[c] = 0;
-          } else if (cg.iters >= maxit || !(cg.rr == cg.rr)) {
-            active[c] = 0;
-            cg.info = maxit;
-          }
-          break;
-        case OP_MEAN_X:
-          cg.mean_q = s[0] / np;
-          break;
-        case OP_CHECKS:
-          checks[c].max_defect = m[0];
-          checks[c].max_force = m[1];
-          checks[c].max_velocity = m[2];
-          checks[c].max_div = m[3];
-          checks[c].nonfinite_force = m[4] != 0.0;
-          checks[c].nonfinite_solution = m[5] != 0.0;
-          break;
-      }
-      any |= active[c];
-    }
-    __syncthreads();
-  }
-  if (use_cond && threadIdx.x == 0 && (op == OP_START || op == OP_CHECK)) {
-    int a = 0;
-    for (int c = 0; c < cols; ++c) a |= active[c];
-    cudaGraphSetConditional(cond, a ? 1u : 0u);
-  }
-}
-
-static inline void scalar(Plan* P, const Exec& X, int op, int nb, int K, int cols, cudaStream_t s) {
-  k_scalar<<<1, kThreads, 0, s>>>(op, P->partial, nb, K, cols, P->cg, P->active, P->g.np, P->ktol, P->maxit,
-                                  P->checks, X.graph ? 1 : 0, X.cond);
-  ++P->launches;
+  last_block_finish(fin, done);
 }
 
 // ----------------------------------------------------------------- solve ---
@@ -283,8 +213,7 @@ static void velocity_inverse(Plan* P, const Launcher<T>& L, Src src, Out* dst, l
   const GridDev& g = P->g;
   L.row_forward_uv(src, cols, active);
   L.column_uv(cols, active, P->shift);
-  DstPacked<T, Out> d{dst, dstride, g.nu, g.nx - 1, g.nx};
-  L.row_inverse_uv(d, cols, active, nullptr);
+  L.row_inverse_uv(DstPacked<T, Out>{dst, dstride, g.nu, g.nx - 1, g.nx}, cols, active);
 }
 
 // One PCG iteration for every active column (all kernels predicated).
@@ -299,18 +228,18 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
   T* q = cells + 5 * np * cols;
   const int rb = red_blocks(np);
   const cudaStream_t s = L.s;
-  // z = M r = IDCT(g * DCT(r)), rho = r . z
+  // z = M r = IDCT(g * DCT(r)); last block: rho = r . z, beta
   L.row_forward_p(SrcCells<T, T>{r, np, g.nx}, cols, P->active);
   L.column_p(cols, P->active, P->shift, T(P->pthr));
-  L.row_inverse_p(DstCellsDot<T>{z, r, np, g.nx}, cols, P->active, P->partial);
-  scalar(P, X, OP_RHO, L.groups_row_p(), 2, cols, s);
+  L.row_inverse_p(DstCellsDot<T>{z, r, np, g.nx}, cols, P->active, P->partial,
+                  make_fin(P, X, OP_RHO, L.groups_row_p(), 2, cols), P->done_counter);
   // q = S pdir = D (mI+kK)^{-1} D^T pdir,  pdir = z + beta p
   velocity_inverse<T>(P, L, SrcLift<T, double, T>{nullptr, 0, z, pd, P->cg, np, g.nx, g.nu, T(g.ihx), T(g.ihy)}, w,
                       sz, cols, P->active);
-  k_div_q<T, T><<<dim3(rb, cols), kThreads, 0, s>>>(g, w, sz, q, z, pd, np, P->cg, P->active, P->partial);
-  scalar(P, X, OP_ALPHA, rb, 3, cols, s);
-  k_cg_update<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, x, r, pd, z, q, np, P->cg, P->active, P->partial);
-  scalar(P, X, OP_CHECK, rb, 1, cols, s);
+  k_div_q<T, T><<<dim3(rb, cols), kThreads, 0, s>>>(g, w, sz, q, z, pd, np, P->cg, P->active, P->partial,
+                                                    make_fin(P, X, OP_ALPHA, rb, 3, cols), P->done_counter);
+  k_cg_update<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, x, r, pd, z, q, np, P->cg, P->active, P->partial,
+                                                     make_fin(P, X, OP_CHECK, rb, 1, cols), P->done_counter);
   P->launches += 2;
 }
 
@@ -318,7 +247,7 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
 // On entry w holds (mI+kK)^{-1} f in T; on exit x holds the pressure iterate
 // and P->cg the per-column counters.
 template <typename T>
-static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int cols) {
+static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int cols, const double* rd = nullptr) {
   const GridDev& g = P->g;
   const long long np = g.np, sz = g.size;
   T* b = cells;
@@ -326,12 +255,13 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
   T* r = cells + 2 * np * cols;
   const int rb = red_blocks(np);
   const cudaStream_t s = X.s;
-  k_pressure_rhs<T, T><<<dim3(rb, cols), kThreads, 0, s>>>(g, w, sz, b, np, P->partial);
-  scalar(P, X, OP_MEAN_B, rb, 1, cols, s);
-  k_cg_start<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, b, x, r, np, P->cg, P->partial);
-  P->launches += 2;
+  k_pressure_rhs<T, T><<<dim3(rb, cols), kThreads, 0, s>>>(g, w, sz, b, np, rd, P->partial,
+                                                           make_fin(P, X, OP_MEAN_B, rb, 1, cols), P->done_counter);
+  ++P->launches;
   if (!X.graph) {
-    scalar(P, X, OP_START, rb, 2, cols, s);
+    k_cg_start<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, b, x, r, np, P->cg, P->partial,
+                                                      make_fin(P, X, OP_START, rb, 2, cols), P->done_counter);
+    ++P->launches;
     for (int it = 0; it < P->maxit; ++it) {
       cudaMemcpyAsync(P->h_active, P->active, sizeof(int) * cols, cudaMemcpyDeviceToHost, s);
       if (cudaStreamSynchronize(s) != cudaSuccess) return MACSAV_ERR_CUDA;
@@ -352,7 +282,10 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
     return MACSAV_ERR_CUDA;
   if (cudaGraphConditionalHandleCreate(&X.cond, graph, 0, cudaGraphCondAssignDefault) != cudaSuccess)
     return MACSAV_ERR_CUDA;
-  scalar(P, X, OP_START, rb, 2, cols, s);  // sets the loop condition
+  // k_cg_start's last block sets the loop condition
+  k_cg_start<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, b, x, r, np, P->cg, P->partial,
+                                                    make_fin(P, X, OP_START, rb, 2, cols), P->done_counter);
+  ++P->launches;
   if (cudaStreamGetCaptureInfo(s, &st, nullptr, &graph, &deps, nullptr, &ndeps) != cudaSuccess)
     return MACSAV_ERR_CUDA;
   cudaGraphNodeParams cp = {};
@@ -382,11 +315,11 @@ static void finish_pressure(Plan* P, const Exec& X, const T* x, double* pres, in
   const long long np = P->g.np;
   const int rb = red_blocks(np);
   const cudaStream_t s = X.s;
-  k_sum_cells<T><<<dim3(rb, cols), kThreads, 0, s>>>(P->g.np, x, np, P->partial);
-  scalar(P, X, OP_MEAN_X, rb, 1, cols, s);
-  k_center_cells<T><<<dim3(rb, cols), kThreads, 0, s>>>(P->g.np, x, np, pres, np, P->cg, P->partial);
-  scalar(P, X, OP_MEAN_X, rb, 1, cols, s);
-  k_center_cells<double><<<dim3(rb, cols), kThreads, 0, s>>>(P->g.np, pres, np, pres, np, P->cg, nullptr);
+  k_center_cells<T><<<dim3(rb, cols), kThreads, 0, s>>>(P->g.np, x, np, nullptr, np, P->cg, 0, P->partial,
+                                                        make_fin(P, X, OP_MEAN_X, rb, 1, cols), P->done_counter);
+  k_center_cells<T><<<dim3(rb, cols), kThreads, 0, s>>>(P->g.np, x, np, pres, np, P->cg, 1, P->partial,
+                                                        make_fin(P, X, OP_MEAN_X, rb, 1, cols), P->done_counter);
+  k_shift_cells<<<dim3(rb, cols), kThreads, 0, s>>>(P->g.np, pres, np, P->cg);
   P->launches += 3;
 }
 
@@ -394,9 +327,9 @@ static void closing_checks(Plan* P, const Exec& X, const double* f, const double
                            const double* shift) {
   const long long n = P->g.size > P->g.np ? P->g.size : P->g.np;
   const int rb = red_blocks(n);
-  k_stokes_check<<<dim3(rb, cols), kThreads, 0, X.s>>>(P->g, vel, pres, f, P->g.size, P->g.np, shift, P->partial);
+  k_stokes_check<<<dim3(rb, cols), kThreads, 0, X.s>>>(P->g, vel, pres, f, P->g.size, P->g.np, shift, P->partial,
+                                                       make_fin(P, X, OP_CHECKS, rb, 6, cols), P->done_counter);
   ++P->launches;
-  scalar(P, X, OP_CHECKS, rb, 6, cols, X.s);
 }
 
 // FP64 solve: TensorStokes.solve with every vector in double.  Shifts are
@@ -422,22 +355,143 @@ int solve_fp64(Plan* P, const double* f, int cols, double mass, double visc, dou
                cudaStream_t s) {
   (void)mass;
   (void)visc;
-  Exec X{s, false, nullptr, 0};
+  Exec X{s, false, nullptr, 0, 0.0};
   return enqueue_solve_fp64(P, X, f, cols, vel, pres);
 }
 
-int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres) {
-  (void)X; (void)f; (void)cols; (void)vel; (void)pres;
-  P->err = "FP32_MIXED solve not built yet";
-  return MACSAV_ERR_UNSUPPORTED;
+// ------------------------------------------------- FP32 + FP64 correction ---
+// FP64 defect of the accumulated solution: ru = f - (m u + k K u - D^T p),
+// rd = -D u (the continuity defect).
+__global__ void __launch_bounds__(kThreads) k_defect64(GridDev g, const double* f, const double* vel,
+                                                       const double* pres, const double* shift, double* ru,
+                                                       double* rd) {
+  const int c = blockIdx.y;
+  const double mass = shift[2 * c], visc = shift[2 * c + 1];
+  const double* u = vel + c * (long long)g.size;
+  const double* pp = pres + c * (long long)g.np;
+  const int n = g.size > g.np ? g.size : g.np;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (i < g.size) {
+      const long long k = c * (long long)g.size + i;
+      ru[k] = f[k] - (mass * u[i] + visc * K_at(u, g, i) - Dt_at(pp, g, i));
+    }
+    if (i < g.np) {
+      const int j = i / g.nx, q = i - j * g.nx;
+      rd[c * (long long)g.np + i] = -D_at(u, g, j, q);
+    }
+  }
 }
 
-// FP32 transforms with FP64 defect correction (filled in below).
+// dst (+)= double(src) over n elements per column.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_accumulate(const T* src, double* dst, long long n, int add) {
+  const int c = blockIdx.y;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long k = c * n + i;
+    dst[k] = add ? dst[k] + double(src[k]) : double(src[k]);
+  }
+}
+
+// One FP32 Stokes solve of (ru, rd): transforms, stencils and Krylov vectors
+// in float, reductions in double.  Leaves the velocity correction in w2 and
+// the pressure correction (x) in the float cell buffer.
+static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, int cols, float* w2) {
+  const GridDev& g = P->g;
+  Launcher<float> L{P->t32, X.s, &P->launches};
+  const long long sz = g.size, np = g.np;
+  float* w = P->w32;
+  velocity_inverse<float>(P, L, SrcPacked<float, double>{ru, sz, g.nu, g.nx - 1, g.nx}, w, sz, cols, nullptr);
+  const double keep = X.ktol;
+  X.ktol = P->inner_ktol;
+  int rc = schur_pcg<float>(P, X, L, w, P->cells32, cols, rd);
+  X.ktol = keep;
+  if (rc != MACSAV_OK) return rc;
+  const float* x = P->cells32 + 1 * np * cols;
+  velocity_inverse<float>(
+      P, L, SrcLift<float, double, float>{ru, sz, x, nullptr, P->cg, np, g.nx, g.nu, float(g.ihx), float(g.ihy)}, w2,
+      sz, cols, nullptr);
+  return MACSAV_OK;
+}
+
+// TensorStokes.solve with FP32 bulk: an FP32 solve, then `corrections`
+// defect-correction sweeps whose defects are formed in FP64, so the result
+// satisfies the same FP64 residual and divergence gates as the FP64 path.
+int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres) {
+  const GridDev& g = P->g;
+  const long long sz = g.size, np = g.np;
+  double* ru = P->w;               // FP64 momentum defect
+  double* rd = P->cells;           // FP64 continuity defect
+  float* du = reinterpret_cast<float*>(P->vel);  // velocity correction (float)
+  const int nbv = red_blocks(sz), nbp = red_blocks(np), nbm = red_blocks(sz > np ? sz : np);
+  for (int sweep = 0; sweep <= P->corrections; ++sweep) {
+    const double* rhs_u = f;
+    const double* rhs_d = nullptr;
+    if (sweep > 0) {
+      k_defect64<<<dim3(nbm, cols), kThreads, 0, X.s>>>(g, f, vel, pres, P->shift, ru, rd);
+      ++P->launches;
+      rhs_u = ru;
+      rhs_d = rd;
+    }
+    int rc = inner_solve32(P, X, rhs_u, rhs_d, cols, du);
+    if (rc != MACSAV_OK) return rc;
+    k_accumulate<float><<<dim3(nbv, cols), kThreads, 0, X.s>>>(du, vel, sz, sweep > 0);
+    k_accumulate<float><<<dim3(nbp, cols), kThreads, 0, X.s>>>(P->cells32 + 1 * np * cols, pres, np, sweep > 0);
+    P->launches += 2;
+  }
+  // mean-zero pressure and the FP64 closing checks, as in the FP64 path
+  finish_pressure<double>(P, X, pres, pres, cols);
+  closing_checks(P, X, f, vel, pres, cols, P->shift);
+  return MACSAV_OK;
+}
+
+// Average device time of `reps` launches of one transform pass over the
+// velocity blocks (two right-hand sides), with its algorithmic bytes per
+// launch (each element of the pass's input read once and output written once).
+//   pass 0: FP32 column pass; 1: FP32 forward row pass (FP64 packed input);
+//   2: FP32 inverse row pass; 3: FP64 column pass.
+int time_pass(Plan* P, int pass, int reps, cudaStream_t s, double* ms, double* bytes) {
+  const GridDev& g = P->g;
+  const int cols = 2;
+  if (P->maxcols < 2 || reps < 1 || pass < 0 || pass > 3) return MACSAV_ERR_VALUE;
+  if (pass < 3 && P->precision != MACSAV_FP32_MIXED) return MACSAV_ERR_VALUE;
+  const double shift[4] = {1.0, 1e-6, 1.0, 1e-6};
+  cudaMemcpyAsync(P->shift, shift, sizeof shift, cudaMemcpyHostToDevice, s);
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const double n = double(g.size) * cols;
+  auto run = [&](int k) {
+    if (pass == 0) Launcher<float>{P->t32, s, &P->launches}.column_uv(cols, nullptr, P->shift);
+    else if (pass == 1)
+      Launcher<float>{P->t32, s, &P->launches}.row_forward_uv(SrcPacked<float, double>{P->w, g.size, g.nu, g.nx - 1,
+                                                                                        g.nx}, cols, nullptr);
+    else if (pass == 2)
+      Launcher<float>{P->t32, s, &P->launches}.row_inverse_uv(DstPacked<float, float>{P->w32, g.size, g.nu,
+                                                                                      g.nx - 1, g.nx}, cols, nullptr);
+    else Launcher<double>{P->t64, s, &P->launches}.column_uv(cols, nullptr, P->shift);
+    (void)k;
+  };
+  run(0);  // warm-up
+  cudaEventRecord(a, s);
+  for (int k = 0; k < reps; ++k) run(k);
+  cudaEventRecord(b, s);
+  cudaError_t e = cudaEventSynchronize(b);
+  float t = 0;
+  cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms = double(t) / reps;
+  *bytes = pass == 0 ? 2 * 4 * n : (pass == 1 ? (8 + 4) * n : (pass == 2 ? (4 + 4) * n : 2 * 8 * n));
+  return e == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
+}
+
 int solve_mixed(Plan* P, const double* f, int cols, double mass, double visc, double* vel, double* pres,
                 cudaStream_t s, int* sweeps) {
-  (void)f; (void)cols; (void)mass; (void)visc; (void)vel; (void)pres; (void)s; (void)sweeps;
-  P->err = "FP32_MIXED solve not built yet";
-  return MACSAV_ERR_UNSUPPORTED;
+  (void)mass;
+  (void)visc;
+  Exec X{s, false, nullptr, 0, 0.0};
+  *sweeps = P->corrections;
+  return enqueue_solve_mixed(P, X, f, cols, vel, pres);
 }
 
 }  // namespace macsav

@@ -46,6 +46,7 @@ struct TBlockDev {
   int px;              // row pairs per CTA in row passes
   int wy;              // columns per CTA in the column pass (even)
   int groups;          // CTAs of this block in the current pass
+  FastDiv fcols, frows, fw, fvpr, fhalf;  // divisors of the element loops
 };
 
 __device__ __forceinline__ int makhoul_pos(int n, int N) { return (n & 1) ? N - 1 - (n >> 1) : (n >> 1); }
@@ -148,9 +149,11 @@ __device__ __forceinline__ int pick_block(int nblk, int g0, int& g) {
   return 0;
 }
 
+constexpr int kStage = 4;  // independent global loads in flight per thread
+
 // Forward x-transform of rows: src(blk, col, row, n) -> H.
 template <typename T, int VMAX, class Src>
-__global__ void __launch_bounds__(kThreads) k_row_forward(RowArgs<T> a, Src src) {
+__global__ void __launch_bounds__(kFFTThreads, sizeof(T) == 4 ? 2 : 1) k_row_forward(RowArgs<T> a, Src src) {
   const int c = blockIdx.y;
   if (a.active && !a.active[c]) return;
   int g;
@@ -158,88 +161,134 @@ __global__ void __launch_bounds__(kThreads) k_row_forward(RowArgs<T> a, Src src)
   const TBlockDev<T>& B = a.blk[b];
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T>* z = reinterpret_cast<cplx<T>*>(smraw);
-  const int N = B.cols, P = B.px, LS = B.lsx;
+  const int N = B.cols, P = B.px, LS = B.lsx, rows = B.rows, kind = B.kx;
   const int row0 = g * 2 * P;
-  const int npairs = min(P, (B.rows - row0 + 1) / 2);
-  for (int e = threadIdx.x; e < npairs * N; e += blockDim.x) {
-    const int q = e / N, n = e - q * N;
-    const int ra = row0 + 2 * q, rb = ra + 1;
-    const T va = src(b, c, ra, n);
-    const T vb = rb < B.rows ? src(b, c, rb, n) : T(0);
-    put_pair(z + q * LS, B.kx, N, n, va, vb);
+  const int npairs = min(P, (rows - row0 + 1) / 2);
+  const int total = npairs * N;
+  for (int base = threadIdx.x; base < total; base += kStage * blockDim.x) {
+    T va[kStage], vb[kStage];
+#pragma unroll
+    for (int u = 0; u < kStage; ++u) {
+      const int e = base + u * blockDim.x;
+      va[u] = T(0);
+      vb[u] = T(0);
+      if (e < total) {
+        const int q = B.fcols.div(e), n = e - q * N, ra = row0 + 2 * q;
+        va[u] = src(b, c, ra, n);
+        if (ra + 1 < rows) vb[u] = src(b, c, ra + 1, n);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kStage; ++u) {
+      const int e = base + u * blockDim.x;
+      if (e < total) {
+        const int q = B.fcols.div(e), n = e - q * N;
+        put_pair(z + q * LS, kind, N, n, va[u], vb[u]);
+      }
+    }
   }
-  if (B.kx == KIND_DST1)
+  if (kind == KIND_DST1)
     for (int q = threadIdx.x; q < npairs; q += blockDim.x) zero_dst1_ends(z + q * LS, N);
   __syncthreads();
   fft_lines<T, VMAX>(z, z + P * LS, B.fx, LS, npairs, B.twx, -1);
   T* H = B.H + c * B.hstride;
-  for (int e = threadIdx.x; e < npairs * N; e += blockDim.x) {
-    const int q = e / N, k = e - q * N;
-    const int ra = row0 + 2 * q, rb = ra + 1;
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    const int q = B.fcols.div(e), k = e - q * N;
+    const int ra = row0 + 2 * q;
     T ya, yb;
-    coef_forward(z + q * LS, B.kx, N, k, B.qx, ya, yb);
+    coef_forward(z + q * LS, kind, N, k, B.qx, ya, yb);
     H[(long long)ra * B.pitch + k] = ya;
-    if (rb < B.rows) H[(long long)rb * B.pitch + k] = yb;
+    if (ra + 1 < rows) H[(long long)ra * B.pitch + B.pitch + k] = yb;
   }
 }
 
-// Inverse x-transform of rows: H -> dst(blk, col, row, n, value, acc).
-// Dst may accumulate up to 2 double sums per thread (block-reduced into
-// partial[c * gridDim.x * 2 + blockIdx.x * 2 + k]).
-template <typename T, int VMAX, class Dst>
-__global__ void __launch_bounds__(kThreads) k_row_inverse(RowArgs<T> a, Dst dst, double* partial) {
+// Inverse x-transform of rows: H -> dst.  Dst has a two-phase interface so
+// its global loads can be issued together: aux = dst.load(b, c, row, n), then
+// dst.store(b, c, row, n, value, aux, acc) with acc two per-thread sums.  When
+// `partial` is set, the sums are block-reduced into
+// partial[(c * gridDim.x + blockIdx.x) * 2 + k] and the last block runs fin().
+template <typename T, int VMAX, class Dst, class Fin>
+__global__ void __launch_bounds__(kFFTThreads, sizeof(T) == 4 ? 2 : 1) k_row_inverse(RowArgs<T> a, Dst dst, double* partial, Fin fin,
+                                                             unsigned int* counter) {
   const int c = blockIdx.y;
-  if (a.active && !a.active[c]) return;
-  int g;
-  const int b = pick_block(a.nblk, a.blk[0].groups, g);
-  const TBlockDev<T>& B = a.blk[b];
-  extern __shared__ __align__(16) unsigned char smraw[];
-  cplx<T>* z = reinterpret_cast<cplx<T>*>(smraw);
   __shared__ double red[64];
-  const int N = B.cols, P = B.px, LS = B.lsx;
-  const int row0 = g * 2 * P;
-  const int npairs = min(P, (B.rows - row0 + 1) / 2);
-  const T* H = B.H + c * B.hstride;
-  if (B.kx == KIND_DST1) {
-    for (int e = threadIdx.x; e < npairs * N; e += blockDim.x) {
-      const int q = e / N, k = e - q * N;
-      const int ra = row0 + 2 * q, rb = ra + 1;
-      const T va = H[(long long)ra * B.pitch + k];
-      const T vb = rb < B.rows ? H[(long long)rb * B.pitch + k] : T(0);
-      put_pair(z + q * LS, KIND_DST1, N, k, va, vb);
-    }
-    for (int q = threadIdx.x; q < npairs; q += blockDim.x) zero_dst1_ends(z + q * LS, N);
-  } else {
-    for (int e = threadIdx.x; e < npairs * N; e += blockDim.x) {
-      const int q = e / N, k = e - q * N;
-      const int ra = row0 + 2 * q, rb = ra + 1;
-      const int m = N - k;  // partner; y_N = 0
-      const T yak = H[(long long)ra * B.pitch + k];
-      const T yam = k ? H[(long long)ra * B.pitch + m] : T(0);
-      T ybk = T(0), ybm = T(0);
-      if (rb < B.rows) {
-        ybk = H[(long long)rb * B.pitch + k];
-        ybm = k ? H[(long long)rb * B.pitch + m] : T(0);
+  const bool live = !a.active || a.active[c];
+  Acc<T> acc[2];
+  if (live) {
+    int g;
+    const int b = pick_block(a.nblk, a.blk[0].groups, g);
+    const TBlockDev<T>& B = a.blk[b];
+    extern __shared__ __align__(16) unsigned char smraw[];
+    cplx<T>* z = reinterpret_cast<cplx<T>*>(smraw);
+    const int N = B.cols, P = B.px, LS = B.lsx, rows = B.rows, kind = B.kx;
+    const int row0 = g * 2 * P;
+    const int npairs = min(P, (rows - row0 + 1) / 2);
+    const int total = npairs * N;
+    const T* H = B.H + c * B.hstride;
+    const long long pitch = B.pitch;
+    for (int base = threadIdx.x; base < total; base += kStage * blockDim.x) {
+      T yak[kStage], yam[kStage], ybk[kStage], ybm[kStage];
+#pragma unroll
+      for (int u = 0; u < kStage; ++u) {
+        const int e = base + u * blockDim.x;
+        yak[u] = yam[u] = ybk[u] = ybm[u] = T(0);
+        if (e < total) {
+          const int q = B.fcols.div(e), k = e - q * N, ra = row0 + 2 * q;
+          const T* ha = H + ra * pitch;
+          const bool hb = ra + 1 < rows;
+          yak[u] = ha[k];
+          if (hb) ybk[u] = ha[pitch + k];
+          if (kind != KIND_DST1 && k) {
+            yam[u] = ha[N - k];
+            if (hb) ybm[u] = ha[pitch + N - k];
+          }
+        }
       }
-      z[q * LS + k] = pre_inverse(yak, yam, ybk, ybm, B.qx[k]);
+#pragma unroll
+      for (int u = 0; u < kStage; ++u) {
+        const int e = base + u * blockDim.x;
+        if (e < total) {
+          const int q = B.fcols.div(e), k = e - q * N;
+          if (kind == KIND_DST1) put_pair(z + q * LS, KIND_DST1, N, k, yak[u], ybk[u]);
+          else z[q * LS + k] = pre_inverse(yak[u], yam[u], ybk[u], ybm[u], B.qx[k]);
+        }
+      }
     }
-  }
-  __syncthreads();
-  fft_lines<T, VMAX>(z, z + P * LS, B.fx, LS, npairs, B.twx, inverse_sign(B.kx));
-  double acc[2] = {0.0, 0.0};
-  for (int e = threadIdx.x; e < npairs * N; e += blockDim.x) {
-    const int q = e / N, n = e - q * N;
-    const int ra = row0 + 2 * q, rb = ra + 1;
-    dst(b, c, ra, n, value_inverse(z + q * LS, B.kx, N, n, 0), acc);
-    if (rb < B.rows) dst(b, c, rb, n, value_inverse(z + q * LS, B.kx, N, n, 1), acc);
+    if (kind == KIND_DST1)
+      for (int q = threadIdx.x; q < npairs; q += blockDim.x) zero_dst1_ends(z + q * LS, N);
+    __syncthreads();
+    fft_lines<T, VMAX>(z, z + P * LS, B.fx, LS, npairs, B.twx, inverse_sign(kind));
+    for (int base = threadIdx.x; base < total; base += kStage * blockDim.x) {
+      typename Dst::aux_t xa[kStage], xb[kStage];
+#pragma unroll
+      for (int u = 0; u < kStage; ++u) {
+        const int e = base + u * blockDim.x;
+        if (e < total) {
+          const int q = B.fcols.div(e), n = e - q * N, ra = row0 + 2 * q;
+          xa[u] = dst.load(b, c, ra, n);
+          if (ra + 1 < rows) xb[u] = dst.load(b, c, ra + 1, n);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kStage; ++u) {
+        const int e = base + u * blockDim.x;
+        if (e < total) {
+          const int q = B.fcols.div(e), n = e - q * N, ra = row0 + 2 * q;
+          dst.store(b, c, ra, n, value_inverse(z + q * LS, kind, N, n, 0), xa[u], acc);
+          if (ra + 1 < rows) dst.store(b, c, ra + 1, n, value_inverse(z + q * LS, kind, N, n, 1), xb[u], acc);
+        }
+      }
+    }
   }
   if (partial) {
-    block_sum<2>(acc, red);
+    double v[2] = {acc[0].value(), acc[1].value()};
+    block_sum<2>(v, red);
     if (threadIdx.x == 0) {
       const int slot = (c * gridDim.x + blockIdx.x) * 2;
-      partial[slot] = acc[0];
-      partial[slot + 1] = acc[1];
+      partial[slot] = v[0];
+      partial[slot + 1] = v[1];
     }
+    last_block_finish(fin, counter);
   }
 }
 
@@ -254,8 +303,11 @@ struct ColArgs {
   T thr;                    // Poisson zero-mode threshold
 };
 
+// Column strips of W columns (W a multiple of the 16-byte vector width, the
+// strip start 16-byte aligned; H's row padding is zero, so full-width vector
+// loads past the last column read zeros).
 template <typename T, int VMAX>
-__global__ void __launch_bounds__(kThreads) k_column(ColArgs<T> a) {
+__global__ void __launch_bounds__(kFFTThreads, sizeof(T) == 4 ? 2 : 1) k_column(ColArgs<T> a) {
   const int c = blockIdx.y;
   if (a.active && !a.active[c]) return;
   int g;
@@ -263,18 +315,46 @@ __global__ void __launch_bounds__(kThreads) k_column(ColArgs<T> a) {
   const TBlockDev<T>& B = a.blk[b];
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T>* z = reinterpret_cast<cplx<T>*>(smraw);
+  using vec_t = typename Vec16<T>::type;
+  constexpr int V = Vec16<T>::n;
   const int N = B.rows, W = B.wy, LS = B.lsy, kind = B.ky;
   const int col0 = g * W;
   const int ncols = min(W, B.cols - col0);
   const int nl = (ncols + 1) / 2;
   T* H = B.H + c * B.hstride;
+  const long long pitch = B.pitch;
   const T mass = T(a.shift[2 * c]), visc = T(a.shift[2 * c + 1]);
-  // load the strip, two columns per complex line
-  for (int e = threadIdx.x; e < N * W; e += blockDim.x) {
-    const int n = e / W, j = e - n * W;
-    if (j < 2 * nl) {
-      const T v = j < ncols ? H[(long long)n * B.pitch + col0 + j] : T(0);
-      put_real(z + (j >> 1) * LS, kind, N, n, j & 1, v);
+  const bool vec = (W % V) == 0;
+  const int vpr = W / V, totv = N * vpr;
+  if (!vec) {  // narrow strips (W < 16 bytes): scalar loads
+    for (int e = threadIdx.x; e < N * W; e += blockDim.x) {
+      const int n = B.fw.div(e), j = e - n * W;
+      if (j < 2 * nl) put_real(z + (j >> 1) * LS, kind, N, n, j & 1, j < ncols ? H[n * pitch + col0 + j] : T(0));
+    }
+  }
+  // load the strip (16-byte vectors), two columns per complex line
+  for (int base = threadIdx.x; vec && base < totv; base += kStage * blockDim.x) {
+    vec_t v[kStage];
+#pragma unroll
+    for (int u = 0; u < kStage; ++u) {
+      const int e = base + u * blockDim.x;
+      if (e < totv) {
+        const int n = B.fvpr.div(e), jv = e - n * vpr;
+        v[u] = *reinterpret_cast<const vec_t*>(H + n * pitch + col0 + jv * V);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kStage; ++u) {
+      const int e = base + u * blockDim.x;
+      if (e < totv) {
+        const int n = B.fvpr.div(e), jv = e - n * vpr;
+        const T* comp = reinterpret_cast<const T*>(&v[u]);
+#pragma unroll
+        for (int k = 0; k < V; ++k) {
+          const int j = jv * V + k;
+          if (j < 2 * nl) put_real(z + (j >> 1) * LS, kind, N, n, j & 1, j < ncols ? comp[k] : T(0));
+        }
+      }
     }
   }
   if (kind == KIND_DST1)
@@ -284,7 +364,7 @@ __global__ void __launch_bounds__(kThreads) k_column(ColArgs<T> a) {
   // forward post-processing, spectral weight, inverse pre-processing (in place)
   if (kind == KIND_DST1) {
     for (int e = threadIdx.x; e < nl * N; e += blockDim.x) {
-      const int q = e / N, k = e - q * N;
+      const int q = B.frows.div(e), k = e - q * N;
       cplx<T>* zl = z + q * LS;
       const int ca = col0 + 2 * q, cb = min(ca + 1, B.cols - 1);
       const T ey = B.eigy[k];
@@ -302,7 +382,7 @@ __global__ void __launch_bounds__(kThreads) k_column(ColArgs<T> a) {
   } else {
     const int half = N / 2 + 1;
     for (int e = threadIdx.x; e < nl * half; e += blockDim.x) {
-      const int q = e / half, k = e - q * half;
+      const int q = B.fhalf.div(e), k = e - q * half;
       cplx<T>* zl = z + q * LS;
       const int m = k == 0 ? 0 : N - k;
       const int ca = col0 + 2 * q, cb = min(ca + 1, B.cols - 1);
@@ -325,9 +405,23 @@ __global__ void __launch_bounds__(kThreads) k_column(ColArgs<T> a) {
   }
   __syncthreads();
   fft_lines<T, VMAX>(z, z + W / 2 * LS, B.fy, LS, nl, B.twy, inverse_sign(kind));
-  for (int e = threadIdx.x; e < N * W; e += blockDim.x) {
-    const int n = e / W, j = e - n * W;
-    if (j < ncols) H[(long long)n * B.pitch + col0 + j] = value_inverse(z + (j >> 1) * LS, kind, N, n, j & 1);
+  if (vec && ncols == W) {
+    for (int e = threadIdx.x; e < totv; e += blockDim.x) {
+      const int n = B.fvpr.div(e), jv = e - n * vpr;
+      vec_t v;
+      T* comp = reinterpret_cast<T*>(&v);
+#pragma unroll
+      for (int k = 0; k < V; ++k) {
+        const int j = jv * V + k;
+        comp[k] = value_inverse(z + (j >> 1) * LS, kind, N, n, j & 1);
+      }
+      *reinterpret_cast<vec_t*>(H + n * pitch + col0 + jv * V) = v;
+    }
+  } else {
+    for (int e = threadIdx.x; e < N * W; e += blockDim.x) {
+      const int n = B.fw.div(e), j = e - n * W;
+      if (j < ncols) H[n * pitch + col0 + j] = value_inverse(z + (j >> 1) * LS, kind, N, n, j & 1);
+    }
   }
 }
 

@@ -97,30 +97,29 @@ class FusedScheme:
                                f"{rec.continuity_residual}")
         _lib.check(code, plan.handle)
 
-    def step(self, model, state, dt: float) -> Trial:
-        if not np.isfinite(dt) or dt <= 0:
-            raise ValueError("Invalid step size")
-        if self.name == "imex_euler" and not np.isfinite(state.t):
-            raise ValueError("Invalid step size or state time")  # imex_euler.py:14-15
-        if self.name == "imex_euler_mrsav" and not np.isfinite([state.t, state.r]).all():
-            raise ValueError("Invalid step size or scalar state")  # imex_euler_mrsav.py:52-53
+    def step_device(self, model, x0: torch.Tensor, t: float, r0: float, dt: float, *, x1=None, emb=None,
+                    pres=None, want_embedded: bool = True, forces=None):
+        """One step on device data: x0 (packed, float64 CUDA) at time t with
+        scalar r0.  Returns (x1, r1, records, pres, emb).  Raises like the
+        reference when a stage check fails."""
         plan = model.plan
         g = model.grid
         n = self.info.n_stages
-        x0 = model.device_vector(state).contiguous()
-        forces = None
-        if not getattr(model.force, "zero", False):
-            forces = torch.stack([model._dev(model.force(state.t + c * dt)).reshape(-1) for c in _NODES[self.name]])
+        if forces is None and not getattr(model.force, "zero", False):
+            forces = torch.stack([model._dev(model.force(t + c * dt)).reshape(-1) for c in _NODES[self.name]])
             forces = forces.contiguous()
-        x1 = torch.empty(g.size, dtype=torch.float64, device=x0.device)
-        emb = torch.empty(g.size, dtype=torch.float64, device=x0.device) if n > 1 else None
-        pres = torch.empty((n, g.np), dtype=torch.float64, device=x0.device)
+        if x1 is None:
+            x1 = torch.empty(g.size, dtype=torch.float64, device=x0.device)
+        if emb is None and want_embedded and n > 1:
+            emb = torch.empty(g.size, dtype=torch.float64, device=x0.device)
+        if pres is None:
+            pres = torch.empty((n, g.np), dtype=torch.float64, device=x0.device)
         recs = (StageRecord * n)()
         r1 = C.c_double()
         lib = _lib.load()
         lib.macsav_plan_set_graph(plan.handle, 1 if getattr(model, "use_graph", False) else 0)
-        code = lib.macsav_step(plan.handle, self._id, float(state.t), float(dt), float(model.nu), self.gamma,
-                               dptr(x0), float(state.r), dptr(forces) if forces is not None else None, dptr(x1),
+        code = lib.macsav_step(plan.handle, self._id, float(t), float(dt), float(model.nu), self.gamma,
+                               dptr(x0), float(r0), dptr(forces) if forces is not None else None, dptr(x1),
                                dptr(emb) if emb is not None else None, dptr(pres), recs, C.byref(r1),
                                stream_handle())
         self.last_records = list(recs)
@@ -129,6 +128,18 @@ class FusedScheme:
             if failing is None:
                 _lib.check(code, plan.handle)
             self._raise(code, failing, plan)
+        return x1, (float(r1.value) if self.sav else 0.0), recs, pres, emb
+
+    def step(self, model, state, dt: float) -> Trial:
+        if not np.isfinite(dt) or dt <= 0:
+            raise ValueError("Invalid step size")
+        if self.name == "imex_euler" and not np.isfinite(state.t):
+            raise ValueError("Invalid step size or state time")  # imex_euler.py:14-15
+        if self.name == "imex_euler_mrsav" and not np.isfinite([state.t, state.r]).all():
+            raise ValueError("Invalid step size or scalar state")  # imex_euler_mrsav.py:52-53
+        g = model.grid
+        x0 = model.device_vector(state).contiguous()
+        x1, r1, recs, pres, emb = self.step_device(model, x0, state.t, state.r, dt)
         stages = []
         for i, rec in enumerate(recs):
             st = Stage(DeviceArray(pres[i].reshape(g.ny, g.nx)), float(rec.residual), float(rec.divergence_inf),
@@ -139,7 +150,7 @@ class FusedScheme:
                 st.corrections = [float(rec.corrections[k]) for k in range(rec.n_corrections)]
                 st.frozen_factor = float(rec.frozen_factor)
             stages.append(st)
-        new_state = model.state(state.t + dt, x1, float(r1.value) if self.sav else 0.0)
+        new_state = model.state(state.t + dt, x1, r1)
         return Trial(new_state, stages, emb)
 
 

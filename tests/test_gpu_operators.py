@@ -176,3 +176,22 @@ def test_diagnostics_and_reductions(env):
     assert abs(res.value - g.inner(x, f)) < 1e-12 * abs(g.inner(x, f)) + 1e-14
     plan.check(plan.lib.macsav_max_abs(plan.handle, stokes.dptr(xd), g.size, C.byref(res), stokes.stream_handle()))
     assert res.value == np.abs(x).max()
+
+
+@pytest.mark.parametrize("name", ["stokes_7x5", "stokes_11x7", "stokes_64"])
+def test_stokes_fp32_mixed_meets_gates_and_matches(env, name):
+    """FP32 transforms + FP64 defect correction: same gates as the reference,
+    within 1e-9 relative L2 of the reference's FP64 solution."""
+    pkg, stokes, lib, torch = env
+    d = golden(name)
+    nx, ny, lx, ly = d["shape"]
+    tol = 1e-9 if name == "stokes_64" else 1e-10
+    solver = stokes.TensorStokes(pkg.MACGrid(int(nx), int(ny), float(lx), float(ly)), tolerance=tol,
+                                 krylov_tolerance=1e-12, precision="fp32")
+    for k, (m, kappa) in enumerate(d["shifts"]):
+        r = solver.solve(d["rhs"], mass=float(m), viscosity=float(kappa))
+        for got, ref in ((r.velocity, d[f"vel{k}"]), (r.pressure, d[f"pres{k}"])):
+            rel = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-300)
+            assert rel <= 1e-9, (name, k, rel)
+        assert r.residual <= tol and r.divergence_inf <= tol * (1 + np.abs(r.velocity).max())
+        assert solver.last_refinements >= 1

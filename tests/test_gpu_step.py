@@ -112,7 +112,7 @@ def test_step_failure_is_reported_like_reference(pkg):
 
     def force(t):
         calls.append(t)
-        return np.full(g.size, np.nan) if t > 0.015 else np.zeros(g.size)
+        return np.full(g.size, np.nan) if t > 0.012 else np.zeros(g.size)
     model.force = force
     res = pkg.integrate(model, pkg.make_scheme("sdirk2_mrsav"), model.state(0.0, x0), [0.01, 0.01, 0.01])
     assert res.status == "failed"
@@ -127,3 +127,18 @@ def test_cg_failure_inside_step(pkg):
     x0 = pkg.fields.packed_curl_velocity(16, 12, 1.0, 1.0, 4, 2)
     with pytest.raises(RuntimeError, match=r"Pressure Schur CG failed with info=1"):
         pkg.make_scheme("sdirk3_mrsav").step(model, model.state(0.0, x0), 0.01)
+
+
+@pytest.mark.parametrize("name", ["sdirk3_mrsav", "sdirk2_mrsav"])
+def test_fp32_mixed_step_close_to_fp64(pkg, name):
+    """The FP32-bulk step keeps the reference's gates and stays within 1e-9
+    (far inside the 1e-6 budget) of the FP64 reference step."""
+    d = golden(f"step_{name}")
+    nx, ny, lx, ly = d["shape"]
+    g = pkg.MACGrid(int(nx), int(ny), float(lx), float(ly))
+    for graph in (False, True):
+        model = pkg.MACNavierStokes(g, float(d["nu"]), precision="fp32", use_graph=graph)
+        state = model.state(float(d["t0"]), d["x0"], float(d["r0"]))
+        trial = pkg.make_scheme(name, gamma=float(d["gamma"])).step(model, state, float(d["dt"]))
+        assert _rel(model.vector(trial.state), d["x1"]) < 1e-9
+        assert abs(trial.state.r - float(d["r1"])) < 1e-10
