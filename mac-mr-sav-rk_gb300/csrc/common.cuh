@@ -69,6 +69,71 @@ template <typename T> struct Vec16;
 template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
 template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
 
+// ---- double-float arithmetic on the FP32 pipe ------------------------------
+// GB300 runs FP64 at a small fraction of FP32, so every reduction of FP32 data
+// is carried as an unevaluated sum hi + lo of two floats (Knuth's TwoSum,
+// Dekker's fast renormalisation): ~48-bit significands without FP64 issue.
+struct df32 {
+  float hi, lo;
+};
+__device__ __forceinline__ df32 df_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  const float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+__device__ __forceinline__ df32 df_add(df32 a, df32 b) {
+  const df32 s = df_two_sum(a.hi, b.hi);
+  const float e = s.lo + (a.lo + b.lo);
+  const float h = s.hi + e;
+  return {h, e - (h - s.hi)};
+}
+__device__ __forceinline__ double df_value(df32 a) { return double(a.hi) + double(a.lo); }
+
+// Conversions between double and float without the FP64 pipe: the binary64
+// fields are re-packed with integer instructions, rounding to nearest even.
+// Values beyond the float range saturate to +-inf; binary32 subnormals flush
+// to zero (the magnitudes seen here are far from both ends).
+__device__ __forceinline__ float d2f_bits(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+  const int e = int((b >> 52) & 0x7ff);
+  unsigned long long m = b & 0xfffffffffffffull;
+  if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));  // inf / nan
+  const int ef = e - 1023 + 127;
+  if (ef <= 0) return __uint_as_float(sign);  // zero, subnormal, underflow
+  unsigned int mf = (unsigned int)(m >> 29);
+  const unsigned int rem = (unsigned int)(m & 0x1fffffffu);
+  unsigned int bits = ((unsigned int)ef << 23) | mf;
+  if (rem > 0x10000000u || (rem == 0x10000000u && (mf & 1u))) ++bits;  // carries into the exponent correctly
+  if (ef >= 255 || bits >= 0x7f800000u) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | bits);
+}
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned int b = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+  const unsigned int e = (b >> 23) & 0xffu;
+  const unsigned long long m = b & 0x7fffffu;
+  if (e == 0) return __longlong_as_double((long long)sign);  // zero (subnormals flush)
+  if (e == 0xff) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull | (m << 29)));
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e - 127 + 1023) << 52) | (m << 29)));
+}
+// Load a double into T without touching the FP64 pipe when T is float.
+template <typename T>
+__device__ __forceinline__ T load_as(const double* p) {
+  if constexpr (sizeof(T) == 4) return d2f_bits(*p);
+  else return *p;
+}
+template <typename T>
+__device__ __forceinline__ T load_as(const float* p) { return T(*p); }
+
+// |x| of a double as an ordered integer key: the maximum key is the maximum
+// |x|, and NaN keys exceed every finite or infinite one (so NaN propagates).
+__device__ __forceinline__ unsigned long long abs_key(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ double key_value(unsigned long long k) { return __longlong_as_double((long long)k); }
+
 // Per-thread accumulator for inner products: plain double for FP64 data;
 // for FP32 data the products are summed in float with Neumaier compensation
 // (error independent of the number of terms), and the block and grid sums
@@ -85,8 +150,89 @@ template <> struct Acc<float> {
     c += (fabsf(s) >= fabsf(x)) ? (s - t) + x : (x - t) + s;
     s = t;
   }
-  __device__ __forceinline__ double value() const { return double(s) + double(c); }
+  __device__ __forceinline__ df32 pair() const { return df_two_sum(s, c); }
+  __device__ __forceinline__ double value() const { return df_value(pair()); }
 };
+
+// Reduction traits: the partial type of FP64 data is double, of FP32 data a
+// double-float pair (stored in the same 8 bytes as a float2).
+template <typename T> struct Red;
+template <> struct Red<double> {
+  using P = double;
+  __device__ __forceinline__ static P from(const Acc<double>& a) { return a.s; }
+  __device__ __forceinline__ static P add(P a, P b) { return a + b; }
+  __device__ __forceinline__ static P shfl_down(P v, int o) { return __shfl_down_sync(0xffffffffu, v, o); }
+  __device__ __forceinline__ static P zero() { return 0.0; }
+  __device__ __forceinline__ static double value(P p) { return p; }
+  __device__ __forceinline__ static P load(const double* p) { return __ldcg(p); }
+  __device__ __forceinline__ static void store(double* p, P v) { *p = v; }
+};
+template <> struct Red<float> {
+  using P = df32;
+  __device__ __forceinline__ static P from(const Acc<float>& a) { return a.pair(); }
+  __device__ __forceinline__ static P add(P a, P b) { return df_add(a, b); }
+  __device__ __forceinline__ static P shfl_down(P v, int o) {
+    return {__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+  }
+  __device__ __forceinline__ static P zero() { return {0.0f, 0.0f}; }
+  __device__ __forceinline__ static double value(P p) { return df_value(p); }
+  __device__ __forceinline__ static P load(const double* p) {
+    const float2 f = __ldcg(reinterpret_cast<const float2*>(p));
+    return {f.x, f.y};
+  }
+  __device__ __forceinline__ static void store(double* p, P v) { *reinterpret_cast<float2*>(p) = make_float2(v.hi, v.lo); }
+};
+
+// Block sum of NV partials (result in thread 0), fixed tree order.
+template <typename T, int NV>
+__device__ __forceinline__ void block_sum_p(typename Red<T>::P (&v)[NV], typename Red<T>::P* scratch /* >= 32*NV */) {
+  using R = Red<T>;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] = R::add(v[k], R::shfl_down(v[k], o));
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) scratch[k * 32 + wid] = v[k];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      v[k] = lane < nw ? scratch[k * 32 + lane] : R::zero();
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[k] = R::add(v[k], R::shfl_down(v[k], o));
+    }
+  }
+  __syncthreads();
+}
+
+// Block maximum of NV integer keys (abs_key of doubles), result in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_max_key(unsigned long long (&v)[NV], unsigned long long* scratch) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] = max(v[k], __shfl_down_sync(0xffffffffu, v[k], o));
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) scratch[k * 32 + wid] = v[k];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      v[k] = lane < nw ? scratch[k * 32 + lane] : 0ull;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[k] = max(v[k], __shfl_down_sync(0xffffffffu, v[k], o));
+    }
+  }
+  __syncthreads();
+}
 
 // ---- deterministic block reductions in double --------------------------------
 __device__ __forceinline__ double warp_sum(double v) {
@@ -147,6 +293,34 @@ __device__ __forceinline__ void block_max(double (&v)[NV], double* scratch) {
   __syncthreads();
 }
 
+
+// Block partial of NV sums (Red<T>) written to partial[(c*gridDim.x+b)*K + k].
+template <typename T, int NV>
+__device__ __forceinline__ void write_sums(const Acc<T> (&acc)[NV], double* partial, int K) {
+  using R = Red<T>;
+  __shared__ typename R::P red[NV * 32];
+  typename R::P v[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = R::from(acc[k]);
+  block_sum_p<T, NV>(v, red);
+  if (threadIdx.x == 0) {
+    double* o = partial + (size_t(blockIdx.y) * gridDim.x + blockIdx.x) * K;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) R::store(o + k, v[k]);
+  }
+}
+
+// Block maximum of NV abs_key values written to slots off..off+NV-1.
+template <int NV>
+__device__ __forceinline__ void write_keys(unsigned long long (&key)[NV], double* partial, int K, int off) {
+  __shared__ unsigned long long redk[NV * 32];
+  block_max_key<NV>(key, redk);
+  if (threadIdx.x == 0) {
+    double* o = partial + (size_t(blockIdx.y) * gridDim.x + blockIdx.x) * K + off;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) reinterpret_cast<unsigned long long*>(o)[k] = key[k];
+  }
+}
 
 // Grid-wide "last block finishes" step: every block calls this once after
 // writing its partials; the block that arrives last (all partials visible)

@@ -1,8 +1,26 @@
 // Device functors, the Krylov scalar logic and the transform launchers.
 #pragma once
+#include <algorithm>
+
+#include "fftp.cuh"
 #include "plan.cuh"
 
 namespace macsav {
+
+// CG scalars in the working type (FP32 kernels read the float copies, so
+// they issue no FP64 conversion).
+template <typename T> __device__ __forceinline__ T cg_beta(const CGScalars& g) {
+  if constexpr (sizeof(T) == 4) return g.beta_t; else return g.beta;
+}
+template <typename T> __device__ __forceinline__ T cg_alpha(const CGScalars& g) {
+  if constexpr (sizeof(T) == 4) return g.alpha_t; else return g.alpha;
+}
+template <typename T> __device__ __forceinline__ T cg_mean_q(const CGScalars& g) {
+  if constexpr (sizeof(T) == 4) return g.mean_q_t; else return g.mean_q;
+}
+template <typename T> __device__ __forceinline__ T cg_mean_b(const CGScalars& g) {
+  if constexpr (sizeof(T) == 4) return g.mean_b_t; else return g.mean_b;
+}
 
 // ------------------------------------------------------------ row sources ---
 // Packed velocity rows: block 0 = u rows (length nx-1), block 1 = v rows (nx).
@@ -13,7 +31,7 @@ struct SrcPacked {
   int off1, n0, n1;
   __device__ T operator()(int b, int c, int row, int n) const {
     const In* base = x + c * cstride;
-    return b == 0 ? T(base[(long long)row * n0 + n]) : T(base[off1 + (long long)row * n1 + n]);
+    return b == 0 ? load_as<T>(base + (long long)row * n0 + n) : load_as<T>(base + off1 + (long long)row * n1 + n);
   }
 };
 
@@ -23,7 +41,7 @@ struct SrcCells {
   const In* x;
   long long cstride;
   int nx;
-  __device__ T operator()(int, int c, int row, int n) const { return T(x[c * cstride + (long long)row * nx + n]); }
+  __device__ T operator()(int, int c, int row, int n) const { return load_as<T>(x + c * cstride + (long long)row * nx + n); }
 };
 
 // f + D^T P with P = p1 (+ beta p2 after the first CG iteration), on u/v rows.
@@ -41,15 +59,15 @@ struct SrcLift {
     const PIn* a = p1 + c * pstride;
     const long long l = (long long)row * nx + n;
     const long long l2 = bk == 0 ? l + 1 : l + nx;
-    T v0 = T(a[l]), v1 = T(a[l2]);
+    T v0 = load_as<T>(a + l), v1 = load_as<T>(a + l2);
     if (p2 && cg[c].iters > 0) {
       const PIn* b = p2 + c * pstride;
-      const T beta = T(cg[c].beta);
-      v0 = v0 + beta * T(b[l]);
-      v1 = v1 + beta * T(b[l2]);
+      const T beta = cg_beta<T>(cg[c]);
+      v0 = v0 + beta * load_as<T>(b + l);
+      v1 = v1 + beta * load_as<T>(b + l2);
     }
     T v = (v0 - v1) * (bk == 0 ? ihx : ihy);
-    if (f) v += T(f[c * fstride + (bk == 0 ? (long long)row * (nx - 1) + n : nu + l)]);
+    if (f) v += load_as<T>(f + c * fstride + (bk == 0 ? (long long)row * (nx - 1) + n : nu + l));
     return v;
   }
 };
@@ -100,10 +118,13 @@ struct DstCellsDot {
 // ------------------------------------------------------- Krylov scalars ---
 enum ScalarOp : int { OP_MEAN_B, OP_START, OP_RHO, OP_ALPHA, OP_CHECK, OP_MEAN_X, OP_CHECKS };
 
-// Block-wide fold of the K-slot partials of `nb` blocks per column (fixed
-// order; sums, and maxima for OP_START slot 1 and every OP_CHECKS slot), then
-// thread 0 updates each column's scalars.  Under graph capture OP_START and
-// OP_CHECK also set the CG while-loop condition to "some column active".
+// Block-wide fold of the K-slot partials of `nb` blocks per column in a
+// fixed order, then thread 0 updates each column's scalars.  Sum slots hold
+// Red<T>::P partials (double, or a double-float pair for FP32 data, so no
+// FP64 instruction is issued for FP32 data until the final scalars); max
+// slots hold abs_key integers.  Under graph capture OP_START and OP_CHECK also
+// set the CG while-loop condition to "some column active".
+template <typename T>
 struct CGFin {
   int op;
   const double* partial;
@@ -117,23 +138,44 @@ struct CGFin {
   int use_cond;
   cudaGraphConditionalHandle cond;
 
+  __device__ int maxmask() const { return op == OP_START ? 0x2 : (op == OP_CHECKS ? 0x3f : 0); }
+
   __device__ void operator()() const {
-    __shared__ double red[6 * 32];
+    using R = Red<T>;
+    __shared__ typename R::P red[6 * 32];
+    __shared__ unsigned long long redk[6 * 32];
     const bool gated = op == OP_RHO || op == OP_ALPHA || op == OP_CHECK;
+    const int mm = maxmask();
     for (int c = 0; c < cols; ++c) {
       if (gated && !active[c]) continue;  // uniform across the block
-      double s[6] = {0, 0, 0, 0, 0, 0}, m[6] = {0, 0, 0, 0, 0, 0};
+      typename R::P s[6];
+      unsigned long long m[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        s[k] = R::zero();
+        m[k] = 0ull;
+      }
       for (int b = threadIdx.x; b < nb; b += blockDim.x) {
         const double* o = partial + (size_t(c) * nb + b) * K;
-        for (int k = 0; k < K && k < 6; ++k) {
-          const double v = __ldcg(o + k);
-          s[k] += v;
-          m[k] = nanmax(m[k], v);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+          if (k < K) {
+            if ((mm >> k) & 1) m[k] = max(m[k], (unsigned long long)__ldcg(reinterpret_cast<const long long*>(o + k)));
+            else s[k] = R::add(s[k], R::load(o + k));
+          }
         }
       }
-      block_sum<6>(s, red);
-      block_max<6>(m, red);
-      if (threadIdx.x == 0) update(c, s, m);
+      block_sum_p<T, 6>(s, red);
+      if (mm) block_max_key<6>(m, redk);
+      if (threadIdx.x == 0) {
+        double sv[6], mv[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+          sv[k] = R::value(s[k]);
+          mv[k] = key_value(m[k]);
+        }
+        update(c, sv, mv);
+      }
       __syncthreads();
     }
     if (use_cond && threadIdx.x == 0 && (op == OP_START || op == OP_CHECK)) {
@@ -148,6 +190,7 @@ struct CGFin {
     switch (op) {
       case OP_MEAN_B:
         g.mean_b = s[0] / np;
+        g.mean_b_t = float(g.mean_b);
         break;
       case OP_START: {
         g.bnorm = sqrt(s[0]);
@@ -157,6 +200,7 @@ struct CGFin {
         g.info = 0;
         g.rho_prev = 0;
         g.beta = 0;
+        g.beta_t = 0.0f;
         g.rr = s[0];
         // zero RHS (tensor_stokes.py:309-311) or already converged: no update
         const bool go = (g.max_b != 0.0) && !(sqrt(g.rr) < g.atol) && (g.bnorm == g.bnorm);
@@ -166,11 +210,14 @@ struct CGFin {
       case OP_RHO:
         g.rho = s[0];
         g.beta = g.iters > 0 ? g.rho / g.rho_prev : 0.0;
+        g.beta_t = float(g.beta);
         break;
       case OP_ALPHA:
         g.mean_q = s[1] / np;
         g.pq = s[0] - s[1] * s[2] / np;  // p . (q - mean(q))
         g.alpha = g.rho / g.pq;
+        g.alpha_t = float(g.alpha);
+        g.mean_q_t = float(g.mean_q);
         break;
       case OP_CHECK:
         g.rr = s[0];
@@ -185,6 +232,7 @@ struct CGFin {
         break;
       case OP_MEAN_X:
         g.mean_q = s[0] / np;
+        g.mean_q_t = float(g.mean_q);
         break;
       case OP_CHECKS:
         checks[c].max_defect = m[0];
@@ -198,9 +246,10 @@ struct CGFin {
   }
 };
 
-inline CGFin make_fin(const Plan* P, const Exec& X, int op, int nb, int K, int cols) {
-  return CGFin{op, P->partial, nb, K, cols, P->cg, P->active, P->g.np, X.ktol > 0 ? X.ktol : P->ktol, P->maxit,
-               P->checks, X.graph ? 1 : 0, X.cond};
+template <typename T>
+inline CGFin<T> make_fin(const Plan* P, const Exec& X, int op, int nb, int K, int cols) {
+  return CGFin<T>{op, P->partial, nb, K, cols, P->cg, P->active, P->g.np, X.ktol > 0 ? X.ktol : P->ktol, P->maxit,
+                  P->checks, X.graph ? 1 : 0, X.cond};
 }
 
 // ------------------------------------------------------------- launching ---
@@ -250,15 +299,49 @@ inline void set_smem(K kernel, size_t bytes) {
   if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
 }
 
+// Row pairs per CTA of a specialised row pass (at least 64 threads per CTA).
+template <typename T>
+inline int p2_pairs(const TBlockDev<T>& B) {
+  const int G = B.fx.L / kE;
+  return std::max(B.px, std::max(1, 64 / G));
+}
+template <typename T>
+inline bool row_p2(const TBlockDev<T>& B) { return B.fx.nstages > 0 && is_p2_length(B.fx.L); }
+template <typename T>
+inline bool col_p2(const TBlockDev<T>& B) { return B.fy.nstages > 0 && is_p2_length(B.fy.L); }
+
 template <typename T>
 struct Launcher {
   const Transforms<T>& t;
   cudaStream_t s;
   long long* counter;
 
+  // number of CTAs along x of a row pass over one block
+  int row_grid(const TBlockDev<T>& B) const {
+    const int P = row_p2(B) ? p2_pairs(B) : B.px;
+    return (B.rows + 2 * P - 1) / (2 * P);
+  }
+
   template <class Src>
   void row_forward(const TBlockDev<T>& a, const TBlockDev<T>* b, size_t smem, Src src, int cols,
                    const int* active) const {
+    if (row_p2(a) && (!b || row_p2(*b))) {
+      for (int bk = 0; bk < (b ? 2 : 1); ++bk) {
+        const TBlockDev<T>& B = bk ? *b : a;
+        const int P = p2_pairs(B), G = B.fx.L / kE;
+        const size_t sm = size_t(P) * B.fx.L * sizeof(cplx<T>);
+#define MACSAV_RF(LL)                                                                        \
+  {                                                                                          \
+    auto k = k_row_forward_p2<T, LL, Src>;                                                   \
+    set_smem(k, sm);                                                                         \
+    k<<<dim3(row_grid(B), cols), P * G, sm, s>>>(B, active, src, bk);                        \
+  }
+        MACSAV_P2_SWITCH(B.fx.L, MACSAV_RF)
+#undef MACSAV_RF
+        ++*counter;
+      }
+      return;
+    }
     RowArgs<T> r = row_args(a, b, active);
     auto k = k_row_forward<T, kVmax, Src>;
     set_smem(k, smem);
@@ -268,6 +351,23 @@ struct Launcher {
   template <class Dst, class Fin>
   void row_inverse(const TBlockDev<T>& a, const TBlockDev<T>* b, size_t smem, Dst dst, int cols, const int* active,
                    double* partial, Fin fin, unsigned int* done) const {
+    if (row_p2(a) && (!b || row_p2(*b)) && (!partial || !b)) {
+      for (int bk = 0; bk < (b ? 2 : 1); ++bk) {
+        const TBlockDev<T>& B = bk ? *b : a;
+        const int P = p2_pairs(B), G = B.fx.L / kE;
+        const size_t sm = size_t(P) * B.fx.L * sizeof(cplx<T>);
+#define MACSAV_RI(LL)                                                                        \
+  {                                                                                          \
+    auto k = k_row_inverse_p2<T, LL, Dst, Fin>;                                              \
+    set_smem(k, sm);                                                                         \
+    k<<<dim3(row_grid(B), cols), P * G, sm, s>>>(B, active, dst, bk, partial, fin, done);    \
+  }
+        MACSAV_P2_SWITCH(B.fx.L, MACSAV_RI)
+#undef MACSAV_RI
+        ++*counter;
+      }
+      return;
+    }
     RowArgs<T> r = row_args(a, b, active);
     auto k = k_row_inverse<T, kVmax, Dst, Fin>;
     set_smem(k, smem);
@@ -276,6 +376,24 @@ struct Launcher {
   }
   void column(const TBlockDev<T>& a, const TBlockDev<T>* b, size_t smem, int cols, const int* active, int mode,
               const double* shift, T thr) const {
+    if (col_p2(a) && (!b || col_p2(*b))) {
+      for (int bk = 0; bk < (b ? 2 : 1); ++bk) {
+        const TBlockDev<T>& B = bk ? *b : a;
+        const int NL = B.wy / 2, G = B.fy.L / kE;
+        const size_t sm = size_t(NL) * B.fy.L * sizeof(cplx<T>);
+        const int grid = (B.cols + B.wy - 1) / B.wy;
+#define MACSAV_CO(LL)                                                                        \
+  {                                                                                          \
+    auto k = k_column_p2<T, LL>;                                                             \
+    set_smem(k, sm);                                                                         \
+    k<<<dim3(grid, cols), NL * G, sm, s>>>(B, active, mode, shift, thr);                     \
+  }
+        MACSAV_P2_SWITCH(B.fy.L, MACSAV_CO)
+#undef MACSAV_CO
+        ++*counter;
+      }
+      return;
+    }
     ColArgs<T> r = col_args(a, b, active, mode, shift, thr);
     auto k = k_column<T, kVmax>;
     set_smem(k, smem);
@@ -305,7 +423,10 @@ struct Launcher {
   void column_p(int cols, const int* active, const double* shift, T thr) const {
     column(t.p, nullptr, t.smem_col_p, cols, active, W_POISSON, shift, thr);
   }
-  int groups_row_p() const { return (t.p.rows + 2 * t.p.px - 1) / (2 * t.p.px); }
+  int groups_row_p() const {
+    if (row_p2(t.p)) return row_grid(t.p);
+    return (t.p.rows + 2 * t.p.px - 1) / (2 * t.p.px);
+  }
 };
 
 }  // namespace macsav

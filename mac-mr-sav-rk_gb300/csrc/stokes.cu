@@ -28,55 +28,56 @@ inline int red_blocks(long long n) {
 }
 
 // ------------------------------------------------------------ CG kernels ---
+// abs_key of a T value (as the key of the same value in double).
+template <typename T>
+__device__ __forceinline__ unsigned long long abs_key_t(T v) {
+  if constexpr (sizeof(T) == 4) return abs_key(f2d_bits(v));
+  else return abs_key(v);
+}
+
 // b = rd - D w (rd: continuity defect of a correction solve, may be null);
 // last block: mean of b (OP_MEAN_B).
 template <typename T, typename WIn>
 __global__ void __launch_bounds__(kThreads) k_pressure_rhs(GridDev g, const WIn* w, long long ws, T* b, long long cs,
-                                                           const double* rd, double* partial, CGFin fin,
+                                                           const double* rd, double* partial, CGFin<T> fin,
                                                            unsigned int* done) {
-  __shared__ double red[64];
   const int c = blockIdx.y;
   const T ihx = T(g.ihx), ihy = T(g.ihy);
-  Acc<T> acc;
+  Acc<T> acc[1];
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < g.np; idx += gridDim.x * blockDim.x) {
     const int j = idx / g.nx, i = idx - j * g.nx;
     T v = -D_atT<T>(w + c * ws, g, j, i, ihx, ihy);
-    if (rd) v += T(rd[c * (long long)g.np + idx]);
+    if (rd) v += load_as<T>(rd + c * (long long)g.np + idx);
     b[c * cs + idx] = v;
-    acc.add(v);
+    acc[0].add(v);
   }
-  double s[1] = {acc.value()};
-  block_sum<1>(s, red);
-  if (threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = s[0];
+  write_sums<T, 1>(acc, partial, 1);
   last_block_finish(fin, done);
 }
 
 // b -= mean; x = 0; r = b; last block: ||b||, max|b| and the start (OP_START).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_cg_start(int np, T* b, T* x, T* r, long long cs, const CGScalars* cg,
-                                                       double* partial, CGFin fin, unsigned int* done) {
-  __shared__ double red[64];
+                                                       double* partial, CGFin<T> fin, unsigned int* done) {
   const int c = blockIdx.y;
-  const T mean = T(cg[c].mean_b);
-  Acc<T> s;
+  const T mean = cg_mean_b<T>(cg[c]);
+  Acc<T> s[1];
   T mt = T(0);
+  bool bad = false;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
     const long long i = c * cs + idx;
     const T v = b[i] - mean;
     b[i] = v;
     r[i] = v;
     x[i] = T(0);
-    s.add(v * v);
+    s[0].add(v * v);
     const T av = v < T(0) ? -v : v;
-    mt = (av != av || mt != mt) ? av + mt : (av > mt ? av : mt);
+    bad |= !(av == av);
+    mt = av > mt ? av : mt;
   }
-  double ss[1] = {s.value()}, m[1] = {double(mt)};
-  block_sum<1>(ss, red);
-  block_max<1>(m, red);
-  if (threadIdx.x == 0) {
-    partial[(c * gridDim.x + blockIdx.x) * 2] = ss[0];
-    partial[(c * gridDim.x + blockIdx.x) * 2 + 1] = m[0];
-  }
+  unsigned long long key[1] = {bad ? 0x7ff8000000000000ull : abs_key_t<T>(mt)};
+  write_sums<T, 1>(s, partial, 2);
+  write_keys<1>(key, partial, 2, 1);
   last_block_finish(fin, done);
 }
 
@@ -84,13 +85,12 @@ __global__ void __launch_bounds__(kThreads) k_cg_start(int np, T* b, T* x, T* r,
 template <typename T, typename WIn>
 __global__ void __launch_bounds__(kThreads) k_div_q(GridDev g, const WIn* w, long long ws, T* q, const T* z, const T* p,
                                                     long long cs, const CGScalars* cg, const int* active,
-                                                    double* partial, CGFin fin, unsigned int* done) {
-  __shared__ double red[96];
+                                                    double* partial, CGFin<T> fin, unsigned int* done) {
   const int c = blockIdx.y;
-  Acc<T> a0, a1, a2;
+  Acc<T> a[3];
   if (active[c]) {
     const bool first = cg[c].iters == 0;
-    const T beta = T(cg[c].beta);
+    const T beta = cg_beta<T>(cg[c]);
     const T ihx = T(g.ihx), ihy = T(g.ihy);
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < g.np; idx += gridDim.x * blockDim.x) {
       const int j = idx / g.nx, i = idx - j * g.nx;
@@ -98,19 +98,12 @@ __global__ void __launch_bounds__(kThreads) k_div_q(GridDev g, const WIn* w, lon
       const T qv = D_atT<T>(w + c * ws, g, j, i, ihx, ihy);
       q[k] = qv;
       const T pd = first ? z[k] : T(z[k] + beta * p[k]);
-      a0.add(pd * qv);
-      a1.add(qv);
-      a2.add(pd);
+      a[0].add(pd * qv);
+      a[1].add(qv);
+      a[2].add(pd);
     }
   }
-  double acc[3] = {a0.value(), a1.value(), a2.value()};
-  block_sum<3>(acc, red);
-  if (threadIdx.x == 0) {
-    double* o = partial + (c * gridDim.x + blockIdx.x) * 3;
-    o[0] = acc[0];
-    o[1] = acc[1];
-    o[2] = acc[2];
-  }
+  write_sums<T, 3>(a, partial, 3);
   last_block_finish(fin, done);
 }
 
@@ -119,13 +112,12 @@ __global__ void __launch_bounds__(kThreads) k_div_q(GridDev g, const WIn* w, lon
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_cg_update(int np, T* x, T* r, T* p, const T* z, const T* q,
                                                         long long cs, const CGScalars* cg, const int* active,
-                                                        double* partial, CGFin fin, unsigned int* done) {
-  __shared__ double red[64];
+                                                        double* partial, CGFin<T> fin, unsigned int* done) {
   const int c = blockIdx.y;
-  Acc<T> acc;
+  Acc<T> acc[1];
   if (active[c]) {
     const bool first = cg[c].iters == 0;
-    const T beta = T(cg[c].beta), alpha = T(cg[c].alpha), mq = T(cg[c].mean_q);
+    const T beta = cg_beta<T>(cg[c]), alpha = cg_alpha<T>(cg[c]), mq = cg_mean_q<T>(cg[c]);
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
       const long long k = c * cs + idx;
       const T pd = first ? z[k] : T(z[k] + beta * p[k]);
@@ -133,32 +125,28 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int np, T* x, T* r, T* p
       x[k] = x[k] + alpha * pd;
       const T rv = r[k] - alpha * (q[k] - mq);
       r[k] = rv;
-      acc.add(rv * rv);
+      acc[0].add(rv * rv);
     }
   }
-  double s[1] = {acc.value()};
-  block_sum<1>(s, red);
-  if (threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = s[0];
+  write_sums<T, 1>(acc, partial, 1);
   last_block_finish(fin, done);
 }
 
 // out = x - mean (the mean held in cg[c].mean_q when `center`); partial sum
-// of out; last block: the new mean (OP_MEAN_X).
+// of out; last block: the new mean (OP_MEAN_X).  FP64 output.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_center_cells(int np, const T* x, long long xs, double* out,
                                                            long long os, const CGScalars* cg, int center,
-                                                           double* partial, CGFin fin, unsigned int* done) {
-  __shared__ double red[64];
+                                                           double* partial, CGFin<double> fin, unsigned int* done) {
   const int c = blockIdx.y;
   const double mean = center ? cg[c].mean_q : 0.0;
-  double acc[1] = {0.0};
+  Acc<double> acc[1];
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
     const double v = double(x[c * xs + idx]) - mean;
     if (out) out[c * os + idx] = v;
-    acc[0] += v;
+    acc[0].add(v);
   }
-  block_sum<1>(acc, red);
-  if (threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = acc[0];
+  write_sums<double, 1>(acc, partial, 1);
   last_block_finish(fin, done);
 }
 
@@ -170,38 +158,37 @@ __global__ void __launch_bounds__(kThreads) k_shift_cells(int np, double* out, l
 }
 
 // Closing checks (tensor_stokes.py:329-351): defect = m u + k K u - D^T p - f.
-// Partial slots: max|defect|, max|f|, max|u|, max|D u|, nonfinite f, nonfinite u/p.
+// Key slots: max|defect|, max|f|, max|u|, max|D u|, nonfinite f, nonfinite u/p.
 __global__ void __launch_bounds__(kThreads) k_stokes_check(GridDev g, const double* vel, const double* pres,
                                                            const double* f, long long vs, long long ps,
-                                                           const double* shift, double* partial, CGFin fin,
-                                                           unsigned int* done) {
-  __shared__ double red[6 * 32];
+                                                           const double* shift, double* partial,
+                                                           CGFin<double> fin, unsigned int* done) {
   const int c = blockIdx.y;
   const double mass = shift[2 * c], visc = shift[2 * c + 1];
   const double* u = vel + c * vs;
   const double* pp = pres + c * ps;
   const double* ff = f + c * vs;
-  double m[6] = {0, 0, 0, 0, 0, 0};
+  unsigned long long m[6] = {0, 0, 0, 0, 0, 0};
+  constexpr unsigned long long kInf = 0x7ff0000000000000ull;
   const int n = g.size > g.np ? g.size : g.np;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
     if (idx < g.size) {
       const double fe = ff[idx], ue = u[idx];
       const double d = mass * ue + visc * K_at(u, g, idx) - Dt_at(pp, g, idx) - fe;
-      m[0] = nanmax(m[0], fabs(d));
-      m[1] = nanmax(m[1], fabs(fe));
-      m[2] = nanmax(m[2], fabs(ue));
-      if (!isfinite(fe)) m[4] = 1.0;
-      if (!isfinite(ue)) m[5] = 1.0;
+      const unsigned long long kf = abs_key(fe), ku = abs_key(ue);
+      m[0] = max(m[0], abs_key(d));
+      m[1] = max(m[1], kf);
+      m[2] = max(m[2], ku);
+      if (kf >= kInf) m[4] = 1;
+      if (ku >= kInf) m[5] = 1;
     }
     if (idx < g.np) {
       const int j = idx / g.nx, i = idx - j * g.nx;
-      m[3] = nanmax(m[3], fabs(D_at(u, g, j, i)));
-      if (!isfinite(pp[idx])) m[5] = 1.0;
+      m[3] = max(m[3], abs_key(D_at(u, g, j, i)));
+      if (abs_key(pp[idx]) >= kInf) m[5] = 1;
     }
   }
-  block_max<6>(m, red);
-  if (threadIdx.x == 0)
-    for (int k = 0; k < 6; ++k) partial[(c * gridDim.x + blockIdx.x) * 6 + k] = m[k];
+  write_keys<6>(m, partial, 6, 0);
   last_block_finish(fin, done);
 }
 
@@ -232,14 +219,14 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
   L.row_forward_p(SrcCells<T, T>{r, np, g.nx}, cols, P->active);
   L.column_p(cols, P->active, P->shift, T(P->pthr));
   L.row_inverse_p(DstCellsDot<T>{z, r, np, g.nx}, cols, P->active, P->partial,
-                  make_fin(P, X, OP_RHO, L.groups_row_p(), 2, cols), P->done_counter);
+                  make_fin<T>(P, X, OP_RHO, L.groups_row_p(), 2, cols), P->done_counter);
   // q = S pdir = D (mI+kK)^{-1} D^T pdir,  pdir = z + beta p
   velocity_inverse<T>(P, L, SrcLift<T, double, T>{nullptr, 0, z, pd, P->cg, np, g.nx, g.nu, T(g.ihx), T(g.ihy)}, w,
                       sz, cols, P->active);
   k_div_q<T, T><<<dim3(rb, cols), kThreads, 0, s>>>(g, w, sz, q, z, pd, np, P->cg, P->active, P->partial,
-                                                    make_fin(P, X, OP_ALPHA, rb, 3, cols), P->done_counter);
+                                                    make_fin<T>(P, X, OP_ALPHA, rb, 3, cols), P->done_counter);
   k_cg_update<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, x, r, pd, z, q, np, P->cg, P->active, P->partial,
-                                                     make_fin(P, X, OP_CHECK, rb, 1, cols), P->done_counter);
+                                                     make_fin<T>(P, X, OP_CHECK, rb, 1, cols), P->done_counter);
   P->launches += 2;
 }
 
@@ -256,11 +243,11 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
   const int rb = red_blocks(np);
   const cudaStream_t s = X.s;
   k_pressure_rhs<T, T><<<dim3(rb, cols), kThreads, 0, s>>>(g, w, sz, b, np, rd, P->partial,
-                                                           make_fin(P, X, OP_MEAN_B, rb, 1, cols), P->done_counter);
+                                                           make_fin<T>(P, X, OP_MEAN_B, rb, 1, cols), P->done_counter);
   ++P->launches;
   if (!X.graph) {
     k_cg_start<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, b, x, r, np, P->cg, P->partial,
-                                                      make_fin(P, X, OP_START, rb, 2, cols), P->done_counter);
+                                                      make_fin<T>(P, X, OP_START, rb, 2, cols), P->done_counter);
     ++P->launches;
     for (int it = 0; it < P->maxit; ++it) {
       cudaMemcpyAsync(P->h_active, P->active, sizeof(int) * cols, cudaMemcpyDeviceToHost, s);
@@ -284,7 +271,7 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
     return MACSAV_ERR_CUDA;
   // k_cg_start's last block sets the loop condition
   k_cg_start<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, b, x, r, np, P->cg, P->partial,
-                                                    make_fin(P, X, OP_START, rb, 2, cols), P->done_counter);
+                                                    make_fin<T>(P, X, OP_START, rb, 2, cols), P->done_counter);
   ++P->launches;
   if (cudaStreamGetCaptureInfo(s, &st, nullptr, &graph, &deps, nullptr, &ndeps) != cudaSuccess)
     return MACSAV_ERR_CUDA;
@@ -316,9 +303,9 @@ static void finish_pressure(Plan* P, const Exec& X, const T* x, double* pres, in
   const int rb = red_blocks(np);
   const cudaStream_t s = X.s;
   k_center_cells<T><<<dim3(rb, cols), kThreads, 0, s>>>(P->g.np, x, np, nullptr, np, P->cg, 0, P->partial,
-                                                        make_fin(P, X, OP_MEAN_X, rb, 1, cols), P->done_counter);
+                                                        make_fin<double>(P, X, OP_MEAN_X, rb, 1, cols), P->done_counter);
   k_center_cells<T><<<dim3(rb, cols), kThreads, 0, s>>>(P->g.np, x, np, pres, np, P->cg, 1, P->partial,
-                                                        make_fin(P, X, OP_MEAN_X, rb, 1, cols), P->done_counter);
+                                                        make_fin<double>(P, X, OP_MEAN_X, rb, 1, cols), P->done_counter);
   k_shift_cells<<<dim3(rb, cols), kThreads, 0, s>>>(P->g.np, pres, np, P->cg);
   P->launches += 3;
 }
@@ -328,7 +315,7 @@ static void closing_checks(Plan* P, const Exec& X, const double* f, const double
   const long long n = P->g.size > P->g.np ? P->g.size : P->g.np;
   const int rb = red_blocks(n);
   k_stokes_check<<<dim3(rb, cols), kThreads, 0, X.s>>>(P->g, vel, pres, f, P->g.size, P->g.np, shift, P->partial,
-                                                       make_fin(P, X, OP_CHECKS, rb, 6, cols), P->done_counter);
+                                                       make_fin<double>(P, X, OP_CHECKS, rb, 6, cols), P->done_counter);
   ++P->launches;
 }
 

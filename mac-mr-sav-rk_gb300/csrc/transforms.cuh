@@ -211,7 +211,6 @@ template <typename T, int VMAX, class Dst, class Fin>
 __global__ void __launch_bounds__(kFFTThreads, sizeof(T) == 4 ? 2 : 1) k_row_inverse(RowArgs<T> a, Dst dst, double* partial, Fin fin,
                                                              unsigned int* counter) {
   const int c = blockIdx.y;
-  __shared__ double red[64];
   const bool live = !a.active || a.active[c];
   Acc<T> acc[2];
   if (live) {
@@ -281,13 +280,7 @@ __global__ void __launch_bounds__(kFFTThreads, sizeof(T) == 4 ? 2 : 1) k_row_inv
     }
   }
   if (partial) {
-    double v[2] = {acc[0].value(), acc[1].value()};
-    block_sum<2>(v, red);
-    if (threadIdx.x == 0) {
-      const int slot = (c * gridDim.x + blockIdx.x) * 2;
-      partial[slot] = v[0];
-      partial[slot + 1] = v[1];
-    }
+    write_sums<T, 2>(acc, partial, 2);
     last_block_finish(fin, counter);
   }
 }

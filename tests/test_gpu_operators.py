@@ -195,3 +195,21 @@ def test_stokes_fp32_mixed_meets_gates_and_matches(env, name):
             assert rel <= 1e-9, (name, k, rel)
         assert r.residual <= tol and r.divergence_inf <= tol * (1 + np.abs(r.velocity).max())
         assert solver.last_refinements >= 1
+
+
+@pytest.mark.parametrize("shape", [(256, 128, 2.0, 1.0), (512, 64, 8.0, 1.0), (96, 192, 0.5, 1.0),
+                                   (1024, 32, 32.0, 1.0)])
+def test_stokes_power_of_two_kernels_match_oracle(env, shape):
+    """Larger grids exercise the compile-time-length FFT kernels (L = 64..2048)
+    and the runtime-radix fallback (96, 192); checked against the oracle."""
+    pkg, stokes, lib, torch = env
+    nx, ny, lx, ly = shape
+    og = O.Grid(nx, ny, lx, ly)
+    rng = np.random.default_rng(nx + ny)
+    rhs = rng.normal(size=(og.size, 2))
+    ref = O.TensorStokesOracle(og, 1e-9, 1e-12).solve(rhs, mass=1.0, viscosity=3e-4)
+    for precision, bar in (("fp64", 1e-11), ("fp32", 1e-9)):
+        solver = stokes.TensorStokes(pkg.MACGrid(nx, ny, lx, ly), tolerance=1e-9, precision=precision)
+        got = solver.solve(rhs, mass=1.0, viscosity=3e-4)
+        for a, b in ((got.velocity, ref.velocity), (got.pressure, ref.pressure)):
+            assert np.linalg.norm(a - b) / np.linalg.norm(b) < bar, precision
