@@ -172,6 +172,13 @@ int macsav_step(macsav_plan* plan, int scheme, double t, double dt, double nu, d
  * (these need a MACSAV_FP32_MIXED plan), 3: FP64 column pass.  Synchronises. */
 int macsav_time_pass(macsav_plan* plan, int pass, int reps, double* ms, double* bytes, void* stream);
 
+/* FP32_MIXED only (no reference counterpart: the reference solves in FP64):
+ * number of FP64 defect-correction sweeps after the first FP32 solve
+ * (default 2) and the relative Krylov tolerance of each FP32 inner solve
+ * (default 1e-4).  The closing FP64 gates are unchanged, so too few sweeps
+ * surface as the reference's Stokes-gate error, never as a silent loss. */
+int macsav_plan_set_refinement(macsav_plan* plan, int corrections, double inner_krylov_tolerance);
+
 /* Run macsav_step as one captured CUDA graph per (scheme, force, embedded)
  * (the pressure CG loop becomes a conditional WHILE node).  Default: off. */
 int macsav_plan_set_graph(macsav_plan* plan, int enable);

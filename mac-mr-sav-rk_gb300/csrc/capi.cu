@@ -253,6 +253,17 @@ int macsav_time_pass(macsav_plan* plan, int pass, int reps, double* ms, double* 
   return rc == MACSAV_ERR_CUDA ? cuda_status(&plan->p) : rc;
 }
 
+int macsav_plan_set_refinement(macsav_plan* plan, int corrections, double inner_krylov_tolerance) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  if (corrections < 0 || corrections > 8 || !(inner_krylov_tolerance > 0) || !(inner_krylov_tolerance < 1))
+    return fail(&plan->p, MACSAV_ERR_VALUE, "corrections must be in 0..8 and 0 < inner tolerance < 1");
+  plan->p.corrections = corrections;
+  plan->p.inner_ktol = inner_krylov_tolerance;
+  for (auto& kv : plan->p.st.graphs) cudaGraphExecDestroy(kv.exec);  // captured with the old sweep count
+  plan->p.st.graphs.clear();
+  return MACSAV_OK;
+}
+
 int macsav_plan_set_graph(macsav_plan* plan, int enable) {
   if (!plan) return MACSAV_ERR_VALUE;
   plan->p.use_graph = enable ? 1 : 0;

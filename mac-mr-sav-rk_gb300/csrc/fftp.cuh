@@ -218,8 +218,8 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_inverse_p2(TBlockDev<T> B, 
         const int e = base + u * blockDim.x;
         if (e < total) {
           const int q = B.fcols.div(e), n = e - q * N, ra = row0 + 2 * q;
-          dst.store(bk, c, ra, n, value_inverse(z + q * L, kind, N, n, 0), xa[u], acc);
-          if (ra + 1 < rows) dst.store(bk, c, ra + 1, n, value_inverse(z + q * L, kind, N, n, 1), xb[u], acc);
+          dst.store(bk, c, ra, n, value_inverse(z + q * L, kind, N, n, 0, B.sx), xa[u], acc);
+          if (ra + 1 < rows) dst.store(bk, c, ra + 1, n, value_inverse(z + q * L, kind, N, n, 1, B.sx), xb[u], acc);
         }
       }
     }
@@ -341,14 +341,14 @@ __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const
 #pragma unroll
       for (int k = 0; k < V; ++k) {
         const int j = jv * V + k;
-        comp[k] = value_inverse(z + (j >> 1) * L, kind, N, n, j & 1);
+        comp[k] = value_inverse(z + (j >> 1) * L, kind, N, n, j & 1, B.sy);
       }
       *reinterpret_cast<vec_t*>(H + n * pitch + col0 + jv * V) = v;
     }
   } else {
     for (int e = threadIdx.x; e < N * W; e += blockDim.x) {
       const int n = B.fw.div(e), j = e - n * W;
-      if (j < ncols) H[n * pitch + col0 + j] = value_inverse(z + (j >> 1) * L, kind, N, n, j & 1);
+      if (j < ncols) H[n * pitch + col0 + j] = value_inverse(z + (j >> 1) * L, kind, N, n, j & 1, B.sy);
     }
   }
 }

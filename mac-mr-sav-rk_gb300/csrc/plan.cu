@@ -83,6 +83,8 @@ static cudaError_t build_block(TBlockDev<T>& B, int rows, int cols, int kx, int 
   B.fw = FastDiv(B.wy);
   B.fvpr = FastDiv(std::max(1, B.wy / int(16 / sizeof(T))));
   B.fhalf = FastDiv(rows / 2 + 1);
+  B.sx = T(kx == KIND_DST1 ? 1.0 / (cols + 1) : 1.0 / cols);
+  B.sy = T(ky == KIND_DST1 ? 1.0 / (rows + 1) : 1.0 / rows);
   // host tables
   std::vector<cplx<T>> twx(Lx), twy(Ly), qx(cols), qy(rows);
   for (int m = 0; m < Lx; ++m) twx[m] = mk(T(std::cos(2 * kPi * m / Lx)), T(-std::sin(2 * kPi * m / Lx)));
@@ -164,11 +166,14 @@ static void free_transforms(Transforms<T>& t) {
   t.H = nullptr;
 }
 
+void set_reduction_cap(int sms);
+
 int plan_build(Plan* p) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) { p->err = std::string("CUDA: ") + cudaGetErrorString(e); return MACSAV_ERR_CUDA; }
+  set_reduction_cap(p->num_sms);
   GridDev& g = p->g;
   const int largest = std::max(fft_length(KIND_DST1, g.nx - 1), fft_length(KIND_DST1, g.ny - 1));
   if (largest > 4096) { p->err = "grid too large: FFT length above 4096"; return MACSAV_ERR_UNSUPPORTED; }

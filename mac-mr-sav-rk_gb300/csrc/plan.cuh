@@ -75,7 +75,7 @@ struct Plan {
   double tol, ktol;
   int maxit, maxcols;
   // FP32_MIXED: inner FP32 Krylov tolerance and defect-correction sweeps
-  double inner_ktol = 1e-5;
+  double inner_ktol = 1e-4;
   int corrections = 2;
   int num_sms;
   std::string err;

@@ -165,8 +165,18 @@ struct CGFin {
           }
         }
       }
-      block_sum_p<T, 6>(s, red);
-      if (mm) block_max_key<6>(m, redk);
+      // fold only the slots in use (K <= 6)
+      for (int k = 0; k < K; ++k) {
+        if ((mm >> k) & 1) {
+          unsigned long long one[1] = {m[k]};
+          block_max_key<1>(one, redk);
+          m[k] = one[0];
+        } else {
+          typename R::P one[1] = {s[k]};
+          block_sum_p<T, 1>(one, red);
+          s[k] = one[0];
+        }
+      }
       if (threadIdx.x == 0) {
         double sv[6], mv[6];
 #pragma unroll

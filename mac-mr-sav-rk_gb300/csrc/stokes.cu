@@ -20,12 +20,15 @@
 
 namespace macsav {
 
-constexpr int kRedMax = 1024;  // cap on blocks of grid-stride reduction kernels
-
+// Blocks of a grid-stride reduction kernel: enough to fill every SM twice,
+// no more (each block costs a block-level reduction, and the last block folds
+// one partial per block).
+static int g_red_cap = 304;
 inline int red_blocks(long long n) {
   long long b = (n + kThreads - 1) / kThreads;
-  return int(b < 1 ? 1 : (b > kRedMax ? kRedMax : b));
+  return int(b < 1 ? 1 : (b > g_red_cap ? g_red_cap : b));
 }
+void set_reduction_cap(int sms) { g_red_cap = sms > 0 ? 2 * sms : 304; }
 
 // ------------------------------------------------------------ CG kernels ---
 // abs_key of a T value (as the key of the same value in double).

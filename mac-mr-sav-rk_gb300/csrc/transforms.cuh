@@ -47,6 +47,7 @@ struct TBlockDev {
   int wy;              // columns per CTA in the column pass (even)
   int groups;          // CTAs of this block in the current pass
   FastDiv fcols, frows, fw, fvpr, fhalf;  // divisors of the element loops
+  T sx, sy;            // inverse normalisation of the x / y transforms
 };
 
 __device__ __forceinline__ int makhoul_pos(int n, int N) { return (n & 1) ? N - 1 - (n >> 1) : (n >> 1); }
@@ -111,28 +112,34 @@ __device__ __forceinline__ cplx<T> pre_inverse(T yak, T yam, T ybk, T ybm, cplx<
 }
 
 // Inverse post-processing: real value n of line a (part 0) or b (part 1),
-// after an unscaled inverse FFT (DCT kinds) or a forward FFT (DST-I).
+// after an unscaled inverse FFT (DCT kinds) or a forward FFT (DST-I); `scale`
+// is the normalisation 1/N (DCT kinds) or 1/(N+1) (DST-I), precomputed.
 template <typename T>
-__device__ __forceinline__ T value_inverse(const cplx<T>* z, int kind, int N, int n, int part) {
+__device__ __forceinline__ T value_inverse(const cplx<T>* z, int kind, int N, int n, int part, T scale) {
   if (kind == KIND_DST1) {
     const cplx<T> Z = z[n + 1];
-    const T s = T(1) / T(N + 1);
-    return part == 0 ? -Z.y * s : Z.x * s;
+    return part == 0 ? -Z.y * scale : Z.x * scale;
   }
   const cplx<T> Z = z[makhoul_pos(n, N)];
-  T v = (part == 0 ? Z.x : Z.y) / T(N);
+  T v = (part == 0 ? Z.x : Z.y) * scale;
   if (kind == KIND_DST2 && (n & 1)) v = -v;
   return v;
 }
 
 __device__ __forceinline__ int inverse_sign(int kind) { return kind == KIND_DST1 ? -1 : 1; }
 
-// Spectral weight of mode (ky, kx).
+// Spectral weight of mode (ky, kx).  The FP32 path (an inexact inner solve
+// under FP64 defect correction) uses the hardware reciprocal; FP64 divides.
+template <typename T>
+__device__ __forceinline__ T recip(T x) {
+  if constexpr (sizeof(T) == 4) return __frcp_rn(x);
+  else return T(1) / x;
+}
 template <typename T>
 __device__ __forceinline__ T spectral_weight(int mode, T mass, T visc, T thr, T ey, T ex) {
   const T lam = ey + ex;
-  if (mode == W_HELMHOLTZ) return T(1) / (mass + visc * lam);
-  return lam > thr ? mass / lam + visc : T(0);
+  if (mode == W_HELMHOLTZ) return recip(mass + visc * lam);
+  return lam > thr ? mass * recip(lam) + visc : T(0);
 }
 
 // ============================================================ row passes ====
@@ -273,8 +280,8 @@ __global__ void __launch_bounds__(kFFTThreads, sizeof(T) == 4 ? 2 : 1) k_row_inv
         const int e = base + u * blockDim.x;
         if (e < total) {
           const int q = B.fcols.div(e), n = e - q * N, ra = row0 + 2 * q;
-          dst.store(b, c, ra, n, value_inverse(z + q * LS, kind, N, n, 0), xa[u], acc);
-          if (ra + 1 < rows) dst.store(b, c, ra + 1, n, value_inverse(z + q * LS, kind, N, n, 1), xb[u], acc);
+          dst.store(b, c, ra, n, value_inverse(z + q * LS, kind, N, n, 0, B.sx), xa[u], acc);
+          if (ra + 1 < rows) dst.store(b, c, ra + 1, n, value_inverse(z + q * LS, kind, N, n, 1, B.sx), xb[u], acc);
         }
       }
     }
@@ -406,14 +413,14 @@ __global__ void __launch_bounds__(kFFTThreads, sizeof(T) == 4 ? 2 : 1) k_column(
 #pragma unroll
       for (int k = 0; k < V; ++k) {
         const int j = jv * V + k;
-        comp[k] = value_inverse(z + (j >> 1) * LS, kind, N, n, j & 1);
+        comp[k] = value_inverse(z + (j >> 1) * LS, kind, N, n, j & 1, B.sy);
       }
       *reinterpret_cast<vec_t*>(H + n * pitch + col0 + jv * V) = v;
     }
   } else {
     for (int e = threadIdx.x; e < N * W; e += blockDim.x) {
       const int n = B.fw.div(e), j = e - n * W;
-      if (j < ncols) H[n * pitch + col0 + j] = value_inverse(z + (j >> 1) * LS, kind, N, n, j & 1);
+      if (j < ncols) H[n * pitch + col0 + j] = value_inverse(z + (j >> 1) * LS, kind, N, n, j & 1, B.sy);
     }
   }
 }
