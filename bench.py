@@ -144,6 +144,27 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def profile_steps(precision: str) -> None:
+    """Two eager steps of the bench workload (the launch list and kernel
+    captures of profiles/ come from this)."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    pkg = __graft_entry__.load_package()
+    w = WORKLOAD
+    g = pkg.MACGrid(w["nx"], w["ny"], w["lx"], w["ly"])
+    model = pkg.MACNavierStokes(g, w["nu"], precision=precision, use_graph=False)
+    scheme = pkg.make_scheme(w["scheme"])
+    x = torch.from_numpy(initial_state(pkg)).to("cuda")
+    t, r = 0.0, 0.0
+    for _ in range(2):
+        x, r, recs, _, _ = scheme.step_device(model, x, t, r, w["dt"], want_embedded=False)
+        t += w["dt"]
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": precision, "launches": model.plan.launches,
+                      "iterations": [list(rc.iterations[:2]) for rc in recs]}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -151,9 +172,14 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", choices=["fp32", "fp64"], default=None,
+                    help="run two eager steps of the workload and exit (for ncu captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.profile:
+        profile_steps(args.profile)
         return
     if args.warmup < 3:
         args.warmup = 3

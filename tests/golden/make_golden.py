@@ -149,7 +149,36 @@ def config1(steps: int = 100) -> None:
          iterations=np.array(model.backend.total_iterations))
 
 
+def adaptive() -> None:
+    """integrate_adaptive with the tensor backend: I control (the reference
+    test's controls) and PI control on a rectangle, seeded periodic forcing."""
+    from solver.adaptivity import IController, PIController, integrate_adaptive
+    cases = {"i_sdirk3": (12, 10, 1.3, 0.8, "sdirk3", dict(atol=1e-12, rtol=1e-8, min_step=1e-7, max_step=.002),
+                          False, 0.002, 0.002),
+             "pi_sdirk3_mrsav": (32, 16, 2.0, 1.0, "sdirk3_mrsav", dict(rtol=1e-5, atol=1e-8), True, 0.01, 1e-3)}
+    out = {}
+    for tag, (nx, ny, lx, ly, scheme, ctl, pi, T, dt0) in cases.items():
+        g = MACGrid(nx, ny, lx, ly)
+        base = np.random.default_rng(nx * ny).normal(size=g.size)
+        model = MACNavierStokes(g, 0.1 if nx == 12 else 5e-3)
+        model.backend = TensorStokes(model.ops, tolerance=1e-9, krylov_tolerance=1e-12)
+        model.force = lambda t, base=base: np.cos(2.0 * t) * base
+        x0 = 0.2 * fields.packed_curl_velocity(nx, ny, lx, ly, 3, 5)
+        controller = (PIController if pi else IController)(**ctl)
+        res = integrate_adaptive(model, make_scheme(scheme), model.state(0.0, x0, 0.1 if "mrsav" in scheme else 0.0),
+                                 T, dt0, controller=controller)
+        assert res.status == "complete", res.error
+        out.update({f"{tag}_shape": [nx, ny, lx, ly], f"{tag}_base": base, f"{tag}_x0": x0,
+                    f"{tag}_accepted": np.array([a["accepted"] for a in res.attempts]),
+                    f"{tag}_steps": np.array([a["step"] for a in res.attempts]),
+                    f"{tag}_errors": np.array([a["error"] for a in res.attempts]),
+                    f"{tag}_x_final": model.vector(res.final), f"{tag}_r_final": res.final.r,
+                    f"{tag}_t_final": res.final.t, f"{tag}_nu": model.nu})
+    save("adaptive", **out)
+
+
 if __name__ == "__main__":
+    adaptive()
     operators()
     stokes()
     scalar()
