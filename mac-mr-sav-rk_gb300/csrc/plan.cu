@@ -209,6 +209,11 @@ int plan_build(Plan* p) {
     if ((e = cudaMallocHost(&p->h_active, sizeof(int) * C))) goto fail;
     if ((e = cudaMallocHost(&p->h_err, sizeof(int)))) goto fail;
     if ((e = cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming))) goto fail;
+    for (int k = 0; k < 2; ++k) {
+      if ((e = cudaStreamCreateWithFlags(&p->aux[k], cudaStreamNonBlocking))) goto fail;
+      if ((e = cudaEventCreateWithFlags(&p->evf[k], cudaEventDisableTiming))) goto fail;
+      if ((e = cudaEventCreateWithFlags(&p->evj[k], cudaEventDisableTiming))) goto fail;
+    }
   }
   // Poisson zero-mode threshold: 100 eps max(lambda) (tensor_stokes.py:165-168)
   {
@@ -238,6 +243,13 @@ void plan_free(Plan* p) {
   p->done_counter = nullptr;
   cudaFreeHost(p->h_cg); cudaFreeHost(p->h_checks); cudaFreeHost(p->h_active); cudaFreeHost(p->h_err);
   if (p->done) cudaEventDestroy(p->done);
+  for (int k = 0; k < 2; ++k) {
+    if (p->aux[k]) cudaStreamDestroy(p->aux[k]);
+    if (p->evf[k]) cudaEventDestroy(p->evf[k]);
+    if (p->evj[k]) cudaEventDestroy(p->evj[k]);
+    p->aux[k] = nullptr;
+    p->evf[k] = p->evj[k] = nullptr;
+  }
   p->w = p->vel = p->cells = p->partial = p->shift = nullptr;
   p->cells32 = p->w32 = nullptr;
   p->cg = nullptr; p->checks = nullptr; p->active = p->errword = nullptr;

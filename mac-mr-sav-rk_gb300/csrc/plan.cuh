@@ -97,6 +97,9 @@ struct Plan {
   double* shift = nullptr;
   int* errword = nullptr;
   unsigned int* done_counter = nullptr;  // last-block counter of reductions
+  // fork streams/events for concurrent u/v passes: [0] main stream, [1] CG body
+  cudaStream_t aux[2] = {nullptr, nullptr};
+  cudaEvent_t evf[2] = {nullptr, nullptr}, evj[2] = {nullptr, nullptr};
   // pinned host mirrors
   CGScalars* h_cg = nullptr;
   SolveChecks* h_checks = nullptr;

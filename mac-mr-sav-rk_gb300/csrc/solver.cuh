@@ -325,6 +325,25 @@ struct Launcher {
   const Transforms<T>& t;
   cudaStream_t s;
   long long* counter;
+  // Optional fork stream: the u- and v-block passes are independent, so they
+  // run concurrently (s2 joins and leaves through events; graph-capturable).
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ef = nullptr, ej = nullptr;
+
+  template <class F>
+  void two_blocks(F launch_one) const {
+    if (s2) {
+      cudaEventRecord(ef, s);
+      cudaStreamWaitEvent(s2, ef, 0);
+      launch_one(0, s);
+      launch_one(1, s2);
+      cudaEventRecord(ej, s2);
+      cudaStreamWaitEvent(s, ej, 0);
+    } else {
+      launch_one(0, s);
+      launch_one(1, s);
+    }
+  }
 
   // number of CTAs along x of a row pass over one block
   int row_grid(const TBlockDev<T>& B) const {
@@ -336,7 +355,7 @@ struct Launcher {
   void row_forward(const TBlockDev<T>& a, const TBlockDev<T>* b, size_t smem, Src src, int cols,
                    const int* active) const {
     if (row_p2(a) && (!b || row_p2(*b))) {
-      for (int bk = 0; bk < (b ? 2 : 1); ++bk) {
+      auto one = [&](int bk, cudaStream_t st) {
         const TBlockDev<T>& B = bk ? *b : a;
         const int P = p2_pairs(B), G = B.fx.L / kE;
         const size_t sm = size_t(P) * B.fx.L * sizeof(cplx<T>);
@@ -344,12 +363,14 @@ struct Launcher {
   {                                                                                          \
     auto k = k_row_forward_p2<T, LL, Src>;                                                   \
     set_smem(k, sm);                                                                         \
-    k<<<dim3(row_grid(B), cols), P * G, sm, s>>>(B, active, src, bk);                        \
+    k<<<dim3(row_grid(B), cols), P * G, sm, st>>>(B, active, src, bk);                       \
   }
         MACSAV_P2_SWITCH(B.fx.L, MACSAV_RF)
 #undef MACSAV_RF
         ++*counter;
-      }
+      };
+      if (b) two_blocks(one);
+      else one(0, s);
       return;
     }
     RowArgs<T> r = row_args(a, b, active);
@@ -362,7 +383,7 @@ struct Launcher {
   void row_inverse(const TBlockDev<T>& a, const TBlockDev<T>* b, size_t smem, Dst dst, int cols, const int* active,
                    double* partial, Fin fin, unsigned int* done) const {
     if (row_p2(a) && (!b || row_p2(*b)) && (!partial || !b)) {
-      for (int bk = 0; bk < (b ? 2 : 1); ++bk) {
+      auto one = [&](int bk, cudaStream_t st) {
         const TBlockDev<T>& B = bk ? *b : a;
         const int P = p2_pairs(B), G = B.fx.L / kE;
         const size_t sm = size_t(P) * B.fx.L * sizeof(cplx<T>);
@@ -370,12 +391,14 @@ struct Launcher {
   {                                                                                          \
     auto k = k_row_inverse_p2<T, LL, Dst, Fin>;                                              \
     set_smem(k, sm);                                                                         \
-    k<<<dim3(row_grid(B), cols), P * G, sm, s>>>(B, active, dst, bk, partial, fin, done);    \
+    k<<<dim3(row_grid(B), cols), P * G, sm, st>>>(B, active, dst, bk, partial, fin, done);   \
   }
         MACSAV_P2_SWITCH(B.fx.L, MACSAV_RI)
 #undef MACSAV_RI
         ++*counter;
-      }
+      };
+      if (b) two_blocks(one);
+      else one(0, s);
       return;
     }
     RowArgs<T> r = row_args(a, b, active);
@@ -387,7 +410,7 @@ struct Launcher {
   void column(const TBlockDev<T>& a, const TBlockDev<T>* b, size_t smem, int cols, const int* active, int mode,
               const double* shift, T thr) const {
     if (col_p2(a) && (!b || col_p2(*b))) {
-      for (int bk = 0; bk < (b ? 2 : 1); ++bk) {
+      auto one = [&](int bk, cudaStream_t st) {
         const TBlockDev<T>& B = bk ? *b : a;
         const int NL = B.wy / 2, G = B.fy.L / kE;
         const size_t sm = size_t(NL) * B.fy.L * sizeof(cplx<T>);
@@ -396,12 +419,14 @@ struct Launcher {
   {                                                                                          \
     auto k = k_column_p2<T, LL>;                                                             \
     set_smem(k, sm);                                                                         \
-    k<<<dim3(grid, cols), NL * G, sm, s>>>(B, active, mode, shift, thr);                     \
+    k<<<dim3(grid, cols), NL * G, sm, st>>>(B, active, mode, shift, thr);                    \
   }
         MACSAV_P2_SWITCH(B.fy.L, MACSAV_CO)
 #undef MACSAV_CO
         ++*counter;
-      }
+      };
+      if (b) two_blocks(one);
+      else one(0, s);
       return;
     }
     ColArgs<T> r = col_args(a, b, active, mode, shift, thr);

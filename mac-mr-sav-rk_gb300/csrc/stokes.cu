@@ -290,7 +290,7 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   if (cudaStreamBeginCaptureToGraph(X.side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
     return MACSAV_ERR_CUDA;
-  Launcher<T> Ls{L.t, X.side, L.counter};
+  Launcher<T> Ls{L.t, X.side, L.counter, P->aux[1], P->evf[1], P->evj[1]};
   Exec Xs = X;
   Xs.s = X.side;
   cg_iteration<T>(P, Xs, Ls, w, cells, cols);
@@ -327,7 +327,7 @@ static void closing_checks(Plan* P, const Exec& X, const double* f, const double
 // solve and the captured stage.
 int enqueue_solve_fp64(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres) {
   const GridDev& g = P->g;
-  Launcher<double> L{P->t64, X.s, &P->launches};
+  Launcher<double> L{P->t64, X.s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
   const long long sz = g.size;
   velocity_inverse<double>(P, L, SrcPacked<double, double>{f, sz, g.nu, g.nx - 1, g.nx}, P->w, sz, cols, nullptr);
   int rc = schur_pcg<double>(P, X, L, P->w, P->cells, cols);
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(kThreads) k_accumulate(const T* src, double* d
 // the pressure correction (x) in the float cell buffer.
 static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, int cols, float* w2) {
   const GridDev& g = P->g;
-  Launcher<float> L{P->t32, X.s, &P->launches};
+  Launcher<float> L{P->t32, X.s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
   const long long sz = g.size, np = g.np;
   float* w = P->w32;
   velocity_inverse<float>(P, L, SrcPacked<float, double>{ru, sz, g.nu, g.nx - 1, g.nx}, w, sz, cols, nullptr);
@@ -451,14 +451,14 @@ int time_pass(Plan* P, int pass, int reps, cudaStream_t s, double* ms, double* b
   cudaEventCreate(&b);
   const double n = double(g.size) * cols;
   auto run = [&](int k) {
-    if (pass == 0) Launcher<float>{P->t32, s, &P->launches}.column_uv(cols, nullptr, P->shift);
+    if (pass == 0) Launcher<float>{P->t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.column_uv(cols, nullptr, P->shift);
     else if (pass == 1)
-      Launcher<float>{P->t32, s, &P->launches}.row_forward_uv(SrcPacked<float, double>{P->w, g.size, g.nu, g.nx - 1,
+      Launcher<float>{P->t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.row_forward_uv(SrcPacked<float, double>{P->w, g.size, g.nu, g.nx - 1,
                                                                                         g.nx}, cols, nullptr);
     else if (pass == 2)
-      Launcher<float>{P->t32, s, &P->launches}.row_inverse_uv(DstPacked<float, float>{P->w32, g.size, g.nu,
+      Launcher<float>{P->t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.row_inverse_uv(DstPacked<float, float>{P->w32, g.size, g.nu,
                                                                                       g.nx - 1, g.nx}, cols, nullptr);
-    else Launcher<double>{P->t64, s, &P->launches}.column_uv(cols, nullptr, P->shift);
+    else Launcher<double>{P->t64, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.column_uv(cols, nullptr, P->shift);
     (void)k;
   };
   run(0);  // warm-up
