@@ -164,6 +164,17 @@ int macsav_step(macsav_plan* plan, int scheme, double t, double dt, double nu, d
                 double r0, const double* forces, double* x1, double* embedded, double* pressures,
                 macsav_stage_record* records, double* r1, void* stream);
 
+/* macsav_step split in two, so that many plans (an ensemble of cavities, one
+ * plan each) can have their steps in flight at once: _enqueue issues the step
+ * on the plan's own stream (in graph mode without any host wait) and returns;
+ * _finish waits for it and fills records / r1 as macsav_step does.  One step
+ * per plan may be in flight.  Arguments as for macsav_step (the reference's
+ * Scheme.step, see above); there the ensemble is a loop over models. */
+int macsav_step_enqueue(macsav_plan* plan, int scheme, double t, double dt, double nu, double gamma,
+                        const double* x0, double r0, const double* forces, double* x1, double* embedded,
+                        double* pressures, void* stream);
+int macsav_step_finish(macsav_plan* plan, macsav_stage_record* records, double* r1);
+
 /* Measurement helper (no reference counterpart: it times this library's own
  * kernels for the roofline): average device milliseconds of `reps`
  * back-to-back launches of one transform pass over the velocity blocks with two

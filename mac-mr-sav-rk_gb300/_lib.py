@@ -58,6 +58,8 @@ _SIGNATURES = {
     "macsav_diagnostics": (_I, [_P, _P, _D, _D, _P, C.POINTER(_D), _P]),
     "macsav_step": (_I, [_P, _I, _D, _D, _D, _D, _P, _D, _P, _P, _P, _P, C.POINTER(StageRecord), C.POINTER(_D), _P]),
     "macsav_plan_set_graph": (_I, [_P, _I]),
+    "macsav_step_enqueue": (_I, [_P, _I, _D, _D, _D, _D, _P, _D, _P, _P, _P, _P, _P]),
+    "macsav_step_finish": (_I, [_P, C.POINTER(StageRecord), C.POINTER(_D)]),
     "macsav_time_pass": (_I, [_P, _I, _I, C.POINTER(_D), C.POINTER(_D), _P]),
     "macsav_plan_set_refinement": (_I, [_P, _I, _D]),
 }

@@ -221,18 +221,7 @@ int macsav_diagnostics(macsav_plan* plan, const double* x, double r, double nu, 
   return macsav::op_diagnostics(&plan->p, x, r, nu, force, out, static_cast<cudaStream_t>(stream));
 }
 
-int macsav_step(macsav_plan* plan, int scheme, double t, double dt, double nu, double gamma, const double* x0,
-                double r0, const double* forces, double* x1, double* embedded, double* pressures,
-                macsav_stage_record* records, double* r1, void* stream) {
-  if (!plan) return MACSAV_ERR_VALUE;
-  Plan* P = &plan->p;
-  if (scheme < 0 || scheme > MACSAV_IMEX_EULER) return fail(P, MACSAV_ERR_VALUE, "Unknown scheme");
-  if (!std::isfinite(dt) || dt <= 0) return fail(P, MACSAV_ERR_VALUE, "Invalid step size");
-  if (!std::isfinite(nu) || nu <= 0) return fail(P, MACSAV_ERR_VALUE, "nu must be positive and finite");
-  if (!std::isfinite(gamma) || gamma < 0) return fail(P, MACSAV_ERR_VALUE, "gamma must be finite and nonnegative");
-  if (!x0 || !records || P->maxcols < 2) return fail(P, MACSAV_ERR_VALUE, "invalid step buffers");
-  const int st = macsav::run_step(P, scheme, t, dt, nu, gamma, x0, r0, forces, x1, embedded, pressures, records, r1,
-                                  static_cast<cudaStream_t>(stream));
+static int stage_status_code(Plan* P, int st) {
   switch (st) {
     case macsav::ST_OK: return MACSAV_OK;
     case macsav::ST_STOKES_RHS: return fail(P, MACSAV_ERR_VALUE, "Invalid Stokes RHS");
@@ -245,6 +234,41 @@ int macsav_step(macsav_plan* plan, int scheme, double t, double dt, double nu, d
     case macsav::ST_STAGE_GATE: return fail(P, MACSAV_ERR_STAGE_GATE, "stage gate");
     default: return st == MACSAV_ERR_CUDA ? cuda_status(P) : st;
   }
+}
+
+int macsav_step(macsav_plan* plan, int scheme, double t, double dt, double nu, double gamma, const double* x0,
+                double r0, const double* forces, double* x1, double* embedded, double* pressures,
+                macsav_stage_record* records, double* r1, void* stream) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  if (scheme < 0 || scheme > MACSAV_IMEX_EULER) return fail(P, MACSAV_ERR_VALUE, "Unknown scheme");
+  if (!std::isfinite(dt) || dt <= 0) return fail(P, MACSAV_ERR_VALUE, "Invalid step size");
+  if (!std::isfinite(nu) || nu <= 0) return fail(P, MACSAV_ERR_VALUE, "nu must be positive and finite");
+  if (!std::isfinite(gamma) || gamma < 0) return fail(P, MACSAV_ERR_VALUE, "gamma must be finite and nonnegative");
+  if (!x0 || !records || P->maxcols < 2) return fail(P, MACSAV_ERR_VALUE, "invalid step buffers");
+  const int st = macsav::run_step(P, scheme, t, dt, nu, gamma, x0, r0, forces, x1, embedded, pressures, records, r1,
+                                  static_cast<cudaStream_t>(stream));
+  return stage_status_code(P, st);
+}
+
+int macsav_step_enqueue(macsav_plan* plan, int scheme, double t, double dt, double nu, double gamma,
+                        const double* x0, double r0, const double* forces, double* x1, double* embedded,
+                        double* pressures, void* stream) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  if (scheme < 0 || scheme > MACSAV_IMEX_EULER) return fail(P, MACSAV_ERR_VALUE, "Unknown scheme");
+  if (!std::isfinite(dt) || dt <= 0) return fail(P, MACSAV_ERR_VALUE, "Invalid step size");
+  if (!std::isfinite(nu) || nu <= 0) return fail(P, MACSAV_ERR_VALUE, "nu must be positive and finite");
+  if (!std::isfinite(gamma) || gamma < 0) return fail(P, MACSAV_ERR_VALUE, "gamma must be finite and nonnegative");
+  if (!x0 || P->maxcols < 2) return fail(P, MACSAV_ERR_VALUE, "invalid step buffers");
+  const int rc = macsav::enqueue_step_async(P, scheme, t, dt, nu, gamma, x0, r0, forces, x1, embedded, pressures,
+                                            static_cast<cudaStream_t>(stream));
+  return rc == MACSAV_ERR_CUDA ? cuda_status(P) : rc;
+}
+
+int macsav_step_finish(macsav_plan* plan, macsav_stage_record* records, double* r1) {
+  if (!plan || !records) return MACSAV_ERR_VALUE;
+  return stage_status_code(&plan->p, macsav::finish_step(&plan->p, records, r1));
 }
 
 int macsav_time_pass(macsav_plan* plan, int pass, int reps, double* ms, double* bytes, void* stream) {

@@ -58,6 +58,7 @@ struct StepBuffers {
   cudaStream_t stream = nullptr, side = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   std::vector<GraphEntry> graphs;
+  int pending_scheme = 0, pending_stages = 0;  // an enqueued step awaiting finish_step
 };
 
 template <typename T>

@@ -550,9 +550,11 @@ static int enqueue_step(Plan* P, Exec& X, int scheme, const StageProgram& G, boo
   return MACSAV_OK;
 }
 
-int run_step(Plan* P, int scheme, double t, double dt, double nu, double gamma, const double* x0, double r0,
-             const double* forces, double* x1, double* embedded, double* pressures, macsav_stage_record* records,
-             double* r1, cudaStream_t user) {
+// Enqueue one step (no host wait in graph mode); finish_step waits for it and
+// folds the stage records.
+int enqueue_step_async(Plan* P, int scheme, double t, double dt, double nu, double gamma, const double* x0,
+                       double r0, const double* forces, double* x1, double* embedded, double* pressures,
+                       cudaStream_t user) {
   (void)t;
   int rc = step_buffers(P);
   if (rc != MACSAV_OK) return rc;
@@ -606,6 +608,19 @@ int run_step(Plan* P, int scheme, double t, double dt, double nu, double gamma, 
   cudaMemcpyAsync(B.h_recs, B.recs, sizeof(StageRec) * n, cudaMemcpyDeviceToHost, s);
   cudaEventRecord(B.ev_out, s);
   cudaStreamWaitEvent(user, B.ev_out, 0);
+  B.pending_scheme = scheme;
+  B.pending_stages = n;
+  return MACSAV_OK;
+}
+
+int finish_step(Plan* P, macsav_stage_record* records, double* r1) {
+  StepBuffers& B = P->st;
+  const int scheme = B.pending_scheme, n = B.pending_stages;
+  if (n <= 0) {
+    P->err = "no step enqueued";
+    return MACSAV_ERR_VALUE;
+  }
+  B.pending_stages = 0;
   if (cudaEventSynchronize(B.ev_out) != cudaSuccess) return MACSAV_ERR_CUDA;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -639,6 +654,14 @@ int run_step(Plan* P, int scheme, double t, double dt, double nu, double gamma, 
   }
   if (r1) *r1 = scheme_sav(scheme) ? B.h_recs[n - 1].r : 0.0;
   return status;
+}
+
+int run_step(Plan* P, int scheme, double t, double dt, double nu, double gamma, const double* x0, double r0,
+             const double* forces, double* x1, double* embedded, double* pressures, macsav_stage_record* records,
+             double* r1, cudaStream_t user) {
+  const int rc = enqueue_step_async(P, scheme, t, dt, nu, gamma, x0, r0, forces, x1, embedded, pressures, user);
+  if (rc != MACSAV_OK) return rc;
+  return finish_step(P, records, r1);
 }
 
 }  // namespace macsav

@@ -26,6 +26,10 @@ void launch_convection(Plan* P, const double* x, double* out, cudaStream_t s);
 int run_step(Plan* P, int scheme, double t, double dt, double nu, double gamma, const double* x0, double r0,
              const double* forces, double* x1, double* embedded, double* pressures, macsav_stage_record* records,
              double* r1, cudaStream_t user);
+int enqueue_step_async(Plan* P, int scheme, double t, double dt, double nu, double gamma, const double* x0,
+                       double r0, const double* forces, double* x1, double* embedded, double* pressures,
+                       cudaStream_t user);
+int finish_step(Plan* P, macsav_stage_record* records, double* r1);
 int scheme_stages(int scheme);
 void step_free(Plan* P);
 
