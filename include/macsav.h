@@ -111,6 +111,23 @@ int macsav_combine(macsav_plan* plan, int nterms, const double* coeffs, const do
 int macsav_inner(macsav_plan* plan, const double* a, const double* b, long long n, double* result, void* stream);
 int macsav_max_abs(macsav_plan* plan, const double* a, long long n, double* result, void* stream);
 
+/* Plan-free form of macsav_inner + macsav_max_abs that takes no device memory
+ * (no counterpart in the reference, which has no device memory to manage).
+ * It is for callers that hold no plan and may not allocate: an error handler
+ * after the device ran out of memory, or a monitor of a state's size and
+ * finiteness while the solver owns the memory.  result[0] = weight*dot(a,b)
+ * (weight*sum(a) when b is NULL), result[1] = max|a| with NaN propagation; a,b
+ * device, result HOST; synchronises `stream`.  Its scratch is a fixed
+ * 64 KiB device array of the library, so n <= MACSAV_STATIC_REDUCE_MAX_N
+ * (larger n: MACSAV_ERR_UNSUPPORTED, before any device work; NULL a/result or
+ * n < 0: MACSAV_ERR_VALUE).  The first call on each device finds the array's
+ * address (this may load the module) and clears its completion counter:
+ * make it outside any stream capture.  Calls share that array, so calls
+ * that overlap on the device race: order them (e.g. one stream). */
+#define MACSAV_STATIC_REDUCE_MAX_N 16777216LL
+int macsav_inner_max_static(const double* a, const double* b, long long n, double weight, double* result,
+                            void* stream);
+
 /* MACNavierStokes.diagnostics (solver/mac_ns.py:95-107) of a packed velocity x
  * with scalar r: out[0..7] = kinetic, modified_energy, divergence_inf,
  * h1_seminorm_squared, r, angular_momentum, power, dissipation.  force may be

@@ -16,6 +16,7 @@ OK, ERR_VALUE, ERR_CUDA, ERR_CG, ERR_STOKES_GATE, ERR_STAGE_GATE, ERR_NEG_ENERGY
 FP64, FP32_MIXED = 0, 1
 DCT2, DST2, DST1 = 0, 1, 2
 MAX_COLUMNS = 4
+STATIC_REDUCE_MAX_N = 16777216  # MACSAV_STATIC_REDUCE_MAX_N
 
 
 class MacsavError(RuntimeError):
@@ -55,6 +56,7 @@ _SIGNATURES = {
     "macsav_combine": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_P), _P, _LL, _P]),
     "macsav_inner": (_I, [_P, _P, _P, _LL, C.POINTER(_D), _P]),
     "macsav_max_abs": (_I, [_P, _P, _LL, C.POINTER(_D), _P]),
+    "macsav_inner_max_static": (_I, [_P, _P, _LL, _D, C.POINTER(_D), _P]),
     "macsav_diagnostics": (_I, [_P, _P, _D, _D, _P, C.POINTER(_D), _P]),
     "macsav_step": (_I, [_P, _I, _D, _D, _D, _D, _P, _D, _P, _P, _P, _P, C.POINTER(StageRecord), C.POINTER(_D), _P]),
     "macsav_plan_set_graph": (_I, [_P, _I]),
