@@ -12,6 +12,13 @@ state, dt)`` with a host ``State``: the velocity goes host->device and the new
 state device->host every step).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload cavity512|ensemble256]
+
+``--workload ensemble256`` measures the mixed-size ensemble instead: 256
+cavities (nx, ny drawn from {64, 96, 128, 192, 256}, domain [0, nx/ny] x
+[0, 1], nu log-uniform in [1e-4, 1e-2], psi modes k,l <= 8, sdirk2_mrsav,
+dt=5e-4), all members' steps in flight at once (``Ensemble``); with N ranks
+the members are sharded by cell count (``scaling: strong``).
 
 Multi-GPU: independent replicas of the cavity, one per rank (a single cavity
 does not shard; the reference has no distributed path), ``scaling: weak``.
@@ -144,6 +151,103 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+ENSEMBLE = {"workload": "ensemble256_sdirk2_mrsav", "members": 256, "seed": 2026, "dt": 5e-4,
+            "scheme": "sdirk2_mrsav", "psi_modes": 8, "stages_per_step": 2}
+
+
+def run_ensemble(args) -> None:
+    """The ensemble workload: FP32-bulk and FP64 ensembles from the same fields."""
+    import torch
+    import torch.distributed as dist
+    import __graft_entry__
+    from importlib import import_module
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    __graft_entry__.build()
+    pkg = __graft_entry__.load_package()
+    E = import_module(pkg.__name__ + ".ensemble")
+    w = ENSEMBLE
+    members = E.ensemble_members(w["members"], seed=w["seed"])
+    mine = [members[i] for i in E.shard_members(members, world, rank)]
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(precision):
+        ens = E.Ensemble(mine, w["scheme"], precision=precision)
+        ens.seed_fields(modes=w["psi_modes"])
+        for _ in range(args.warmup):
+            ens.step(w["dt"])
+        barrier()
+        total = 0.0
+        with ClockSampler(local) as clk:
+            for _ in range(args.steps):
+                flush.fill_(1.0)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                ens.step(w["dt"])
+                b.record(stream)
+                b.synchronize()
+                total += a.elapsed_time(b)
+        return ens, total, clk.summary()
+
+    e32, ms32, clk = timed("fp32")
+    e64, ms64, _ = timed("fp64")
+    # kernels per ensemble step: one eager step of a copy of the FP32 ensemble
+    eager = E.Ensemble(mine, w["scheme"], precision="fp32", use_graph=False)
+    for i in range(len(mine)):
+        eager.set_state(i, e32.velocity(i), r=e32.r[i], t=e32.t[i])
+    before = sum(m.plan.launches for m in eager.models)
+    eager.step(w["dt"])
+    launches_per_step = sum(m.plan.launches for m in eager.models) - before
+    del eager
+    err = max(float(torch.linalg.vector_norm(e32.velocity(i) - e64.velocity(i))
+                    / torch.linalg.vector_norm(e64.velocity(i))) for i in range(len(mine)))
+    # end to end: host states in, host states out, every step
+    hosts = [e32.velocity(i).cpu().numpy() for i in range(len(mine))]
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for i, x in enumerate(hosts):
+            e32.set_state(i, x, r=e32.r[i], t=e32.t[i])
+        e32.step(w["dt"])
+        hosts = [e32.velocity(i).cpu().numpy() for i in range(len(mine))]
+    e2e_sec = time.perf_counter() - t0
+    tot = torch.tensor([ms32, ms64, e2e_sec, err], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(tot, op=dist.ReduceOp.MAX)
+    ms32, ms64, e2e_sec, err = (float(v) for v in tot)
+    if rank == 0:
+        cells = sum(m.cells for m in members) * w["stages_per_step"] * args.steps
+        size_bytes = sum(m.grid().size for m in members) * 8
+        launches = launches_per_step * args.steps  # of this rank; every rank runs the same kind of shard
+        line = {
+            "metric": METRIC, "value": cells / (ms32 / 1e3), "unit": "cell-stage/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32 / args.steps,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "fp32+fp64",
+            "data": "synthetic (seeded stream-function curl fields, one seed per member)",
+            "config": {"workload": w["workload"], "members": w["members"], "cells": sum(m.cells for m in members),
+                       "dt": w["dt"], "scheme": w["scheme"], "psi_modes": w["psi_modes"],
+                       "parallelism": f"shards{world}", "l2": "flushed (256 MiB write) before every timed step",
+                       "graph": "one CUDA graph per member step, all members in flight"},
+            "fp64": {"value": cells / (ms64 / 1e3), "ms_per_step": ms64 / args.steps, "unit": "cell-stage/s"},
+            "error_vs_fp64": {"max_rel_l2_velocity": err, "after_steps": args.warmup + args.steps},
+            "clocks": clk,
+            "e2e": {"value": cells / e2e_sec, "unit": "cell-stage/s", "h2d_bytes_per_step": size_bytes,
+                    "d2h_bytes_per_step": size_bytes},
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
 def profile_steps(precision: str) -> None:
     """Two eager steps of the bench workload (the launch list and kernel
     captures of profiles/ come from this)."""
@@ -172,6 +276,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["cavity512", "ensemble256"], default="cavity512")
     ap.add_argument("--profile", choices=["fp32", "fp64"], default=None,
                     help="run two eager steps of the workload and exit (for ncu captures)")
     args = ap.parse_args()
@@ -183,6 +288,9 @@ def main() -> None:
         return
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "ensemble256":
+        run_ensemble(args)
+        return
 
     import torch
     import torch.distributed as dist
