@@ -192,6 +192,51 @@ int macsav_step_enqueue(macsav_plan* plan, int scheme, double t, double dt, doub
                         double* pressures, void* stream);
 int macsav_step_finish(macsav_plan* plan, macsav_stage_record* records, double* r1);
 
+/* ---- learned preconditioner (no reference counterpart: the reference's
+ * pressure CG uses the spectral preconditioner only, tensor_stokes.py:313-321).
+ * A bias-free 4-level U-Net (channels c0..c3, default 16/32/64/64; BF16
+ * activations, FP32 accumulation) maps a unit-RMS pressure residual to a
+ * correction of the spectral preconditioner: z = M r + s(r) net(r / rms(r)),
+ * s(r) = rms(r) (r.Mr)/(r.r), projected to mean zero, inside flexible CG
+ * (Polak-Ribiere beta) in the FP32 inner solves.  A column whose learned
+ * attempt has not converged after learned_max_iterations (or turned
+ * non-finite) restarts plain PCG from zero, and the FP64 defect correction
+ * and closing gates judge the result as before.  Grids need nx, ny
+ * multiples of 8.  Inputs/outputs of the network calls are device FP32
+ * [batch][ny][nx]; parameters are host FP32 in layer order, each layer
+ * [c_out][c_in][k][k]. */
+typedef struct macsav_unet macsav_unet;
+int macsav_unet_create(macsav_unet** net, const int* channels /* 4 values or NULL */);
+void macsav_unet_destroy(macsav_unet* net);
+const char* macsav_unet_error(const macsav_unet* net);
+long long macsav_unet_num_params(const macsav_unet* net);
+int macsav_unet_set_params(macsav_unet* net, const float* params);
+int macsav_unet_get_params(const macsav_unet* net, float* params);
+int macsav_unet_forward(macsav_unet* net, const float* in, int batch, int ny, int nx, float* out, void* stream);
+/* loss = mean((net(in) - target)^2); grads = d loss / d params (host). */
+int macsav_unet_gradients(macsav_unet* net, const float* in, const float* target, int batch, int ny, int nx,
+                          double* loss, float* grads, void* stream);
+/* One Adam step (beta 0.9 / 0.999) on that loss; *loss (host, may be NULL) is
+ * the loss before the step. */
+int macsav_unet_train_step(macsav_unet* net, const float* in, const float* target, int batch, int ny, int nx,
+                           float lr, double* loss, void* stream);
+/* Attach (net != NULL) or detach the learned preconditioner of an FP32_MIXED
+ * plan.  The plan keeps a pointer: destroy the plan (or detach) first. */
+int macsav_plan_set_preconditioner(macsav_plan* plan, macsav_unet* net, int learned_max_iterations);
+/* Per-column CG counters since the start of the last macsav_stokes_solve:
+ * iterations of every inner solve, those run with the network, and plain-PCG
+ * restarts. */
+int macsav_plan_cg_counters(macsav_plan* plan, int columns, int* iterations, int* learned_iterations,
+                            int* fallbacks);
+/* One-column FP64 solve that logs, for every PCG iteration k, the residual
+ * r_k, the spectrally preconditioned residual M r_k and the iterate p_k
+ * (device arrays of max_pairs x np doubles; `iterates` has max_pairs + 1 rows,
+ * the last row after the loop holds the converged iterate).  The exact error
+ * of iterate k, p* - p_k, solves S e = r_k: these are the training pairs of
+ * the learned preconditioner. */
+int macsav_stokes_log(macsav_plan* plan, const double* rhs, double mass, double viscosity, int max_pairs,
+                      double* residuals, double* preconditioned, double* iterates, int* pairs, void* stream);
+
 /* Measurement helper (no reference counterpart: it times this library's own
  * kernels for the roofline): average device milliseconds of `reps`
  * back-to-back launches of one transform pass over the velocity blocks with two

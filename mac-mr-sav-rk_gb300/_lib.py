@@ -60,6 +60,18 @@ _SIGNATURES = {
     "macsav_diagnostics": (_I, [_P, _P, _D, _D, _P, C.POINTER(_D), _P]),
     "macsav_step": (_I, [_P, _I, _D, _D, _D, _D, _P, _D, _P, _P, _P, _P, C.POINTER(StageRecord), C.POINTER(_D), _P]),
     "macsav_plan_set_graph": (_I, [_P, _I]),
+    "macsav_unet_create": (_I, [C.POINTER(_P), _P]),
+    "macsav_unet_destroy": (None, [_P]),
+    "macsav_unet_error": (C.c_char_p, [_P]),
+    "macsav_unet_num_params": (_LL, [_P]),
+    "macsav_unet_set_params": (_I, [_P, _P]),
+    "macsav_unet_get_params": (_I, [_P, _P]),
+    "macsav_unet_forward": (_I, [_P, _P, _I, _I, _I, _P, _P]),
+    "macsav_unet_gradients": (_I, [_P, _P, _P, _I, _I, _I, C.POINTER(_D), _P, _P]),
+    "macsav_unet_train_step": (_I, [_P, _P, _P, _I, _I, _I, C.c_float, C.POINTER(_D), _P]),
+    "macsav_plan_set_preconditioner": (_I, [_P, _P, _I]),
+    "macsav_plan_cg_counters": (_I, [_P, _I, _P, _P, _P]),
+    "macsav_stokes_log": (_I, [_P, _P, _D, _D, _I, _P, _P, _P, C.POINTER(_I), _P]),
     "macsav_step_enqueue": (_I, [_P, _I, _D, _D, _D, _D, _P, _D, _P, _P, _P, _P, _P]),
     "macsav_step_finish": (_I, [_P, C.POINTER(StageRecord), C.POINTER(_D)]),
     "macsav_time_pass": (_I, [_P, _I, _I, C.POINTER(_D), C.POINTER(_D), _P]),

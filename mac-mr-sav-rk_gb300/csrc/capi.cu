@@ -9,6 +9,11 @@ struct macsav_plan {
   macsav::Plan p;
 };
 
+struct macsav_unet {
+  macsav::UNet net;
+  macsav::NetWork work;  // training / stand-alone forward workspace
+};
+
 namespace macsav {
 int solve_fp64(Plan* P, const double* f, int cols, double mass, double visc, double* vel, double* pres,
                cudaStream_t s);
@@ -22,6 +27,7 @@ int op_diagnostics(Plan* P, const double* x, double r, double nu, const double* 
                    cudaStream_t s);
 int op_transform(Plan* P, int kind, int inverse, int rows, int n, const double* in, double* out, cudaStream_t s);
 int time_pass(Plan* P, int pass, int reps, cudaStream_t s, double* ms, double* bytes);
+void reset_cg_counters(Plan* P, int cols, cudaStream_t s);
 }  // namespace macsav
 
 using macsav::Plan;
@@ -149,6 +155,7 @@ int macsav_stokes_solve(macsav_plan* plan, const double* rhs, int columns, doubl
     shift[2 * c + 1] = viscosity;
   }
   cudaMemcpyAsync(P->shift, shift, sizeof(double) * 2 * columns, cudaMemcpyHostToDevice, s);
+  macsav::reset_cg_counters(P, columns, s);
   int sweeps = 0;
   int rc = P->precision == MACSAV_FP64
                ? macsav::solve_fp64(P, rhs, columns, mass, viscosity, velocity, pressure, s)
@@ -269,6 +276,177 @@ int macsav_step_enqueue(macsav_plan* plan, int scheme, double t, double dt, doub
 int macsav_step_finish(macsav_plan* plan, macsav_stage_record* records, double* r1) {
   if (!plan || !records) return MACSAV_ERR_VALUE;
   return stage_status_code(&plan->p, macsav::finish_step(&plan->p, records, r1));
+}
+
+// ------------------------------------------------ learned preconditioner ---
+static int net_fail(macsav_unet* net, int code, const char* msg) {
+  net->net.err = msg;
+  return code;
+}
+
+int macsav_unet_create(macsav_unet** out, const int* channels) {
+  if (!out) return MACSAV_ERR_VALUE;
+  *out = nullptr;
+  macsav_unet* h = new macsav_unet();
+  const int rc = macsav::unet_init(&h->net, channels);
+  if (rc != MACSAV_OK) {
+    g_create_error = h->net.err.empty() ? std::string("U-Net allocation failed") : h->net.err;
+    macsav::unet_free(&h->net);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return MACSAV_OK;
+}
+
+void macsav_unet_destroy(macsav_unet* net) {
+  if (!net) return;
+  cudaDeviceSynchronize();
+  macsav::net_work_free(&net->work);
+  macsav::unet_free(&net->net);
+  delete net;
+}
+
+const char* macsav_unet_error(const macsav_unet* net) { return net ? net->net.err.c_str() : g_create_error.c_str(); }
+
+long long macsav_unet_num_params(const macsav_unet* net) { return net ? net->net.nparams : 0; }
+
+int macsav_unet_set_params(macsav_unet* net, const float* params) {
+  if (!net || !params) return MACSAV_ERR_VALUE;
+  macsav::UNet& N = net->net;
+  if (cudaMemcpy(N.w32, params, sizeof(float) * N.nparams, cudaMemcpyHostToDevice) != cudaSuccess)
+    return net_fail(net, MACSAV_ERR_CUDA, "parameter upload failed");
+  cudaMemset(N.m1, 0, sizeof(float) * N.nparams);
+  cudaMemset(N.m2, 0, sizeof(float) * N.nparams);
+  cudaMemset(N.grad, 0, sizeof(float) * N.nparams);
+  N.adam_t = 0;
+  macsav::unet_sync_bf16(&N, nullptr);
+  return cudaDeviceSynchronize() == cudaSuccess ? MACSAV_OK : net_fail(net, MACSAV_ERR_CUDA, "parameter upload failed");
+}
+
+int macsav_unet_get_params(const macsav_unet* net, float* params) {
+  if (!net || !params) return MACSAV_ERR_VALUE;
+  return cudaMemcpy(params, net->net.w32, sizeof(float) * net->net.nparams, cudaMemcpyDeviceToHost) == cudaSuccess
+             ? MACSAV_OK
+             : MACSAV_ERR_CUDA;
+}
+
+int macsav_unet_forward(macsav_unet* net, const float* in, int batch, int ny, int nx, float* out, void* stream) {
+  if (!net || !in || !out) return MACSAV_ERR_VALUE;
+  int rc = macsav::net_work_ensure(&net->net, &net->work, batch, ny, nx, net->work.grad);
+  if (rc != MACSAV_OK) return net_fail(net, rc, "U-Net needs batch >= 1 and ny, nx multiples of 8");
+  rc = macsav::unet_forward(&net->net, &net->work, in, nullptr, batch, ny, nx, out, nullptr,
+                            static_cast<cudaStream_t>(stream));
+  return rc == MACSAV_OK ? MACSAV_OK : net_fail(net, rc, "U-Net forward failed");
+}
+
+static int net_backward(macsav_unet* net, const float* in, const float* target, int batch, int ny, int nx,
+                        cudaStream_t s) {
+  int rc = macsav::net_work_ensure(&net->net, &net->work, batch, ny, nx, true);
+  if (rc != MACSAV_OK) return net_fail(net, rc, "U-Net needs batch >= 1 and ny, nx multiples of 8");
+  cudaMemsetAsync(net->net.loss, 0, sizeof(double), s);
+  rc = macsav::unet_backward(&net->net, &net->work, in, target, batch, ny, nx, s);
+  return rc == MACSAV_OK ? MACSAV_OK : net_fail(net, rc, "U-Net backward failed");
+}
+
+int macsav_unet_gradients(macsav_unet* net, const float* in, const float* target, int batch, int ny, int nx,
+                          double* loss, float* grads, void* stream) {
+  if (!net || !in || !target || !loss || !grads) return MACSAV_ERR_VALUE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  macsav::UNet& N = net->net;
+  cudaMemsetAsync(N.grad, 0, sizeof(float) * N.nparams, s);
+  int rc = net_backward(net, in, target, batch, ny, nx, s);
+  if (rc != MACSAV_OK) return rc;
+  cudaMemcpyAsync(grads, N.grad, sizeof(float) * N.nparams, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(loss, N.loss, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaMemsetAsync(N.grad, 0, sizeof(float) * N.nparams, s);
+  return cudaStreamSynchronize(s) == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
+}
+
+int macsav_unet_train_step(macsav_unet* net, const float* in, const float* target, int batch, int ny, int nx,
+                           float lr, double* loss, void* stream) {
+  if (!net || !in || !target || !(lr > 0)) return MACSAV_ERR_VALUE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = net_backward(net, in, target, batch, ny, nx, s);
+  if (rc != MACSAV_OK) return rc;
+  if ((rc = macsav::unet_adam(&net->net, lr, s)) != MACSAV_OK) return net_fail(net, rc, "Adam step failed");
+  if (loss) {
+    cudaMemcpyAsync(loss, net->net.loss, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return MACSAV_ERR_CUDA;
+  }
+  return cudaGetLastError() == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
+}
+
+int macsav_plan_set_preconditioner(macsav_plan* plan, macsav_unet* net, int learned_max_iterations) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  cudaDeviceSynchronize();
+  for (auto& kv : P->st.graphs) cudaGraphExecDestroy(kv.exec);  // captured with the old preconditioner
+  P->st.graphs.clear();
+  if (!net) {
+    P->net = nullptr;
+    return MACSAV_OK;
+  }
+  if (P->precision != MACSAV_FP32_MIXED)
+    return fail(P, MACSAV_ERR_UNSUPPORTED, "the learned preconditioner runs in the FP32 inner solves (FP32_MIXED)");
+  if (learned_max_iterations < 1 || learned_max_iterations > 1000)
+    return fail(P, MACSAV_ERR_VALUE, "learned_max_iterations must be in 1..1000");
+  const int rc = macsav::net_work_ensure(&net->net, &P->netw, P->maxcols, P->g.ny, P->g.nx, false);
+  if (rc == MACSAV_ERR_UNSUPPORTED) return fail(P, rc, "the learned preconditioner needs nx, ny multiples of 8");
+  if (rc != MACSAV_OK) return cuda_status(P);
+  const size_t cells = size_t(P->maxcols) * P->g.np;
+  if (!P->net_out) {
+    if (cudaMalloc(&P->net_out, cells * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&P->net_rold, cells * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&P->net_scale, 2 * MACSAV_MAX_COLUMNS * sizeof(float)) != cudaSuccess)
+      return cuda_status(P);
+    cudaMemset(P->net_rold, 0, cells * sizeof(float));
+  }
+  P->net = &net->net;
+  P->net_maxit = learned_max_iterations;
+  return cudaDeviceSynchronize() == cudaSuccess ? MACSAV_OK : cuda_status(P);
+}
+
+int macsav_plan_cg_counters(macsav_plan* plan, int columns, int* iterations, int* learned_iterations,
+                            int* fallbacks) {
+  if (!plan || columns < 1 || columns > plan->p.maxcols) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  if (cudaMemcpy(P->h_cg, P->cg, sizeof(macsav::CGScalars) * columns, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return cuda_status(P);
+  for (int c = 0; c < columns; ++c) {
+    if (iterations) iterations[c] = P->h_cg[c].cum_iters;
+    if (learned_iterations) learned_iterations[c] = P->h_cg[c].cum_net_iters;
+    if (fallbacks) fallbacks[c] = P->h_cg[c].cum_fallbacks;
+  }
+  return MACSAV_OK;
+}
+
+int macsav_stokes_log(macsav_plan* plan, const double* rhs, double mass, double viscosity, int max_pairs,
+                      double* residuals, double* preconditioned, double* iterates, int* pairs, void* stream) {
+  if (!plan || !rhs || !residuals || !preconditioned || !iterates || !pairs || max_pairs < 1) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  if (P->precision != MACSAV_FP64) return fail(P, MACSAV_ERR_UNSUPPORTED, "the CG log needs an FP64 plan");
+  P->log_r = residuals;
+  P->log_z = preconditioned;
+  P->log_x = iterates;
+  P->log_cap = max_pairs;
+  P->log_n = 0;
+  macsav_stokes_info info;
+  double* vel = nullptr;
+  double* pres = nullptr;
+  int rc = MACSAV_OK;
+  if (cudaMalloc(&vel, sizeof(double) * P->g.size) != cudaSuccess ||
+      cudaMalloc(&pres, sizeof(double) * P->g.np) != cudaSuccess)
+    rc = cuda_status(P);
+  if (rc == MACSAV_OK) rc = macsav_stokes_solve(plan, rhs, 1, mass, viscosity, vel, pres, &info, stream);
+  cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+  *pairs = P->log_n;
+  P->log_cap = 0;
+  P->log_n = 0;
+  P->log_r = P->log_z = P->log_x = nullptr;
+  cudaFree(vel);
+  cudaFree(pres);
+  return rc;
 }
 
 int macsav_time_pass(macsav_plan* plan, int pass, int reps, double* ms, double* bytes, void* stream) {

@@ -240,6 +240,8 @@ void plan_free(Plan* p) {
   cudaFree(p->partial); cudaFree(p->cg); cudaFree(p->checks); cudaFree(p->active); cudaFree(p->shift);
   cudaFree(p->errword);
   cudaFree(p->done_counter);
+  cudaFree(p->net_out); cudaFree(p->net_rold); cudaFree(p->net_scale);
+  net_work_free(&p->netw);
   p->done_counter = nullptr;
   cudaFreeHost(p->h_cg); cudaFreeHost(p->h_checks); cudaFreeHost(p->h_active); cudaFreeHost(p->h_err);
   if (p->done) cudaEventDestroy(p->done);

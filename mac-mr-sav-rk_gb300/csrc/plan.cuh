@@ -5,14 +5,19 @@
 
 #include "stencils.cuh"
 #include "transforms.cuh"
+#include "unet.cuh"
 
 namespace macsav {
 
 // Per-RHS-column Krylov scalars (device resident, mirrored to pinned memory).
 struct CGScalars {
-  double bnorm, atol, rho, rho_prev, alpha, beta, pq, rr, mean_q, mean_b, max_b;
-  float alpha_t, beta_t, mean_q_t, mean_b_t;  // the same scalars rounded once for FP32 kernels
-  int active, iters, info, pad;
+  double bnorm, atol, rho, rho_prev, alpha, beta, pq, rr, mean_q, mean_b, max_b, mean_z;
+  float alpha_t, beta_t, mean_q_t, mean_b_t, mean_z_t, pad_t;  // the same scalars rounded once for FP32 kernels
+  int active, iters, info;
+  // learned preconditioner (flexible CG): on for this column, restart pending
+  // (plain PCG from zero after the learned attempt failed), and counters that
+  // accumulate over the solves since the last reset
+  int net_on, restart, cum_iters, cum_net_iters, cum_fallbacks;
 };
 
 // Results of the closing checks of one solve (device resident).
@@ -114,6 +119,21 @@ struct Plan {
 
   // counters of kernel launches issued by this plan (for reporting)
   long long launches = 0;
+
+  // learned correction of the pressure preconditioner (FP32_MIXED inner
+  // solves); the network is owned by the caller, the buffers by the plan
+  UNet* net = nullptr;
+  NetWork netw;
+  float* net_out = nullptr;    // network output, [maxcols][np]
+  float* net_rold = nullptr;   // previous residual (Polak-Ribiere beta), [maxcols][np]
+  float* net_scale = nullptr;  // per-column input and output scales, [2][maxcols]
+  int net_maxit = 20;          // learned iterations before the plain-PCG restart
+
+  // residual / preconditioned residual / iterate log of eager FP64 solves
+  double* log_r = nullptr;
+  double* log_z = nullptr;
+  double* log_x = nullptr;
+  int log_cap = 0, log_n = 0;
 };
 
 // Execution context of one enqueue: eager (the host drives the CG loop on the
@@ -125,6 +145,7 @@ struct Exec {
   cudaStream_t side;  // body capture stream (graph mode)
   cudaGraphConditionalHandle cond;
   double ktol;        // Krylov tolerance of the solve being enqueued (0: the plan's)
+  int net = 0;        // use the plan's learned preconditioner (flexible CG)
 };
 
 int plan_build(Plan* p);

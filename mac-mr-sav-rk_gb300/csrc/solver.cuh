@@ -116,7 +116,7 @@ struct DstCellsDot {
 };
 
 // ------------------------------------------------------- Krylov scalars ---
-enum ScalarOp : int { OP_MEAN_B, OP_START, OP_RHO, OP_ALPHA, OP_CHECK, OP_MEAN_X, OP_CHECKS };
+enum ScalarOp : int { OP_MEAN_B, OP_START, OP_RHO, OP_ALPHA, OP_CHECK, OP_MEAN_X, OP_CHECKS, OP_FCG };
 
 // Block-wide fold of the K-slot partials of `nb` blocks per column in a
 // fixed order, then thread 0 updates each column's scalars.  Sum slots hold
@@ -137,6 +137,7 @@ struct CGFin {
   SolveChecks* checks;
   int use_cond;
   cudaGraphConditionalHandle cond;
+  int use_net, net_maxit;
 
   __device__ int maxmask() const { return op == OP_START ? 0x2 : (op == OP_CHECKS ? 0x3f : 0); }
 
@@ -144,7 +145,7 @@ struct CGFin {
     using R = Red<T>;
     __shared__ typename R::P red[6 * 32];
     __shared__ unsigned long long redk[6 * 32];
-    const bool gated = op == OP_RHO || op == OP_ALPHA || op == OP_CHECK;
+    const bool gated = op == OP_RHO || op == OP_ALPHA || op == OP_CHECK || op == OP_FCG;
     const int mm = maxmask();
     for (int c = 0; c < cols; ++c) {
       if (gated && !active[c]) continue;  // uniform across the block
@@ -212,6 +213,8 @@ struct CGFin {
         g.beta = 0;
         g.beta_t = 0.0f;
         g.rr = s[0];
+        g.net_on = use_net;
+        g.restart = 0;
         // zero RHS (tensor_stokes.py:309-311) or already converged: no update
         const bool go = (g.max_b != 0.0) && !(sqrt(g.rr) < g.atol) && (g.bnorm == g.bnorm);
         active[c] = go ? 1 : 0;
@@ -232,14 +235,38 @@ struct CGFin {
       case OP_CHECK:
         g.rr = s[0];
         g.iters += 1;
+        g.cum_iters += 1;
+        if (g.net_on) g.cum_net_iters += 1;
         g.rho_prev = g.rho;
         if (sqrt(g.rr) < g.atol) {
           active[c] = 0;
+        } else if (g.net_on && (g.iters >= net_maxit || !(g.rr == g.rr))) {
+          // the learned attempt did not converge: plain PCG from zero
+          g.net_on = 0;
+          g.restart = 1;
+          g.cum_fallbacks += 1;
+          g.iters = 0;
+          g.rho_prev = 0;
+          g.beta = 0;
+          g.beta_t = 0.0f;
+          g.rr = g.bnorm * g.bnorm;
         } else if (g.iters >= maxit || !(g.rr == g.rr)) {
           active[c] = 0;
           g.info = maxit;
         }
         break;
+      case OP_FCG: {
+        // z = M r + net(r): mean of z, rho = r.(z - mean), Polak-Ribiere beta
+        // (r - r_old).(z - mean) / rho_prev (flexible CG)
+        g.mean_z = s[0] / np;
+        g.mean_z_t = float(g.mean_z);
+        g.rho = s[1] - g.mean_z * s[3];
+        const double rzo = s[2] - g.mean_z * s[4];
+        g.beta = g.iters > 0 ? (g.rho - rzo) / g.rho_prev : 0.0;
+        g.beta_t = float(g.beta);
+        g.restart = 0;
+        break;
+      }
       case OP_MEAN_X:
         g.mean_q = s[0] / np;
         g.mean_q_t = float(g.mean_q);
@@ -259,7 +286,7 @@ struct CGFin {
 template <typename T>
 inline CGFin<T> make_fin(const Plan* P, const Exec& X, int op, int nb, int K, int cols) {
   return CGFin<T>{op, P->partial, nb, K, cols, P->cg, P->active, P->g.np, X.ktol > 0 ? X.ktol : P->ktol, P->maxit,
-                  P->checks, X.graph ? 1 : 0, X.cond};
+                  P->checks, X.graph ? 1 : 0, X.cond, X.net && P->net ? 1 : 0, P->net_maxit};
 }
 
 // ------------------------------------------------------------- launching ---

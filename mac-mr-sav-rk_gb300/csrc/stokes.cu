@@ -111,9 +111,9 @@ __global__ void __launch_bounds__(kThreads) k_div_q(GridDev g, const WIn* w, lon
 }
 
 // p = z + beta p; x += alpha p; r -= alpha (q - mean q); last block: ||r||
-// and the convergence test (OP_CHECK).
+// and the convergence test (OP_CHECK).  r_old (flexible CG) keeps the old r.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_cg_update(int np, T* x, T* r, T* p, const T* z, const T* q,
+__global__ void __launch_bounds__(kThreads) k_cg_update(int np, T* x, T* r, T* p, const T* z, const T* q, T* r_old,
                                                         long long cs, const CGScalars* cg, const int* active,
                                                         double* partial, CGFin<T> fin, unsigned int* done) {
   const int c = blockIdx.y;
@@ -126,13 +126,89 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int np, T* x, T* r, T* p
       const T pd = first ? z[k] : T(z[k] + beta * p[k]);
       p[k] = pd;
       x[k] = x[k] + alpha * pd;
-      const T rv = r[k] - alpha * (q[k] - mq);
+      const T ro = r[k];
+      if (r_old) r_old[k] = ro;
+      const T rv = ro - alpha * (q[k] - mq);
       r[k] = rv;
       acc[0].add(rv * rv);
     }
   }
   write_sums<T, 1>(acc, partial, 1);
   last_block_finish(fin, done);
+}
+
+// ------------------------------------------- learned preconditioner (FCG) ---
+// Columns whose learned attempt failed restart plain PCG from zero: x = 0, r = b.
+__global__ void __launch_bounds__(kThreads) k_fcg_restart(int np, const float* b, float* x, float* r, long long cs,
+                                                          const CGScalars* cg) {
+  const int c = blockIdx.y;
+  if (!cg[c].restart) return;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
+    const long long k = c * cs + idx;
+    x[k] = 0.0f;
+    r[k] = b[k];
+  }
+}
+
+// Network input scale 1/rms(r) and output scale rms(r) rho/rr (rho = r.Mr of
+// the spectral preconditioner): the network sees unit-RMS residuals and
+// answers in units of the spectral preconditioner's Rayleigh quotient.
+// Columns without the network get 0 (a zero correction).
+__global__ void k_net_scales(const CGScalars* cg, const int* active, int cols, int np, float* scale) {
+  const int c = threadIdx.x;
+  if (c >= cols) return;
+  const CGScalars& g = cg[c];
+  const bool on = active[c] && g.net_on && g.rr > 0.0 && g.rho > 0.0;
+  const double rms = on ? sqrt(g.rr / np) : 0.0;
+  scale[c] = on ? float(1.0 / rms) : 0.0f;
+  scale[cols + c] = on ? float(rms * g.rho / g.rr) : 0.0f;
+}
+
+// z += net output; partial sums of z, r.z, r_old.z, r, r_old (OP_FCG).
+__global__ void __launch_bounds__(kThreads) k_fcg_z(int np, float* z, const float* add, const float* r,
+                                                    const float* r_old, long long cs, const CGScalars* cg,
+                                                    const int* active, double* partial, CGFin<float> fin,
+                                                    unsigned int* done) {
+  const int c = blockIdx.y;
+  Acc<float> a[5];
+  if (active[c]) {
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
+      const long long k = c * cs + idx;
+      const float zn = z[k] + add[k];
+      z[k] = zn;
+      const float rv = r[k], ro = r_old[k];
+      a[0].add(zn);
+      a[1].add(rv * zn);
+      a[2].add(ro * zn);
+      a[3].add(rv);
+      a[4].add(ro);
+    }
+  }
+  write_sums<float, 5>(a, partial, 5);
+  last_block_finish(fin, done);
+}
+
+// z -= mean(z): the mean-zero projection of the flexible preconditioner.
+__global__ void __launch_bounds__(kThreads) k_fcg_center(int np, float* z, long long cs, const CGScalars* cg,
+                                                         const int* active) {
+  const int c = blockIdx.y;
+  if (!active[c]) return;
+  const float m = cg[c].mean_z_t;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) z[c * cs + idx] -= m;
+}
+
+__global__ void k_reset_counters(CGScalars* cg, int cols) {
+  const int c = threadIdx.x;
+  if (c < cols) {
+    cg[c].cum_iters = 0;
+    cg[c].cum_net_iters = 0;
+    cg[c].cum_fallbacks = 0;
+  }
+}
+
+void reset_cg_counters(Plan* P, int cols, cudaStream_t s) {
+  k_reset_counters<<<1, 32, 0, s>>>(P->cg, cols);
+  ++P->launches;
 }
 
 // out = x - mean (the mean held in cg[c].mean_q when `center`); partial sum
@@ -206,11 +282,14 @@ static void velocity_inverse(Plan* P, const Launcher<T>& L, Src src, Out* dst, l
   L.row_inverse_uv(DstPacked<T, Out>{dst, dstride, g.nu, g.nx - 1, g.nx}, cols, active);
 }
 
-// One PCG iteration for every active column (all kernels predicated).
+// One PCG iteration for every active column (all kernels predicated).  With
+// the learned preconditioner (X.net, FP32 only) z = M r + net(r), projected to
+// mean zero, and beta is the Polak-Ribiere form of flexible CG.
 template <typename T>
 static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* cells, int cols) {
   const GridDev& g = P->g;
   const long long np = g.np, sz = g.size;
+  T* b = cells;
   T* x = cells + 1 * np * cols;
   T* r = cells + 2 * np * cols;
   T* z = cells + 3 * np * cols;
@@ -218,17 +297,39 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
   T* q = cells + 5 * np * cols;
   const int rb = red_blocks(np);
   const cudaStream_t s = L.s;
+  T* r_old = nullptr;
+  bool net = false;
+  if constexpr (std::is_same<T, float>::value) {
+    net = X.net && P->net;
+    if (net) {
+      r_old = P->net_rold;
+      k_fcg_restart<<<dim3(rb, cols), kThreads, 0, s>>>(g.np, b, x, r, np, P->cg);
+      ++P->launches;
+    }
+  }
+  (void)b;
   // z = M r = IDCT(g * DCT(r)); last block: rho = r . z, beta
   L.row_forward_p(SrcCells<T, T>{r, np, g.nx}, cols, P->active);
   L.column_p(cols, P->active, P->shift, T(P->pthr));
   L.row_inverse_p(DstCellsDot<T>{z, r, np, g.nx}, cols, P->active, P->partial,
                   make_fin<T>(P, X, OP_RHO, L.groups_row_p(), 2, cols), P->done_counter);
+  if constexpr (std::is_same<T, float>::value) {
+    if (net) {
+      k_net_scales<<<1, 32, 0, s>>>(P->cg, P->active, cols, g.np, P->net_scale);
+      ++P->launches;
+      unet_forward(P->net, &P->netw, r, P->net_scale, cols, g.ny, g.nx, P->net_out, P->net_scale + cols, s);
+      k_fcg_z<<<dim3(rb, cols), kThreads, 0, s>>>(g.np, z, P->net_out, r, r_old, np, P->cg, P->active, P->partial,
+                                                  make_fin<float>(P, X, OP_FCG, rb, 5, cols), P->done_counter);
+      k_fcg_center<<<dim3(rb, cols), kThreads, 0, s>>>(g.np, z, np, P->cg, P->active);
+      P->launches += 2;
+    }
+  }
   // q = S pdir = D (mI+kK)^{-1} D^T pdir,  pdir = z + beta p
   velocity_inverse<T>(P, L, SrcLift<T, double, T>{nullptr, 0, z, pd, P->cg, np, g.nx, g.nu, T(g.ihx), T(g.ihy)}, w,
                       sz, cols, P->active);
   k_div_q<T, T><<<dim3(rb, cols), kThreads, 0, s>>>(g, w, sz, q, z, pd, np, P->cg, P->active, P->partial,
                                                     make_fin<T>(P, X, OP_ALPHA, rb, 3, cols), P->done_counter);
-  k_cg_update<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, x, r, pd, z, q, np, P->cg, P->active, P->partial,
+  k_cg_update<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, x, r, pd, z, q, r_old, np, P->cg, P->active, P->partial,
                                                      make_fin<T>(P, X, OP_CHECK, rb, 1, cols), P->done_counter);
   P->launches += 2;
 }
@@ -252,13 +353,37 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
     k_cg_start<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, b, x, r, np, P->cg, P->partial,
                                                       make_fin<T>(P, X, OP_START, rb, 2, cols), P->done_counter);
     ++P->launches;
-    for (int it = 0; it < P->maxit; ++it) {
+    const int limit = P->maxit + (X.net && P->net ? P->net_maxit : 0);
+    for (int it = 0; it < limit; ++it) {
       cudaMemcpyAsync(P->h_active, P->active, sizeof(int) * cols, cudaMemcpyDeviceToHost, s);
       if (cudaStreamSynchronize(s) != cudaSuccess) return MACSAV_ERR_CUDA;
       bool any = false;
       for (int c = 0; c < cols; ++c) any |= P->h_active[c] != 0;
       if (!any) break;
+      bool log = false;
+      if constexpr (std::is_same<T, double>::value) {
+        // residual / iterate / preconditioned residual log (column 0)
+        log = P->log_cap > 0 && P->log_n < P->log_cap;
+        if (log) {
+          cudaMemcpyAsync(P->log_r + P->log_n * np, cells + 2 * np * cols, sizeof(double) * np,
+                          cudaMemcpyDeviceToDevice, s);
+          cudaMemcpyAsync(P->log_x + P->log_n * np, cells + 1 * np * cols, sizeof(double) * np,
+                          cudaMemcpyDeviceToDevice, s);
+        }
+      }
       cg_iteration<T>(P, X, L, w, cells, cols);
+      if constexpr (std::is_same<T, double>::value) {
+        if (log) {
+          cudaMemcpyAsync(P->log_z + P->log_n * np, cells + 3 * np * cols, sizeof(double) * np,
+                          cudaMemcpyDeviceToDevice, s);
+          ++P->log_n;
+        }
+      }
+    }
+    if constexpr (std::is_same<T, double>::value) {
+      if (P->log_cap > 0)  // the converged iterate closes the log
+        cudaMemcpyAsync(P->log_x + P->log_n * np, cells + 1 * np * cols, sizeof(double) * np,
+                        cudaMemcpyDeviceToDevice, s);
     }
     return MACSAV_OK;
   }
@@ -392,9 +517,12 @@ static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, i
   float* w = P->w32;
   velocity_inverse<float>(P, L, SrcPacked<float, double>{ru, sz, g.nu, g.nx - 1, g.nx}, w, sz, cols, nullptr);
   const double keep = X.ktol;
+  const int keep_net = X.net;
   X.ktol = P->inner_ktol;
+  X.net = P->net ? 1 : 0;
   int rc = schur_pcg<float>(P, X, L, w, P->cells32, cols, rd);
   X.ktol = keep;
+  X.net = keep_net;
   if (rc != MACSAV_OK) return rc;
   const float* x = P->cells32 + 1 * np * cols;
   velocity_inverse<float>(

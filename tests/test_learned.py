@@ -1,0 +1,146 @@
+"""Learned preconditioner: CUDA U-Net kernels against a PyTorch CPU oracle
+(forward and gradients), training on pairs logged by plain Schur CG, and
+flexible CG that keeps the plain solve's answer, falls back when the network
+is bad, and reports what the trained network gains."""
+import numpy as np
+import pytest
+
+from helpers import load_package
+import unet_torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+    from importlib import import_module
+    pkg = load_package()
+    L = import_module(pkg.__name__ + ".learned")
+    return pkg, L, torch
+
+
+def test_param_count_and_layout(env):
+    pkg, L, torch = env
+    net = L.UNet()
+    shapes = L.layer_shapes()
+    assert net.num_params == sum(co * ci * k * k for co, ci, k in shapes)
+    assert 1.5e5 < net.num_params < 3e5
+    p = net.params()
+    np.testing.assert_array_equal(p, net.initial_params(0, 1e-2))
+
+
+def test_forward_matches_torch_oracle(env):
+    pkg, L, torch = env
+    net = L.UNet(seed=3, output_gain=1.0)
+    x = torch.randn(2, 32, 48, generator=torch.Generator().manual_seed(1))
+    got = net.forward(x).cpu()
+    ref = unet_torch.forward(unet_torch.split_params(net.params(), L.layer_shapes()), x).detach()
+    err = float((got - ref).norm() / ref.norm())
+    assert err < 2e-2, err
+    # positive homogeneity of the bias-free ReLU network
+    got2 = net.forward(4.0 * x).cpu()
+    assert float((got2 - 4.0 * got).norm() / got.norm().mul(4)) < 2e-2
+
+
+def test_gradients_match_torch_autograd(env):
+    pkg, L, torch = env
+    net = L.UNet(seed=5, output_gain=1.0)
+    gen = torch.Generator().manual_seed(2)
+    x = torch.randn(3, 16, 24, generator=gen)
+    t = torch.randn(3, 16, 24, generator=gen)
+    loss, grads = net.gradients(x, t)
+    ws = [w.requires_grad_(True) for w in unet_torch.split_params(net.params(), L.layer_shapes())]
+    ref_loss = ((unet_torch.forward(ws, x) - t) ** 2).mean()
+    ref_loss.backward()
+    ref = torch.cat([w.grad.reshape(-1) for w in ws]).numpy()
+    assert loss == pytest.approx(float(ref_loss.detach()), rel=2e-2)
+    rel = np.linalg.norm(grads - ref) / np.linalg.norm(ref)
+    cos = float(grads @ ref / (np.linalg.norm(grads) * np.linalg.norm(ref)))
+    assert rel < 5e-2 and cos > 0.998, (rel, cos)
+    # every layer receives a gradient of the right size
+    off = 0
+    for co, ci, k in L.layer_shapes():
+        n = co * ci * k * k
+        g, r = grads[off:off + n], ref[off:off + n]
+        assert np.linalg.norm(g - r) <= 0.1 * np.linalg.norm(r) + 1e-12
+        off += n
+
+
+def _stage_rhs(pkg, grid, seeds, torch):
+    """Stage-like Stokes right-hand sides: seeded curl fields and their convection."""
+    out = []
+    model = pkg.MACNavierStokes(grid, 1e-3)
+    for s in seeds:
+        x = pkg.fields.packed_curl_velocity(grid.nx, grid.ny, grid.lx, grid.ly, 8, s)
+        out.append(x)
+        out.append(model.nonlinear(x).cpu().numpy() * 1e-3)
+    return out
+
+
+def _trained(env, grid, steps=300):
+    pkg, L, torch = env
+    shift = (1.0, 1e-3 * 2.5e-4 * 0.4358665215)
+    pairs = L.collect_pairs(grid, _stage_rhs(pkg, grid, range(6), torch), *shift)
+    net = L.UNet(seed=0)
+    losses = L.train(net, pairs, steps=steps, batch=8, lr=1e-3)
+    return net, pairs, losses, shift
+
+
+def test_pairs_and_training(env):
+    pkg, L, torch = env
+    grid = pkg.MACGrid(64, 64)
+    net, pairs, losses, _ = _trained(env, grid)
+    assert pairs.inputs.shape[1:] == (64, 64) and pairs.inputs.shape == pairs.targets.shape
+    assert min(pairs.iterations) >= 2
+    rms = pairs.inputs.pow(2).mean(dim=(1, 2)).sqrt()
+    assert torch.allclose(rms, torch.ones_like(rms), rtol=1e-5)
+    assert np.isfinite(losses).all()
+    assert np.mean(losses[-20:]) < 0.7 * np.mean(losses[:5])
+
+
+def test_flexible_cg_keeps_answer_and_falls_back(env):
+    pkg, L, torch = env
+    grid = pkg.MACGrid(64, 64)
+    net, pairs, _, shift = _trained(env, grid, steps=150)
+    rhs = np.column_stack(_stage_rhs(pkg, grid, [101], torch))
+    plain = pkg.TensorStokes(grid, precision="fp32")
+    base = plain.solve(rhs, mass=shift[0], viscosity=shift[1])
+    learned = pkg.TensorStokes(grid, precision="fp32")
+    L.attach(learned, net)
+    res = learned.solve(rhs, mass=shift[0], viscosity=shift[1])
+    cnt = L.cg_counters(learned, 2)
+    assert sum(cnt["learned_iterations"]) > 0
+    for a, b in ((res.velocity, base.velocity), (res.pressure, base.pressure)):
+        assert np.linalg.norm(a - b) <= 1e-8 * np.linalg.norm(b)
+    assert res.residual <= 1e-9 and base.residual <= 1e-9
+    # a deliberately bad network: the learned attempt fails, plain PCG restarts
+    bad = L.UNet(seed=9, output_gain=1e4)
+    L.attach(learned, bad, learned_max_iterations=2)
+    res_bad = learned.solve(rhs, mass=shift[0], viscosity=shift[1])
+    cnt_bad = L.cg_counters(learned, 2)
+    assert sum(cnt_bad["fallbacks"]) > 0
+    assert np.linalg.norm(res_bad.velocity - base.velocity) <= 1e-8 * np.linalg.norm(base.velocity)
+    L.attach(learned, None)
+    again = learned.solve(rhs, mass=shift[0], viscosity=shift[1])
+    assert L.cg_counters(learned, 2)["learned_iterations"] == [0, 0]
+    np.testing.assert_allclose(again.velocity, base.velocity, rtol=0, atol=1e-12 * np.abs(base.velocity).max())
+
+
+def test_gain_of_trained_network(env):
+    """What the trained network gains over the same flexible CG with an
+    untrained network and over plain PCG (iterations, printed; the trained
+    network must not need more iterations than the untrained one)."""
+    pkg, L, torch = env
+    grid = pkg.MACGrid(128, 128)
+    net, _, _, shift = _trained(env, grid, steps=300)
+    rhs = np.column_stack(_stage_rhs(pkg, grid, [202, 203], torch))
+    counts = {}
+    for name, n in (("plain", None), ("untrained", L.UNet(seed=1)), ("trained", net)):
+        ts = pkg.TensorStokes(grid, precision="fp32", max_columns=4)
+        if n is not None:
+            L.attach(ts, n)
+        ts.solve(rhs, mass=shift[0], viscosity=shift[1])
+        counts[name] = sum(L.cg_counters(ts, 4)["iterations"])
+    print("CG iterations (4 columns, all inner solves):", counts)
+    assert counts["trained"] <= counts["untrained"]
