@@ -248,6 +248,73 @@ def run_ensemble(args) -> None:
         dist.destroy_process_group()
 
 
+def learned_leg(pkg, g, w, x0_host, dev, args, x64) -> dict:
+    """FP32 bulk with the learned preconditioner on the same steps as ``value``:
+    the U-Net is trained here, on the GPU, on pairs logged by plain FP64 Schur
+    CG on 256^2 cavities with this workload's physics (stage shift of
+    sdirk3_mrsav: mass 1, viscosity nu*dt/4), then attached to a fresh FP32
+    model whose graph-captured steps are timed like ``value``."""
+    import torch
+    from importlib import import_module
+    L = import_module(pkg.__name__ + ".learned")
+    t0 = time.perf_counter()
+    grid = pkg.MACGrid(256, 256)
+    helper = pkg.MACNavierStokes(grid, w["nu"])
+    rhs = []
+    for s in range(4):
+        x = pkg.fields.packed_curl_velocity(256, 256, 1.0, 1.0, w["psi_modes"], 1000 + s)
+        rhs += [x, helper.nonlinear(x).cpu().numpy() * w["dt"]]
+    pairs = L.collect_pairs(grid, rhs, 1.0, w["nu"] * w["dt"] / 4)
+    net = L.UNet(seed=0)
+    losses = L.train(net, pairs, steps=200, batch=8, lr=1e-3)
+    torch.cuda.synchronize()
+    train_sec = time.perf_counter() - t0
+    scheme = pkg.make_scheme(w["scheme"])
+    stream = torch.cuda.current_stream()
+
+    def run(net_or_none):
+        model = pkg.MACNavierStokes(g, w["nu"], precision="fp32", use_graph=True)
+        if net_or_none is not None:
+            L.attach(model, net_or_none)
+        x = torch.from_numpy(x0_host.copy()).to(dev)
+        y = torch.empty_like(x)
+        pres = torch.empty((4, g.np), dtype=torch.float64, device=dev)
+        t, r = 0.0, 0.0
+        for _ in range(args.warmup):
+            y, r, _, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
+            x, y, t = y, x, t + w["dt"]
+        before = L.cg_counters(model, 2)
+        total = 0.0
+        for _ in range(args.steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            y, r, _, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
+            b.record(stream)
+            b.synchronize()
+            total += a.elapsed_time(b)
+            x, y, t = y, x, t + w["dt"]
+        after = L.cg_counters(model, 2)
+        delta = {k: (sum(after[k]) - sum(before[k])) / args.steps for k in after}
+        return total / args.steps, delta, x
+
+    ms_plain, c_plain, _ = run(None)
+    ms_learned, c_learned, x = run(net)
+    cells = w["nx"] * w["ny"] * w["stages_per_step"]
+    err = float(torch.linalg.vector_norm(x - x64) / torch.linalg.vector_norm(x64))
+    return {"value": cells / (ms_learned / 1e3), "unit": "cell-stage/s", "ms_per_step": ms_learned,
+            "plain_fp32_ms_per_step": ms_plain, "speedup_vs_plain_fp32": ms_plain / ms_learned,
+            "cg_iterations_per_step": c_learned["iterations"],
+            "learned_iterations_per_step": c_learned["learned_iterations"],
+            "fallbacks_per_step": c_learned["fallbacks"],
+            "plain_fp32_cg_iterations_per_step": c_plain["iterations"],
+            "error_vs_fp64": err,
+            "network": {"params": net.num_params, "channels": list(net.channels), "activations": "bf16",
+                        "convolutions": "direct, CUDA cores (not tensor cores)"},
+            "training": {"pairs": int(pairs.inputs.shape[0]), "grid": "256x256", "steps": len(losses),
+                         "loss_first": float(np.mean(losses[:5])), "loss_last": float(np.mean(losses[-5:])),
+                         "seconds": train_sec}}
+
+
 def profile_steps(precision: str) -> None:
     """Two eager steps of the bench workload (the launch list and kernel
     captures of profiles/ come from this)."""
@@ -277,6 +344,7 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["cavity512", "ensemble256"], default="cavity512")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner leg")
     ap.add_argument("--profile", choices=["fp32", "fp64"], default=None,
                     help="run two eager steps of the workload and exit (for ncu captures)")
     args = ap.parse_args()
@@ -403,6 +471,8 @@ def main() -> None:
     if tf.exists():
         traffic = json.loads(tf.read_text()).get("traffic_bytes_per_launch")
 
+    learned = None if args.no_learned else learned_leg(pkg, g, w, x0_host, dev, args, x64)
+
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -416,7 +486,7 @@ def main() -> None:
         "config": {"workload": w["workload"], "nx": w["nx"], "ny": w["ny"], "nu": w["nu"], "dt": w["dt"],
                    "scheme": w["scheme"], "psi_modes": w["psi_modes"], "parallelism": f"replicas{world}",
                    "form": "fp32 transforms/stencils/Krylov + fp64 reductions + fp64 defect correction",
-                   "preconditioner": "spectral m(DD^T)^+ + kI (learned preconditioner not built)",
+                   "preconditioner": "spectral m(DD^T)^+ + kI (the learned variant is reported under learned)",
                    "l2": "flushed (256 MiB write) before every timed step", "graph": "one CUDA graph per step"},
         "fp64": {"value": value64, "ms_per_step": ms64 / args.steps, "unit": "cell-stage/s"},
         "speedup_vs_fp64": value / value64,
@@ -431,6 +501,8 @@ def main() -> None:
                      "peak_source": "measured" if pk.exists() else "fallback",
                      "traffic": traffic, "bytes_per_launch": bytes_k.value, "ms_per_launch": ms_k.value},
     }
+    if learned is not None:
+        line["learned"] = learned
     if base is not None:
         line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line), flush=True)

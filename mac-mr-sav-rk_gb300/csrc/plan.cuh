@@ -11,7 +11,7 @@ namespace macsav {
 
 // Per-RHS-column Krylov scalars (device resident, mirrored to pinned memory).
 struct CGScalars {
-  double bnorm, atol, rho, rho_prev, alpha, beta, pq, rr, mean_q, mean_b, max_b, mean_z;
+  double bnorm, atol, atol2, rho, rho_prev, alpha, beta, pq, rr, mean_q, mean_b, max_b, mean_z;
   float alpha_t, beta_t, mean_q_t, mean_b_t, mean_z_t, pad_t;  // the same scalars rounded once for FP32 kernels
   int active, iters, info;
   // learned preconditioner (flexible CG): on for this column, restart pending

@@ -138,75 +138,67 @@ struct CGFin {
   int use_cond;
   cudaGraphConditionalHandle cond;
   int use_net, net_maxit;
+  double inv_np;
 
   __device__ int maxmask() const { return op == OP_START ? 0x2 : (op == OP_CHECKS ? 0x3f : 0); }
 
+  // One warp per (column, slot) folds that slot's nb block partials (lane
+  // stride, then a shuffle tree: a fixed order), so all columns and slots are
+  // folded at once with a single block barrier; then one thread per column
+  // forms its scalars.
   __device__ void operator()() const {
     using R = Red<T>;
-    __shared__ typename R::P red[6 * 32];
-    __shared__ unsigned long long redk[6 * 32];
+    __shared__ double vals[MACSAV_MAX_COLUMNS][6];
     const bool gated = op == OP_RHO || op == OP_ALPHA || op == OP_CHECK || op == OP_FCG;
     const int mm = maxmask();
-    for (int c = 0; c < cols; ++c) {
-      if (gated && !active[c]) continue;  // uniform across the block
-      typename R::P s[6];
-      unsigned long long m[6];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int pr = wid; pr < cols * K; pr += nw) {
+      const int c = pr / K, k = pr - c * K;
+      if (gated && !active[c]) continue;  // uniform across the warp
+      const double* o = partial + size_t(c) * nb * K + k;
+      if ((mm >> k) & 1) {
+        unsigned long long m = 0ull;
+        for (int b = lane; b < nb; b += 32)
+          m = max(m, (unsigned long long)__ldcg(reinterpret_cast<const long long*>(o + size_t(b) * K)));
 #pragma unroll
-      for (int k = 0; k < 6; ++k) {
-        s[k] = R::zero();
-        m[k] = 0ull;
-      }
-      for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-        const double* o = partial + (size_t(c) * nb + b) * K;
+        for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, off));
+        if (lane == 0) vals[c][k] = key_value(m);
+      } else {
+        typename R::P v = R::zero();
+        for (int b = lane; b < nb; b += 32) v = R::add(v, R::load(o + size_t(b) * K));
 #pragma unroll
-        for (int k = 0; k < 6; ++k) {
-          if (k < K) {
-            if ((mm >> k) & 1) m[k] = max(m[k], (unsigned long long)__ldcg(reinterpret_cast<const long long*>(o + k)));
-            else s[k] = R::add(s[k], R::load(o + k));
-          }
-        }
+        for (int off = 16; off > 0; off >>= 1) v = R::add(v, R::shfl_down(v, off));
+        if (lane == 0) vals[c][k] = R::value(v);
       }
-      // fold only the slots in use (K <= 6)
-      for (int k = 0; k < K; ++k) {
-        if ((mm >> k) & 1) {
-          unsigned long long one[1] = {m[k]};
-          block_max_key<1>(one, redk);
-          m[k] = one[0];
-        } else {
-          typename R::P one[1] = {s[k]};
-          block_sum_p<T, 1>(one, red);
-          s[k] = one[0];
-        }
-      }
-      if (threadIdx.x == 0) {
-        double sv[6], mv[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-          sv[k] = R::value(s[k]);
-          mv[k] = key_value(m[k]);
-        }
-        update(c, sv, mv);
-      }
-      __syncthreads();
     }
-    if (use_cond && threadIdx.x == 0 && (op == OP_START || op == OP_CHECK)) {
-      int a = 0;
-      for (int c = 0; c < cols; ++c) a |= active[c];
-      cudaGraphSetConditional(cond, a ? 1u : 0u);
+    __syncthreads();
+    if (threadIdx.x < cols) {
+      const int c = threadIdx.x;
+      if (!(gated && !active[c])) update(c, vals[c], vals[c]);
+    }
+    if (use_cond && (op == OP_START || op == OP_CHECK)) {
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int a = 0;
+        for (int c = 0; c < cols; ++c) a |= active[c];
+        cudaGraphSetConditional(cond, a ? 1u : 0u);
+      }
     }
   }
 
-  __device__ void update(int c, const double (&s)[6], const double (&m)[6]) const {
+  // s[k] / m[k]: the folded sum / maximum of slot k (one array, per maxmask)
+  __device__ void update(int c, const double* s, const double* m) const {
     CGScalars& g = cg[c];
     switch (op) {
       case OP_MEAN_B:
-        g.mean_b = s[0] / np;
+        g.mean_b = s[0] * inv_np;
         g.mean_b_t = float(g.mean_b);
         break;
       case OP_START: {
         g.bnorm = sqrt(s[0]);
         g.max_b = m[1];
         g.atol = ktol * g.bnorm;  // _get_atol_rtol: max(atol=0, rtol*||b||)
+        g.atol2 = g.atol * g.atol;
         g.iters = 0;
         g.info = 0;
         g.rho_prev = 0;
@@ -226,8 +218,8 @@ struct CGFin {
         g.beta_t = float(g.beta);
         break;
       case OP_ALPHA:
-        g.mean_q = s[1] / np;
-        g.pq = s[0] - s[1] * s[2] / np;  // p . (q - mean(q))
+        g.mean_q = s[1] * inv_np;
+        g.pq = s[0] - s[1] * s[2] * inv_np;  // p . (q - mean(q))
         g.alpha = g.rho / g.pq;
         g.alpha_t = float(g.alpha);
         g.mean_q_t = float(g.mean_q);
@@ -238,7 +230,7 @@ struct CGFin {
         g.cum_iters += 1;
         if (g.net_on) g.cum_net_iters += 1;
         g.rho_prev = g.rho;
-        if (sqrt(g.rr) < g.atol) {
+        if (g.rr < g.atol2) {  // ||r|| < atol without the FP64 square root
           active[c] = 0;
         } else if (g.net_on && (g.iters >= net_maxit || !(g.rr == g.rr))) {
           // the learned attempt did not converge: plain PCG from zero
@@ -258,7 +250,7 @@ struct CGFin {
       case OP_FCG: {
         // z = M r + net(r): mean of z, rho = r.(z - mean), Polak-Ribiere beta
         // (r - r_old).(z - mean) / rho_prev (flexible CG)
-        g.mean_z = s[0] / np;
+        g.mean_z = s[0] * inv_np;
         g.mean_z_t = float(g.mean_z);
         g.rho = s[1] - g.mean_z * s[3];
         const double rzo = s[2] - g.mean_z * s[4];
@@ -268,7 +260,7 @@ struct CGFin {
         break;
       }
       case OP_MEAN_X:
-        g.mean_q = s[0] / np;
+        g.mean_q = s[0] * inv_np;
         g.mean_q_t = float(g.mean_q);
         break;
       case OP_CHECKS:
@@ -286,7 +278,7 @@ struct CGFin {
 template <typename T>
 inline CGFin<T> make_fin(const Plan* P, const Exec& X, int op, int nb, int K, int cols) {
   return CGFin<T>{op, P->partial, nb, K, cols, P->cg, P->active, P->g.np, X.ktol > 0 ? X.ktol : P->ktol, P->maxit,
-                  P->checks, X.graph ? 1 : 0, X.cond, X.net && P->net ? 1 : 0, P->net_maxit};
+                  P->checks, X.graph ? 1 : 0, X.cond, X.net && P->net ? 1 : 0, P->net_maxit, 1.0 / P->g.np};
 }
 
 // ------------------------------------------------------------- launching ---

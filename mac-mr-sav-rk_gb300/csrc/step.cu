@@ -39,7 +39,9 @@ const double kC3[5] = {0., 1. / 4, 4. / 5, 1., 1.};                             
 __global__ void __launch_bounds__(kThreads) k_combine2(CombineArgs a, const double* coef, long long n,
                                                        double* partial) {
   __shared__ double red[6 * 32];
-  double m[2] = {0.0, 0.0}, s[1] = {0.0};
+  __shared__ unsigned long long redk[2 * 32];
+  unsigned long long m[2] = {0ull, 0ull};  // abs_key maxima: integer pipe, NaN propagates
+  double s[1] = {0.0};
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     for (int o = 0; o < a.nout; ++o) {
       double acc = 0.0;
@@ -48,17 +50,17 @@ __global__ void __launch_bounds__(kThreads) k_combine2(CombineArgs a, const doub
         if (src) acc += coef[a.idx[o][t]] * src[i];
       }
       a.out[o][i] = acc;
-      m[o] = nanmax(m[o], fabs(acc));
+      m[o] = max(m[o], abs_key(acc));
       if (o == 1) s[0] += acc * acc;
     }
   }
-  block_max<2>(m, red);
+  block_max_key<2>(m, redk);
   block_sum<1>(s, red);
   if (threadIdx.x == 0) {
-    double* o = partial + blockIdx.x * 3;
+    unsigned long long* o = reinterpret_cast<unsigned long long*>(partial + blockIdx.x * 3);
     o[0] = m[0];
     o[1] = m[1];
-    o[2] = s[0];
+    partial[blockIdx.x * 3 + 2] = s[0];
   }
 }
 
@@ -109,10 +111,10 @@ __global__ void __launch_bounds__(kThreads) k_stage_defect(GridDev g, const doub
                                                            const double* rhs, const double* N, double* KU,
                                                            const StageRec* rec, const double* coef, int dt_idx,
                                                            int kappa_idx, int sav, double* partial) {
-  __shared__ double red[6 * 32];
+  __shared__ unsigned long long redk[4 * 32];
   const double dt = coef[dt_idx], kappa = coef[kappa_idx];
   const double dtc = sav ? dt * rec->coupling : 0.0;
-  double m[4] = {0, 0, 0, 0};
+  unsigned long long m[4] = {0, 0, 0, 0};  // abs_key maxima
   const int n = g.size > g.np ? g.size : g.np;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     if (i < g.size) {
@@ -123,18 +125,20 @@ __global__ void __launch_bounds__(kThreads) k_stage_defect(GridDev g, const doub
       d = d - dt * Dt_at(pi, g, i);
       d = d - rhs[i];
       if (sav) d = d + dtc * N[i];
-      m[0] = nanmax(m[0], fabs(d));
-      m[1] = nanmax(m[1], fabs(u));
+      m[0] = max(m[0], abs_key(d));
+      m[1] = max(m[1], abs_key(u));
     }
     if (i < g.np) {
       const int j = i / g.nx, k = i - j * g.nx;
-      m[2] = nanmax(m[2], fabs(D_at(U, g, j, k)));
-      m[3] = nanmax(m[3], fabs(pi[i]));
+      m[2] = max(m[2], abs_key(D_at(U, g, j, k)));
+      m[3] = max(m[3], abs_key(pi[i]));
     }
   }
-  block_max<4>(m, red);
-  if (threadIdx.x == 0)
-    for (int k = 0; k < 4; ++k) partial[blockIdx.x * 4 + k] = m[k];
+  block_max_key<4>(m, redk);
+  if (threadIdx.x == 0) {
+    unsigned long long* o = reinterpret_cast<unsigned long long*>(partial + blockIdx.x * 4);
+    for (int k = 0; k < 4; ++k) o[k] = m[k];
+  }
 }
 
 __device__ double fold_sum(const double* partial, int nb, int K, int k, double* red) {
@@ -143,11 +147,14 @@ __device__ double fold_sum(const double* partial, int nb, int K, int k, double* 
   block_sum<1>(s, red);
   return s[0];
 }
+// Maximum of abs_key partials (slot k of K per block), as a double.
 __device__ double fold_max(const double* partial, int nb, int K, int k, double* red) {
-  double m[1] = {0.0};
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) m[0] = nanmax(m[0], partial[b * K + k]);
-  block_max<1>(m, red);
-  return m[0];
+  unsigned long long* redk = reinterpret_cast<unsigned long long*>(red);
+  unsigned long long m[1] = {0ull};
+  const unsigned long long* p = reinterpret_cast<const unsigned long long*>(partial);
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) m[0] = max(m[0], p[b * K + k]);
+  block_max_key<1>(m, redk);
+  return key_value(m[0]);
 }
 
 // Stokes outcome of the stage: residual / divergence over both columns
