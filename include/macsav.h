@@ -237,6 +237,15 @@ int macsav_plan_cg_counters(macsav_plan* plan, int columns, int* iterations, int
 int macsav_stokes_log(macsav_plan* plan, const double* rhs, double mass, double viscosity, int max_pairs,
                       double* residuals, double* preconditioned, double* iterates, int* pairs, void* stream);
 
+/* After a step that produced an embedded velocity (macsav_step, or
+ * macsav_step_finish): out[0] = <x1 - emb, x1 - emb>_h, out[1] = <x0, x0>_h,
+ * out[2] = <x1, x1>_h (inner = hx*hy*dot, solver/mac/grid.py:67-68) and
+ * out[3] = 1 if emb has a non-finite entry, else 0.  These are the inner
+ * products of the adaptive controller's embedded error (controller.py:112-123),
+ * formed on the device inside the step, so an adaptive attempt costs one
+ * device round trip.  Reads host memory only. */
+int macsav_step_embedded_norms(macsav_plan* plan, double* out);
+
 /* Measurement helper (no reference counterpart: it times this library's own
  * kernels for the roofline): average device milliseconds of `reps`
  * back-to-back launches of one transform pass over the velocity blocks with two

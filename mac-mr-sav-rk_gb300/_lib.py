@@ -72,6 +72,7 @@ _SIGNATURES = {
     "macsav_plan_set_preconditioner": (_I, [_P, _P, _I]),
     "macsav_plan_cg_counters": (_I, [_P, _I, _P, _P, _P]),
     "macsav_stokes_log": (_I, [_P, _P, _D, _D, _I, _P, _P, _P, C.POINTER(_I), _P]),
+    "macsav_step_embedded_norms": (_I, [_P, C.POINTER(_D)]),
     "macsav_step_enqueue": (_I, [_P, _I, _D, _D, _D, _D, _P, _D, _P, _P, _P, _P, _P]),
     "macsav_step_finish": (_I, [_P, C.POINTER(StageRecord), C.POINTER(_D)]),
     "macsav_time_pass": (_I, [_P, _I, _I, C.POINTER(_D), C.POINTER(_D), _P]),

@@ -118,6 +118,15 @@ def _finite(model, x) -> bool:
     return bool(np.isfinite(model.max_abs(x)))
 
 
+def _error_from_norms(norms, controller: IController) -> float:
+    """``_error`` from the step's device inner products (sq, old_sq, high_sq)."""
+    sq, old_sq, high_sq = norms[:3]
+    if not np.isfinite([sq, old_sq, high_sq]).all() or min(sq, old_sq, high_sq) < 0:
+        return float("inf")
+    scale = controller.atol + controller.rtol * max(np.sqrt(old_sq), np.sqrt(high_sq))
+    return float(np.sqrt(sq) / scale)
+
+
 def _error(model, old, high, low, controller: IController, error_norm) -> float:
     """Scaled embedded error (``controller.py:112-123``)."""
     difference = model.combine((1., high), (-1., low))
@@ -227,11 +236,16 @@ def integrate_adaptive(model, scheme, initial, T: float, initial_step: float, *,
             high = model.vector(trial.state)
             if terminal:
                 trial.state = model.state(end, high, trial.state.r)
-            if not np.isfinite(high).all() or not _finite(model, trial.embedded_velocity) \
-                    or not np.isfinite(trial.state.r):
+            # a fused GPU step brings the embedded-error inner products with it
+            norms = getattr(trial, "embedded_norms", None) if error_norm is None else None
+            emb_finite = (norms[3] == 0.0) if norms is not None else _finite(model, trial.embedded_velocity)
+            if not np.isfinite(high).all() or not emb_finite or not np.isfinite(trial.state.r):
                 raise FloatingPointError("Nonfinite trial state")
-            error_u = _error(model, model.vector(result.final), high, trial.embedded_velocity, controller,
-                             error_norm)
+            if norms is not None:
+                error_u = _error_from_norms(norms, controller)
+            else:
+                error_u = _error(model, model.vector(result.final), high, trial.embedded_velocity, controller,
+                                 error_norm)
             error = error_u
             if scalar_control is not None:
                 scalar_defect = scalar_control.defect(result.final.r, trial.state.r, step)

@@ -449,6 +449,15 @@ int macsav_stokes_log(macsav_plan* plan, const double* rhs, double mass, double 
   return rc;
 }
 
+int macsav_step_embedded_norms(macsav_plan* plan, double* out) {
+  if (!plan || !out) return MACSAV_ERR_VALUE;
+  const macsav::StepBuffers& B = plan->p.st;
+  if (!B.h_enorm || !B.have_enorm || B.pending_stages > 0)
+    return fail(&plan->p, MACSAV_ERR_VALUE, "no finished step with an embedded velocity");
+  for (int k = 0; k < 4; ++k) out[k] = B.h_enorm[k];
+  return MACSAV_OK;
+}
+
 int macsav_time_pass(macsav_plan* plan, int pass, int reps, double* ms, double* bytes, void* stream) {
   if (!plan || !ms || !bytes) return MACSAV_ERR_VALUE;
   const int rc = macsav::time_pass(&plan->p, pass, reps, static_cast<cudaStream_t>(stream), ms, bytes);

@@ -58,7 +58,7 @@ static int pick_pairs(int L, int rows, int sms) {
 static int pick_strip(int L, int cols, int sms, int elem_bytes) {
   int W = 2;
   while (W < 32 && (W * 2 / 2) * L <= 4096 && W * 2 * L / 2 <= 4096) W *= 2;
-  const int wmin = std::min(W, std::max(2, 32 / elem_bytes));
+  const int wmin = std::min(W, std::max(2, 16 / elem_bytes));
   while (W > wmin && (cols + W - 1) / W < 2 * sms) W /= 2;
   return W;
 }

@@ -64,6 +64,9 @@ struct StepBuffers {
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   std::vector<GraphEntry> graphs;
   int pending_scheme = 0, pending_stages = 0;  // an enqueued step awaiting finish_step
+  double* enorm = nullptr;    // embedded-error inner products of the last step (device)
+  double* h_enorm = nullptr;  // and their pinned host copy
+  bool have_enorm = false;
 };
 
 template <typename T>

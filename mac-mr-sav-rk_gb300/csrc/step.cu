@@ -297,6 +297,59 @@ __global__ void k_set_shift(double* shift, const double* coef, int kappa_idx, in
   }
 }
 
+// Embedded-error inner products of a step (controller.py:112-123 needs
+// <x1-emb, x1-emb>, <x0, x0>, <x1, x1> with the grid weight hx*hy) and a
+// non-finite flag of emb, folded by the last block into out[0..3].
+struct EmbFin {
+  const double* partial;
+  int nb;
+  double w;
+  double* out;
+  __device__ void operator()() const {
+    __shared__ double red[3 * 32];
+    double s[3] = {0.0, 0.0, 0.0};
+    int bad = 0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+      for (int k = 0; k < 3; ++k) s[k] += __ldcg(partial + b * 4 + k);
+      bad |= __ldcg(partial + b * 4 + 3) != 0.0;
+    }
+    bad = __syncthreads_or(bad);
+    block_sum<3>(s, red);
+    if (threadIdx.x == 0) {
+      out[0] = w * s[0];
+      out[1] = w * s[1];
+      out[2] = w * s[2];
+      out[3] = bad ? 1.0 : 0.0;
+    }
+  }
+};
+__global__ void __launch_bounds__(kThreads) k_emb_norms(const double* x0, const double* x1, const double* emb,
+                                                        long long n, double* partial, EmbFin fin,
+                                                        unsigned int* done) {
+  __shared__ double red[3 * 32];
+  constexpr unsigned long long kInf = 0x7ff0000000000000ull;
+  double s[3] = {0.0, 0.0, 0.0};
+  int bad = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double a = x0[i], b = x1[i], e = emb[i];
+    const double d = b - e;
+    s[0] += d * d;
+    s[1] += a * a;
+    s[2] += b * b;
+    bad |= abs_key(e) >= kInf;
+  }
+  bad = __syncthreads_or(bad);
+  block_sum<3>(s, red);
+  if (threadIdx.x == 0) {
+    double* o = partial + blockIdx.x * 4;
+    o[0] = s[0];
+    o[1] = s[1];
+    o[2] = s[2];
+    o[3] = bad ? 1.0 : 0.0;
+  }
+  last_block_finish(fin, done);
+}
+
 __global__ void k_clear_recs(StageRec* recs, int n) {
   if (threadIdx.x < n) {
     StageRec z;
@@ -335,6 +388,8 @@ int step_buffers(Plan* P) {
   if (cudaMalloc(&B.recs, sizeof(StageRec) * 4) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (cudaMallocHost(&B.h_recs, sizeof(StageRec) * 4) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (cudaMallocHost(&B.h_coef, sizeof(double) * 256) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaMalloc(&B.enorm, sizeof(double) * 4) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaMallocHost(&B.h_enorm, sizeof(double) * 4) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (cudaStreamCreateWithFlags(&B.side, cudaStreamNonBlocking) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (cudaEventCreateWithFlags(&B.ev_in, cudaEventDisableTiming) != cudaSuccess) return MACSAV_ERR_CUDA;
@@ -350,6 +405,8 @@ void step_free(Plan* P) {
   cudaFree(B.recs);
   cudaFreeHost(B.h_recs);
   cudaFreeHost(B.h_coef);
+  cudaFree(B.enorm);
+  cudaFreeHost(B.h_enorm);
   if (B.stream) cudaStreamDestroy(B.stream);
   if (B.side) cudaStreamDestroy(B.side);
   if (B.ev_in) cudaEventDestroy(B.ev_in);
@@ -553,6 +610,13 @@ static int enqueue_step(Plan* P, Exec& X, int scheme, const StageProgram& G, boo
     }
     k_combine2<<<nbs, kThreads, 0, s>>>(e, B.coef, sz, P->partial);
     ++P->launches;
+    // the adaptive controller's inner products, so an attempt needs no more
+    // device round trips than the step itself
+    const int nbe = nbs < 1024 ? nbs : 1024;
+    k_emb_norms<<<nbe, kThreads, 0, s>>>(B.X, B.X + G.nstages * sz, B.EMB, sz, P->partial + 4096,
+                                         EmbFin{P->partial + 4096, nbe, P->g.hx * P->g.hy, B.enorm},
+                                         P->done_counter);
+    ++P->launches;
   }
   return MACSAV_OK;
 }
@@ -613,6 +677,8 @@ int enqueue_step_async(Plan* P, int scheme, double t, double dt, double nu, doub
   if (want_emb && G.emb_terms) cudaMemcpyAsync(embedded, B.EMB, sizeof(double) * sz, cudaMemcpyDeviceToDevice, s);
   if (pressures) cudaMemcpyAsync(pressures, B.PS, sizeof(double) * np * n, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(B.h_recs, B.recs, sizeof(StageRec) * n, cudaMemcpyDeviceToHost, s);
+  B.have_enorm = want_emb && G.emb_terms;
+  if (B.have_enorm) cudaMemcpyAsync(B.h_enorm, B.enorm, sizeof(double) * 4, cudaMemcpyDeviceToHost, s);
   cudaEventRecord(B.ev_out, s);
   cudaStreamWaitEvent(user, B.ev_out, 0);
   B.pending_scheme = scheme;

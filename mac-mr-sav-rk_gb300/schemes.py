@@ -151,7 +151,14 @@ class FusedScheme:
                 st.frozen_factor = float(rec.frozen_factor)
             stages.append(st)
         new_state = model.state(state.t + dt, x1, r1)
-        return Trial(new_state, stages, emb)
+        trial = Trial(new_state, stages, emb)
+        if emb is not None:
+            # <x1-emb, x1-emb>_h, <x0,x0>_h, <x1,x1>_h and emb's finiteness,
+            # formed on the device inside the step (for the adaptive driver)
+            norms = (C.c_double * 4)()
+            _lib.check(_lib.load().macsav_step_embedded_norms(model.plan.handle, norms), model.plan.handle)
+            trial.embedded_norms = tuple(float(v) for v in norms)
+        return trial
 
 
 def make_scheme(name: str, gamma: float = 1.0) -> FusedScheme:

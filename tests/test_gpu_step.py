@@ -142,3 +142,25 @@ def test_fp32_mixed_step_close_to_fp64(pkg, name):
         trial = pkg.make_scheme(name, gamma=float(d["gamma"])).step(model, state, float(d["dt"]))
         assert _rel(model.vector(trial.state), d["x1"]) < 1e-9
         assert abs(trial.state.r - float(d["r1"])) < 1e-10
+
+
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("name", ["sdirk3_mrsav", "sdirk2", "imex_euler"])
+def test_embedded_norms_match_host_inner_products(pkg, name, graph):
+    """The step's device inner products for the adaptive controller equal
+    the model's own inner products of the returned fields."""
+    d = golden("step_sdirk3_mrsav")
+    nx, ny, lx, ly = d["shape"]
+    g = pkg.MACGrid(int(nx), int(ny), float(lx), float(ly))
+    model = pkg.MACNavierStokes(g, float(d["nu"]), use_graph=graph)
+    state = model.state(0.1, d["x0"], 0.05)
+    trial = pkg.make_scheme(name).step(model, state, 0.01)
+    if trial.embedded_velocity is None:
+        assert not hasattr(trial, "embedded_norms")
+        return
+    high = model.device_vector(trial.state)
+    diff = model.combine((1.0, high), (-1.0, trial.embedded_velocity))
+    expect = (model.inner(diff, diff), model.inner(state.device, state.device), model.inner(high, high))
+    for got, want in zip(trial.embedded_norms[:3], expect):
+        assert got == pytest.approx(want, rel=1e-12, abs=1e-300)
+    assert trial.embedded_norms[3] == 0.0
