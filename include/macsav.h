@@ -246,6 +246,41 @@ int macsav_stokes_log(macsav_plan* plan, const double* rhs, double mass, double 
  * device round trip.  Reads host memory only. */
 int macsav_step_embedded_norms(macsav_plan* plan, double* out);
 
+/* ---- channel MAC: periodic x, no-slip walls in y (solver/channel/*.py).
+ * Packed free vector (grid.py:64-77): u faces (j, i), i < nx, then the v faces
+ * of the interior rows; cells (j, i).  All arithmetic FP64, device pointers,
+ * column-blocked multi-RHS data as for the cavity. */
+typedef struct macsav_channel macsav_channel;
+/* ChannelGrid(nx, ny, lx, ly) with FFTStokes(tolerance, cache_size)
+ * (fft_stokes.py:48-58); nx <= 2048. */
+int macsav_channel_create(macsav_channel** ch, int nx, int ny, double lx, double ly, double tolerance,
+                          int cache_size);
+void macsav_channel_destroy(macsav_channel* ch);
+const char* macsav_channel_error(const macsav_channel* ch);
+/* which: 0 K (operators.py:15-18), 1 D, 2 G = -D^T (operators.py:19-25),
+ * 3 skew convection (kernels.py:9-41). */
+int macsav_channel_apply(macsav_channel* ch, int which, const double* in, double* out, int columns, void* stream);
+/* out = sum_k coeffs[k] fields[k] in the order given (model.py:57-61); host
+ * coeffs, host array of device field pointers, nterms <= 8. */
+int macsav_channel_combine(macsav_channel* ch, int nterms, const double* coeffs, const double* const* fields,
+                           double* out, long long n, void* stream);
+/* result[0] = hx*hy*dot(a, b) (0 when b is NULL), result[1] = max|a| with NaN
+ * propagation (grid.py:79-80, model.py:81-82); host result, synchronises. */
+int macsav_channel_reduce(macsav_channel* ch, const double* a, const double* b, long long n, double* result,
+                          void* stream);
+/* flow rate through each x column: hy * sum_j u[j, i] (model.py:94-96), nx device values. */
+int macsav_channel_flow_rates(macsav_channel* ch, const double* velocity, double* out, void* stream);
+/* FFTStokes.solve (fft_stokes.py:94-137): orthonormal real FFTs along x, one
+ * banded saddle solve per x mode (factors cached per (mass, viscosity),
+ * least recently used evicted), inverse FFTs, pressure mean removed, FP64
+ * closing checks.  *factorized = 1 when this call factored a new shift.
+ * Errors: MACSAV_ERR_VALUE (shifts, RHS), MACSAV_ERR_CG (a singular band
+ * factor), MACSAV_ERR_STOKES_GATE ("Channel FFT residual=..., divergence=...").
+ * Synchronises. */
+int macsav_channel_solve(macsav_channel* ch, const double* rhs, int columns, double mass, double viscosity,
+                         double* velocity, double* pressure, double* residual, double* divergence, int* factorized,
+                         void* stream);
+
 /* Measurement helper (no reference counterpart: it times this library's own
  * kernels for the roofline): average device milliseconds of `reps`
  * back-to-back launches of one transform pass over the velocity blocks with two

@@ -15,10 +15,15 @@ from .integrate import Result, integrate, nearest_node_indices, schedule_nodes, 
 
 __all__ = ["MACGrid", "grid_of", "fields", "State", "Stage", "Trial", "DeviceArray", "stage_diagnostics",
            "Result", "integrate", "step_sizes", "schedule_nodes", "nearest_node_indices",
-           "TensorStokes", "StokesResult", "Plan", "MACNavierStokes", "make_scheme", "scheme_info", "SCHEMES"]
+           "TensorStokes", "StokesResult", "Plan", "MACNavierStokes", "make_scheme", "scheme_info", "SCHEMES",
+           "ChannelGrid", "ChannelModel", "ChannelOperators", "FFTStokes", "Ensemble", "ensemble_members",
+           "shard_members", "UNet", "integrate_adaptive", "IController", "PIController"]
 
 _LAZY = {"TensorStokes": "stokes", "StokesResult": "stokes", "Plan": "stokes", "MACNavierStokes": "model",
-         "make_scheme": "schemes", "scheme_info": "schemes", "SCHEMES": "schemes", "FusedScheme": "schemes"}
+         "make_scheme": "schemes", "scheme_info": "schemes", "SCHEMES": "schemes", "FusedScheme": "schemes",
+         "ChannelGrid": "channel", "ChannelModel": "channel", "ChannelOperators": "channel", "FFTStokes": "channel",
+         "Ensemble": "ensemble", "ensemble_members": "ensemble", "shard_members": "ensemble", "UNet": "learned",
+         "integrate_adaptive": "adaptivity", "IController": "adaptivity", "PIController": "adaptivity"}
 
 
 def __getattr__(name):

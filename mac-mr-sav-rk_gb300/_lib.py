@@ -73,6 +73,14 @@ _SIGNATURES = {
     "macsav_plan_cg_counters": (_I, [_P, _I, _P, _P, _P]),
     "macsav_stokes_log": (_I, [_P, _P, _D, _D, _I, _P, _P, _P, C.POINTER(_I), _P]),
     "macsav_step_embedded_norms": (_I, [_P, C.POINTER(_D)]),
+    "macsav_channel_create": (_I, [C.POINTER(_P), _I, _I, _D, _D, _D, _I]),
+    "macsav_channel_destroy": (None, [_P]),
+    "macsav_channel_error": (C.c_char_p, [_P]),
+    "macsav_channel_apply": (_I, [_P, _I, _P, _P, _I, _P]),
+    "macsav_channel_combine": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_P), _P, _LL, _P]),
+    "macsav_channel_reduce": (_I, [_P, _P, _P, _LL, C.POINTER(_D), _P]),
+    "macsav_channel_flow_rates": (_I, [_P, _P, _P, _P]),
+    "macsav_channel_solve": (_I, [_P, _P, _I, _D, _D, _P, _P, C.POINTER(_D), C.POINTER(_D), C.POINTER(_I), _P]),
     "macsav_step_enqueue": (_I, [_P, _I, _D, _D, _D, _D, _P, _D, _P, _P, _P, _P, _P]),
     "macsav_step_finish": (_I, [_P, C.POINTER(StageRecord), C.POINTER(_D)]),
     "macsav_time_pass": (_I, [_P, _I, _I, C.POINTER(_D), C.POINTER(_D), _P]),

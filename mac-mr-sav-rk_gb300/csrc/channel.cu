@@ -1,0 +1,819 @@
+// Channel MAC (periodic x, stationary no-slip walls in y) on the GPU: the
+// operators, the skew convection and the FFT Stokes backend of the reference
+// (solver/channel/operators.py, kernels.py, fft_stokes.py).
+//
+// Packed free vector (solver/channel/grid.py:64-77): u faces (j, i), j < ny,
+// i < nx (the periodic duplicate u[:, nx] = u[:, 0] is not stored) at j*nx+i,
+// then v faces of the interior rows J = 1..ny-1 at n_u + (J-1)*nx + i.
+//
+// FFT Stokes (fft_stokes.py:34-137): an orthonormal real FFT along x of every
+// row (two real rows per complex FFT, shared-memory FFT of fft.cuh), then for
+// each x mode m one solve of the banded saddle system in the interleaved
+// unknown order [u_j, p_j, v_j] (bandwidth 3):
+//   hu u - conj(d) p = fu,  hv v - Dy^T p = fv,  -d u - Dy v = 0,
+//   d = (exp(i theta) - 1)/hx (-2/hx at the Nyquist mode), lambda =
+//   4 sin^2(theta/2)/hx^2, hu = (m + k lambda) I + k Ly(ny, half-cell wall),
+//   hv = (m + k lambda) I + k Ly(ny-1, Dirichlet)
+// by banded LU with partial pivoting (the elimination of LAPACK's gbtf2 /
+// gbtrs, one thread per mode for the factors, one per (mode, column) for the
+// solves); mode 0 is a tridiagonal solve for u with v = 0 and p from the
+// cumulative sum of fv (mean removed); then the inverse FFTs and the FP64
+// closing checks.  Factors are cached per (mass, viscosity) like the
+// reference; all arithmetic is FP64.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fft.cuh"
+
+namespace macsav {
+
+FFTPlan make_fft_plan(int L);
+
+namespace {
+
+using cd = cplx<double>;
+constexpr int kKL = 3, kKU = 3, kLD = 2 * kKL + kKU + 1;  // band storage rows
+constexpr int kChThreads = 256;
+
+struct ChanGrid {
+  int nx, ny, nu, nv, size, np, nm;  // nm = nx/2 + 1 x modes
+  double hx, hy, ihx, ihy, ihx2, ihy2;
+};
+
+__device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+// u at (j, i) with periodic i; v at physical face row J (0 and ny are walls)
+__device__ __forceinline__ double cu_(const double* x, const ChanGrid& g, int j, int i) {
+  return x[j * g.nx + wrap(i, g.nx)];
+}
+__device__ __forceinline__ double cv_(const double* x, const ChanGrid& g, int J, int i) {
+  return (J <= 0 || J >= g.ny) ? 0.0 : x[g.nu + (J - 1) * g.nx + wrap(i, g.nx)];
+}
+
+// (K x)_e (operators.py:11-18): periodic second difference in x; in y the
+// half-cell tangential wall rows for u and the Dirichlet rows for v.
+__device__ double ch_K(const double* x, const ChanGrid& g, int e) {
+  if (e < g.nu) {
+    const int j = e / g.nx, i = e - j * g.nx;
+    const double c = x[e];
+    const double l = cu_(x, g, j, i - 1), r = cu_(x, g, j, i + 1);
+    const double s = j > 0 ? x[e - g.nx] : -c, n = j < g.ny - 1 ? x[e + g.nx] : -c;
+    return (2.0 * c - l - r) * g.ihx2 + (2.0 * c - s - n) * g.ihy2;
+  }
+  const int f = e - g.nu, k = f / g.nx, i = f - k * g.nx;
+  const double c = x[e];
+  const double l = x[g.nu + k * g.nx + wrap(i - 1, g.nx)], r = x[g.nu + k * g.nx + wrap(i + 1, g.nx)];
+  const double s = k > 0 ? x[e - g.nx] : 0.0, n = k < g.ny - 2 ? x[e + g.nx] : 0.0;
+  return (2.0 * c - l - r) * g.ihx2 + (2.0 * c - s - n) * g.ihy2;
+}
+// (D x) at cell (j, i) (operators.py:19-23)
+__device__ double ch_D(const double* x, const ChanGrid& g, int j, int i) {
+  return (cu_(x, g, j, i + 1) - cu_(x, g, j, i)) * g.ihx + (cv_(x, g, j + 1, i) - cv_(x, g, j, i)) * g.ihy;
+}
+// (G p)_e = -(D^T p)_e (operators.py:25)
+__device__ double ch_G(const double* p, const ChanGrid& g, int e) {
+  if (e < g.nu) {
+    const int j = e / g.nx, i = e - j * g.nx;
+    return (p[j * g.nx + i] - p[j * g.nx + wrap(i - 1, g.nx)]) * g.ihx;
+  }
+  const int f = e - g.nu, k = f / g.nx, i = f - k * g.nx;
+  return (p[(k + 1) * g.nx + i] - p[k * g.nx + i]) * g.ihy;
+}
+// Skew dual-cell convection (kernels.py:9-41)
+__device__ double ch_conv(const double* x, const ChanGrid& g, int e) {
+  if (e < g.nu) {
+    const int j = e / g.nx, i = e - j * g.nx;
+    const double uc = x[e], ue = cu_(x, g, j, i + 1), uw = cu_(x, g, j, i - 1);
+    const double east = 0.5 * (uc + ue), west = 0.5 * (uc + uw);
+    const double north = 0.5 * (cv_(x, g, j + 1, i - 1) + cv_(x, g, j + 1, i));
+    const double south = 0.5 * (cv_(x, g, j, i - 1) + cv_(x, g, j, i));
+    const double un = j < g.ny - 1 ? x[e + g.nx] : -uc, us = j > 0 ? x[e - g.nx] : -uc;
+    double r = (east * east - west * west) * g.ihx;
+    r += (north * 0.5 * (uc + un) - south * 0.5 * (uc + us)) * g.ihy;
+    r -= 0.5 * uc * ((east - west) * g.ihx + (north - south) * g.ihy);
+    return r;
+  }
+  const int f = e - g.nu, J = f / g.nx + 1, i = f - (J - 1) * g.nx;
+  const double vc = x[e];
+  const double east = 0.5 * (cu_(x, g, J - 1, i + 1) + cu_(x, g, J, i + 1));
+  const double west = 0.5 * (cu_(x, g, J - 1, i) + cu_(x, g, J, i));
+  const double vn = cv_(x, g, J + 1, i), vs = cv_(x, g, J - 1, i);
+  const double north = 0.5 * (vc + vn), south = 0.5 * (vc + vs);
+  double r = (east * 0.5 * (vc + cv_(x, g, J, i + 1)) - west * 0.5 * (vc + cv_(x, g, J, i - 1))) * g.ihx;
+  r += (north * north - south * south) * g.ihy;
+  r -= 0.5 * vc * ((east - west) * g.ihx + (north - south) * g.ihy);
+  return r;
+}
+
+// which: 0 K, 1 D (velocity -> cells), 2 G (cells -> velocity), 3 convection
+__global__ void k_ch_apply(ChanGrid g, int which, const double* in, double* out) {
+  const int c = blockIdx.y;
+  const int n = which == 1 ? g.np : g.size;
+  const long long is = which == 2 ? g.np : g.size, os = which == 1 ? g.np : g.size;
+  const double* x = in + c * is;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    double v;
+    if (which == 0) v = ch_K(x, g, e);
+    else if (which == 1) v = ch_D(x, g, e / g.nx, e - (e / g.nx) * g.nx);
+    else if (which == 2) v = ch_G(x, g, e);
+    else v = ch_conv(x, g, e);
+    out[c * os + e] = v;
+  }
+}
+
+// out = sum_k a_k f_k over n values, accumulated in the order given
+struct ChTerms {
+  const double* f[8];
+  double a[8];
+  int n;
+};
+__global__ void k_ch_combine(ChTerms t, double* out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < t.n; ++k) s += t.a[k] * t.f[k][i];
+    out[i] = s;
+  }
+}
+
+// Per-block partial sums / maxima for dot(a,b) and max|a| (abs keys).
+__global__ void k_ch_dot(const double* a, const double* b, long long n, double* partial) {
+  __shared__ double red[32];
+  __shared__ unsigned long long redk[32];
+  double s[1] = {0.0};
+  unsigned long long m[1] = {0ull};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double av = a[i];
+    if (b) s[0] += av * b[i];
+    m[0] = max(m[0], abs_key(av));
+  }
+  block_sum<1>(s, red);
+  block_max_key<1>(m, redk);
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x] = s[0];
+    reinterpret_cast<unsigned long long*>(partial)[2 * blockIdx.x + 1] = m[0];
+  }
+}
+__global__ void k_ch_dot_fold(const double* partial, int nb, double* out) {
+  __shared__ double red[32];
+  __shared__ unsigned long long redk[32];
+  double s[1] = {0.0};
+  unsigned long long m[1] = {0ull};
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    s[0] += partial[2 * b];
+    m[0] = max(m[0], reinterpret_cast<const unsigned long long*>(partial)[2 * b + 1]);
+  }
+  block_sum<1>(s, red);
+  block_max_key<1>(m, redk);
+  if (threadIdx.x == 0) {
+    out[0] = s[0];
+    out[1] = key_value(m[0]);
+  }
+}
+
+// flow rate through each x column of u faces: hy * sum_j u[j, i] (model.py:94-96)
+__global__ void k_ch_flow(ChanGrid g, const double* x, double* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.nx; i += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < g.ny; ++j) s += x[j * g.nx + i];
+    out[i] = g.hy * s;
+  }
+}
+
+// ------------------------------------------------------------ real FFTs ---
+// rows of length nx, two real rows per complex line; spectral layout
+// [column][row][nm] complex (orthonormal scaling).
+__global__ void k_ch_rfft(const double* in, long long cstride, int rows, int nx, int nm, cd* out,
+                          long long ostride, FFTPlan plan, const cd* tw, double scale, int nl) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cd* buf = reinterpret_cast<cd*>(smraw);
+  cd* tmp = buf + nl * nx;
+  const int c = blockIdx.y;
+  const int pair0 = blockIdx.x * nl;
+  const int npairs = (rows + 1) / 2;
+  const double* x = in + c * cstride;
+  for (int e = threadIdx.x; e < nl * nx; e += blockDim.x) {
+    const int q = e / nx, i = e - q * nx, pr = pair0 + q;
+    const int ra = 2 * pr, rb = 2 * pr + 1;
+    const double a = (pr < npairs && ra < rows) ? x[(long long)ra * nx + i] : 0.0;
+    const double b = (pr < npairs && rb < rows) ? x[(long long)rb * nx + i] : 0.0;
+    buf[e] = mk(a, b);
+  }
+  __syncthreads();
+  fft_lines<double, 8>(buf, tmp, plan, nx, nl, tw, -1);
+  cd* o = out + c * ostride;
+  for (int e = threadIdx.x; e < nl * nm; e += blockDim.x) {
+    const int q = e / nm, k = e - q * nm, pr = pair0 + q;
+    if (pr >= npairs) continue;
+    const cd zk = buf[q * nx + k], zm = buf[q * nx + (k == 0 ? 0 : nx - k)];
+    const cd cz = conjg(zm);
+    // A = (Z_k + conj Z_{N-k}) / 2, B = (Z_k - conj Z_{N-k}) / (2i)
+    const cd A = mk(0.5 * (zk.x + cz.x) * scale, 0.5 * (zk.y + cz.y) * scale);
+    const cd B = mk(0.5 * (zk.y - cz.y) * scale, -0.5 * (zk.x - cz.x) * scale);
+    const int ra = 2 * pr, rb = 2 * pr + 1;
+    o[(long long)ra * nm + k] = A;
+    if (rb < rows) o[(long long)rb * nm + k] = B;
+  }
+}
+
+// inverse of k_ch_rfft (numpy irfft semantics: the imaginary parts of the
+// mode-0 and Nyquist coefficients are ignored)
+__global__ void k_ch_irfft(const cd* in, long long istride, int rows, int nx, int nm, double* out, long long cstride,
+                           FFTPlan plan, const cd* tw, double scale, int nl) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cd* buf = reinterpret_cast<cd*>(smraw);
+  cd* tmp = buf + nl * nx;
+  const int c = blockIdx.y;
+  const int pair0 = blockIdx.x * nl;
+  const int npairs = (rows + 1) / 2;
+  const cd* s = in + c * istride;
+  const bool even = (nx % 2) == 0;
+  for (int e = threadIdx.x; e < nl * nx; e += blockDim.x) {
+    const int q = e / nx, k = e - q * nx, pr = pair0 + q;
+    const int ra = 2 * pr, rb = 2 * pr + 1;
+    cd A = mk(0.0, 0.0), B = mk(0.0, 0.0);
+    const int kk = k < nm ? k : nx - k;
+    if (pr < npairs) {
+      A = s[(long long)ra * nm + kk];
+      if (rb < rows) B = s[(long long)rb * nm + kk];
+    }
+    if (kk == 0 || (even && kk == nx / 2)) {
+      A.y = 0.0;
+      B.y = 0.0;
+    }
+    if (k >= nm) {  // Hermitian half: Z_k = conj(A_{N-k}) + i conj(B_{N-k})
+      A = conjg(A);
+      B = conjg(B);
+    }
+    buf[e] = mk(A.x - B.y, A.y + B.x);  // A + i B
+  }
+  __syncthreads();
+  fft_lines<double, 8>(buf, tmp, plan, nx, nl, tw, +1);
+  double* x = out + c * cstride;
+  for (int e = threadIdx.x; e < nl * nx; e += blockDim.x) {
+    const int q = e / nx, i = e - q * nx, pr = pair0 + q;
+    if (pr >= npairs) continue;
+    const int ra = 2 * pr, rb = 2 * pr + 1;
+    x[(long long)ra * nx + i] = buf[e].x * scale;
+    if (rb < rows) x[(long long)rb * nx + i] = buf[e].y * scale;
+  }
+}
+
+// ---------------------------------------------------------- mode solves ---
+struct ModeCoef {
+  cd d;
+  double lam;
+};
+__device__ ModeCoef mode_coef(const ChanGrid& g, int m) {
+  const double kPi = 3.14159265358979323846264338327950288;
+  const double theta = 2.0 * kPi * m / g.nx;
+  ModeCoef r;
+  if ((g.nx % 2) == 0 && m == g.nx / 2) r.d = mk(-2.0 * g.ihx, 0.0);
+  else r.d = mk((cos(theta) - 1.0) * g.ihx, sin(theta) * g.ihx);
+  const double sh = sin(0.5 * theta);
+  r.lam = 4.0 * sh * sh * g.ihx2;
+  return r;
+}
+
+// band element (i, j) of mode m's factor array (LAPACK band layout: column
+// j holds rows j-KU-KL .. j+KL at offsets 0 .. LD-1)
+__device__ __forceinline__ cd& band(cd* ab, int i, int j) { return ab[(long long)j * kLD + (kKL + kKU + i - j)]; }
+
+// Assemble and factor the saddle system of every mode m >= 1 (one thread per
+// mode); mode 0 stores the Thomas factors of hu0 = m I + k Ly(ny, wall).
+__global__ void k_ch_factor(ChanGrid g, double mass, double visc, cd* lu, int* piv, double* zero, int* status) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= g.nm) return;
+  const int ny = g.ny;
+  const double iy2 = g.ihy2;
+  if (m == 0) {
+    // Thomas: diag a_j = mass + visc*wall_j/hy^2, off = -visc/hy^2
+    double* cp = zero;        // modified super-diagonal
+    double* dn = zero + ny;   // pivots
+    const double off = -visc * iy2;
+    for (int j = 0; j < ny; ++j) {
+      const double a = mass + visc * ((j == 0 || j == ny - 1) ? 3.0 : 2.0) * iy2;
+      const double den = j == 0 ? a : a - off * cp[j - 1];
+      dn[j] = den;
+      cp[j] = off / den;
+      if (!(den != 0.0)) status[0] = 1;
+    }
+    return;
+  }
+  const int n = 3 * ny - 1;
+  cd* ab = lu + (long long)(m - 1) * n * kLD;
+  int* pv = piv + (long long)(m - 1) * n;
+  for (long long e = 0; e < (long long)n * kLD; ++e) ab[e] = mk(0.0, 0.0);
+  const ModeCoef mc = mode_coef(g, m);
+  const double a0 = mass + visc * mc.lam;
+  const cd d = mc.d, dc = conjg(d);
+  for (int j = 0; j < ny; ++j) {
+    const int ru = 3 * j, rp = 3 * j + 1, rv = 3 * j + 2;
+    // u_j momentum: hu, -conj(d) p_j
+    band(ab, ru, ru) = mk(a0 + visc * ((j == 0 || j == ny - 1) ? 3.0 : 2.0) * iy2, 0.0);
+    if (j > 0) band(ab, ru, ru - 3) = mk(-visc * iy2, 0.0);
+    if (j < ny - 1) band(ab, ru, ru + 3) = mk(-visc * iy2, 0.0);
+    band(ab, ru, rp) = mk(-dc.x, -dc.y);
+    // continuity j (negated): -d u_j - (v_j - v_{j-1})/hy
+    band(ab, rp, ru) = mk(-d.x, -d.y);
+    if (j < ny - 1) band(ab, rp, rv) = mk(-g.ihy, 0.0);
+    if (j > 0) band(ab, rp, rv - 3) = mk(g.ihy, 0.0);
+    // v_j momentum (face j+1): hv, -(p_j - p_{j+1})/hy
+    if (j < ny - 1) {
+      band(ab, rv, rv) = mk(a0 + 2.0 * visc * iy2, 0.0);
+      if (j > 0) band(ab, rv, rv - 3) = mk(-visc * iy2, 0.0);
+      if (j < ny - 2) band(ab, rv, rv + 3) = mk(-visc * iy2, 0.0);
+      band(ab, rv, rp) = mk(-g.ihy, 0.0);
+      band(ab, rv, rp + 3) = mk(g.ihy, 0.0);
+    }
+  }
+  // banded LU with partial pivoting (the elimination order of gbtf2)
+  int ju = 0;
+  for (int k = 0; k < n; ++k) {
+    const int km = min(kKL, n - 1 - k);
+    int p = 0;
+    double best = -1.0;
+    for (int r = 0; r <= km; ++r) {
+      const cd v = band(ab, k + r, k);
+      const double a = fabs(v.x) + fabs(v.y);  // |re| + |im|, as izamax
+      if (a > best) {
+        best = a;
+        p = r;
+      }
+    }
+    pv[k] = k + p;
+    if (!(best > 0.0)) {
+      status[0] = 2;
+      continue;
+    }
+    ju = max(ju, min(k + kKU + p, n - 1));
+    if (p != 0)
+      for (int j = k; j <= ju; ++j) {
+        const cd t = band(ab, k, j);
+        band(ab, k, j) = band(ab, k + p, j);
+        band(ab, k + p, j) = t;
+      }
+    const cd piv_v = band(ab, k, k);
+    const double den = piv_v.x * piv_v.x + piv_v.y * piv_v.y;
+    const cd inv = mk(piv_v.x / den, -piv_v.y / den);
+    for (int r = 1; r <= km; ++r) band(ab, k + r, k) = cmul(band(ab, k + r, k), inv);
+    for (int j = k + 1; j <= ju; ++j) {
+      const cd akj = band(ab, k, j);
+      if (akj.x == 0.0 && akj.y == 0.0) continue;
+      for (int r = 1; r <= km; ++r) {
+        cd& t = band(ab, k + r, j);
+        t = t - cmul(band(ab, k + r, k), akj);
+      }
+    }
+  }
+}
+
+// One thread per (mode, column): right-hand side in the interleaved order,
+// gbtrs-style forward and back substitution, scatter to u/v/p spectra.
+__global__ void k_ch_solve(ChanGrid g, const cd* fu, const cd* fv, long long fstride, const cd* lu, const int* piv,
+                           const double* zero, cd* uo, cd* vo, cd* po, long long vstride, long long pstride, cd* work,
+                           int cols, double mass, double visc) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = t % g.nm, c = t / g.nm;
+  if (c >= cols) return;
+  const int ny = g.ny, nm = g.nm;
+  const cd* fuc = fu + c * fstride;
+  const cd* fvc = fv + c * fstride;
+  cd* uc = uo + c * vstride;
+  cd* vc = vo + c * vstride;
+  cd* pc = po + c * pstride;
+  if (m == 0) {
+    const double* cp = zero;
+    const double* dn = zero + ny;
+    const double off = -visc * g.ihy2;
+    // hu0 u = fu (Thomas), v = 0, p_{k+1} = p_k + hy fv_k, mean removed
+    cd prev = mk(0.0, 0.0);
+    for (int j = 0; j < ny; ++j) {
+      const cd f = fuc[(long long)j * nm];
+      const cd y = j == 0 ? mk(f.x / dn[0], f.y / dn[0])
+                          : mk((f.x - off * prev.x) / dn[j], (f.y - off * prev.y) / dn[j]);
+      uc[(long long)j * nm] = y;
+      prev = y;
+    }
+    for (int j = ny - 2; j >= 0; --j) {
+      const cd nx1 = uc[(long long)(j + 1) * nm];
+      const cd y = uc[(long long)j * nm];
+      uc[(long long)j * nm] = mk(y.x - cp[j] * nx1.x, y.y - cp[j] * nx1.y);
+    }
+    for (int k = 0; k < ny - 1; ++k) vc[(long long)k * nm] = mk(0.0, 0.0);
+    cd p = mk(0.0, 0.0), sum = mk(0.0, 0.0);
+    for (int j = 0; j < ny; ++j) {
+      if (j > 0) {
+        const cd f = fvc[(long long)(j - 1) * nm];
+        p = mk(p.x + g.hy * f.x, p.y + g.hy * f.y);
+      }
+      pc[(long long)j * nm] = p;
+      sum = sum + p;
+    }
+    const cd mean = mk(sum.x / ny, sum.y / ny);
+    for (int j = 0; j < ny; ++j) pc[(long long)j * nm] = pc[(long long)j * nm] - mean;
+    return;
+  }
+  const int n = 3 * ny - 1;
+  const cd* ab = lu + (long long)(m - 1) * n * kLD;
+  const int* pv = piv + (long long)(m - 1) * n;
+  cd* b = work + ((long long)c * nm + m) * n;
+  for (int j = 0; j < ny; ++j) {
+    b[3 * j] = fuc[(long long)j * nm + m];
+    b[3 * j + 1] = mk(0.0, 0.0);
+    if (j < ny - 1) b[3 * j + 2] = fvc[(long long)j * nm + m];
+  }
+  auto A = [&](int i, int j) { return ab[(long long)j * kLD + (kKL + kKU + i - j)]; };
+  for (int k = 0; k < n; ++k) {
+    const int p = pv[k];
+    if (p != k) {
+      const cd tmp = b[k];
+      b[k] = b[p];
+      b[p] = tmp;
+    }
+    const int km = min(kKL, n - 1 - k);
+    const cd bk = b[k];
+    for (int r = 1; r <= km; ++r) b[k + r] = b[k + r] - cmul(A(k + r, k), bk);
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    cd s = b[k];
+    const int last = min(n - 1, k + kKL + kKU);
+    for (int j = k + 1; j <= last; ++j) s = s - cmul(A(k, j), b[j]);
+    const cd pk = A(k, k);
+    const double den = pk.x * pk.x + pk.y * pk.y;
+    b[k] = mk((s.x * pk.x + s.y * pk.y) / den, (s.y * pk.x - s.x * pk.y) / den);
+  }
+  for (int j = 0; j < ny; ++j) {
+    uc[(long long)j * nm + m] = b[3 * j];
+    pc[(long long)j * nm + m] = b[3 * j + 1];
+    if (j < ny - 1) vc[(long long)j * nm + m] = b[3 * j + 2];
+  }
+  (void)mass;
+}
+
+// pressure -= mean over all cells, per column (fft_stokes.py:122)
+__global__ void k_ch_center(double* p, int np, double* partial) {
+  __shared__ double red[32];
+  const int c = blockIdx.x;
+  double s[1] = {0.0};
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s[0] += p[(long long)c * np + i];
+  block_sum<1>(s, red);
+  __shared__ double mean;
+  if (threadIdx.x == 0) mean = s[0] / np;
+  __syncthreads();
+  for (int i = threadIdx.x; i < np; i += blockDim.x) p[(long long)c * np + i] -= mean;
+}
+
+// Closing checks (fft_stokes.py:124-131): max|defect|, max|f|, max|u|,
+// max|D u|, non-finite velocity/pressure; abs keys folded per column.
+__global__ void k_ch_check(ChanGrid g, const double* vel, const double* pres, const double* f, double mass,
+                           double visc, unsigned long long* keys) {
+  constexpr unsigned long long kInf = 0x7ff0000000000000ull;
+  __shared__ unsigned long long redk[5 * 32];
+  const int c = blockIdx.y;
+  const double* u = vel + (long long)c * g.size;
+  const double* p = pres + (long long)c * g.np;
+  const double* ff = f + (long long)c * g.size;
+  unsigned long long m[5] = {0, 0, 0, 0, 0};
+  const int n = g.size > g.np ? g.size : g.np;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    if (e < g.size) {
+      const double d = mass * u[e] + visc * ch_K(u, g, e) + ch_G(p, g, e) - ff[e];
+      m[0] = max(m[0], abs_key(d));
+      m[1] = max(m[1], abs_key(ff[e]));
+      const unsigned long long ku = abs_key(u[e]);
+      m[2] = max(m[2], ku);
+      if (ku >= kInf) m[4] = 1;
+    }
+    if (e < g.np) {
+      const int j = e / g.nx, i = e - j * g.nx;
+      m[3] = max(m[3], abs_key(ch_D(u, g, j, i)));
+      if (abs_key(p[e]) >= kInf) m[4] = 1;
+    }
+  }
+  block_max_key<5>(m, redk);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 5; ++k) atomicMax(keys + c * 5 + k, m[k]);
+}
+
+}  // namespace
+
+struct Channel {
+  ChanGrid g;
+  double lx, ly, tol;
+  int cache_size;
+  std::string err;
+  FFTPlan plan;
+  cd* tw = nullptr;
+  int nl = 1;
+  size_t smem = 0;
+  // factor cache: (mass, visc) -> slot
+  struct Slot {
+    double mass, visc;
+    cd* lu;
+    int* piv;
+    double* zero;
+    long long last_use;
+  };
+  std::vector<Slot> slots;
+  long long clock = 0;
+  int* status = nullptr;
+  int* h_status = nullptr;
+  // per-solve buffers (maxcols columns)
+  int maxcols = 0;
+  cd *fspec = nullptr, *uspec = nullptr, *pspec = nullptr, *work = nullptr;
+  unsigned long long* keys = nullptr;
+  unsigned long long* h_keys = nullptr;
+  double* partial = nullptr;
+  double* h_red = nullptr;
+  double* d_red = nullptr;
+};
+
+}  // namespace macsav
+
+using macsav::Channel;
+using macsav::cd;
+
+struct macsav_channel {
+  Channel ch;
+};
+
+namespace {
+
+int ch_fail(Channel* C, int code, const char* msg) {
+  C->err = msg;
+  return code;
+}
+int ch_cuda(Channel* C) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    C->err = std::string("CUDA: ") + cudaGetErrorString(e);
+    return MACSAV_ERR_CUDA;
+  }
+  return MACSAV_OK;
+}
+int ch_grid_blocks(long long n) {
+  long long b = (n + macsav::kChThreads - 1) / macsav::kChThreads;
+  return int(b < 1 ? 1 : (b > 1024 ? 1024 : b));
+}
+
+int ensure_buffers(Channel* C, int cols) {
+  if (cols <= C->maxcols) return MACSAV_OK;
+  cudaFree(C->fspec);
+  cudaFree(C->uspec);
+  cudaFree(C->pspec);
+  cudaFree(C->work);
+  cudaFree(C->keys);
+  cudaFreeHost(C->h_keys);
+  const auto& g = C->g;
+  const size_t rows = size_t(2 * g.ny - 1);
+  if (cudaMalloc(&C->fspec, sizeof(cd) * rows * g.nm * cols) != cudaSuccess ||
+      cudaMalloc(&C->uspec, sizeof(cd) * rows * g.nm * cols) != cudaSuccess ||
+      cudaMalloc(&C->pspec, sizeof(cd) * size_t(g.ny) * g.nm * cols) != cudaSuccess ||
+      cudaMalloc(&C->work, sizeof(cd) * size_t(3 * g.ny - 1) * g.nm * cols) != cudaSuccess ||
+      cudaMalloc(&C->keys, sizeof(unsigned long long) * 5 * cols) != cudaSuccess ||
+      cudaMallocHost(&C->h_keys, sizeof(unsigned long long) * 5 * cols) != cudaSuccess)
+    return ch_cuda(C);
+  C->maxcols = cols;
+  return MACSAV_OK;
+}
+
+void launch_fft(Channel* C, bool inverse, const void* in, long long istride, int rows, void* out, long long ostride,
+                int cols, cudaStream_t s) {
+  const auto& g = C->g;
+  const int npairs = (rows + 1) / 2;
+  const dim3 grid((npairs + C->nl - 1) / C->nl, cols);
+  const double scale = 1.0 / std::sqrt(double(g.nx));
+  if (!inverse)
+    macsav::k_ch_rfft<<<grid, macsav::kChThreads, C->smem, s>>>(static_cast<const double*>(in), istride, rows, g.nx,
+                                                               g.nm, static_cast<cd*>(out), ostride, C->plan, C->tw,
+                                                               scale, C->nl);
+  else
+    macsav::k_ch_irfft<<<grid, macsav::kChThreads, C->smem, s>>>(static_cast<const cd*>(in), istride, rows, g.nx,
+                                                                g.nm, static_cast<double*>(out), ostride, C->plan,
+                                                                C->tw, scale, C->nl);
+}
+
+}  // namespace
+
+extern "C" {
+
+int macsav_channel_create(macsav_channel** out, int nx, int ny, double lx, double ly, double tolerance,
+                          int cache_size) {
+  if (!out) return MACSAV_ERR_VALUE;
+  *out = nullptr;
+  if (nx < 3 || ny < 3 || !std::isfinite(lx) || !std::isfinite(ly) || lx <= 0 || ly <= 0) return MACSAV_ERR_VALUE;
+  if (cache_size < 1 || !(tolerance > 0) || !std::isfinite(tolerance)) return MACSAV_ERR_VALUE;
+  if (nx > 2048) return MACSAV_ERR_UNSUPPORTED;
+  macsav_channel* h = new macsav_channel();
+  Channel& C = h->ch;
+  auto& g = C.g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nu = nx * ny;
+  g.nv = nx * (ny - 1);
+  g.size = g.nu + g.nv;
+  g.np = nx * ny;
+  g.nm = nx / 2 + 1;
+  g.hx = lx / nx;
+  g.hy = ly / ny;
+  g.ihx = 1.0 / g.hx;
+  g.ihy = 1.0 / g.hy;
+  g.ihx2 = g.ihx * g.ihx;
+  g.ihy2 = g.ihy * g.ihy;
+  C.lx = lx;
+  C.ly = ly;
+  C.tol = tolerance;
+  C.cache_size = cache_size;
+  C.plan = macsav::make_fft_plan(nx);
+  std::vector<cd> tw(nx);
+  const double kPi = 3.14159265358979323846264338327950288;
+  for (int m = 0; m < nx; ++m) tw[m] = macsav::mk(std::cos(2 * kPi * m / nx), -std::sin(2 * kPi * m / nx));
+  C.nl = std::max(1, 2048 / nx);
+  C.smem = size_t(2) * C.nl * nx * sizeof(cd);
+  int rc = MACSAV_OK;
+  if (cudaMalloc(&C.tw, sizeof(cd) * nx) != cudaSuccess ||
+      cudaMemcpy(C.tw, tw.data(), sizeof(cd) * nx, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMalloc(&C.status, sizeof(int)) != cudaSuccess || cudaMallocHost(&C.h_status, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&C.partial, sizeof(double) * 2 * 1024) != cudaSuccess ||
+      cudaMalloc(&C.d_red, sizeof(double) * 2) != cudaSuccess ||
+      cudaMallocHost(&C.h_red, sizeof(double) * 2) != cudaSuccess)
+    rc = MACSAV_ERR_CUDA;
+  if (rc == MACSAV_OK && C.smem > 48 * 1024) {
+    cudaFuncSetAttribute(macsav::k_ch_rfft, cudaFuncAttributeMaxDynamicSharedMemorySize, int(C.smem));
+    cudaFuncSetAttribute(macsav::k_ch_irfft, cudaFuncAttributeMaxDynamicSharedMemorySize, int(C.smem));
+  }
+  if (rc == MACSAV_OK) rc = ensure_buffers(&C, 2);
+  if (rc != MACSAV_OK) {
+    macsav_channel_destroy(h);
+    return MACSAV_ERR_CUDA;
+  }
+  *out = h;
+  return MACSAV_OK;
+}
+
+void macsav_channel_destroy(macsav_channel* h) {
+  if (!h) return;
+  Channel& C = h->ch;
+  cudaDeviceSynchronize();
+  for (auto& s : C.slots) {
+    cudaFree(s.lu);
+    cudaFree(s.piv);
+    cudaFree(s.zero);
+  }
+  cudaFree(C.tw);
+  cudaFree(C.status);
+  cudaFreeHost(C.h_status);
+  cudaFree(C.fspec);
+  cudaFree(C.uspec);
+  cudaFree(C.pspec);
+  cudaFree(C.work);
+  cudaFree(C.keys);
+  cudaFreeHost(C.h_keys);
+  cudaFree(C.partial);
+  cudaFree(C.d_red);
+  cudaFreeHost(C.h_red);
+  delete h;
+}
+
+const char* macsav_channel_error(const macsav_channel* h) { return h ? h->ch.err.c_str() : ""; }
+
+int macsav_channel_apply(macsav_channel* h, int which, const double* in, double* out, int cols, void* stream) {
+  if (!h || !in || !out || which < 0 || which > 3 || cols < 1) return MACSAV_ERR_VALUE;
+  Channel& C = h->ch;
+  const int n = which == 1 ? C.g.np : C.g.size;
+  macsav::k_ch_apply<<<dim3(ch_grid_blocks(n), cols), macsav::kChThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      C.g, which, in, out);
+  return ch_cuda(&C);
+}
+
+int macsav_channel_combine(macsav_channel* h, int nterms, const double* coeffs, const double* const* fields,
+                           double* out, long long n, void* stream) {
+  if (!h || nterms < 1 || nterms > 8 || !coeffs || !fields || !out || n < 0) return MACSAV_ERR_VALUE;
+  macsav::ChTerms t;
+  t.n = nterms;
+  for (int k = 0; k < nterms; ++k) {
+    t.f[k] = fields[k];
+    t.a[k] = coeffs[k];
+  }
+  macsav::k_ch_combine<<<ch_grid_blocks(n), macsav::kChThreads, 0, static_cast<cudaStream_t>(stream)>>>(t, out, n);
+  return ch_cuda(&h->ch);
+}
+
+int macsav_channel_reduce(macsav_channel* h, const double* a, const double* b, long long n, double* result,
+                          void* stream) {
+  if (!h || !a || !result || n < 0) return MACSAV_ERR_VALUE;
+  Channel& C = h->ch;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int nb = ch_grid_blocks(n);
+  macsav::k_ch_dot<<<nb, macsav::kChThreads, 0, s>>>(a, b, n, C.partial);
+  macsav::k_ch_dot_fold<<<1, macsav::kChThreads, 0, s>>>(C.partial, nb, C.d_red);
+  cudaMemcpyAsync(C.h_red, C.d_red, sizeof(double) * 2, cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return ch_cuda(&C);
+  result[0] = C.h_red[0] * C.g.hx * C.g.hy;
+  result[1] = C.h_red[1];
+  return ch_cuda(&C);
+}
+
+int macsav_channel_flow_rates(macsav_channel* h, const double* x, double* out, void* stream) {
+  if (!h || !x || !out) return MACSAV_ERR_VALUE;
+  macsav::k_ch_flow<<<ch_grid_blocks(h->ch.g.nx), macsav::kChThreads, 0, static_cast<cudaStream_t>(stream)>>>(h->ch.g,
+                                                                                                            x, out);
+  return ch_cuda(&h->ch);
+}
+
+int macsav_channel_solve(macsav_channel* h, const double* rhs, int cols, double mass, double viscosity, double* vel,
+                         double* pres, double* residual, double* divergence, int* factorized, void* stream) {
+  if (!h) return MACSAV_ERR_VALUE;
+  Channel& C = h->ch;
+  const auto& g = C.g;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!std::isfinite(mass) || !std::isfinite(viscosity) || std::fmin(mass, viscosity) < 0 || mass + viscosity <= 0)
+    return ch_fail(&C, MACSAV_ERR_VALUE, "Require nonnegative mass/viscosity with nonzero total");
+  if (!rhs || !vel || !pres || cols < 1) return ch_fail(&C, MACSAV_ERR_VALUE, "Invalid channel FFT RHS");
+  int rc = ensure_buffers(&C, cols);
+  if (rc != MACSAV_OK) return rc;
+  if (factorized) *factorized = 0;
+  // factor cache (fft_stokes.py:64-92): least recently used slot is evicted
+  Channel::Slot* slot = nullptr;
+  for (auto& sl : C.slots)
+    if (sl.mass == mass && sl.visc == viscosity) slot = &sl;
+  if (!slot) {
+    Channel::Slot fresh{mass, viscosity, nullptr, nullptr, nullptr, 0};
+    if (int(C.slots.size()) >= C.cache_size) {
+      size_t old = 0;
+      for (size_t k = 1; k < C.slots.size(); ++k)
+        if (C.slots[k].last_use < C.slots[old].last_use) old = k;
+      fresh.lu = C.slots[old].lu;
+      fresh.piv = C.slots[old].piv;
+      fresh.zero = C.slots[old].zero;
+      C.slots.erase(C.slots.begin() + old);
+    } else {
+      const long long n = 3LL * g.ny - 1;
+      const long long nmodes = std::max(1, g.nm - 1);
+      if (cudaMalloc(&fresh.lu, sizeof(cd) * n * macsav::kLD * nmodes) != cudaSuccess ||
+          cudaMalloc(&fresh.piv, sizeof(int) * n * nmodes) != cudaSuccess ||
+          cudaMalloc(&fresh.zero, sizeof(double) * 2 * g.ny) != cudaSuccess)
+        return ch_cuda(&C);
+    }
+    cudaMemsetAsync(C.status, 0, sizeof(int), s);
+    macsav::k_ch_factor<<<(g.nm + 63) / 64, 64, 0, s>>>(g, mass, viscosity, fresh.lu, fresh.piv, fresh.zero,
+                                                        C.status);
+    cudaMemcpyAsync(C.h_status, C.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return ch_cuda(&C);
+    if (C.h_status[0] != 0) {
+      cudaFree(fresh.lu);
+      cudaFree(fresh.piv);
+      cudaFree(fresh.zero);
+      return ch_fail(&C, MACSAV_ERR_CG, "Channel band factorization failed");
+    }
+    C.slots.push_back(fresh);
+    slot = &C.slots.back();
+    if (factorized) *factorized = 1;
+  }
+  slot->last_use = ++C.clock;
+  const int rows = 2 * g.ny - 1;
+  const long long fstride = (long long)rows * g.nm;
+  // forward FFTs of the loads (u rows then v rows: one (2ny-1) x nx matrix)
+  launch_fft(&C, false, rhs, g.size, rows, C.fspec, fstride, cols, s);
+  // mode solves into u/v spectra (uspec: u rows then v rows) and pspec
+  const int threads = g.nm * cols;
+  macsav::k_ch_solve<<<(threads + 63) / 64, 64, 0, s>>>(g, C.fspec, C.fspec + (long long)g.ny * g.nm, fstride,
+                                                        slot->lu, slot->piv, slot->zero, C.uspec,
+                                                        C.uspec + (long long)g.ny * g.nm, C.pspec, fstride,
+                                                        (long long)g.ny * g.nm, C.work, cols, mass, viscosity);
+  launch_fft(&C, true, C.uspec, fstride, rows, vel, g.size, cols, s);
+  launch_fft(&C, true, C.pspec, (long long)g.ny * g.nm, g.ny, pres, g.np, cols, s);
+  macsav::k_ch_center<<<cols, macsav::kChThreads, 0, s>>>(pres, g.np, nullptr);
+  cudaMemsetAsync(C.keys, 0, sizeof(unsigned long long) * 5 * cols, s);
+  const int n = g.size > g.np ? g.size : g.np;
+  macsav::k_ch_check<<<dim3(ch_grid_blocks(n), cols), macsav::kChThreads, 0, s>>>(g, vel, pres, rhs, mass,
+                                                                                  viscosity, C.keys);
+  cudaMemcpyAsync(C.h_keys, C.keys, sizeof(unsigned long long) * 5 * cols, cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return ch_cuda(&C);
+  if ((rc = ch_cuda(&C)) != MACSAV_OK) return rc;
+  double maxdef = 0, maxf = 0, maxu = 0, maxdiv = 0;
+  bool bad = false;
+  auto mx = [](double a, double b) { return (a != a || b != b) ? NAN : (a > b ? a : b); };
+  for (int c = 0; c < cols; ++c) {
+    const unsigned long long* k = C.h_keys + 5 * c;
+    double v[4];
+    for (int q = 0; q < 4; ++q) std::memcpy(&v[q], &k[q], sizeof(double));
+    maxdef = mx(maxdef, v[0]);
+    maxf = mx(maxf, v[1]);
+    maxu = mx(maxu, v[2]);
+    maxdiv = mx(maxdiv, v[3]);
+    bad |= k[4] != 0;
+  }
+  const double res = maxdef / (1.0 + maxf);
+  if (residual) *residual = res;
+  if (divergence) *divergence = maxdiv;
+  if (bad || !(res <= C.tol) || !(maxdiv <= C.tol * (1.0 + maxu))) {
+    char buf[160];
+    std::snprintf(buf, sizeof(buf), "Channel FFT residual=%.3e, divergence=%.3e", res, maxdiv);
+    return ch_fail(&C, MACSAV_ERR_STOKES_GATE, buf);
+  }
+  return MACSAV_OK;
+}
+
+}  // extern "C"

@@ -177,7 +177,50 @@ def adaptive() -> None:
     save("adaptive", **out)
 
 
+def channel() -> None:
+    """Channel MAC (periodic x): FFTStokes solves on the reference tests'
+    shapes and shifts, convection of a random field, and a short
+    integration of two schemes on the FFT-backed ChannelModel."""
+    from solver.channel import ChannelGrid, ChannelModel
+    from solver.channel.kernels import convection as ch_conv
+    out = {}
+    for nx, ny in ((7, 5), (8, 6), (17, 9)):
+        grid = ChannelGrid(nx, ny, 2.3, .8)
+        model = ChannelModel(grid, .1, backend="fft")
+        loads = np.random.default_rng(54).normal(size=(grid.size, 2))
+        for k, (mass, alpha) in enumerate(((1., 0.), (1., .013), (0., .2))):
+            sol = model.solve(loads, mass=mass, viscosity=alpha)
+            tag = f"solve_{nx}x{ny}_{k}"
+            out.update({f"{tag}_loads": loads, f"{tag}_shift": [mass, alpha], f"{tag}_vel": sol.velocity,
+                        f"{tag}_pres": sol.pressure, f"{tag}_res": sol.residual, f"{tag}_div": sol.divergence_inf})
+    grid = ChannelGrid(9, 7, 2., .8)
+    model = ChannelModel(grid, .1)
+    w = np.random.default_rng(43).normal(size=grid.size)
+    u, v = grid.unpack(w)
+    out.update({"conv_w": w, "conv_n": grid.pack(*ch_conv(u, v, grid.hx, grid.hy)),
+                "conv_K": model.apply_K(w), "conv_D": model.apply_D(w),
+                "conv_G": model.apply_G(np.random.default_rng(44).normal(size=grid.np)),
+                "conv_p": np.random.default_rng(44).normal(size=grid.np)})
+    grid = ChannelGrid(12, 9, 2 * np.pi, 1.)
+    x, y = grid.coordinates("vertex")
+    psi = (np.sin(2 * np.pi * x / grid.lx) + .3 * np.cos(4 * np.pi * x / grid.lx)) * np.sin(np.pi * y / grid.ly) ** 2
+    psi[[0, -1]] = 0.
+    x0 = .5 * grid.curl(psi)
+    out["run_x0"] = x0
+    for name in ("sdirk2_mrsav", "sdirk3"):
+        model = ChannelModel(grid, .1, backend="fft")
+        res = integrate(model, make_scheme(name, 1000.), model.state(0., x0, 1.0 if "mrsav" in name else 0.),
+                        [.01, .02, .01])
+        assert res.status == "complete", res.error
+        out.update({f"run_{name}_x": model.vector(res.final), f"run_{name}_r": res.final.r,
+                    f"run_{name}_p": np.array([s.pressure for s in res.final_stages]),
+                    f"run_{name}_diag": np.array([res.diagnostics[-1][k] for k in sorted(res.diagnostics[-1])]),
+                    f"run_{name}_diag_keys": np.array(sorted(res.diagnostics[-1]))})
+    save("channel", **out)
+
+
 if __name__ == "__main__":
+    channel()
     adaptive()
     operators()
     stokes()
