@@ -213,6 +213,10 @@ long long macsav_unet_num_params(const macsav_unet* net);
 int macsav_unet_set_params(macsav_unet* net, const float* params);
 int macsav_unet_get_params(const macsav_unet* net, float* params);
 int macsav_unet_forward(macsav_unet* net, const float* in, int batch, int ny, int nx, float* out, void* stream);
+/* Forward 3x3 convolutions with 16/32/64 output channels on the tcgen05
+ * tensor cores (implicit GEMM, BF16 operands, FP32 accumulation in tensor
+ * memory; enable = 1, the default) or on the CUDA-core kernels (0). */
+int macsav_unet_set_tensor_cores(macsav_unet* net, int enable);
 /* loss = mean((net(in) - target)^2); grads = d loss / d params (host). */
 int macsav_unet_gradients(macsav_unet* net, const float* in, const float* target, int batch, int ny, int nx,
                           double* loss, float* grads, void* stream);

@@ -67,6 +67,7 @@ _SIGNATURES = {
     "macsav_unet_set_params": (_I, [_P, _P]),
     "macsav_unet_get_params": (_I, [_P, _P]),
     "macsav_unet_forward": (_I, [_P, _P, _I, _I, _I, _P, _P]),
+    "macsav_unet_set_tensor_cores": (_I, [_P, _I]),
     "macsav_unet_gradients": (_I, [_P, _P, _P, _I, _I, _I, C.POINTER(_D), _P, _P]),
     "macsav_unet_train_step": (_I, [_P, _P, _P, _I, _I, _I, C.c_float, C.POINTER(_D), _P]),
     "macsav_plan_set_preconditioner": (_I, [_P, _P, _I]),

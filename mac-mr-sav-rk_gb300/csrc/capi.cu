@@ -331,13 +331,26 @@ int macsav_unet_get_params(const macsav_unet* net, float* params) {
              : MACSAV_ERR_CUDA;
 }
 
+int macsav_unet_set_tensor_cores(macsav_unet* net, int enable) {
+  if (!net) return MACSAV_ERR_VALUE;
+  net->net.tensor_cores = enable != 0;
+  return MACSAV_OK;
+}
+
 int macsav_unet_forward(macsav_unet* net, const float* in, int batch, int ny, int nx, float* out, void* stream) {
   if (!net || !in || !out) return MACSAV_ERR_VALUE;
   int rc = macsav::net_work_ensure(&net->net, &net->work, batch, ny, nx, net->work.grad);
   if (rc != MACSAV_OK) return net_fail(net, rc, "U-Net needs batch >= 1 and ny, nx multiples of 8");
   rc = macsav::unet_forward(&net->net, &net->work, in, nullptr, batch, ny, nx, out, nullptr,
                             static_cast<cudaStream_t>(stream));
-  return rc == MACSAV_OK ? MACSAV_OK : net_fail(net, rc, "U-Net forward failed");
+  if (rc != MACSAV_OK) return net_fail(net, rc, "U-Net forward failed");
+  if (net->net.tensor_cores) {  // a tensor-core wait that ran out is reported here
+    int flag = 0;
+    cudaMemcpyAsync(&flag, net->net.tc_err, sizeof(int), cudaMemcpyDeviceToHost, static_cast<cudaStream_t>(stream));
+    if (cudaStreamSynchronize(static_cast<cudaStream_t>(stream)) != cudaSuccess) return MACSAV_ERR_CUDA;
+    if (flag) return net_fail(net, MACSAV_ERR_CUDA, "tensor-core convolution wait ran out");
+  }
+  return MACSAV_OK;
 }
 
 static int net_backward(macsav_unet* net, const float* in, const float* target, int batch, int ny, int nx,

@@ -5,6 +5,7 @@
 // pixel.  The data gradient is the same kernel on the flipped, transposed
 // weights; the weight gradient reduces tile products and adds them atomically.
 #include <cmath>
+#include <cstdint>
 #include <vector>
 
 #include "unet.cuh"
@@ -112,6 +113,179 @@ __global__ void __launch_bounds__(256) k_conv(ConvArgs q) {
       if (q.yf) q.yf[((long long)b * cout + oo) * HW + off] = v;
       else q.yb[((long long)b * cout + oo) * HW + off] = f2bf(v);
     }
+  }
+}
+
+// ------------------------------------------- tcgen05 implicit-GEMM conv ---
+// Forward 3x3 convolution on the 5th-generation tensor cores (tcgen05.mma,
+// kind::f16 with BF16 A and B, FP32 accumulation in tensor memory) as nine
+// shifted GEMMs per 16-channel chunk: D[128 px, co] += A_t[128 px, 16 ci] .
+// B_t[co, 16 ci]^T for the taps t, with no im2col.  A CTA of 128 threads owns
+// a 16x8 pixel tile (rows y0.., columns x0..) of one image and all co (16, 32
+// or 64).  Per chunk its threads stage the 18x10 halo of 16 channels in shared
+// memory as [channel group of 8][halo pixel][8 channels], so that for tap
+// (dy, dx) the operand A_t is the no-swizzle K-major core-matrix layout
+// starting at halo pixel (dy, dx): 8 consecutive pixels of a tile row form a
+// core matrix (16 B rows), SBO = 10 pixels * 16 B = 160 B steps one tile row,
+// LBO = 180 pixels * 16 B = 2880 B steps to the next 8 channels.  B_t is
+// staged as [tap][co/8][2][8 rows x 16 B] (SBO 256 B, LBO 128 B).  One elected
+// thread issues the nine MMAs and commits them to an mbarrier; all threads
+// wait (bounded) before the tiles are reused.  The epilogue reads accumulator
+// rows with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = tile pixels),
+// applies ReLU and stores BF16.  On a wait that runs out the kernel sets
+// *err, waits (bounded) once more, frees its tensor memory and returns.
+constexpr int kTcC = 16;                          // input channels per chunk (K of one MMA)
+constexpr int kTcHx = 10, kTcHy = 18;             // halo columns / rows
+constexpr int kTcHalo = kTcHx * kTcHy;            // 180 halo pixels
+constexpr uint32_t kTcALBO = kTcHalo * 16;        // 2880: next 8 channels
+constexpr uint32_t kTcASBO = kTcHx * 16;          // 160: next tile row
+constexpr uint32_t kTcBLBO = 128, kTcBSBO = 256;  // B: next 8 channels / next 8 rows
+constexpr size_t kTcSmemHalo = size_t(2) * kTcHalo * 16;  // 5760
+constexpr size_t kTcSmemB = size_t(9) * 8 * kTcBSBO;      // 18432 (co <= 64)
+constexpr size_t kTcSmem = kTcSmemHalo + kTcSmemB;
+constexpr long long kTcSpin = 1LL << 22;          // mbarrier poll limit
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+// no-swizzle K-major shared-memory matrix descriptor (version 1, base offset 0)
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= uint64_t((saddr >> 4) & 0x3FFF);
+  d |= uint64_t((lbo >> 4) & 0x3FFF) << 16;
+  d |= uint64_t((sbo >> 4) & 0x3FFF) << 32;
+  d |= uint64_t(1) << 46;
+  return d;
+}
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
+  for (long long it = 0; it < kTcSpin; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs q, int* err) {
+  extern __shared__ __align__(1024) unsigned char tcsm[];
+  __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(tcsm);
+  unsigned char* Bs = tcsm + kTcSmemHalo;
+  __shared__ __align__(8) unsigned long long mbar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int failed;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int N = q.co, cin = q.ca + q.cb, nchunks = (cin + kTcC - 1) / kTcC;
+  const int H = q.H, W = q.W;
+  const long long HW = (long long)H * W;
+  const int b = blockIdx.z, x0 = blockIdx.x * 8, y0 = blockIdx.y * 16;
+  constexpr uint32_t kCols = 64;  // tensor-memory columns (N <= 64)
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    failed = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  const uint32_t mb = smem_u32(&mbar);
+  // instruction descriptor: FP32 accumulator, BF16 A and B, K-major, M=128, N
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(128 >> 4) << 24);
+  const uint32_t halo_s = smem_u32(halo), b_s = smem_u32(Bs);
+  const uint32_t btap = uint32_t(N >> 3) * kTcBSBO;  // bytes of one tap's B tile
+  uint32_t phase = 0;
+  const __nv_bfloat16 zero = __float2bfloat16_rn(0.f);
+  for (int ch = 0; ch < nchunks; ++ch) {
+    const int ci0 = ch * kTcC;
+    // halo [c/8][pixel][c%8] of the chunk's channels (zero outside the image / cin)
+    for (int e = tid; e < kTcC * kTcHalo; e += 128) {
+      const int c = e / kTcHalo, pix = e - c * kTcHalo, hy = pix / kTcHx, hx = pix - hy * kTcHx;
+      const int ci = ci0 + c, gy = y0 + hy - 1, gx = x0 + hx - 1;
+      __nv_bfloat16 v = zero;
+      if (ci < cin && gy >= 0 && gy < H && gx >= 0 && gx < W) {
+        const long long off = (long long)gy * W + gx;
+        v = ci < q.ca ? q.xa[((long long)b * q.ca + ci) * HW + off] : q.xb[((long long)b * q.cb + (ci - q.ca)) * HW + off];
+      }
+      halo[((c >> 3) * kTcHalo + pix) * 8 + (c & 7)] = v;
+    }
+    // B_t[co][c] = w[co][ci0 + c][t], 8 channels per 16-byte store
+    for (int e = tid; e < 9 * N * 2; e += 128) {
+      const int t = e / (N * 2), r = e - t * N * 2, row = r >> 1, kg = r & 1;
+      __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int ci = ci0 + kg * 8 + j;
+        v[j] = ci < cin ? q.w[((long long)row * cin + ci) * 9 + t] : zero;
+      }
+      *reinterpret_cast<uint4*>(Bs + t * btap + (row >> 3) * kTcBSBO + kg * kTcBLBO + (row & 7) * 16) =
+          *reinterpret_cast<const uint4*>(v);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        const uint32_t a_start = halo_s + uint32_t((t / 3) * kTcHx + (t % 3)) * 16;
+        const uint64_t ad = tc_desc(a_start, kTcALBO, kTcASBO);
+        const uint64_t bd = tc_desc(b_s + t * btap, kTcBLBO, kTcBSBO);
+        const uint32_t acc = (ch > 0 || t > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
+                   : "memory");
+    }
+    if (!tc_wait(mb, phase)) failed = 1;
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (failed) break;
+  }
+  if (failed) {
+    if (tid == 0) atomicExch(err, 1);
+    tc_wait(mb, phase);  // bounded: lets an MMA still in flight finish
+  } else {
+    // epilogue: lane p = tile pixel (row p/8, column p%8), columns are co
+    const int p = warp * 32 + lane;
+    const int gy = y0 + (p >> 3), gx = x0 + (p & 7);
+    const bool inside = gy < H && gx < W;
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t addr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(addr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (inside) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          float v = __uint_as_float(r[j]);
+          if (q.relu) v = fmaxf(v, 0.f);
+          if (q.out_scale) v *= q.out_scale[b];
+          q.yb[((long long)b * N + c0 + j) * HW + (long long)gy * W + gx] = f2bf(v);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
   }
 }
 
@@ -342,6 +516,17 @@ void conv_fwd(UNet* N, int li, const __nv_bfloat16* xa, const __nv_bfloat16* xb,
   q.B = B;
   q.H = H;
   q.W = W;
+  if (N->tensor_cores && L.ks == 3 && yb && (L.co == 16 || L.co == 32 || L.co == 64)) {
+    const dim3 tgrid((W + 7) / 8, (H + 15) / 16, B);
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTcSmem));
+      attr = true;
+    }
+    k_conv3_tc<<<tgrid, 128, kTcSmem, s>>>(q, N->tc_err);
+    ++N->launches;
+    return;
+  }
   const dim3 grid((W + kTile - 1) / kTile, (H + kTile - 1) / kTile, B * ((L.co + kCT - 1) / kCT));
   if (L.ks == 3) k_conv<3, false><<<grid, 256, 0, s>>>(q);
   else k_conv<1, false><<<grid, 256, 0, s>>>(q);
@@ -449,8 +634,9 @@ int unet_init(UNet* N, const int* channels) {
   if (cudaMalloc(&N->w32, n * sizeof(float)) != cudaSuccess || cudaMalloc(&N->grad, n * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&N->m1, n * sizeof(float)) != cudaSuccess || cudaMalloc(&N->m2, n * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&N->wb, n * sizeof(__nv_bfloat16)) != cudaSuccess ||
-      cudaMalloc(&N->loss, sizeof(double)) != cudaSuccess)
+      cudaMalloc(&N->loss, sizeof(double)) != cudaSuccess || cudaMalloc(&N->tc_err, sizeof(int)) != cudaSuccess)
     return MACSAV_ERR_CUDA;
+  cudaMemset(N->tc_err, 0, sizeof(int));
   cudaMemset(N->w32, 0, n * sizeof(float));
   cudaMemset(N->grad, 0, n * sizeof(float));
   cudaMemset(N->m1, 0, n * sizeof(float));
@@ -467,6 +653,8 @@ void unet_free(UNet* N) {
   cudaFree(N->m2);
   cudaFree(N->wb);
   cudaFree(N->loss);
+  cudaFree(N->tc_err);
+  N->tc_err = nullptr;
   N->w32 = N->grad = N->m1 = N->m2 = nullptr;
   N->wb = nullptr;
   N->loss = nullptr;

@@ -38,6 +38,8 @@ struct UNet {
   float *m1 = nullptr, *m2 = nullptr;   // Adam moments
   long long adam_t = 0;
   double* loss = nullptr;               // device loss accumulator
+  bool tensor_cores = true;             // forward 3x3 convolutions on tcgen05 (k_conv3_tc)
+  int* tc_err = nullptr;                // set when a tensor-core wait ran out
   std::string err;
   long long launches = 0;
 };

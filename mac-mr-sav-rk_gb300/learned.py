@@ -56,6 +56,7 @@ class UNet:
         if code != _lib.OK:
             raise ValueError(self.lib.macsav_unet_error(None).decode())
         self.handle = handle
+        self.tensor_cores = True  # the library default: 3x3 forward convolutions on tcgen05
         self.set_params(self.initial_params(seed, output_gain))
 
     def __del__(self) -> None:
@@ -63,6 +64,11 @@ class UNet:
         if h is not None and h.value:
             self.lib.macsav_unet_destroy(h)
             self.handle = None
+
+    def set_tensor_cores(self, enable: bool) -> None:
+        """Forward 3x3 convolutions on the tcgen05 tensor cores (or the CUDA cores)."""
+        self._check(self.lib.macsav_unet_set_tensor_cores(self.handle, 1 if enable else 0))
+        self.tensor_cores = bool(enable)
 
     def _check(self, code: int) -> None:
         if code != _lib.OK:

@@ -144,3 +144,32 @@ def test_gain_of_trained_network(env):
         counts[name] = sum(L.cg_counters(ts, 4)["iterations"])
     print("CG iterations (4 columns, all inner solves):", counts)
     assert counts["trained"] <= counts["untrained"]
+
+
+@pytest.mark.parametrize("shape", [(2, 32, 48), (1, 64, 64), (3, 24, 40)])
+def test_tensor_core_forward_matches_cuda_core_forward(env, shape):
+    """The tcgen05 implicit-GEMM convolutions give the CUDA-core result (same
+    BF16 operands, FP32 sums in another order) and the oracle's."""
+    import time
+    pkg, L, torch = env
+    net = L.UNet(seed=7, output_gain=1.0)
+    x = torch.randn(*shape, generator=torch.Generator().manual_seed(3))
+    net.set_tensor_cores(False)
+    ref = net.forward(x).cpu()
+    net.set_tensor_cores(True)
+    got = net.forward(x).cpu()
+    err = float((got - ref).norm() / ref.norm())
+    assert err < 2e-2, err
+    oracle = unet_torch.forward(unet_torch.split_params(net.params(), L.layer_shapes()), x).detach()
+    assert float((got - oracle).norm() / oracle.norm()) < 3e-2
+    # timing of both paths on a larger batch (printed, informational)
+    xb = torch.randn(4, 256, 256, generator=torch.Generator().manual_seed(4)).cuda()
+    for flag in (False, True):
+        net.set_tensor_cores(flag)
+        net.forward(xb)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(5):
+            net.forward(xb)
+        torch.cuda.synchronize()
+        print(f"U-Net forward 4x256x256 tensor_cores={flag}: {(time.perf_counter() - t0) / 5 * 1e3:.2f} ms")
