@@ -315,6 +315,22 @@ def learned_leg(pkg, g, w, x0_host, dev, args, x64) -> dict:
                          "seconds": train_sec}}
 
 
+def profile_unet() -> None:
+    """Three forward passes of the learned preconditioner's U-Net on a batch
+    of 4 256x256 residual fields (the tcgen05 convolution capture of
+    profiles/ comes from this)."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    pkg = __graft_entry__.load_package()
+    net = pkg.UNet(seed=0, output_gain=1.0)
+    x = torch.randn(4, 256, 256, generator=torch.Generator().manual_seed(0)).cuda()
+    for _ in range(3):
+        y = net.forward(x)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "unet", "out_norm": float(y.norm())}))
+
+
 def profile_steps(precision: str) -> None:
     """Two eager steps of the bench workload (the launch list and kernel
     captures of profiles/ come from this)."""
@@ -345,11 +361,14 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["cavity512", "ensemble256"], default="cavity512")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner leg")
-    ap.add_argument("--profile", choices=["fp32", "fp64"], default=None,
+    ap.add_argument("--profile", choices=["fp32", "fp64", "unet"], default=None,
                     help="run two eager steps of the workload and exit (for ncu captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.profile == "unet":
+        profile_unet()
         return
     if args.profile:
         profile_steps(args.profile)
