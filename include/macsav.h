@@ -285,6 +285,26 @@ int macsav_channel_solve(macsav_channel* ch, const double* rhs, int columns, dou
                          double* velocity, double* pressure, double* residual, double* divergence, int* factorized,
                          void* stream);
 
+/* ---- ensembles of equal-shape cavities in one plan (no reference
+ * counterpart: the reference steps one model at a time).  A plan created for
+ * `members` cavities (1..32) of the same grid steps all of them with one
+ * launch per kernel: every stage kernel covers all members, the Stokes solve
+ * treats their 2 x members right-hand sides as columns with per-member
+ * shifts, and every member keeps its own viscosity, SAV scalar, records and
+ * gates.  Each member's result is bitwise the single-cavity step's. */
+int macsav_plan_create_members(macsav_plan** plan, int nx, int ny, double lx, double ly, int precision,
+                               double tolerance, double krylov_tolerance, int max_iterations, int members);
+int macsav_plan_members(const macsav_plan* plan);
+/* nus, r0: host arrays of `members` values; x0, x1, embedded: device
+ * [members][size]; forces: device [members][stages][size] or NULL;
+ * pressures: device [members][stages][np]. */
+int macsav_step_members_enqueue(macsav_plan* plan, int scheme, double t, double dt, const double* nus, double gamma,
+                                const double* x0, const double* r0, const double* forces, double* x1,
+                                double* embedded, double* pressures, void* stream);
+/* records: host [members][stages]; r1: host [members].  Returns the first
+ * failing member's code (its records carry the status). */
+int macsav_step_members_finish(macsav_plan* plan, macsav_stage_record* records, double* r1);
+
 /* Measurement helper (no reference counterpart: it times this library's own
  * kernels for the roofline): average device milliseconds of `reps`
  * back-to-back launches of one transform pass over the velocity blocks with two

@@ -82,6 +82,10 @@ _SIGNATURES = {
     "macsav_channel_reduce": (_I, [_P, _P, _P, _LL, C.POINTER(_D), _P]),
     "macsav_channel_flow_rates": (_I, [_P, _P, _P, _P]),
     "macsav_channel_solve": (_I, [_P, _P, _I, _D, _D, _P, _P, C.POINTER(_D), C.POINTER(_D), C.POINTER(_I), _P]),
+    "macsav_plan_create_members": (_I, [C.POINTER(_P), _I, _I, _D, _D, _I, _D, _D, _I, _I]),
+    "macsav_plan_members": (_I, [_P]),
+    "macsav_step_members_enqueue": (_I, [_P, _I, _D, _D, C.POINTER(_D), _D, _P, C.POINTER(_D), _P, _P, _P, _P, _P]),
+    "macsav_step_members_finish": (_I, [_P, _P, C.POINTER(_D)]),
     "macsav_step_enqueue": (_I, [_P, _I, _D, _D, _D, _D, _P, _D, _P, _P, _P, _P, _P]),
     "macsav_step_finish": (_I, [_P, C.POINTER(StageRecord), C.POINTER(_D)]),
     "macsav_time_pass": (_I, [_P, _I, _I, C.POINTER(_D), C.POINTER(_D), _P]),

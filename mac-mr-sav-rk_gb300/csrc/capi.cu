@@ -47,8 +47,32 @@ static int cuda_status(Plan* P) {
 
 extern "C" {
 
+static int create_plan(macsav_plan** out, int nx, int ny, double lx, double ly, int precision, double tolerance,
+                       double krylov_tolerance, int max_iterations, int max_columns, int members);
+
 int macsav_plan_create(macsav_plan** out, int nx, int ny, double lx, double ly, int precision, double tolerance,
                        double krylov_tolerance, int max_iterations, int max_columns) {
+  if (max_columns < 1 || max_columns > MACSAV_MAX_COLUMNS) {
+    g_create_error = "max_columns must be in 1..4";
+    if (out) *out = nullptr;
+    return MACSAV_ERR_VALUE;
+  }
+  return create_plan(out, nx, ny, lx, ly, precision, tolerance, krylov_tolerance, max_iterations, max_columns, 1);
+}
+
+int macsav_plan_create_members(macsav_plan** out, int nx, int ny, double lx, double ly, int precision,
+                               double tolerance, double krylov_tolerance, int max_iterations, int members) {
+  if (members < 1 || members > macsav::kMaxMembers) {
+    g_create_error = "members must be in 1..32";
+    if (out) *out = nullptr;
+    return MACSAV_ERR_VALUE;
+  }
+  return create_plan(out, nx, ny, lx, ly, precision, tolerance, krylov_tolerance, max_iterations, 2 * members,
+                     members);
+}
+
+static int create_plan(macsav_plan** out, int nx, int ny, double lx, double ly, int precision, double tolerance,
+                       double krylov_tolerance, int max_iterations, int max_columns, int members) {
   if (!out) return MACSAV_ERR_VALUE;
   *out = nullptr;
   // solver/mac/grid.py:15-19 and solver/mac/tensor_stokes.py:137-143
@@ -63,10 +87,6 @@ int macsav_plan_create(macsav_plan** out, int nx, int ny, double lx, double ly, 
   }
   if (precision != MACSAV_FP64 && precision != MACSAV_FP32_MIXED) {
     g_create_error = "precision must be MACSAV_FP64 or MACSAV_FP32_MIXED";
-    return MACSAV_ERR_VALUE;
-  }
-  if (max_columns < 1 || max_columns > MACSAV_MAX_COLUMNS) {
-    g_create_error = "max_columns must be in 1..4";
     return MACSAV_ERR_VALUE;
   }
   macsav_plan* h = new macsav_plan();
@@ -91,6 +111,7 @@ int macsav_plan_create(macsav_plan** out, int nx, int ny, double lx, double ly, 
   p.ktol = krylov_tolerance;
   p.maxit = max_iterations;
   p.maxcols = max_columns;
+  p.members = members;
   const int rc = macsav::plan_build(&p);
   if (rc != MACSAV_OK) {
     g_create_error = p.err;
@@ -147,7 +168,7 @@ int macsav_stokes_solve(macsav_plan* plan, const double* rhs, int columns, doubl
   // tensor_stokes.py:246-251
   if (!std::isfinite(mass) || !std::isfinite(viscosity) || std::fmin(mass, viscosity) < 0 || mass + viscosity <= 0)
     return fail(P, MACSAV_ERR_VALUE, "Require mass,viscosity >= 0 and nonzero total");
-  if (!rhs || !velocity || !pressure || columns < 1 || columns > P->maxcols)
+  if (!rhs || !velocity || !pressure || columns < 1 || columns > P->maxcols || columns > MACSAV_MAX_COLUMNS)
     return fail(P, MACSAV_ERR_VALUE, "Invalid Stokes RHS");
   double shift[2 * MACSAV_MAX_COLUMNS];
   for (int c = 0; c < columns; ++c) {
@@ -272,6 +293,29 @@ int macsav_step_enqueue(macsav_plan* plan, int scheme, double t, double dt, doub
                                             static_cast<cudaStream_t>(stream));
   return rc == MACSAV_ERR_CUDA ? cuda_status(P) : rc;
 }
+
+int macsav_step_members_enqueue(macsav_plan* plan, int scheme, double t, double dt, const double* nus, double gamma,
+                                const double* x0, const double* r0, const double* forces, double* x1,
+                                double* embedded, double* pressures, void* stream) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  if (scheme < 0 || scheme > MACSAV_IMEX_EULER) return fail(P, MACSAV_ERR_VALUE, "Unknown scheme");
+  if (!std::isfinite(dt) || dt <= 0) return fail(P, MACSAV_ERR_VALUE, "Invalid step size");
+  if (!std::isfinite(gamma) || gamma < 0) return fail(P, MACSAV_ERR_VALUE, "gamma must be finite and nonnegative");
+  if (!nus || !r0 || !x0) return fail(P, MACSAV_ERR_VALUE, "invalid step buffers");
+  for (int m = 0; m < P->members; ++m)
+    if (!std::isfinite(nus[m]) || nus[m] <= 0) return fail(P, MACSAV_ERR_VALUE, "nu must be positive and finite");
+  const int rc = macsav::enqueue_members(P, scheme, t, dt, nus, gamma, x0, r0, forces, x1, embedded, pressures,
+                                         static_cast<cudaStream_t>(stream));
+  return rc == MACSAV_ERR_CUDA ? cuda_status(P) : rc;
+}
+
+int macsav_step_members_finish(macsav_plan* plan, macsav_stage_record* records, double* r1) {
+  if (!plan || !records) return MACSAV_ERR_VALUE;
+  return stage_status_code(&plan->p, macsav::finish_members(&plan->p, records, r1));
+}
+
+int macsav_plan_members(const macsav_plan* plan) { return plan ? plan->p.members : 0; }
 
 int macsav_step_finish(macsav_plan* plan, macsav_stage_record* records, double* r1) {
   if (!plan || !records) return MACSAV_ERR_VALUE;
@@ -411,7 +455,7 @@ int macsav_plan_set_preconditioner(macsav_plan* plan, macsav_unet* net, int lear
   if (!P->net_out) {
     if (cudaMalloc(&P->net_out, cells * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&P->net_rold, cells * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&P->net_scale, 2 * MACSAV_MAX_COLUMNS * sizeof(float)) != cudaSuccess)
+        cudaMalloc(&P->net_scale, 2 * macsav::kMaxCols * sizeof(float)) != cudaSuccess)
       return cuda_status(P);
     cudaMemset(P->net_rold, 0, cells * sizeof(float));
   }

@@ -9,6 +9,9 @@
 
 namespace macsav {
 
+constexpr int kMaxCols = 64;     // Stokes right-hand-side columns of one plan
+constexpr int kMaxMembers = 32;  // members of one plan (2 columns each)
+
 // Per-RHS-column Krylov scalars (device resident, mirrored to pinned memory).
 struct CGScalars {
   double bnorm, atol, atol2, rho, rho_prev, alpha, beta, pq, rr, mean_q, mean_b, max_b, mean_z;
@@ -83,6 +86,7 @@ struct Plan {
   int precision;  // MACSAV_FP64 or MACSAV_FP32_MIXED
   double tol, ktol;
   int maxit, maxcols;
+  int members = 1;  // equal-shape cavities stepped together (2 Stokes columns each)
   // FP32_MIXED: inner FP32 Krylov tolerance and defect-correction sweeps
   double inner_ktol = 1e-4;
   int corrections = 2;

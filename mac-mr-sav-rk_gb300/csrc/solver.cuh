@@ -148,7 +148,7 @@ struct CGFin {
   // forms its scalars.
   __device__ void operator()() const {
     using R = Red<T>;
-    __shared__ double vals[MACSAV_MAX_COLUMNS][6];
+    __shared__ double vals[kMaxCols][6];
     const bool gated = op == OP_RHO || op == OP_ALPHA || op == OP_CHECK || op == OP_FCG;
     const int mm = maxmask();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;

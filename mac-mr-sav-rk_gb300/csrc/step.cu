@@ -34,12 +34,27 @@ const double kDH3[4][4] = {{1. / 4, 0, 0, 0}, {-33. / 50, 121. / 100, 0, 0}, {23
 const double kC3[5] = {0., 1. / 4, 4. / 5, 1., 1.};                                      // sdirk3.py:13
 
 // ------------------------------------------------------------- kernels ---
+// Every kernel serves all M members of the plan at once (an ensemble of
+// equal-shape cavities, M = 1 for a single cavity): member m is blockIdx.y
+// (or blockIdx.x for the one-block scalar kernels) and reads its copy of each
+// array at base + m * stride (MemberStrides), its coefficient table at coef +
+// m * kCoefStride, its stage records at recs + m * kRecStride and its block
+// partials at partial + m * kPartStride.
+constexpr int kCoefStride = 256;
+constexpr int kRecStride = 4;  // stage records per member
+constexpr long long kPartStride = 16384;  // per-member partial region (doubles)
+constexpr long long kPartNu = 8192;       // <N,U> partials within the region
+constexpr long long kPartEmb = 4096;      // embedded-error partials within the region
+
 // out[k] = sum_t coef[idx[k][t]] * src[k][t]  for two outputs (rhs and the
 // convection combination); partial slots: max|out0|, max|out1|, sum out1^2.
 __global__ void __launch_bounds__(kThreads) k_combine2(CombineArgs a, const double* coef, long long n,
                                                        double* partial) {
   __shared__ double red[6 * 32];
   __shared__ unsigned long long redk[2 * 32];
+  const int mem = blockIdx.y;
+  coef += mem * kCoefStride;
+  partial += mem * kPartStride;
   unsigned long long m[2] = {0ull, 0ull};  // abs_key maxima: integer pipe, NaN propagates
   double s[1] = {0.0};
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -47,9 +62,9 @@ __global__ void __launch_bounds__(kThreads) k_combine2(CombineArgs a, const doub
       double acc = 0.0;
       for (int t = 0; t < a.nterm[o]; ++t) {
         const double* src = a.src[o][t];
-        if (src) acc += coef[a.idx[o][t]] * src[i];
+        if (src) acc += coef[a.idx[o][t]] * src[mem * a.sstr[o][t] + i];
       }
-      a.out[o][i] = acc;
+      a.out[o][mem * a.ostr + i] = acc;
       m[o] = max(m[o], abs_key(acc));
       if (o == 1) s[0] += acc * acc;
     }
@@ -65,9 +80,14 @@ __global__ void __launch_bounds__(kThreads) k_combine2(CombineArgs a, const doub
 }
 
 // Partial sums of <N,V>, <N,W>, <W,W> with V, W the two Stokes columns.
-__global__ void __launch_bounds__(kThreads) k_dots3(const double* N, const double* V, const double* W, long long n,
+__global__ void __launch_bounds__(kThreads) k_dots3(const double* N, const double* V, long long n, long long vstr,
                                                     double* partial) {
   __shared__ double red[6 * 32];
+  const int mem = blockIdx.y;
+  N += mem * vstr;
+  V += mem * vstr;
+  const double* W = V + n;
+  partial += mem * kPartStride;
   double s[3] = {0, 0, 0};
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const double nv = N[i], w = W[i];
@@ -80,13 +100,27 @@ __global__ void __launch_bounds__(kThreads) k_dots3(const double* N, const doubl
     for (int k = 0; k < 3; ++k) partial[blockIdx.x * 3 + k] = s[k];
 }
 
+// Member strides (elements) of the step arrays.
+struct MemberStrides {
+  long long X, KU, NN, F, VW, PI, PS;
+};
+
 // U = V - dt*coupling*W ; pi = piV/dt - coupling*piW ; partial <N,U>.
 // Plain schemes (sav == 0): U = V, pi = piV/dt.
 __global__ void __launch_bounds__(kThreads) k_recombine(GridDev g, const double* VW, const double* PI,
-                                                        const double* N, double* U, double* pi,
-                                                        const StageRec* rec, const double* coef, int dt_idx, int sav,
-                                                        double* partial) {
+                                                        const double* N, double* U, double* pi, const StageRec* rec,
+                                                        const double* coef, int dt_idx, int sav, double* partial,
+                                                        MemberStrides ms) {
   __shared__ double red[64];
+  const int mem = blockIdx.y;
+  VW += mem * ms.VW;
+  PI += mem * ms.PI;
+  N += mem * ms.F;
+  U += mem * ms.X;
+  pi += mem * ms.PS;
+  rec += mem * kRecStride;
+  coef += mem * kCoefStride;
+  partial += mem * kPartStride;
   const double dt = coef[dt_idx];
   const double cpl = sav ? rec->coupling : 0.0;
   const double resp = dt * cpl;
@@ -108,10 +142,19 @@ __global__ void __launch_bounds__(kThreads) k_recombine(GridDev g, const double*
 // defect = U + kappa K U + dt G pi - rhs + dt*coupling*N,  G = -D^T.
 // Partial slots: max|defect|, max|U|, max|D U|, max|pi|.
 __global__ void __launch_bounds__(kThreads) k_stage_defect(GridDev g, const double* U, const double* pi,
-                                                           const double* rhs, const double* N, double* KU,
-                                                           const StageRec* rec, const double* coef, int dt_idx,
-                                                           int kappa_idx, int sav, double* partial) {
+                                                           const double* rhs, double* KU, const StageRec* rec,
+                                                           const double* coef, int dt_idx, int kappa_idx, int sav,
+                                                           double* partial, MemberStrides ms) {
   __shared__ unsigned long long redk[4 * 32];
+  const int mem = blockIdx.y;
+  U += mem * ms.X;
+  pi += mem * ms.PS;
+  rhs += mem * ms.F;
+  const double* N = rhs + g.size;
+  KU += mem * ms.KU;
+  rec += mem * kRecStride;
+  coef += mem * kCoefStride;
+  partial += mem * kPartStride;
   const double dt = coef[dt_idx], kappa = coef[kappa_idx];
   const double dtc = sav ? dt * rec->coupling : 0.0;
   unsigned long long m[4] = {0, 0, 0, 0};  // abs_key maxima
@@ -120,7 +163,7 @@ __global__ void __launch_bounds__(kThreads) k_stage_defect(GridDev g, const doub
     if (i < g.size) {
       const double u = U[i];
       const double ku = K_at(U, g, i);
-      if (KU) KU[i] = ku;
+      KU[i] = ku;
       double d = u + kappa * ku;
       d = d - dt * Dt_at(pi, g, i);
       d = d - rhs[i];
@@ -141,6 +184,14 @@ __global__ void __launch_bounds__(kThreads) k_stage_defect(GridDev g, const doub
   }
 }
 
+// Skew convection of every member's stage velocity (kernels.py:6-35).
+__global__ void k_conv_members(GridDev g, const double* x, long long xstr, double* out, long long ostr) {
+  const int mem = blockIdx.y;
+  x += mem * xstr;
+  out += mem * ostr;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < g.size; e += gridDim.x * blockDim.x) out[e] = conv_at(x, g, e);
+}
+
 __device__ double fold_sum(const double* partial, int nb, int K, int k, double* red) {
   double s[1] = {0.0};
   for (int b = threadIdx.x; b < nb; b += blockDim.x) s[0] += partial[b * K + k];
@@ -157,21 +208,24 @@ __device__ double fold_max(const double* partial, int nb, int K, int k, double* 
   return key_value(m[0]);
 }
 
-// Stokes outcome of the stage: residual / divergence over both columns
-// (tensor_stokes.py:338-351) and the iteration counts.
-__global__ void k_stage_stokes(const SolveChecks* checks, const CGScalars* cg, int cols, double tol,
-                               StageRec* rec) {
-  if (threadIdx.x != 0) return;
+// Stokes outcome of the stage: residual / divergence over the member's
+// columns (tensor_stokes.py:338-351) and the iteration counts; thread = member.
+__global__ void k_stage_stokes(const SolveChecks* checks, const CGScalars* cg, int cols, int members, double tol,
+                               StageRec* recs_i) {
+  const int mem = threadIdx.x;
+  if (mem >= members) return;
+  StageRec* rec = recs_i + mem * kRecStride;
   double md = 0, mf = 0, mu = 0, mdiv = 0;
   int bad_rhs = 0, bad_sol = 0, info = 0;
-  for (int c = 0; c < cols; ++c) {
+  for (int k = 0; k < cols; ++k) {
+    const int c = mem * cols + k;
     md = nanmax(md, checks[c].max_defect);
     mf = nanmax(mf, checks[c].max_force);
     mu = nanmax(mu, checks[c].max_velocity);
     mdiv = nanmax(mdiv, checks[c].max_div);
     bad_rhs |= checks[c].nonfinite_force;
     bad_sol |= checks[c].nonfinite_solution;
-    rec->iters[c] = cg[c].iters;
+    rec->iters[k] = cg[c].iters;
     if (!info && cg[c].info) info = cg[c].info;
   }
   const double res = md / (1.0 + mf);
@@ -185,10 +239,14 @@ __global__ void k_stage_stokes(const SolveChecks* checks, const CGScalars* cg, i
 }
 
 // The frozen SAV scalar map for one stage (scalar_correction.py:29-52 and the
-// alpha/beta guard of sdirk3_mrsav.py:92-100).
+// alpha/beta guard of sdirk3_mrsav.py:92-100); one block per member.
 __global__ void __launch_bounds__(kThreads) k_stage_sav(const double* partial, int nb, StageRec* recs, int stage,
                                                         const double* coef, SavIdx ix, double area) {
   __shared__ double red[64];
+  const int mem = blockIdx.x;
+  partial += mem * kPartStride;
+  recs += mem * kRecStride;
+  coef += mem * kCoefStride;
   const double nv = fold_sum(partial, nb, 3, 0, red);
   const double nw = fold_sum(partial, nb, 3, 1, red);
   const double ww = fold_sum(partial, nb, 3, 2, red);
@@ -244,18 +302,22 @@ __global__ void __launch_bounds__(kThreads) k_stage_sav(const double* partial, i
   R.coupling = c * (1.0 - z);
 }
 
-// Closing scalar checks of the stage (sdirk3_mrsav.py:105-114).
-// gate: 1 = the stage defect gate (mr-SAV schemes, IMEX Euler); 0 = none
-// (plain SDIRK2/3 report the Stokes residual, sdirk3.py:52-55).
-__global__ void __launch_bounds__(kThreads) k_stage_close(const double* pdefect, int nbd, const double* pnu, int nbn,
-                                                          StageRec* recs, int stage, const double* coef, SavIdx ix,
-                                                          double area, int sav, int gate) {
+// Closing scalar checks of the stage (sdirk3_mrsav.py:105-114); one block per
+// member.  gate: 1 = the stage defect gate (mr-SAV schemes, IMEX Euler);
+// 0 = none (plain SDIRK2/3 report the Stokes residual, sdirk3.py:52-55).
+__global__ void __launch_bounds__(kThreads) k_stage_close(const double* partial, int nbd, int nbn, StageRec* recs,
+                                                          int stage, const double* coef, SavIdx ix, double area,
+                                                          int sav, int gate) {
   __shared__ double red[64];
-  const double maxdef = fold_max(pdefect, nbd, 4, 0, red);
-  const double maxu = fold_max(pdefect, nbd, 4, 1, red);
-  const double maxdiv = fold_max(pdefect, nbd, 4, 2, red);
-  const double maxpi = fold_max(pdefect, nbd, 4, 3, red);
-  const double nu_dot = sav ? fold_sum(pnu, nbn, 1, 0, red) : 0.0;
+  const int mem = blockIdx.x;
+  partial += mem * kPartStride;
+  recs += mem * kRecStride;
+  coef += mem * kCoefStride;
+  const double maxdef = fold_max(partial, nbd, 4, 0, red);
+  const double maxu = fold_max(partial, nbd, 4, 1, red);
+  const double maxdiv = fold_max(partial, nbd, 4, 2, red);
+  const double maxpi = fold_max(partial, nbd, 4, 3, red);
+  const double nu_dot = sav ? fold_sum(partial + kPartNu, nbn, 1, 0, red) : 0.0;
   if (threadIdx.x != 0) return;
   StageRec& R = recs[stage];
   const double dt = coef[ix.dt];
@@ -278,56 +340,72 @@ __global__ void __launch_bounds__(kThreads) k_stage_close(const double* pdefect,
     R.status = ST_STAGE_GATE;
 }
 
-__global__ void k_fold_combine(const double* partial, int nb, StageRec* rec) {
+// one block per member
+__global__ void k_fold_combine(const double* partial, int nb, StageRec* recs_i) {
   __shared__ double red[64];
+  const int mem = blockIdx.x;
+  partial += mem * kPartStride;
   const double m0 = fold_max(partial, nb, 3, 0, red);
   const double m1 = fold_max(partial, nb, 3, 1, red);
   const double s2 = fold_sum(partial, nb, 3, 2, red);
   if (threadIdx.x == 0) {
+    StageRec* rec = recs_i + mem * kRecStride;
     rec->max_rhs = m0;
     rec->max_conv = m1;
     rec->nn = s2;
   }
 }
 
-__global__ void k_set_shift(double* shift, const double* coef, int kappa_idx, int cols) {
-  if (threadIdx.x < cols) {
-    shift[2 * threadIdx.x] = 1.0;
-    shift[2 * threadIdx.x + 1] = coef[kappa_idx];
+// shifts of every member's Stokes columns: mass 1, viscosity kappa (member's table)
+__global__ void k_set_shift(double* shift, const double* coef, int kappa_idx, int cols, int total) {
+  const int c = threadIdx.x;
+  if (c < total) {
+    shift[2 * c] = 1.0;
+    shift[2 * c + 1] = coef[(c / cols) * kCoefStride + kappa_idx];
   }
 }
 
 // Embedded-error inner products of a step (controller.py:112-123 needs
 // <x1-emb, x1-emb>, <x0, x0>, <x1, x1> with the grid weight hx*hy) and a
-// non-finite flag of emb, folded by the last block into out[0..3].
+// non-finite flag of emb, folded per member by the last block into
+// out[4m .. 4m+3].
 struct EmbFin {
   const double* partial;
-  int nb;
+  int nb, members;
   double w;
   double* out;
   __device__ void operator()() const {
     __shared__ double red[3 * 32];
-    double s[3] = {0.0, 0.0, 0.0};
-    int bad = 0;
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-      for (int k = 0; k < 3; ++k) s[k] += __ldcg(partial + b * 4 + k);
-      bad |= __ldcg(partial + b * 4 + 3) != 0.0;
-    }
-    bad = __syncthreads_or(bad);
-    block_sum<3>(s, red);
-    if (threadIdx.x == 0) {
-      out[0] = w * s[0];
-      out[1] = w * s[1];
-      out[2] = w * s[2];
-      out[3] = bad ? 1.0 : 0.0;
+    for (int mem = 0; mem < members; ++mem) {
+      const double* p = partial + mem * kPartStride;
+      double s[3] = {0.0, 0.0, 0.0};
+      int bad = 0;
+      for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        for (int k = 0; k < 3; ++k) s[k] += __ldcg(p + b * 4 + k);
+        bad |= __ldcg(p + b * 4 + 3) != 0.0;
+      }
+      bad = __syncthreads_or(bad);
+      block_sum<3>(s, red);
+      if (threadIdx.x == 0) {
+        out[4 * mem + 0] = w * s[0];
+        out[4 * mem + 1] = w * s[1];
+        out[4 * mem + 2] = w * s[2];
+        out[4 * mem + 3] = bad ? 1.0 : 0.0;
+      }
+      __syncthreads();
     }
   }
 };
-__global__ void __launch_bounds__(kThreads) k_emb_norms(const double* x0, const double* x1, const double* emb,
-                                                        long long n, double* partial, EmbFin fin,
+__global__ void __launch_bounds__(kThreads) k_emb_norms(const double* X, long long xstr, long long last,
+                                                        const double* emb, long long n, double* partial, EmbFin fin,
                                                         unsigned int* done) {
   __shared__ double red[3 * 32];
   constexpr unsigned long long kInf = 0x7ff0000000000000ull;
+  const int mem = blockIdx.y;
+  const double* x0 = X + mem * xstr;
+  const double* x1 = x0 + last;
+  emb += mem * n;
+  double* part = partial + mem * kPartStride;
   double s[3] = {0.0, 0.0, 0.0};
   int bad = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -341,7 +419,7 @@ __global__ void __launch_bounds__(kThreads) k_emb_norms(const double* x0, const 
   bad = __syncthreads_or(bad);
   block_sum<3>(s, red);
   if (threadIdx.x == 0) {
-    double* o = partial + blockIdx.x * 4;
+    double* o = part + blockIdx.x * 4;
     o[0] = s[0];
     o[1] = s[1];
     o[2] = s[2];
@@ -351,10 +429,10 @@ __global__ void __launch_bounds__(kThreads) k_emb_norms(const double* x0, const 
 }
 
 __global__ void k_clear_recs(StageRec* recs, int n) {
-  if (threadIdx.x < n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
     StageRec z;
     memset(&z, 0, sizeof(z));
-    recs[threadIdx.x] = z;
+    recs[i] = z;
   }
 }
 
@@ -366,30 +444,31 @@ static int red_nb(long long n) {
   return int(b < 1 ? 1 : (b > 1024 ? 1024 : b));
 }
 
+// Member-major step buffers: member m's block of each array at base + m * stride.
 int step_buffers(Plan* P) {
   if (P->st.X) return MACSAV_OK;
-  const size_t sz = P->g.size, np = P->g.np;
+  const size_t sz = P->g.size, np = P->g.np, M = size_t(P->members);
   StepBuffers& B = P->st;
-  const size_t total = sizeof(double) * (sz * (5 + 4 + 4 + 2 + 2 + 4 + 1) + np * (2 + 4)) + 256 * sizeof(double);
+  const size_t per = sz * (5 + 4 + 4 + 2 + 2 + 4 + 1) + np * (2 + 4) + kCoefStride;
   void* d = nullptr;
-  if (cudaMalloc(&d, total) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaMalloc(&d, sizeof(double) * per * M) != cudaSuccess) return MACSAV_ERR_CUDA;
   B.base = d;
   double* p = static_cast<double*>(d);
-  B.X = p; p += 5 * sz;
-  B.KU = p; p += 4 * sz;
-  B.NN = p; p += 4 * sz;
-  B.F = p; p += 2 * sz;
-  B.VW = p; p += 2 * sz;
-  B.FORCE = p; p += 4 * sz;
-  B.EMB = p; p += sz;
-  B.PI = p; p += 2 * np;
-  B.PS = p; p += 4 * np;
+  B.X = p; p += 5 * sz * M;
+  B.KU = p; p += 4 * sz * M;
+  B.NN = p; p += 4 * sz * M;
+  B.F = p; p += 2 * sz * M;
+  B.VW = p; p += 2 * sz * M;
+  B.FORCE = p; p += 4 * sz * M;
+  B.EMB = p; p += sz * M;
+  B.PI = p; p += 2 * np * M;
+  B.PS = p; p += 4 * np * M;
   B.coef = p;
-  if (cudaMalloc(&B.recs, sizeof(StageRec) * 4) != cudaSuccess) return MACSAV_ERR_CUDA;
-  if (cudaMallocHost(&B.h_recs, sizeof(StageRec) * 4) != cudaSuccess) return MACSAV_ERR_CUDA;
-  if (cudaMallocHost(&B.h_coef, sizeof(double) * 256) != cudaSuccess) return MACSAV_ERR_CUDA;
-  if (cudaMalloc(&B.enorm, sizeof(double) * 4) != cudaSuccess) return MACSAV_ERR_CUDA;
-  if (cudaMallocHost(&B.h_enorm, sizeof(double) * 4) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaMalloc(&B.recs, sizeof(StageRec) * kRecStride * M) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaMallocHost(&B.h_recs, sizeof(StageRec) * kRecStride * M) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaMallocHost(&B.h_coef, sizeof(double) * kCoefStride * M) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaMalloc(&B.enorm, sizeof(double) * 4 * M) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaMallocHost(&B.h_enorm, sizeof(double) * 4 * M) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (cudaStreamCreateWithFlags(&B.side, cudaStreamNonBlocking) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (cudaEventCreateWithFlags(&B.ev_in, cudaEventDisableTiming) != cudaSuccess) return MACSAV_ERR_CUDA;
@@ -455,14 +534,19 @@ static void build_program(Plan* P, int scheme, bool has_force, double dt, double
   auto NN = [&](int k) { return B.NN + k * sz; };
   auto FF = [&](int k) { return has_force ? B.FORCE + k * sz : (const double*)nullptr; };
   const bool sav = scheme_sav(scheme);
+  // member stride of a source: stage velocities hold 5 vectors per member,
+  // K U, N and the forces 4
+  auto mstride = [&](const double* src) { return (src >= B.X && src < B.X + 5 * sz * P->members) ? 5 * sz : 4 * sz; };
   for (int i = 0; i < G.nstages; ++i) {
     CombineArgs& c = G.comb[i];
     c.nout = 2;
     c.out[0] = B.F;
     c.out[1] = B.F + sz;
+    c.ostr = (sav ? 2 : 1) * sz;
     auto add = [&](int o, const double* src, double v) {
       const int t = c.nterm[o]++;
       c.src[o][t] = src;
+      c.sstr[o][t] = src ? mstride(src) : 0;
       c.idx[o][t] = slot(v);
     };
     SavIdx& s = G.sav[i];
@@ -552,96 +636,103 @@ static void build_program(Plan* P, int scheme, bool has_force, double dt, double
   }
 }
 
-// Enqueue one whole step on X.s reading U_0 from B.X (and forces from B.FORCE),
-// writing U_n to B.X + n*size, stage pressures to B.PS, records to B.recs.
+// Enqueue one whole step of all members on X.s reading U_0 from B.X (and
+// forces from B.FORCE), writing U_n to B.X + n*size, stage pressures to B.PS
+// and records to B.recs (member-major layouts, see step_buffers).
 static int enqueue_step(Plan* P, Exec& X, int scheme, const StageProgram& G, bool want_emb) {
   StepBuffers& B = P->st;
   const GridDev& g = P->g;
   const long long sz = g.size, np = g.np;
+  const int M = P->members;
   const cudaStream_t s = X.s;
   const int nbs = red_nb(sz), nbn = red_nb(sz > np ? sz : np);
   const bool sav = scheme_sav(scheme);
   const int cols = sav ? 2 : 1;
   const double area = g.hx * g.hy;
-  (void)np;
-  k_clear_recs<<<1, 32, 0, s>>>(B.recs, 4);
-  ++P->launches;
+  const MemberStrides ms{5 * sz, 4 * sz, 4 * sz, cols * sz, cols * sz, cols * np, 4 * np};
+  k_clear_recs<<<1, 128, 0, s>>>(B.recs, kRecStride * M);
   // N(U_0)
-  launch_convection(P, B.X, B.NN, s);
+  k_conv_members<<<dim3(red_nb(sz), M), kThreads, 0, s>>>(g, B.X, ms.X, B.NN, ms.NN);
+  P->launches += 2;
   for (int i = 0; i < G.nstages; ++i) {
     StageRec* rec = B.recs + i;
     double* U = B.X + (i + 1) * sz;
     CombineArgs ca = G.comb[i];
     if (!sav) ca.nout = 1;
-    k_combine2<<<nbs, kThreads, 0, s>>>(ca, B.coef, sz, P->partial);
-    k_fold_combine<<<1, kThreads, 0, s>>>(P->partial, nbs, rec);
-    k_set_shift<<<1, 32, 0, s>>>(P->shift, B.coef, G.kappa[i], cols);
+    k_combine2<<<dim3(nbs, M), kThreads, 0, s>>>(ca, B.coef, sz, P->partial);
+    k_fold_combine<<<M, kThreads, 0, s>>>(P->partial, nbs, rec);
+    k_set_shift<<<1, kMaxCols, 0, s>>>(P->shift, B.coef, G.kappa[i], cols, cols * M);
     P->launches += 3;
-    int rc = P->precision == MACSAV_FP64 ? enqueue_solve_fp64(P, X, B.F, cols, B.VW, B.PI)
-                                         : enqueue_solve_mixed(P, X, B.F, cols, B.VW, B.PI);
+    int rc = P->precision == MACSAV_FP64 ? enqueue_solve_fp64(P, X, B.F, cols * M, B.VW, B.PI)
+                                         : enqueue_solve_mixed(P, X, B.F, cols * M, B.VW, B.PI);
     if (rc != MACSAV_OK) return rc;
-    k_stage_stokes<<<1, 32, 0, s>>>(P->checks, P->cg, cols, P->tol, rec);
+    k_stage_stokes<<<1, kMaxMembers, 0, s>>>(P->checks, P->cg, cols, M, P->tol, rec);
     ++P->launches;
     if (sav) {
-      k_dots3<<<nbs, kThreads, 0, s>>>(B.F + sz, B.VW, B.VW + sz, sz, P->partial);
-      k_stage_sav<<<1, kThreads, 0, s>>>(P->partial, nbs, B.recs, i, B.coef, G.sav[i], area);
+      k_dots3<<<dim3(nbs, M), kThreads, 0, s>>>(B.F + sz, B.VW, sz, ms.F, P->partial);
+      k_stage_sav<<<M, kThreads, 0, s>>>(P->partial, nbs, B.recs, i, B.coef, G.sav[i], area);
       P->launches += 2;
     }
     double* pi = B.PS + i * np;
-    double* pnu = P->partial + 8192;
-    k_recombine<<<nbn, kThreads, 0, s>>>(g, B.VW, B.PI, B.F + sz, U, pi, rec, B.coef, G.dt_idx, sav ? 1 : 0, pnu);
-    k_stage_defect<<<nbn, kThreads, 0, s>>>(g, U, pi, B.F, B.F + sz, B.KU + i * sz, rec, B.coef, G.dt_idx,
-                                            G.kappa[i], sav ? 1 : 0, P->partial);
+    k_recombine<<<dim3(nbn, M), kThreads, 0, s>>>(g, B.VW, B.PI, B.F + sz, U, pi, rec, B.coef, G.dt_idx, sav ? 1 : 0,
+                                                   P->partial + kPartNu, ms);
+    k_stage_defect<<<dim3(nbn, M), kThreads, 0, s>>>(g, U, pi, B.F, B.KU + i * sz, rec, B.coef, G.dt_idx,
+                                                      G.kappa[i], sav ? 1 : 0, P->partial, ms);
     const int gate = (scheme == MACSAV_SDIRK2 || scheme == MACSAV_SDIRK3) ? 0 : 1;
-    k_stage_close<<<1, kThreads, 0, s>>>(P->partial, nbn, pnu, nbn, B.recs, i, B.coef, G.sav[i], area,
-                                         sav ? 1 : 0, gate);
+    k_stage_close<<<M, kThreads, 0, s>>>(P->partial, nbn, nbn, B.recs, i, B.coef, G.sav[i], area, sav ? 1 : 0, gate);
     P->launches += 3;
-    if (i + 1 < G.nstages) launch_convection(P, U, B.NN + (i + 1) * sz, s);
+    if (i + 1 < G.nstages) {
+      k_conv_members<<<dim3(red_nb(sz), M), kThreads, 0, s>>>(g, U, ms.X, B.NN + (i + 1) * sz, ms.NN);
+      ++P->launches;
+    }
   }
   if (want_emb && G.emb_terms) {
     CombineArgs e;
     std::memset(&e, 0, sizeof(e));
     e.nout = 1;
     e.out[0] = B.EMB;
+    e.ostr = sz;
     e.nterm[0] = G.emb_terms;
     for (int k = 0; k < G.emb_terms; ++k) {
       e.src[0][k] = B.X + G.emb_node[k] * sz;
+      e.sstr[0][k] = ms.X;
       e.idx[0][k] = G.emb_idx[k];
     }
-    k_combine2<<<nbs, kThreads, 0, s>>>(e, B.coef, sz, P->partial);
+    k_combine2<<<dim3(nbs, M), kThreads, 0, s>>>(e, B.coef, sz, P->partial);
     ++P->launches;
     // the adaptive controller's inner products, so an attempt needs no more
     // device round trips than the step itself
-    const int nbe = nbs < 1024 ? nbs : 1024;
-    k_emb_norms<<<nbe, kThreads, 0, s>>>(B.X, B.X + G.nstages * sz, B.EMB, sz, P->partial + 4096,
-                                         EmbFin{P->partial + 4096, nbe, P->g.hx * P->g.hy, B.enorm},
-                                         P->done_counter);
+    k_emb_norms<<<dim3(nbs, M), kThreads, 0, s>>>(B.X, ms.X, G.nstages * sz, B.EMB, sz, P->partial + kPartEmb,
+                                                   EmbFin{P->partial + kPartEmb, nbs, M, g.hx * g.hy, B.enorm},
+                                                   P->done_counter);
     ++P->launches;
   }
   return MACSAV_OK;
 }
 
-// Enqueue one step (no host wait in graph mode); finish_step waits for it and
-// folds the stage records.
-int enqueue_step_async(Plan* P, int scheme, double t, double dt, double nu, double gamma, const double* x0,
-                       double r0, const double* forces, double* x1, double* embedded, double* pressures,
-                       cudaStream_t user) {
+// Enqueue one step of all members (no host wait in graph mode); finish_members
+// waits for it and folds the stage records.
+int enqueue_members(Plan* P, int scheme, double t, double dt, const double* nus, double gamma, const double* x0,
+                    const double* r0, const double* forces, double* x1, double* embedded, double* pressures,
+                    cudaStream_t user) {
   (void)t;
   int rc = step_buffers(P);
   if (rc != MACSAV_OK) return rc;
   StepBuffers& B = P->st;
   const long long sz = P->g.size, np = P->g.np;
+  const int M = P->members;
   StageProgram G;
-  double* coef = B.h_coef;
-  build_program(P, scheme, forces != nullptr, dt, nu, gamma, r0, G, coef);
+  for (int m = 0; m < M; ++m)  // the same program; per-member coefficient values
+    build_program(P, scheme, forces != nullptr, dt, nus[m], gamma, r0[m], G, B.h_coef + m * kCoefStride);
   const int n = G.nstages;
   // inputs onto the plan's stream
   cudaEventRecord(B.ev_in, user);
   cudaStreamWaitEvent(B.stream, B.ev_in, 0);
   const cudaStream_t s = B.stream;
-  cudaMemcpyAsync(B.coef, coef, sizeof(double) * 256, cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(B.X, x0, sizeof(double) * sz, cudaMemcpyDeviceToDevice, s);
-  if (forces) cudaMemcpyAsync(B.FORCE, forces, sizeof(double) * sz * n, cudaMemcpyDeviceToDevice, s);
+  const size_t d8 = sizeof(double);
+  cudaMemcpyAsync(B.coef, B.h_coef, d8 * kCoefStride * M, cudaMemcpyHostToDevice, s);
+  cudaMemcpy2DAsync(B.X, d8 * 5 * sz, x0, d8 * sz, d8 * sz, M, cudaMemcpyDeviceToDevice, s);
+  if (forces) cudaMemcpy2DAsync(B.FORCE, d8 * 4 * sz, forces, d8 * n * sz, d8 * n * sz, M, cudaMemcpyDeviceToDevice, s);
   const bool want_emb = embedded != nullptr;
   if (!P->use_graph) {
     Exec X{s, false, nullptr, 0, 0.0};
@@ -673,12 +764,13 @@ int enqueue_step_async(Plan* P, int scheme, double t, double dt, double nu, doub
     }
     if (cudaGraphLaunch(exec, s) != cudaSuccess) return MACSAV_ERR_CUDA;
   }
-  if (x1) cudaMemcpyAsync(x1, B.X + n * sz, sizeof(double) * sz, cudaMemcpyDeviceToDevice, s);
-  if (want_emb && G.emb_terms) cudaMemcpyAsync(embedded, B.EMB, sizeof(double) * sz, cudaMemcpyDeviceToDevice, s);
-  if (pressures) cudaMemcpyAsync(pressures, B.PS, sizeof(double) * np * n, cudaMemcpyDeviceToDevice, s);
-  cudaMemcpyAsync(B.h_recs, B.recs, sizeof(StageRec) * n, cudaMemcpyDeviceToHost, s);
+  if (x1) cudaMemcpy2DAsync(x1, d8 * sz, B.X + n * sz, d8 * 5 * sz, d8 * sz, M, cudaMemcpyDeviceToDevice, s);
+  if (want_emb && G.emb_terms) cudaMemcpyAsync(embedded, B.EMB, d8 * sz * M, cudaMemcpyDeviceToDevice, s);
+  if (pressures)
+    cudaMemcpy2DAsync(pressures, d8 * n * np, B.PS, d8 * 4 * np, d8 * n * np, M, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(B.h_recs, B.recs, sizeof(StageRec) * kRecStride * M, cudaMemcpyDeviceToHost, s);
   B.have_enorm = want_emb && G.emb_terms;
-  if (B.have_enorm) cudaMemcpyAsync(B.h_enorm, B.enorm, sizeof(double) * 4, cudaMemcpyDeviceToHost, s);
+  if (B.have_enorm) cudaMemcpyAsync(B.h_enorm, B.enorm, d8 * 4 * M, cudaMemcpyDeviceToHost, s);
   cudaEventRecord(B.ev_out, s);
   cudaStreamWaitEvent(user, B.ev_out, 0);
   B.pending_scheme = scheme;
@@ -686,9 +778,11 @@ int enqueue_step_async(Plan* P, int scheme, double t, double dt, double nu, doub
   return MACSAV_OK;
 }
 
-int finish_step(Plan* P, macsav_stage_record* records, double* r1) {
+// records: [M][stages] host array; r1: M host values.  Returns the first
+// failing member's stage status (ST_OK when all passed).
+int finish_members(Plan* P, macsav_stage_record* records, double* r1) {
   StepBuffers& B = P->st;
-  const int scheme = B.pending_scheme, n = B.pending_stages;
+  const int scheme = B.pending_scheme, n = B.pending_stages, M = P->members;
   if (n <= 0) {
     P->err = "no step enqueued";
     return MACSAV_ERR_VALUE;
@@ -701,33 +795,48 @@ int finish_step(Plan* P, macsav_stage_record* records, double* r1) {
     return MACSAV_ERR_CUDA;
   }
   int status = MACSAV_OK;
-  for (int i = 0; i < n; ++i) {
-    const StageRec& R = B.h_recs[i];
-    macsav_stage_record& o = records[i];
-    std::memset(&o, 0, sizeof(o));
-    o.r = R.r;
-    o.residual = R.residual;
-    o.scalar_residual = R.scalar_residual;
-    o.divergence_inf = R.divergence;
-    o.continuity_residual = R.divergence;
-    o.correction_predictor = scheme_sav(scheme) ? R.predictor : NAN;
-    o.frozen_factor = scheme_sav(scheme) ? R.factor : NAN;
-    o.n_corrections = scheme_sav(scheme) ? R.n_corr : 0;
-    o.corrections[0] = R.corr[0];
-    o.corrections[1] = R.corr[1];
-    o.iterations[0] = R.iters[0];
-    o.iterations[1] = R.iters[1];
-    o.stokes_residual = R.stokes_residual;
-    o.stokes_divergence = R.stokes_divergence;
-    o.max_velocity = R.max_velocity;
-    o.max_pressure = R.max_pressure;
-    o.cg_info = R.cg_info;
-    o.status = R.status;
-    if (status == MACSAV_OK && R.status) status = R.status;
+  const bool sav = scheme_sav(scheme);
+  for (int m = 0; m < M; ++m) {
+    for (int i = 0; i < n; ++i) {
+      const StageRec& R = B.h_recs[m * kRecStride + i];
+      macsav_stage_record& o = records[m * n + i];
+      std::memset(&o, 0, sizeof(o));
+      o.r = R.r;
+      o.residual = R.residual;
+      o.scalar_residual = R.scalar_residual;
+      o.divergence_inf = R.divergence;
+      o.continuity_residual = R.divergence;
+      o.correction_predictor = sav ? R.predictor : NAN;
+      o.frozen_factor = sav ? R.factor : NAN;
+      o.n_corrections = sav ? R.n_corr : 0;
+      o.corrections[0] = R.corr[0];
+      o.corrections[1] = R.corr[1];
+      o.iterations[0] = R.iters[0];
+      o.iterations[1] = R.iters[1];
+      o.stokes_residual = R.stokes_residual;
+      o.stokes_divergence = R.stokes_divergence;
+      o.max_velocity = R.max_velocity;
+      o.max_pressure = R.max_pressure;
+      o.cg_info = R.cg_info;
+      o.status = R.status;
+      if (status == MACSAV_OK && R.status) status = R.status;
+    }
+    if (r1) r1[m] = sav ? B.h_recs[m * kRecStride + n - 1].r : 0.0;
   }
-  if (r1) *r1 = scheme_sav(scheme) ? B.h_recs[n - 1].r : 0.0;
   return status;
 }
+
+int enqueue_step_async(Plan* P, int scheme, double t, double dt, double nu, double gamma, const double* x0,
+                       double r0, const double* forces, double* x1, double* embedded, double* pressures,
+                       cudaStream_t user) {
+  if (P->members != 1) {
+    P->err = "a plan with several members steps through macsav_step_members";
+    return MACSAV_ERR_VALUE;
+  }
+  return enqueue_members(P, scheme, t, dt, &nu, gamma, x0, &r0, forces, x1, embedded, pressures, user);
+}
+
+int finish_step(Plan* P, macsav_stage_record* records, double* r1) { return finish_members(P, records, r1); }
 
 int run_step(Plan* P, int scheme, double t, double dt, double nu, double gamma, const double* x0, double r0,
              const double* forces, double* x1, double* embedded, double* pressures, macsav_stage_record* records,

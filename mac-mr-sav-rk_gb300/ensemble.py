@@ -3,13 +3,17 @@
 The reference steps one model at a time; an ensemble there is a loop of
 ``integrate`` calls over models (its documentation recommends process-level
 parallelism over members, docs/linear-stokes-acceleration-research.md:263-277,
-without implementing it).  Here every member has its own model (a plan with
-device tables and buffers) and its own captured step graph, and one ensemble
-step enqueues every member's step (``macsav_step_enqueue``) on the member's own
-stream before it waits for any (``macsav_step_finish``).  The GPU therefore
-overlaps the members' kernels, and the host waits once per ensemble step.
-Each member computes exactly what a lone ``make_scheme(name).step`` computes on
-it: same kernels, same launch shapes, same order, so results are bitwise equal.
+without implementing it).  Here equal-shape members share one plan
+(``macsav_plan_create_members``, up to 32 members): every stage kernel runs
+once for all of them (member = blockIdx.y), the Stokes solve treats their
+2 x M right-hand sides as columns with per-member shifts, and each member
+keeps its own viscosity, SAV scalar, records and gates.  Every plan has its
+own stream and captured step graph; one ensemble step enqueues all plans'
+steps (``macsav_step_members_enqueue``) before it waits for any
+(``macsav_step_members_finish``), so the shape groups overlap on the GPU and
+the host waits once per ensemble step.  Each member computes exactly what a
+lone ``make_scheme(name).step`` computes on it (the per-column arithmetic and
+launch shapes are those of a single cavity), so results are bitwise equal.
 
 ``ensemble_members`` draws the mixed-size workload (grids from
 {64, 96, 128, 192, 256}^2 on [0, nx/ny] x [0, 1], nu log-uniform in
@@ -28,9 +32,8 @@ import torch
 from . import _lib, fields
 from ._lib import StageRecord
 from .grid import MACGrid
-from .model import MACNavierStokes
 from .schemes import make_scheme
-from .stokes import dptr
+from .stokes import PRECISIONS, dptr, stream_handle
 
 SIZES = (64, 96, 128, 192, 256)
 
@@ -87,31 +90,71 @@ class EnsembleError(RuntimeError):
         self.index = index
 
 
+class _Unit:
+    """One plan stepping ``len(indices)`` equal-shape members together
+    (``macsav_plan_create_members``), with its stream and state buffers."""
+
+    def __init__(self, lib, members: Sequence[Member], indices: list[int], scheme, precision: str, use_graph: bool,
+                 tolerance: float, krylov_tolerance: float) -> None:
+        self.lib, self.indices = lib, indices
+        grid = members[indices[0]].grid()
+        self.grid = grid
+        handle = C.c_void_p()
+        code = lib.macsav_plan_create_members(C.byref(handle), grid.nx, grid.ny, float(grid.lx), float(grid.ly),
+                                              PRECISIONS[precision], float(tolerance), float(krylov_tolerance), 100,
+                                              len(indices))
+        if code != _lib.OK:
+            _lib.check(code, None)
+        self.handle = handle
+        lib.macsav_plan_set_graph(handle, 1 if use_graph else 0)
+        M, n = len(indices), scheme.info.n_stages
+        self.nus = (C.c_double * M)(*[members[i].nu for i in indices])
+        self.x = torch.zeros((2, M, grid.size), dtype=torch.float64, device="cuda")
+        self.pres = torch.empty((M, n, grid.np), dtype=torch.float64, device="cuda")
+        self.cur = 0
+        self.stream = torch.cuda.Stream()
+
+    def __del__(self) -> None:
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                torch.cuda.synchronize()
+            except Exception:
+                pass
+            self.lib.macsav_plan_destroy(h)
+            self.handle = None
+
+
 class Ensemble:
     """Members stepped concurrently with one fused scheme (see module docstring).
 
-    ``precision`` "fp32" is the FP32-bulk Stokes form (FP64 reductions, SAV
-    scalars and gates); "fp64" is the plain path.
+    ``batched=True`` (default) groups equal-shape members into plans of up to
+    ``max_group`` members, so each stage kernel runs once for the group;
+    ``batched=False`` gives every member its own plan.  Either way every
+    member's result is bitwise that of a lone step.  ``precision`` "fp32" is
+    the FP32-bulk Stokes form (FP64 reductions, SAV scalars and gates);
+    "fp64" is the plain path.
     """
 
     def __init__(self, members: Sequence[Member], scheme: str = "sdirk2_mrsav", gamma: float = 1.0, *,
                  precision: str = "fp32", use_graph: bool = True, tolerance: float = 1e-9,
-                 krylov_tolerance: float = 1e-12) -> None:
+                 krylov_tolerance: float = 1e-12, batched: bool = True, max_group: int = 16) -> None:
         if not members:
             raise ValueError("an ensemble needs at least one member")
+        if not 1 <= max_group <= 32:
+            raise ValueError("max_group must be in 1..32")
         self.members = list(members)
         self.scheme = make_scheme(scheme, gamma)
-        self.models = [MACNavierStokes(m.grid(), m.nu, precision=precision, use_graph=use_graph,
-                                       tolerance=tolerance, krylov_tolerance=krylov_tolerance)
-                       for m in self.members]
         self.lib = _lib.load()
-        for model in self.models:
-            self.lib.macsav_plan_set_graph(model.plan.handle, 1 if use_graph else 0)
-        self.streams = [torch.cuda.Stream() for _ in self.members]
-        n = self.scheme.info.n_stages
-        self._x = [torch.zeros((2, m.grid().size), dtype=torch.float64, device="cuda") for m in self.members]
-        self._pres = [torch.empty((n, m.cells), dtype=torch.float64, device="cuda") for m in self.members]
-        self._cur = [0] * len(self.members)
+        torch.cuda.init()
+        groups: dict[tuple[int, int], list[int]] = {}
+        for i, m in enumerate(self.members):
+            groups.setdefault((m.nx, m.ny), []).append(i)
+        size = max_group if batched else 1
+        self.units = [_Unit(self.lib, self.members, idx[k:k + size], self.scheme, precision, use_graph, tolerance,
+                            krylov_tolerance)
+                      for idx in groups.values() for k in range(0, len(idx), size)]
+        self._where = {i: (u, j) for u in self.units for j, i in enumerate(u.indices)}
         self.t = np.zeros(len(self.members))
         self.r = np.zeros(len(self.members))
         self.last_records: list[list[StageRecord]] = []
@@ -124,8 +167,10 @@ class Ensemble:
         return sum(m.cells for m in self.members)
 
     def set_state(self, index: int, velocity, r: float = 0.0, t: float = 0.0) -> None:
-        x = self.models[index]._dev(velocity).reshape(-1)
-        self._x[index][self._cur[index]].copy_(x)
+        unit, j = self._where[index]
+        x = velocity if isinstance(velocity, torch.Tensor) else torch.from_numpy(
+            np.ascontiguousarray(np.asarray(velocity, dtype=np.float64)))
+        unit.x[unit.cur, j].copy_(x.to("cuda", torch.float64).reshape(-1))
         self.r[index] = float(r)
         self.t[index] = float(t)
 
@@ -138,12 +183,13 @@ class Ensemble:
             self.set_state(i, fields.packed_curl_velocity(m.nx, m.ny, g.lx, g.ly, modes, m.seed), r0)
 
     def velocity(self, index: int) -> torch.Tensor:
-        return self._x[index][self._cur[index]]
+        unit, j = self._where[index]
+        return unit.x[unit.cur, j]
 
     def step(self, dt: float) -> list[list[StageRecord]]:
         """One step of every member; raises ``EnsembleError`` for the first
         failing member after all enqueued steps have finished (the states of
-        the members are then left as they were before the step)."""
+        all members are then left as they were before the step)."""
         if not np.isfinite(dt) or dt <= 0:
             raise ValueError("Invalid step size")
         ready = torch.cuda.Event()
@@ -151,62 +197,79 @@ class Ensemble:
         sid = self.scheme._id
         n = self.scheme.info.n_stages
         enqueued, failure = [], None
-        for i, (model, stream) in enumerate(zip(self.models, self.streams)):
-            stream.wait_event(ready)
-            x = self._x[i]
-            code = self.lib.macsav_step_enqueue(
-                model.plan.handle, sid, float(self.t[i]), float(dt), float(model.nu), self.scheme.gamma,
-                dptr(x[self._cur[i]]), float(self.r[i]), None, dptr(x[1 - self._cur[i]]), None,
-                dptr(self._pres[i]), C.c_void_p(stream.cuda_stream))
+        for u in self.units:
+            u.stream.wait_event(ready)
+            M = len(u.indices)
+            r0 = (C.c_double * M)(*[self.r[i] for i in u.indices])
+            t0 = float(self.t[u.indices[0]])
+            code = self.lib.macsav_step_members_enqueue(
+                u.handle, sid, t0, float(dt), u.nus, self.scheme.gamma, dptr(u.x[u.cur]), r0, None,
+                dptr(u.x[1 - u.cur]), None, dptr(u.pres), C.c_void_p(u.stream.cuda_stream))
             if code != _lib.OK:
-                failure = failure or (i, code, None)
+                failure = failure or (u.indices[0], code, None, u)
                 break
-            enqueued.append(i)
+            enqueued.append(u)
         records: list[list[StageRecord]] = [[] for _ in self.members]
         r1s = {}
-        for i in enqueued:
-            recs = (StageRecord * n)()
-            r1 = C.c_double()
-            code = self.lib.macsav_step_finish(self.models[i].plan.handle, recs, C.byref(r1))
-            records[i] = list(recs)
-            r1s[i] = float(r1.value)
+        for u in enqueued:
+            M = len(u.indices)
+            recs = (StageRecord * (M * n))()
+            r1 = (C.c_double * M)()
+            code = self.lib.macsav_step_members_finish(u.handle, recs, r1)
+            for j, i in enumerate(u.indices):
+                records[i] = list(recs[j * n:(j + 1) * n])
+                r1s[i] = float(r1[j])
             if code != _lib.OK and failure is None:
-                failure = (i, code, recs)
-        torch.cuda.current_stream().wait_event(self._done_event())
+                bad = next((i for i in u.indices if any(rc.status for rc in records[i])), u.indices[0])
+                failure = (bad, code, records[bad], u)
+        done = torch.cuda.Event()
+        for u in self.units:
+            done.record(u.stream)
+            torch.cuda.current_stream().wait_event(done)
         self.last_records = records
         if failure is not None:
-            i, code, recs = failure
+            i, code, recs, u = failure
             try:
-                failing = next((r for r in recs if r.status), None) if recs is not None else None
+                failing = next((rc for rc in recs if rc.status), None) if recs else None
                 if failing is None:
-                    _lib.check(code, self.models[i].plan.handle)
-                self.scheme._raise(code, failing, self.models[i].plan)
+                    _lib.check(code, u.handle)
+                self.scheme._raise(code, failing, _PlanRef(u.handle))
             except Exception as error:  # the reference's exception for the failing stage
                 raise EnsembleError(i, error) from error
-        for i in enqueued:
-            self._cur[i] = 1 - self._cur[i]
-            self.t[i] += dt
-            if self.scheme.sav:
-                self.r[i] = r1s[i]
+        for u in enqueued:
+            u.cur = 1 - u.cur
+            for i in u.indices:
+                self.t[i] += dt
+                if self.scheme.sav:
+                    self.r[i] = r1s[i]
         return records
-
-    def _done_event(self) -> torch.cuda.Event:
-        ev = torch.cuda.Event()
-        for stream in self.streams:
-            ev.record(stream)
-            torch.cuda.current_stream().wait_event(ev)
-        return ev
 
     def run(self, steps: int, dt: float) -> None:
         for _ in range(steps):
             self.step(dt)
+
+    def launches(self) -> int:
+        """Kernel launches issued so far by all plans (eager steps only count
+        their launches; a graph replay counts none)."""
+        return sum(int(self.lib.macsav_plan_launches(u.handle)) for u in self.units)
 
     def diagnostics(self) -> list[dict[str, float]]:
         """``MACNavierStokes.diagnostics`` of every member's current state."""
         keys = ("kinetic", "modified_energy", "divergence_inf", "h1_seminorm_squared", "r", "angular_momentum",
                 "power", "dissipation")
         out = []
-        for i, model in enumerate(self.models):
-            d = model._diagnostics(self.velocity(i), float(self.r[i]), None)
-            out.append(dict(zip(keys, (float(v) for v in d))))
+        for i, m in enumerate(self.members):
+            unit, _ = self._where[i]
+            res = (C.c_double * 8)()
+            x = self.velocity(i).contiguous()
+            _lib.check(self.lib.macsav_diagnostics(unit.handle, dptr(x), float(self.r[i]), float(m.nu), None, res,
+                                                   stream_handle()), unit.handle)
+            out.append(dict(zip(keys, (float(v) for v in res))))
         return out
+
+
+class _PlanRef:
+    """The ``plan.handle`` view that ``FusedScheme._raise`` expects."""
+
+    def __init__(self, handle) -> None:
+        self.handle = handle

@@ -73,13 +73,16 @@ def test_two_rank_gloo_sharding(tmp_path):
 # ----------------------------------------------------------------- GPU ---
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("batched", [True, False])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_ensemble_step_equals_lone_steps(precision):
+def test_ensemble_step_equals_lone_steps(precision, batched):
     import torch
     pkg = load_package()
     E = _ens()
-    members = [E.Member(64, 96, 3e-3, 11), E.Member(96, 64, 2e-4, 12), E.Member(128, 128, 8e-3, 13)]
-    ens = E.Ensemble(members, "sdirk2_mrsav", precision=precision)
+    members = [E.Member(64, 96, 3e-3, 11), E.Member(96, 64, 2e-4, 12), E.Member(128, 128, 8e-3, 13),
+               E.Member(64, 96, 9e-4, 14), E.Member(64, 96, 1e-2, 15)]
+    ens = E.Ensemble(members, "sdirk2_mrsav", precision=precision, batched=batched)
+    assert len(ens.units) == (3 if batched else 5)
     ens.seed_fields(modes=8)
     x0 = [ens.velocity(i).clone() for i in range(len(members))]
     for _ in range(3):
@@ -94,6 +97,27 @@ def test_ensemble_step_equals_lone_steps(precision):
         assert state.r == ens.r[i] and state.t == pytest.approx(ens.t[i])
     d = ens.diagnostics()
     assert all(np.isfinite(list(x.values())).all() and x["divergence_inf"] < 1e-8 for x in d)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme", ["sdirk3_mrsav", "sdirk2"])
+def test_batched_plan_matches_single_member_plans(scheme):
+    """Members sharing a plan (one launch per kernel for all of them) give
+    bitwise the results of one plan per member, eager and graph."""
+    import torch
+    E = _ens()
+    members = [E.Member(96, 64, nu, 40 + k) for k, nu in enumerate((1e-4, 3e-4, 1e-3, 3e-3, 1e-2))]
+    runs = []
+    for batched, graph in ((True, False), (True, True), (False, True)):
+        ens = E.Ensemble(members, scheme, precision="fp32", batched=batched, use_graph=graph)
+        ens.seed_fields(modes=8)
+        ens.run(2, 5e-4)
+        runs.append((ens, [ens.velocity(i).clone() for i in range(len(members))]))
+    for ens, xs in runs[1:]:
+        for a, b in zip(runs[0][1], xs):
+            assert torch.equal(a, b)
+        np.testing.assert_array_equal(ens.r, runs[0][0].r)
+    assert runs[0][0].launches() > 0
 
 
 @pytest.mark.gpu
