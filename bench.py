@@ -12,7 +12,7 @@ state, dt)`` with a host ``State``: the velocity goes host->device and the new
 state device->host every step).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload cavity512|ensemble256]
+                  [--workload cavity512|ensemble256|adaptive2048]
 
 ``--workload ensemble256`` measures the mixed-size ensemble instead: 256
 cavities (nx, ny drawn from {64, 96, 128, 192, 256}, domain [0, nx/ny] x
@@ -249,6 +249,66 @@ def run_ensemble(args) -> None:
         dist.destroy_process_group()
 
 
+ADAPTIVE = {"workload": "adaptive2048x1024_sdirk3_mrsav", "nx": 2048, "ny": 1024, "lx": 2.0, "ly": 1.0,
+            "nu": 5e-5, "psi_modes": 64, "seed": 20261205, "t_end": 0.05, "dt0": 1e-4, "rtol": 1e-5,
+            "scheme": "sdirk3_mrsav", "stages_per_step": 4}
+
+
+def run_adaptive(args) -> None:
+    """The adaptive run: 2048x1024 on [0,2]x[0,1], nu=5e-5, psi modes <= 64,
+    sdirk3_mrsav with SDIRK3(2) PI control (rtol 1e-5), dt0=1e-4 to t=0.05
+    through ``integrate_adaptive`` (every attempt one fused step), FP32 bulk
+    and FP64; reports accepted / rejected attempts and the FP32 run's error
+    against the FP64 run at t_end."""
+    import torch
+    import __graft_entry__
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    __graft_entry__.build()
+    pkg = __graft_entry__.load_package()
+    w = ADAPTIVE
+    g = pkg.MACGrid(w["nx"], w["ny"], w["lx"], w["ly"])
+    x0 = pkg.fields.packed_curl_velocity(w["nx"], w["ny"], w["lx"], w["ly"], w["psi_modes"], w["seed"])
+    runs = {}
+    with ClockSampler(local) as clk:
+        for precision in ("fp32", "fp64"):
+            model = pkg.MACNavierStokes(g, w["nu"], precision=precision, use_graph=True)
+            scheme = pkg.make_scheme(w["scheme"])
+            ctl = pkg.PIController(rtol=w["rtol"])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = pkg.integrate_adaptive(model, scheme, model.state(0.0, x0, 1.0), w["t_end"], w["dt0"],
+                                         controller=ctl, retain_history=False)
+            torch.cuda.synchronize()
+            runs[precision] = (res, time.perf_counter() - t0, model.vector(res.final))
+    if rank != 0:
+        return
+    res32, sec32, x32 = runs["fp32"]
+    res64, sec64, x64 = runs["fp64"]
+    attempts32 = len(res32.attempts)
+    acc32 = sum(1 for a in res32.attempts if a["accepted"])
+    acc64 = sum(1 for a in res64.attempts if a["accepted"])
+    cells = w["nx"] * w["ny"] * w["stages_per_step"]
+    err = float(np.linalg.norm(x32 - x64) / np.linalg.norm(x64))
+    line = {"metric": METRIC, "value": cells * attempts32 / sec32, "unit": "cell-stage/s", "n_gpus": world,
+            "steps": attempts32, "warmup": 0, "ms_per_step": 1e3 * sec32 / attempts32, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64",
+            "data": "synthetic (seeded stream-function curl field, psi modes <= 64)",
+            "config": {"workload": w["workload"], **{k: w[k] for k in ("nx", "ny", "lx", "ly", "nu", "t_end", "dt0",
+                                                                       "rtol", "scheme")},
+                       "controller": "PIController (SDIRK3(2) embedded error)",
+                       "note": "wall time of the whole integrate_adaptive call (host decisions included)"},
+            "status": res32.status, "t_end_reached": float(res32.final.t),
+            "accepted": acc32, "rejected": attempts32 - acc32,
+            "fp64": {"value": cells * len(res64.attempts) / sec64, "seconds": sec64, "accepted": acc64,
+                     "rejected": len(res64.attempts) - acc64, "unit": "cell-stage/s"},
+            "error_vs_fp64_at_t_end": {"rel_l2_velocity": err},
+            "clocks": clk.summary(),
+            "e2e": {"value": cells * attempts32 / sec32, "unit": "cell-stage/s",
+                    "h2d_bytes_per_step": g.size * 8, "d2h_bytes_per_step": g.size * 8}}
+    print(json.dumps(line), flush=True)
+
+
 def learned_leg(pkg, g, w, x0_host, dev, args, x64) -> dict:
     """FP32 bulk with the learned preconditioner on the same steps as ``value``:
     the U-Net is trained here, on the GPU, on pairs logged by plain FP64 Schur
@@ -360,7 +420,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["cavity512", "ensemble256"], default="cavity512")
+    ap.add_argument("--workload", choices=["cavity512", "ensemble256", "adaptive2048"], default="cavity512")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner leg")
     ap.add_argument("--profile", choices=["fp32", "fp64", "unet"], default=None,
                     help="run two eager steps of the workload and exit (for ncu captures)")
@@ -378,6 +438,9 @@ def main() -> None:
         args.warmup = 3
     if args.workload == "ensemble256":
         run_ensemble(args)
+        return
+    if args.workload == "adaptive2048":
+        run_adaptive(args)
         return
 
     import torch
