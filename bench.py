@@ -285,9 +285,8 @@ def run_adaptive(args) -> None:
         return
     res32, sec32, x32 = runs["fp32"]
     res64, sec64, x64 = runs["fp64"]
-    attempts32 = len(res32.attempts)
-    acc32 = sum(1 for a in res32.attempts if a["accepted"])
-    acc64 = sum(1 for a in res64.attempts if a["accepted"])
+    attempts32, acc32 = res32.attempted_steps, res32.accepted_steps
+    attempts64, acc64 = res64.attempted_steps, res64.accepted_steps
     cells = w["nx"] * w["ny"] * w["stages_per_step"]
     err = float(np.linalg.norm(x32 - x64) / np.linalg.norm(x64))
     line = {"metric": METRIC, "value": cells * attempts32 / sec32, "unit": "cell-stage/s", "n_gpus": world,
@@ -300,8 +299,8 @@ def run_adaptive(args) -> None:
                        "note": "wall time of the whole integrate_adaptive call (host decisions included)"},
             "status": res32.status, "t_end_reached": float(res32.final.t),
             "accepted": acc32, "rejected": attempts32 - acc32,
-            "fp64": {"value": cells * len(res64.attempts) / sec64, "seconds": sec64, "accepted": acc64,
-                     "rejected": len(res64.attempts) - acc64, "unit": "cell-stage/s"},
+            "fp64": {"value": cells * attempts64 / sec64, "seconds": sec64, "accepted": acc64,
+                     "rejected": attempts64 - acc64, "unit": "cell-stage/s"},
             "error_vs_fp64_at_t_end": {"rel_l2_velocity": err},
             "clocks": clk.summary(),
             "e2e": {"value": cells * attempts32 / sec32, "unit": "cell-stage/s",

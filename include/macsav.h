@@ -305,6 +305,12 @@ int macsav_step_members_enqueue(macsav_plan* plan, int scheme, double t, double 
  * failing member's code (its records carry the status). */
 int macsav_step_members_finish(macsav_plan* plan, macsav_stage_record* records, double* r1);
 
+/* Process-wide switch (no reference counterpart): launch the solver and step
+ * kernels with programmatic dependent launch (default 1), so each kernel's
+ * launch and ramp-up overlap the tail of the previous one; 0 launches them in
+ * plain stream order.  Affects steps captured after the call. */
+int macsav_set_programmatic_launch(int enable);
+
 /* Measurement helper (no reference counterpart: it times this library's own
  * kernels for the roofline): average device milliseconds of `reps`
  * back-to-back launches of one transform pass over the velocity blocks with two

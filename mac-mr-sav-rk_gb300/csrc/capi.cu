@@ -515,6 +515,11 @@ int macsav_step_embedded_norms(macsav_plan* plan, double* out) {
   return MACSAV_OK;
 }
 
+int macsav_set_programmatic_launch(int enable) {
+  macsav::g_launch_pdl = enable != 0;
+  return MACSAV_OK;
+}
+
 int macsav_time_pass(macsav_plan* plan, int pass, int reps, double* ms, double* bytes, void* stream) {
   if (!plan || !ms || !bytes) return MACSAV_ERR_VALUE;
   const int rc = macsav::time_pass(&plan->p, pass, reps, static_cast<cudaStream_t>(stream), ms, bytes);

@@ -342,6 +342,33 @@ __device__ __forceinline__ void last_block_finish(const Fin& fin, unsigned int* 
   }
 }
 
+// Programmatic dependent launch.  Kernels started with launch_k may be
+// launched while the previous kernel of their stream drains; such a kernel
+// calls pdl_wait() first, which returns once the previous grid has completed
+// and its writes are visible (a no-op for a kernel launched without the
+// attribute).  No kernel triggers its dependents early: measured on GB300, an
+// early trigger let waiting blocks of the next kernel take SM slots and
+// slowed the step by 8-19%, while the plain form gains the launch latency.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+inline bool g_launch_pdl = true;  // launch_k uses the programmatic-serialization attribute
+
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                     Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = g_launch_pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 struct NoFin {
   __device__ void operator()() const {}
 };

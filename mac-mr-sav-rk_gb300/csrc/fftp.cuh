@@ -105,6 +105,7 @@ __device__ __forceinline__ void fft_p2(cplx<T>* z, int t, const cplx<T>* __restr
 // One block (u, v or p) per launch; NL = blockDim.x / (L/8) line pairs per CTA.
 template <typename T, int L, class Src>
 __global__ void __launch_bounds__(kFFTThreads) k_row_forward_p2(TBlockDev<T> B, const int* active, Src src, int bk) {
+  pdl_wait();
   const int c = blockIdx.y;
   if (active && !active[c]) return;
   constexpr int G = L / kE;
@@ -155,6 +156,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_forward_p2(TBlockDev<T> B, 
 template <typename T, int L, class Dst, class Fin>
 __global__ void __launch_bounds__(kFFTThreads) k_row_inverse_p2(TBlockDev<T> B, const int* active, Dst dst, int bk,
                                                                 double* partial, Fin fin, unsigned int* counter) {
+  pdl_wait();
   const int c = blockIdx.y;
   constexpr int G = L / kE;
   const bool live = !active || active[c];
@@ -235,6 +237,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_inverse_p2(TBlockDev<T> B, 
 template <typename T, int L>
 __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const int* active, int mode,
                                                           const double* shift, T thr) {
+  pdl_wait();
   const int c = blockIdx.y;
   if (active && !active[c]) return;
   constexpr int G = L / kE;

@@ -382,7 +382,7 @@ struct Launcher {
   {                                                                                          \
     auto k = k_row_forward_p2<T, LL, Src>;                                                   \
     set_smem(k, sm);                                                                         \
-    k<<<dim3(row_grid(B), cols), P * G, sm, st>>>(B, active, src, bk);                       \
+    launch_k(k, dim3(row_grid(B), cols), P * G, sm, st, B, active, src, bk);                       \
   }
         MACSAV_P2_SWITCH(B.fx.L, MACSAV_RF)
 #undef MACSAV_RF
@@ -395,7 +395,7 @@ struct Launcher {
     RowArgs<T> r = row_args(a, b, active);
     auto k = k_row_forward<T, kVmax, Src>;
     set_smem(k, smem);
-    k<<<dim3(total_groups(r), cols), kFFTThreads, smem, s>>>(r, src);
+    launch_k(k, dim3(total_groups(r), cols), kFFTThreads, smem, s, r, src);
     ++*counter;
   }
   template <class Dst, class Fin>
@@ -410,7 +410,7 @@ struct Launcher {
   {                                                                                          \
     auto k = k_row_inverse_p2<T, LL, Dst, Fin>;                                              \
     set_smem(k, sm);                                                                         \
-    k<<<dim3(row_grid(B), cols), P * G, sm, st>>>(B, active, dst, bk, partial, fin, done);   \
+    launch_k(k, dim3(row_grid(B), cols), P * G, sm, st, B, active, dst, bk, partial, fin, done);   \
   }
         MACSAV_P2_SWITCH(B.fx.L, MACSAV_RI)
 #undef MACSAV_RI
@@ -423,7 +423,7 @@ struct Launcher {
     RowArgs<T> r = row_args(a, b, active);
     auto k = k_row_inverse<T, kVmax, Dst, Fin>;
     set_smem(k, smem);
-    k<<<dim3(total_groups(r), cols), kFFTThreads, smem, s>>>(r, dst, partial, fin, done);
+    launch_k(k, dim3(total_groups(r), cols), kFFTThreads, smem, s, r, dst, partial, fin, done);
     ++*counter;
   }
   void column(const TBlockDev<T>& a, const TBlockDev<T>* b, size_t smem, int cols, const int* active, int mode,
@@ -438,7 +438,7 @@ struct Launcher {
   {                                                                                          \
     auto k = k_column_p2<T, LL>;                                                             \
     set_smem(k, sm);                                                                         \
-    k<<<dim3(grid, cols), NL * G, sm, st>>>(B, active, mode, shift, thr);                    \
+    launch_k(k, dim3(grid, cols), NL * G, sm, st, B, active, mode, shift, thr);                    \
   }
         MACSAV_P2_SWITCH(B.fy.L, MACSAV_CO)
 #undef MACSAV_CO
@@ -451,7 +451,7 @@ struct Launcher {
     ColArgs<T> r = col_args(a, b, active, mode, shift, thr);
     auto k = k_column<T, kVmax>;
     set_smem(k, smem);
-    k<<<dim3(total_groups(r), cols), kFFTThreads, smem, s>>>(r);
+    launch_k(k, dim3(total_groups(r), cols), kFFTThreads, smem, s, r);
     ++*counter;
   }
 

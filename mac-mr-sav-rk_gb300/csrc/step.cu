@@ -50,6 +50,7 @@ constexpr long long kPartEmb = 4096;      // embedded-error partials within the 
 // convection combination); partial slots: max|out0|, max|out1|, sum out1^2.
 __global__ void __launch_bounds__(kThreads) k_combine2(CombineArgs a, const double* coef, long long n,
                                                        double* partial) {
+  pdl_wait();
   __shared__ double red[6 * 32];
   __shared__ unsigned long long redk[2 * 32];
   const int mem = blockIdx.y;
@@ -82,6 +83,7 @@ __global__ void __launch_bounds__(kThreads) k_combine2(CombineArgs a, const doub
 // Partial sums of <N,V>, <N,W>, <W,W> with V, W the two Stokes columns.
 __global__ void __launch_bounds__(kThreads) k_dots3(const double* N, const double* V, long long n, long long vstr,
                                                     double* partial) {
+  pdl_wait();
   __shared__ double red[6 * 32];
   const int mem = blockIdx.y;
   N += mem * vstr;
@@ -111,6 +113,7 @@ __global__ void __launch_bounds__(kThreads) k_recombine(GridDev g, const double*
                                                         const double* N, double* U, double* pi, const StageRec* rec,
                                                         const double* coef, int dt_idx, int sav, double* partial,
                                                         MemberStrides ms) {
+  pdl_wait();
   __shared__ double red[64];
   const int mem = blockIdx.y;
   VW += mem * ms.VW;
@@ -145,6 +148,7 @@ __global__ void __launch_bounds__(kThreads) k_stage_defect(GridDev g, const doub
                                                            const double* rhs, double* KU, const StageRec* rec,
                                                            const double* coef, int dt_idx, int kappa_idx, int sav,
                                                            double* partial, MemberStrides ms) {
+  pdl_wait();
   __shared__ unsigned long long redk[4 * 32];
   const int mem = blockIdx.y;
   U += mem * ms.X;
@@ -186,6 +190,7 @@ __global__ void __launch_bounds__(kThreads) k_stage_defect(GridDev g, const doub
 
 // Skew convection of every member's stage velocity (kernels.py:6-35).
 __global__ void k_conv_members(GridDev g, const double* x, long long xstr, double* out, long long ostr) {
+  pdl_wait();
   const int mem = blockIdx.y;
   x += mem * xstr;
   out += mem * ostr;
@@ -212,6 +217,7 @@ __device__ double fold_max(const double* partial, int nb, int K, int k, double* 
 // columns (tensor_stokes.py:338-351) and the iteration counts; thread = member.
 __global__ void k_stage_stokes(const SolveChecks* checks, const CGScalars* cg, int cols, int members, double tol,
                                StageRec* recs_i) {
+  pdl_wait();
   const int mem = threadIdx.x;
   if (mem >= members) return;
   StageRec* rec = recs_i + mem * kRecStride;
@@ -242,6 +248,7 @@ __global__ void k_stage_stokes(const SolveChecks* checks, const CGScalars* cg, i
 // alpha/beta guard of sdirk3_mrsav.py:92-100); one block per member.
 __global__ void __launch_bounds__(kThreads) k_stage_sav(const double* partial, int nb, StageRec* recs, int stage,
                                                         const double* coef, SavIdx ix, double area) {
+  pdl_wait();
   __shared__ double red[64];
   const int mem = blockIdx.x;
   partial += mem * kPartStride;
@@ -308,6 +315,7 @@ __global__ void __launch_bounds__(kThreads) k_stage_sav(const double* partial, i
 __global__ void __launch_bounds__(kThreads) k_stage_close(const double* partial, int nbd, int nbn, StageRec* recs,
                                                           int stage, const double* coef, SavIdx ix, double area,
                                                           int sav, int gate) {
+  pdl_wait();
   __shared__ double red[64];
   const int mem = blockIdx.x;
   partial += mem * kPartStride;
@@ -342,6 +350,7 @@ __global__ void __launch_bounds__(kThreads) k_stage_close(const double* partial,
 
 // one block per member
 __global__ void k_fold_combine(const double* partial, int nb, StageRec* recs_i) {
+  pdl_wait();
   __shared__ double red[64];
   const int mem = blockIdx.x;
   partial += mem * kPartStride;
@@ -358,6 +367,7 @@ __global__ void k_fold_combine(const double* partial, int nb, StageRec* recs_i) 
 
 // shifts of every member's Stokes columns: mass 1, viscosity kappa (member's table)
 __global__ void k_set_shift(double* shift, const double* coef, int kappa_idx, int cols, int total) {
+  pdl_wait();
   const int c = threadIdx.x;
   if (c < total) {
     shift[2 * c] = 1.0;
@@ -399,6 +409,7 @@ struct EmbFin {
 __global__ void __launch_bounds__(kThreads) k_emb_norms(const double* X, long long xstr, long long last,
                                                         const double* emb, long long n, double* partial, EmbFin fin,
                                                         unsigned int* done) {
+  pdl_wait();
   __shared__ double red[3 * 32];
   constexpr unsigned long long kInf = 0x7ff0000000000000ull;
   const int mem = blockIdx.y;
@@ -429,6 +440,7 @@ __global__ void __launch_bounds__(kThreads) k_emb_norms(const double* X, long lo
 }
 
 __global__ void k_clear_recs(StageRec* recs, int n) {
+  pdl_wait();
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     StageRec z;
     memset(&z, 0, sizeof(z));
@@ -650,39 +662,39 @@ static int enqueue_step(Plan* P, Exec& X, int scheme, const StageProgram& G, boo
   const int cols = sav ? 2 : 1;
   const double area = g.hx * g.hy;
   const MemberStrides ms{5 * sz, 4 * sz, 4 * sz, cols * sz, cols * sz, cols * np, 4 * np};
-  k_clear_recs<<<1, 128, 0, s>>>(B.recs, kRecStride * M);
+  launch_k(k_clear_recs, 1, 128, 0, s, B.recs, kRecStride * M);
   // N(U_0)
-  k_conv_members<<<dim3(red_nb(sz), M), kThreads, 0, s>>>(g, B.X, ms.X, B.NN, ms.NN);
+  launch_k(k_conv_members, dim3(red_nb(sz), M), kThreads, 0, s, g, B.X, ms.X, B.NN, ms.NN);
   P->launches += 2;
   for (int i = 0; i < G.nstages; ++i) {
     StageRec* rec = B.recs + i;
     double* U = B.X + (i + 1) * sz;
     CombineArgs ca = G.comb[i];
     if (!sav) ca.nout = 1;
-    k_combine2<<<dim3(nbs, M), kThreads, 0, s>>>(ca, B.coef, sz, P->partial);
-    k_fold_combine<<<M, kThreads, 0, s>>>(P->partial, nbs, rec);
-    k_set_shift<<<1, kMaxCols, 0, s>>>(P->shift, B.coef, G.kappa[i], cols, cols * M);
+    launch_k(k_combine2, dim3(nbs, M), kThreads, 0, s, ca, B.coef, sz, P->partial);
+    launch_k(k_fold_combine, M, kThreads, 0, s, P->partial, nbs, rec);
+    launch_k(k_set_shift, 1, kMaxCols, 0, s, P->shift, B.coef, G.kappa[i], cols, cols * M);
     P->launches += 3;
     int rc = P->precision == MACSAV_FP64 ? enqueue_solve_fp64(P, X, B.F, cols * M, B.VW, B.PI)
                                          : enqueue_solve_mixed(P, X, B.F, cols * M, B.VW, B.PI);
     if (rc != MACSAV_OK) return rc;
-    k_stage_stokes<<<1, kMaxMembers, 0, s>>>(P->checks, P->cg, cols, M, P->tol, rec);
+    launch_k(k_stage_stokes, 1, kMaxMembers, 0, s, P->checks, P->cg, cols, M, P->tol, rec);
     ++P->launches;
     if (sav) {
-      k_dots3<<<dim3(nbs, M), kThreads, 0, s>>>(B.F + sz, B.VW, sz, ms.F, P->partial);
-      k_stage_sav<<<M, kThreads, 0, s>>>(P->partial, nbs, B.recs, i, B.coef, G.sav[i], area);
+      launch_k(k_dots3, dim3(nbs, M), kThreads, 0, s, B.F + sz, B.VW, sz, ms.F, P->partial);
+      launch_k(k_stage_sav, M, kThreads, 0, s, P->partial, nbs, B.recs, i, B.coef, G.sav[i], area);
       P->launches += 2;
     }
     double* pi = B.PS + i * np;
-    k_recombine<<<dim3(nbn, M), kThreads, 0, s>>>(g, B.VW, B.PI, B.F + sz, U, pi, rec, B.coef, G.dt_idx, sav ? 1 : 0,
+    launch_k(k_recombine, dim3(nbn, M), kThreads, 0, s, g, B.VW, B.PI, B.F + sz, U, pi, rec, B.coef, G.dt_idx, sav ? 1 : 0,
                                                    P->partial + kPartNu, ms);
-    k_stage_defect<<<dim3(nbn, M), kThreads, 0, s>>>(g, U, pi, B.F, B.KU + i * sz, rec, B.coef, G.dt_idx,
+    launch_k(k_stage_defect, dim3(nbn, M), kThreads, 0, s, g, U, pi, B.F, B.KU + i * sz, rec, B.coef, G.dt_idx,
                                                       G.kappa[i], sav ? 1 : 0, P->partial, ms);
     const int gate = (scheme == MACSAV_SDIRK2 || scheme == MACSAV_SDIRK3) ? 0 : 1;
-    k_stage_close<<<M, kThreads, 0, s>>>(P->partial, nbn, nbn, B.recs, i, B.coef, G.sav[i], area, sav ? 1 : 0, gate);
+    launch_k(k_stage_close, M, kThreads, 0, s, P->partial, nbn, nbn, B.recs, i, B.coef, G.sav[i], area, sav ? 1 : 0, gate);
     P->launches += 3;
     if (i + 1 < G.nstages) {
-      k_conv_members<<<dim3(red_nb(sz), M), kThreads, 0, s>>>(g, U, ms.X, B.NN + (i + 1) * sz, ms.NN);
+      launch_k(k_conv_members, dim3(red_nb(sz), M), kThreads, 0, s, g, U, ms.X, B.NN + (i + 1) * sz, ms.NN);
       ++P->launches;
     }
   }
@@ -698,11 +710,11 @@ static int enqueue_step(Plan* P, Exec& X, int scheme, const StageProgram& G, boo
       e.sstr[0][k] = ms.X;
       e.idx[0][k] = G.emb_idx[k];
     }
-    k_combine2<<<dim3(nbs, M), kThreads, 0, s>>>(e, B.coef, sz, P->partial);
+    launch_k(k_combine2, dim3(nbs, M), kThreads, 0, s, e, B.coef, sz, P->partial);
     ++P->launches;
     // the adaptive controller's inner products, so an attempt needs no more
     // device round trips than the step itself
-    k_emb_norms<<<dim3(nbs, M), kThreads, 0, s>>>(B.X, ms.X, G.nstages * sz, B.EMB, sz, P->partial + kPartEmb,
+    launch_k(k_emb_norms, dim3(nbs, M), kThreads, 0, s, B.X, ms.X, G.nstages * sz, B.EMB, sz, P->partial + kPartEmb,
                                                    EmbFin{P->partial + kPartEmb, nbs, M, g.hx * g.hy, B.enorm},
                                                    P->done_counter);
     ++P->launches;

@@ -44,6 +44,7 @@ template <typename T, typename WIn>
 __global__ void __launch_bounds__(kThreads) k_pressure_rhs(GridDev g, const WIn* w, long long ws, T* b, long long cs,
                                                            const double* rd, double* partial, CGFin<T> fin,
                                                            unsigned int* done) {
+  pdl_wait();
   const int c = blockIdx.y;
   const T ihx = T(g.ihx), ihy = T(g.ihy);
   Acc<T> acc[1];
@@ -62,6 +63,7 @@ __global__ void __launch_bounds__(kThreads) k_pressure_rhs(GridDev g, const WIn*
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_cg_start(int np, T* b, T* x, T* r, long long cs, const CGScalars* cg,
                                                        double* partial, CGFin<T> fin, unsigned int* done) {
+  pdl_wait();
   const int c = blockIdx.y;
   const T mean = cg_mean_b<T>(cg[c]);
   Acc<T> s[1];
@@ -89,6 +91,7 @@ template <typename T, typename WIn>
 __global__ void __launch_bounds__(kThreads) k_div_q(GridDev g, const WIn* w, long long ws, T* q, const T* z, const T* p,
                                                     long long cs, const CGScalars* cg, const int* active,
                                                     double* partial, CGFin<T> fin, unsigned int* done) {
+  pdl_wait();
   const int c = blockIdx.y;
   Acc<T> a[3];
   if (active[c]) {
@@ -116,6 +119,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_cg_update(int np, T* x, T* r, T* p, const T* z, const T* q, T* r_old,
                                                         long long cs, const CGScalars* cg, const int* active,
                                                         double* partial, CGFin<T> fin, unsigned int* done) {
+  pdl_wait();
   const int c = blockIdx.y;
   Acc<T> acc[1];
   if (active[c]) {
@@ -141,6 +145,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int np, T* x, T* r, T* p
 // Columns whose learned attempt failed restart plain PCG from zero: x = 0, r = b.
 __global__ void __launch_bounds__(kThreads) k_fcg_restart(int np, const float* b, float* x, float* r, long long cs,
                                                           const CGScalars* cg) {
+  pdl_wait();
   const int c = blockIdx.y;
   if (!cg[c].restart) return;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
@@ -155,6 +160,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_restart(int np, const float* b
 // answers in units of the spectral preconditioner's Rayleigh quotient.
 // Columns without the network get 0 (a zero correction).
 __global__ void k_net_scales(const CGScalars* cg, const int* active, int cols, int np, float* scale) {
+  pdl_wait();
   const int c = threadIdx.x;
   if (c >= cols) return;
   const CGScalars& g = cg[c];
@@ -169,6 +175,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_z(int np, float* z, const floa
                                                     const float* r_old, long long cs, const CGScalars* cg,
                                                     const int* active, double* partial, CGFin<float> fin,
                                                     unsigned int* done) {
+  pdl_wait();
   const int c = blockIdx.y;
   Acc<float> a[5];
   if (active[c]) {
@@ -191,6 +198,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_z(int np, float* z, const floa
 // z -= mean(z): the mean-zero projection of the flexible preconditioner.
 __global__ void __launch_bounds__(kThreads) k_fcg_center(int np, float* z, long long cs, const CGScalars* cg,
                                                          const int* active) {
+  pdl_wait();
   const int c = blockIdx.y;
   if (!active[c]) return;
   const float m = cg[c].mean_z_t;
@@ -198,6 +206,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_center(int np, float* z, long 
 }
 
 __global__ void k_reset_counters(CGScalars* cg, int cols) {
+  pdl_wait();
   const int c = threadIdx.x;
   if (c < cols) {
     cg[c].cum_iters = 0;
@@ -207,7 +216,7 @@ __global__ void k_reset_counters(CGScalars* cg, int cols) {
 }
 
 void reset_cg_counters(Plan* P, int cols, cudaStream_t s) {
-  k_reset_counters<<<1, 32, 0, s>>>(P->cg, cols);
+  launch_k(k_reset_counters, 1, 32, 0, s, P->cg, cols);
   ++P->launches;
 }
 
@@ -217,6 +226,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_center_cells(int np, const T* x, long long xs, double* out,
                                                            long long os, const CGScalars* cg, int center,
                                                            double* partial, CGFin<double> fin, unsigned int* done) {
+  pdl_wait();
   const int c = blockIdx.y;
   const double mean = center ? cg[c].mean_q : 0.0;
   Acc<double> acc[1];
@@ -230,6 +240,7 @@ __global__ void __launch_bounds__(kThreads) k_center_cells(int np, const T* x, l
 }
 
 __global__ void __launch_bounds__(kThreads) k_shift_cells(int np, double* out, long long os, const CGScalars* cg) {
+  pdl_wait();
   const int c = blockIdx.y;
   const double mean = cg[c].mean_q;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x)
@@ -242,6 +253,7 @@ __global__ void __launch_bounds__(kThreads) k_stokes_check(GridDev g, const doub
                                                            const double* f, long long vs, long long ps,
                                                            const double* shift, double* partial,
                                                            CGFin<double> fin, unsigned int* done) {
+  pdl_wait();
   const int c = blockIdx.y;
   const double mass = shift[2 * c], visc = shift[2 * c + 1];
   const double* u = vel + c * vs;
@@ -303,7 +315,7 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
     net = X.net && P->net;
     if (net) {
       r_old = P->net_rold;
-      k_fcg_restart<<<dim3(rb, cols), kThreads, 0, s>>>(g.np, b, x, r, np, P->cg);
+      launch_k(k_fcg_restart, dim3(rb, cols), kThreads, 0, s, g.np, b, x, r, np, P->cg);
       ++P->launches;
     }
   }
@@ -315,21 +327,21 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
                   make_fin<T>(P, X, OP_RHO, L.groups_row_p(), 2, cols), P->done_counter);
   if constexpr (std::is_same<T, float>::value) {
     if (net) {
-      k_net_scales<<<1, 32, 0, s>>>(P->cg, P->active, cols, g.np, P->net_scale);
+      launch_k(k_net_scales, 1, 32, 0, s, P->cg, P->active, cols, g.np, P->net_scale);
       ++P->launches;
       unet_forward(P->net, &P->netw, r, P->net_scale, cols, g.ny, g.nx, P->net_out, P->net_scale + cols, s);
-      k_fcg_z<<<dim3(rb, cols), kThreads, 0, s>>>(g.np, z, P->net_out, r, r_old, np, P->cg, P->active, P->partial,
+      launch_k(k_fcg_z, dim3(rb, cols), kThreads, 0, s, g.np, z, P->net_out, r, r_old, np, P->cg, P->active, P->partial,
                                                   make_fin<float>(P, X, OP_FCG, rb, 5, cols), P->done_counter);
-      k_fcg_center<<<dim3(rb, cols), kThreads, 0, s>>>(g.np, z, np, P->cg, P->active);
+      launch_k(k_fcg_center, dim3(rb, cols), kThreads, 0, s, g.np, z, np, P->cg, P->active);
       P->launches += 2;
     }
   }
   // q = S pdir = D (mI+kK)^{-1} D^T pdir,  pdir = z + beta p
   velocity_inverse<T>(P, L, SrcLift<T, double, T>{nullptr, 0, z, pd, P->cg, np, g.nx, g.nu, T(g.ihx), T(g.ihy)}, w,
                       sz, cols, P->active);
-  k_div_q<T, T><<<dim3(rb, cols), kThreads, 0, s>>>(g, w, sz, q, z, pd, np, P->cg, P->active, P->partial,
+  launch_k(k_div_q<T, T>, dim3(rb, cols), kThreads, 0, s, g, w, sz, q, z, pd, np, P->cg, P->active, P->partial,
                                                     make_fin<T>(P, X, OP_ALPHA, rb, 3, cols), P->done_counter);
-  k_cg_update<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, x, r, pd, z, q, r_old, np, P->cg, P->active, P->partial,
+  launch_k(k_cg_update<T>, dim3(rb, cols), kThreads, 0, s, g.np, x, r, pd, z, q, r_old, np, P->cg, P->active, P->partial,
                                                      make_fin<T>(P, X, OP_CHECK, rb, 1, cols), P->done_counter);
   P->launches += 2;
 }
@@ -346,11 +358,11 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
   T* r = cells + 2 * np * cols;
   const int rb = red_blocks(np);
   const cudaStream_t s = X.s;
-  k_pressure_rhs<T, T><<<dim3(rb, cols), kThreads, 0, s>>>(g, w, sz, b, np, rd, P->partial,
+  launch_k(k_pressure_rhs<T, T>, dim3(rb, cols), kThreads, 0, s, g, w, sz, b, np, rd, P->partial,
                                                            make_fin<T>(P, X, OP_MEAN_B, rb, 1, cols), P->done_counter);
   ++P->launches;
   if (!X.graph) {
-    k_cg_start<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, b, x, r, np, P->cg, P->partial,
+    launch_k(k_cg_start<T>, dim3(rb, cols), kThreads, 0, s, g.np, b, x, r, np, P->cg, P->partial,
                                                       make_fin<T>(P, X, OP_START, rb, 2, cols), P->done_counter);
     ++P->launches;
     const int limit = P->maxit + (X.net && P->net ? P->net_maxit : 0);
@@ -398,7 +410,7 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
   if (cudaGraphConditionalHandleCreate(&X.cond, graph, 0, cudaGraphCondAssignDefault) != cudaSuccess)
     return MACSAV_ERR_CUDA;
   // k_cg_start's last block sets the loop condition
-  k_cg_start<T><<<dim3(rb, cols), kThreads, 0, s>>>(g.np, b, x, r, np, P->cg, P->partial,
+  launch_k(k_cg_start<T>, dim3(rb, cols), kThreads, 0, s, g.np, b, x, r, np, P->cg, P->partial,
                                                     make_fin<T>(P, X, OP_START, rb, 2, cols), P->done_counter);
   ++P->launches;
   if (cudaStreamGetCaptureInfo(s, &st, nullptr, &graph, &deps, nullptr, &ndeps) != cudaSuccess)
@@ -430,11 +442,11 @@ static void finish_pressure(Plan* P, const Exec& X, const T* x, double* pres, in
   const long long np = P->g.np;
   const int rb = red_blocks(np);
   const cudaStream_t s = X.s;
-  k_center_cells<T><<<dim3(rb, cols), kThreads, 0, s>>>(P->g.np, x, np, nullptr, np, P->cg, 0, P->partial,
+  launch_k(k_center_cells<T>, dim3(rb, cols), kThreads, 0, s, P->g.np, x, np, nullptr, np, P->cg, 0, P->partial,
                                                         make_fin<double>(P, X, OP_MEAN_X, rb, 1, cols), P->done_counter);
-  k_center_cells<T><<<dim3(rb, cols), kThreads, 0, s>>>(P->g.np, x, np, pres, np, P->cg, 1, P->partial,
+  launch_k(k_center_cells<T>, dim3(rb, cols), kThreads, 0, s, P->g.np, x, np, pres, np, P->cg, 1, P->partial,
                                                         make_fin<double>(P, X, OP_MEAN_X, rb, 1, cols), P->done_counter);
-  k_shift_cells<<<dim3(rb, cols), kThreads, 0, s>>>(P->g.np, pres, np, P->cg);
+  launch_k(k_shift_cells, dim3(rb, cols), kThreads, 0, s, P->g.np, pres, np, P->cg);
   P->launches += 3;
 }
 
@@ -442,7 +454,7 @@ static void closing_checks(Plan* P, const Exec& X, const double* f, const double
                            const double* shift) {
   const long long n = P->g.size > P->g.np ? P->g.size : P->g.np;
   const int rb = red_blocks(n);
-  k_stokes_check<<<dim3(rb, cols), kThreads, 0, X.s>>>(P->g, vel, pres, f, P->g.size, P->g.np, shift, P->partial,
+  launch_k(k_stokes_check, dim3(rb, cols), kThreads, 0, X.s, P->g, vel, pres, f, P->g.size, P->g.np, shift, P->partial,
                                                        make_fin<double>(P, X, OP_CHECKS, rb, 6, cols), P->done_counter);
   ++P->launches;
 }
@@ -480,6 +492,7 @@ int solve_fp64(Plan* P, const double* f, int cols, double mass, double visc, dou
 __global__ void __launch_bounds__(kThreads) k_defect64(GridDev g, const double* f, const double* vel,
                                                        const double* pres, const double* shift, double* ru,
                                                        double* rd) {
+  pdl_wait();
   const int c = blockIdx.y;
   const double mass = shift[2 * c], visc = shift[2 * c + 1];
   const double* u = vel + c * (long long)g.size;
@@ -500,6 +513,7 @@ __global__ void __launch_bounds__(kThreads) k_defect64(GridDev g, const double* 
 // dst (+)= double(src) over n elements per column.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_accumulate(const T* src, double* dst, long long n, int add) {
+  pdl_wait();
   const int c = blockIdx.y;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const long long k = c * n + i;
@@ -545,15 +559,15 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
     const double* rhs_u = f;
     const double* rhs_d = nullptr;
     if (sweep > 0) {
-      k_defect64<<<dim3(nbm, cols), kThreads, 0, X.s>>>(g, f, vel, pres, P->shift, ru, rd);
+      launch_k(k_defect64, dim3(nbm, cols), kThreads, 0, X.s, g, f, vel, pres, P->shift, ru, rd);
       ++P->launches;
       rhs_u = ru;
       rhs_d = rd;
     }
     int rc = inner_solve32(P, X, rhs_u, rhs_d, cols, du);
     if (rc != MACSAV_OK) return rc;
-    k_accumulate<float><<<dim3(nbv, cols), kThreads, 0, X.s>>>(du, vel, sz, sweep > 0);
-    k_accumulate<float><<<dim3(nbp, cols), kThreads, 0, X.s>>>(P->cells32 + 1 * np * cols, pres, np, sweep > 0);
+    launch_k(k_accumulate<float>, dim3(nbv, cols), kThreads, 0, X.s, du, vel, sz, sweep > 0);
+    launch_k(k_accumulate<float>, dim3(nbp, cols), kThreads, 0, X.s, P->cells32 + 1 * np * cols, pres, np, sweep > 0);
     P->launches += 2;
   }
   // mean-zero pressure and the FP64 closing checks, as in the FP64 path

@@ -161,6 +161,7 @@ constexpr int kStage = 4;  // independent global loads in flight per thread
 // Forward x-transform of rows: src(blk, col, row, n) -> H.
 template <typename T, int VMAX, class Src>
 __global__ void __launch_bounds__(kFFTThreads, sizeof(T) == 4 ? 2 : 1) k_row_forward(RowArgs<T> a, Src src) {
+  pdl_wait();
   const int c = blockIdx.y;
   if (a.active && !a.active[c]) return;
   int g;
@@ -217,6 +218,7 @@ __global__ void __launch_bounds__(kFFTThreads, sizeof(T) == 4 ? 2 : 1) k_row_for
 template <typename T, int VMAX, class Dst, class Fin>
 __global__ void __launch_bounds__(kFFTThreads, sizeof(T) == 4 ? 2 : 1) k_row_inverse(RowArgs<T> a, Dst dst, double* partial, Fin fin,
                                                              unsigned int* counter) {
+  pdl_wait();
   const int c = blockIdx.y;
   const bool live = !a.active || a.active[c];
   Acc<T> acc[2];
@@ -308,6 +310,7 @@ struct ColArgs {
 // loads past the last column read zeros).
 template <typename T, int VMAX>
 __global__ void __launch_bounds__(kFFTThreads, sizeof(T) == 4 ? 2 : 1) k_column(ColArgs<T> a) {
+  pdl_wait();
   const int c = blockIdx.y;
   if (a.active && !a.active[c]) return;
   int g;
