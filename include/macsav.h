@@ -128,6 +128,12 @@ int macsav_max_abs(macsav_plan* plan, const double* a, long long n, double* resu
 int macsav_inner_max_static(const double* a, const double* b, long long n, double weight, double* result,
                             void* stream);
 
+/* MACGrid.unpack (direction 0: packed -> u (ny, nx+1), v (ny+1, nx), zero
+ * normal wall faces) and MACGrid.pack (direction 1: u, v -> packed)
+ * (solver/mac/grid.py:52-65), on device arrays, so host states cross the bus
+ * as plain copies. */
+int macsav_layout(macsav_plan* plan, int direction, double* packed, double* u, double* v, void* stream);
+
 /* MACNavierStokes.diagnostics (solver/mac_ns.py:95-107) of a packed velocity x
  * with scalar r: out[0..7] = kinetic, modified_energy, divergence_inf,
  * h1_seminorm_squared, r, angular_momentum, power, dissipation.  force may be

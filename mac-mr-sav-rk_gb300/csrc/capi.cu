@@ -20,6 +20,7 @@ int solve_fp64(Plan* P, const double* f, int cols, double mass, double visc, dou
 int solve_mixed(Plan* P, const double* f, int cols, double mass, double visc, double* vel, double* pres,
                 cudaStream_t s, int* sweeps);
 int op_apply(Plan* P, int which, const double* in, double* out, int cols, cudaStream_t s);
+int op_layout(Plan* P, int direction, double* packed, double* u, double* v, cudaStream_t s);
 int op_combine(Plan* P, int nterms, const double* coeffs, const double* const* fields, double* out, long long n,
                cudaStream_t s);
 int op_dot_max(Plan* P, const double* a, const double* b, long long n, double* result, cudaStream_t s);
@@ -241,6 +242,12 @@ int macsav_max_abs(macsav_plan* plan, const double* a, long long n, double* resu
   const int rc = macsav::op_dot_max(&plan->p, a, nullptr, n, r, static_cast<cudaStream_t>(stream));
   *result = r[1];
   return rc;
+}
+
+int macsav_layout(macsav_plan* plan, int direction, double* packed, double* u, double* v, void* stream) {
+  if (!plan || !packed || !u || !v || direction < 0 || direction > 1) return MACSAV_ERR_VALUE;
+  const int rc = macsav::op_layout(&plan->p, direction, packed, u, v, static_cast<cudaStream_t>(stream));
+  return rc == MACSAV_OK ? MACSAV_OK : cuda_status(&plan->p);
 }
 
 int macsav_diagnostics(macsav_plan* plan, const double* x, double r, double nu, const double* force, double* out,

@@ -184,6 +184,41 @@ int op_apply(Plan* P, int which, const double* in, double* out, int cols, cudaSt
   return cudaGetLastError() == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
 }
 
+// Packed free vector <-> full face arrays u (ny, nx+1) and v (ny+1, nx)
+// (MACGrid.pack / unpack, solver/mac/grid.py:52-65); unpack writes the zero
+// normal wall faces.
+__global__ void k_unpack(GridDev g, const double* x, double* u, double* v) {
+  const int nU = g.ny * (g.nx + 1), nV = (g.ny + 1) * g.nx;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nU + nV; e += gridDim.x * blockDim.x) {
+    if (e < nU) {
+      const int j = e / (g.nx + 1), I = e - j * (g.nx + 1);
+      u[e] = (I == 0 || I == g.nx) ? 0.0 : x[j * (g.nx - 1) + I - 1];
+    } else {
+      const int f = e - nU, J = f / g.nx, i = f - J * g.nx;
+      v[f] = (J == 0 || J == g.ny) ? 0.0 : x[g.nu + (J - 1) * g.nx + i];
+    }
+  }
+}
+__global__ void k_pack(GridDev g, const double* u, const double* v, double* x) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < g.size; e += gridDim.x * blockDim.x) {
+    if (e < g.nu) {
+      const int j = e / (g.nx - 1), i = e - j * (g.nx - 1);
+      x[e] = u[j * (g.nx + 1) + i + 1];
+    } else {
+      const int f = e - g.nu, k = f / g.nx, i = f - k * g.nx;
+      x[e] = v[(k + 1) * g.nx + i];
+    }
+  }
+}
+
+int op_layout(Plan* P, int direction, double* packed, double* u, double* v, cudaStream_t s) {
+  const GridDev& g = P->g;
+  if (direction == 0) k_unpack<<<op_blocks(g.ny * (g.nx + 1) + (g.ny + 1) * g.nx), kThreads, 0, s>>>(g, packed, u, v);
+  else k_pack<<<op_blocks(g.size), kThreads, 0, s>>>(g, u, v, packed);
+  ++P->launches;
+  return cudaGetLastError() == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
+}
+
 void launch_convection(Plan* P, const double* x, double* out, cudaStream_t s) {
   k_convection<<<dim3(op_blocks(P->g.size), 1), kThreads, 0, s>>>(P->g, x, out);
   ++P->launches;

@@ -80,16 +80,37 @@ class MACNavierStokes:
         return self.grid.pack(state.u, state.v)
 
     def device_vector(self, state: State) -> torch.Tensor:
-        """Packed device velocity of a state (its cached copy when it has one)."""
+        """Packed device velocity of a state (its cached copy when it has one).
+        A host state crosses as its two face arrays, packed on the device
+        (after the wall-face check of MACGrid.pack, solver/mac/grid.py:52-57)."""
         cached = getattr(state, "device", None)
         if cached is not None:
             return cached
-        return self._dev(self.vector(state))
+        g = self.grid
+        u, v = np.asarray(state.u, dtype=np.float64), np.asarray(state.v, dtype=np.float64)
+        if u.shape != (g.ny, g.nx + 1) or v.shape != (g.ny + 1, g.nx):
+            raise ValueError("Incorrect MAC array shapes")
+        if np.any(u[:, [0, -1]] != 0) or np.any(v[[0, -1], :] != 0):
+            raise ValueError("Normal boundary velocities must be zero")
+        ud = torch.from_numpy(np.ascontiguousarray(u)).to(self.device)
+        vd = torch.from_numpy(np.ascontiguousarray(v)).to(self.device)
+        x = torch.empty(g.size, dtype=torch.float64, device=self.device)
+        self.plan.check(self.plan.lib.macsav_layout(self.plan.handle, 1, dptr(x), dptr(ud), dptr(vd),
+                                                    stream_handle()))
+        return x
 
     def state(self, t: float, velocity, r: float = 0.0) -> State:
+        """A host State (face arrays unpacked on the device, then copied) that
+        also keeps the packed device vector."""
         dv = self._dev(velocity).contiguous()
-        host = dv.cpu().numpy()
-        u, v = self.grid.unpack(host)
+        g = self.grid
+        if dv.numel() != g.size:
+            raise ValueError("Incorrect free-vector shape")
+        ud = torch.empty((g.ny, g.nx + 1), dtype=torch.float64, device=self.device)
+        vd = torch.empty((g.ny + 1, g.nx), dtype=torch.float64, device=self.device)
+        self.plan.check(self.plan.lib.macsav_layout(self.plan.handle, 0, dptr(dv), dptr(ud), dptr(vd),
+                                                    stream_handle()))
+        u, v = ud.cpu().numpy(), vd.cpu().numpy()
         u.flags.writeable = False
         v.flags.writeable = False
         return State(t, u, v, float(r), dv)
