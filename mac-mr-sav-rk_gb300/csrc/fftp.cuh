@@ -4,15 +4,55 @@
 // is transformed by G = L/8 threads, each owning one radix-8 butterfly per
 // Stockham pass (register-resident 8-point DFTs, the last pass radix 2 or 4
 // when log2 L is not a multiple of 3), so log8(L) passes with all index
-// arithmetic folded to shifts and masks.  A CTA holds NL = blockDim.x / G
-// lines.  Packing, spectral weights and the post/pre-processing are the same
-// as in the generic kernels (transforms.cuh).
+// arithmetic folded to shifts and masks.  A CTA holds NL = blockDim.x / tpl
+// lines (tpl = G or 2G threads per line, below).  Packing, spectral weights
+// and the post/pre-processing are the same as in the generic kernels
+// (transforms.cuh).
+//
+// Shared lines are stored bank-swizzled (SwIx below).  Small blocks (at most
+// 512 x 512, FP32) launch 2G threads per line: the packing and unpacking
+// loops, the longer dependent chains of these latency-bound passes, then run
+// on twice as many warps, while the extra threads only join the FFT
+// barriers (TBlockDev::tpl carries the launch's threads per line).
+// Measured on GB300 (512^2 sdirk3_mrsav step): the swizzle and the doubled
+// threads take the FP32 step from 4.74 to 4.63 ms and the swizzle the FP64
+// step from 11.54 to 11.13 ms; doubled threads slow the 1024^2 and 2048^2
+// passes (throughput-bound), so larger blocks keep G.  A ping-pong buffer
+// pair (one barrier per pass) and a shared copy of the twiddle table gave
+// nothing on top and are not used.
 #pragma once
 #include "transforms.cuh"
 
 namespace macsav {
 
 constexpr int kE = 8;  // elements per thread per line
+
+// Threads per line (pair) for a launch over block B with `lines` lines per
+// CTA: 2G for small FP32 blocks while the CTA stays within kFFTThreads.
+template <typename T>
+inline int p2_threads_per_line(const TBlockDev<T>& B, int L, int lines) {
+  const int G = L / kE;
+  const bool twice = sizeof(T) == 4 && (long long)B.rows * B.cols <= 512LL * 512 && 2 * G * lines <= kFFTThreads;
+  return twice ? 2 * G : G;
+}
+
+// Shared bytes of a CTA holding `lines` lines of length L.
+template <typename T>
+inline size_t p2_smem(int L, int lines) {
+  return size_t(lines) * size_t(L) * sizeof(cplx<T>);
+}
+
+// Bank swizzle of element i of a shared line (a bijection on each aligned
+// group of 128 elements).  The first Stockham pass writes each thread's 8
+// outputs contiguously (thread stride 8 elements) and the second writes
+// groups of 8 that are 64 elements apart; unswizzled, those stores are
+// 8-way and 2-way bank conflicts for 8-byte elements (8-way for 16-byte
+// ones).  XOR-ing bits 0-2 with bits 3-5 and bit 3 with bit 6 makes every
+// pass's loads and stores conflict-free (16 threads of 8 bytes or 8 threads
+// of 16 bytes per shared-memory wavefront).
+struct SwIx {
+  __device__ __forceinline__ int operator()(int i) const { return i ^ ((i >> 3) & 7) ^ (((i >> 6) & 1) << 3); }
+};
 
 template <typename T, int SIGN>
 __device__ __forceinline__ cplx<T> tw_at(const cplx<T>* __restrict__ tw, int m) {
@@ -65,9 +105,10 @@ __device__ __forceinline__ void dftR(cplx<T> (&v)[R]) {
   }
 }
 
-// Stockham passes on one line z (stride 1) by the G = L/8 threads of the
-// line; thread t owns butterflies j = t + q G.  Every thread of the CTA must
-// call this (it synchronises the block twice per pass).
+// Stockham passes on one (swizzled) line z by its first G = L/8 threads;
+// thread t < G owns butterflies j = t + q G, threads t >= G (doubled
+// launches) only join the barriers.  Every thread of the CTA must call this
+// (two block barriers per pass).
 template <typename T, int L, int NS, int SIGN>
 __device__ __forceinline__ void fft_p2(cplx<T>* z, int t, const cplx<T>* __restrict__ tw) {
   constexpr int R = (L / NS >= kE) ? kE : L / NS;
@@ -75,43 +116,50 @@ __device__ __forceinline__ void fft_p2(cplx<T>* z, int t, const cplx<T>* __restr
   constexpr int NB = kE / R;
   constexpr int STRIDE = L / R;
   constexpr int TWS = L / (NS * R);
+  const SwIx ix;
   cplx<T> v[NB][R];
+  const bool own = t < G;
+  if (own) {
 #pragma unroll
-  for (int q = 0; q < NB; ++q) {
-    const int j = t + q * G;
-    const int k = j & (NS - 1);
+    for (int q = 0; q < NB; ++q) {
+      const int j = t + q * G;
+      const int k = j & (NS - 1);
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[q][r] = z[j + r * STRIDE];
-    if constexpr (NS > 1) {
+      for (int r = 0; r < R; ++r) v[q][r] = z[ix(j + r * STRIDE)];
+      if constexpr (NS > 1) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], tw_at<T, SIGN>(tw, r * k * TWS));
+        for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], tw_at<T, SIGN>(tw, r * k * TWS));
+      }
+      dftR<T, R, SIGN>(v[q]);
     }
-    dftR<T, R, SIGN>(v[q]);
   }
   __syncthreads();
+  if (own) {
 #pragma unroll
-  for (int q = 0; q < NB; ++q) {
-    const int j = t + q * G;
-    const int k = j & (NS - 1);
-    const int base = (j - k) * R + k;
+    for (int q = 0; q < NB; ++q) {
+      const int j = t + q * G;
+      const int k = j & (NS - 1);
+      const int base = (j - k) * R + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) z[base + r * NS] = v[q][r];
+      for (int r = 0; r < R; ++r) z[ix(base + r * NS)] = v[q][r];
+    }
   }
   __syncthreads();
   if constexpr (NS * R < L) fft_p2<T, L, NS * R, SIGN>(z, t, tw);
 }
 
 // ------------------------------------------------------------ row passes ---
-// One block (u, v or p) per launch; NL = blockDim.x / (L/8) line pairs per CTA.
+// One block (u, v or p) per launch; NL = blockDim.x / B.tpl line pairs per CTA.
 template <typename T, int L, class Src>
 __global__ void __launch_bounds__(kFFTThreads) k_row_forward_p2(TBlockDev<T> B, const int* active, Src src, int bk) {
   pdl_wait();
   const int c = blockIdx.y;
   if (active && !active[c]) return;
-  constexpr int G = L / kE;
+  const int TPL = B.tpl;
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T>* z = reinterpret_cast<cplx<T>*>(smraw);
-  const int NL = blockDim.x / G;
+  const int NL = blockDim.x / TPL;
+  const cplx<T>* tw = B.twx;
   const int N = B.cols, rows = B.rows, kind = B.kx;
   const int row0 = blockIdx.x * 2 * NL;
   const int npairs = min(NL, (rows - row0 + 1) / 2);
@@ -134,20 +182,20 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_forward_p2(TBlockDev<T> B, 
       const int e = base + u * blockDim.x;
       if (e < total) {
         const int q = B.fcols.div(e), n = e - q * N;
-        put_pair(z + q * L, kind, N, n, va[u], vb[u]);
+        put_pair(z + q * L, kind, N, n, va[u], vb[u], SwIx{});
       }
     }
   }
   if (kind == KIND_DST1)
-    for (int q = threadIdx.x; q < npairs; q += blockDim.x) zero_dst1_ends(z + q * L, N);
+    for (int q = threadIdx.x; q < npairs; q += blockDim.x) zero_dst1_ends(z + q * L, N, SwIx{});
   __syncthreads();
-  fft_p2<T, L, 1, -1>(z + (threadIdx.x / G) * L, threadIdx.x % G, B.twx);
+  fft_p2<T, L, 1, -1>(z + (threadIdx.x / TPL) * L, threadIdx.x % TPL, tw);
   T* H = B.H + c * B.hstride;
   for (int e = threadIdx.x; e < total; e += blockDim.x) {
     const int q = B.fcols.div(e), k = e - q * N;
     const int ra = row0 + 2 * q;
     T ya, yb;
-    coef_forward(z + q * L, kind, N, k, B.qx, ya, yb);
+    coef_forward(z + q * L, kind, N, k, B.qx, ya, yb, SwIx{});
     H[(long long)ra * B.pitch + k] = ya;
     if (ra + 1 < rows) H[(long long)ra * B.pitch + B.pitch + k] = yb;
   }
@@ -158,13 +206,14 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_inverse_p2(TBlockDev<T> B, 
                                                                 double* partial, Fin fin, unsigned int* counter) {
   pdl_wait();
   const int c = blockIdx.y;
-  constexpr int G = L / kE;
+  const int TPL = B.tpl;
   const bool live = !active || active[c];
   Acc<T> acc[2];
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T>* z = reinterpret_cast<cplx<T>*>(smraw);
   if (live) {
-    const int NL = blockDim.x / G;
+    const int NL = blockDim.x / TPL;
+    const cplx<T>* tw = B.twx;
     const int N = B.cols, rows = B.rows, kind = B.kx;
     const int row0 = blockIdx.x * 2 * NL;
     const int npairs = min(NL, (rows - row0 + 1) / 2);
@@ -194,17 +243,18 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_inverse_p2(TBlockDev<T> B, 
         const int e = base + u * blockDim.x;
         if (e < total) {
           const int q = B.fcols.div(e), k = e - q * N;
-          if (kind == KIND_DST1) put_pair(z + q * L, KIND_DST1, N, k, yak[u], ybk[u]);
-          else z[q * L + k] = pre_inverse(yak[u], yam[u], ybk[u], ybm[u], B.qx[k]);
+          if (kind == KIND_DST1) put_pair(z + q * L, KIND_DST1, N, k, yak[u], ybk[u], SwIx{});
+          else z[q * L + SwIx{}(k)] = pre_inverse(yak[u], yam[u], ybk[u], ybm[u], B.qx[k]);
         }
       }
     }
     if (kind == KIND_DST1)
-      for (int q = threadIdx.x; q < npairs; q += blockDim.x) zero_dst1_ends(z + q * L, N);
-    __syncthreads();
-    if (kind == KIND_DST1) fft_p2<T, L, 1, -1>(z + (threadIdx.x / G) * L, threadIdx.x % G, B.twx);
-    else fft_p2<T, L, 1, 1>(z + (threadIdx.x / G) * L, threadIdx.x % G, B.twx);
-    for (int base = threadIdx.x; base < total; base += kStage * blockDim.x) {
+      for (int q = threadIdx.x; q < npairs; q += blockDim.x) zero_dst1_ends(z + q * L, N, SwIx{});
+      __syncthreads();
+    cplx<T>* za = z + (threadIdx.x / TPL) * L;
+    if (kind == KIND_DST1) fft_p2<T, L, 1, -1>(za, threadIdx.x % TPL, tw);
+    else fft_p2<T, L, 1, 1>(za, threadIdx.x % TPL, tw);
+      for (int base = threadIdx.x; base < total; base += kStage * blockDim.x) {
       typename Dst::aux_t xa[kStage], xb[kStage];
 #pragma unroll
       for (int u = 0; u < kStage; ++u) {
@@ -220,8 +270,8 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_inverse_p2(TBlockDev<T> B, 
         const int e = base + u * blockDim.x;
         if (e < total) {
           const int q = B.fcols.div(e), n = e - q * N, ra = row0 + 2 * q;
-          dst.store(bk, c, ra, n, value_inverse(z + q * L, kind, N, n, 0, B.sx), xa[u], acc);
-          if (ra + 1 < rows) dst.store(bk, c, ra + 1, n, value_inverse(z + q * L, kind, N, n, 1, B.sx), xb[u], acc);
+          dst.store(bk, c, ra, n, value_inverse(z + q * L, kind, N, n, 0, B.sx, SwIx{}), xa[u], acc);
+          if (ra + 1 < rows) dst.store(bk, c, ra + 1, n, value_inverse(z + q * L, kind, N, n, 1, B.sx, SwIx{}), xb[u], acc);
         }
       }
     }
@@ -240,12 +290,13 @@ __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const
   pdl_wait();
   const int c = blockIdx.y;
   if (active && !active[c]) return;
-  constexpr int G = L / kE;
+  const int TPL = B.tpl;
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T>* z = reinterpret_cast<cplx<T>*>(smraw);
   using vec_t = typename Vec16<T>::type;
   constexpr int V = Vec16<T>::n;
-  const int NL = blockDim.x / G;
+  const int NL = blockDim.x / TPL;
+  const cplx<T>* tw = B.twy;
   const int W = 2 * NL;
   const int N = B.rows, kind = B.ky;
   const int col0 = blockIdx.x * W;
@@ -259,7 +310,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const
   if (!vec) {
     for (int e = threadIdx.x; e < N * W; e += blockDim.x) {
       const int n = B.fw.div(e), j = e - n * W;
-      if (j < 2 * nl) put_real(z + (j >> 1) * L, kind, N, n, j & 1, j < ncols ? H[n * pitch + col0 + j] : T(0));
+      if (j < 2 * nl) put_real(z + (j >> 1) * L, kind, N, n, j & 1, j < ncols ? H[n * pitch + col0 + j] : T(0), SwIx{});
     }
   }
   for (int base = threadIdx.x; vec && base < totv; base += kStage * blockDim.x) {
@@ -281,17 +332,16 @@ __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const
 #pragma unroll
         for (int k = 0; k < V; ++k) {
           const int j = jv * V + k;
-          if (j < 2 * nl) put_real(z + (j >> 1) * L, kind, N, n, j & 1, j < ncols ? comp[k] : T(0));
+          if (j < 2 * nl) put_real(z + (j >> 1) * L, kind, N, n, j & 1, j < ncols ? comp[k] : T(0), SwIx{});
         }
       }
     }
   }
   if (kind == KIND_DST1)
-    for (int q = threadIdx.x; q < nl; q += blockDim.x) zero_dst1_ends(z + q * L, N);
+    for (int q = threadIdx.x; q < nl; q += blockDim.x) zero_dst1_ends(z + q * L, N, SwIx{});
   __syncthreads();
-  cplx<T>* zl = z + (threadIdx.x / G) * L;
-  const int t = threadIdx.x % G;
-  fft_p2<T, L, 1, -1>(zl, t, B.twy);
+  const int line = threadIdx.x / TPL, t = threadIdx.x % TPL;
+  fft_p2<T, L, 1, -1>(z + line * L, t, tw);
   if (kind == KIND_DST1) {
     for (int e = threadIdx.x; e < nl * N; e += blockDim.x) {
       const int q = B.frows.div(e), k = e - q * N;
@@ -300,23 +350,25 @@ __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const
       const T ey = B.eigy[k];
       const T wa = spectral_weight<T>(mode, mass, visc, thr, ey, B.eigx[ca]);
       const T wb = spectral_weight<T>(mode, mass, visc, thr, ey, B.eigx[cb]);
-      const cplx<T> Z = y[k + 1];
+      const SwIx ix;
+      const cplx<T> Z = y[ix(k + 1)];
       const T sa = -Z.y * T(0.5) * wa, sb = Z.x * T(0.5) * wb;
-      y[k + 1] = mk(sa, sb);
-      y[2 * (N + 1) - 1 - k] = mk(-sa, -sb);
+      y[ix(k + 1)] = mk(sa, sb);
+      y[ix(2 * (N + 1) - 1 - k)] = mk(-sa, -sb);
       if (k == 0) {
-        y[0] = mk(T(0), T(0));
-        y[N + 1] = mk(T(0), T(0));
+        y[ix(0)] = mk(T(0), T(0));
+        y[ix(N + 1)] = mk(T(0), T(0));
       }
     }
   } else {
     const int half = N / 2 + 1;
     for (int e = threadIdx.x; e < nl * half; e += blockDim.x) {
       const int q = B.fhalf.div(e), k = e - q * half;
-      cplx<T>* y = z + q * L;
       const int m = k == 0 ? 0 : N - k;
       const int ca = col0 + 2 * q, cb = min(ca + 1, B.cols - 1);
-      const cplx<T> Zk = y[k], Zm = y[m];
+      cplx<T>* y = z + q * L;
+      const SwIx ix;
+      const cplx<T> Zk = y[ix(k)], Zm = y[ix(m)];
       const cplx<T> qk = B.qy[k], qm = B.qy[m];
       T yak = cmul(qk, Zk + conjg(Zm)).x, ybk = cmul(qk, Zk - conjg(Zm)).y;
       T yam = cmul(qm, Zm + conjg(Zk)).x, ybm = cmul(qm, Zm - conjg(Zk)).y;
@@ -326,16 +378,16 @@ __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const
       yam *= spectral_weight<T>(mode, mass, visc, thr, eym, exa);
       ybm *= spectral_weight<T>(mode, mass, visc, thr, eym, exb);
       if (k == 0) {
-        y[0] = pre_inverse(yak, T(0), ybk, T(0), qk);
+        y[ix(0)] = pre_inverse(yak, T(0), ybk, T(0), qk);
       } else {
-        y[k] = pre_inverse(yak, yam, ybk, ybm, qk);
-        if (m != k) y[m] = pre_inverse(yam, yak, ybm, ybk, qm);
+        y[ix(k)] = pre_inverse(yak, yam, ybk, ybm, qk);
+        if (m != k) y[ix(m)] = pre_inverse(yam, yak, ybm, ybk, qm);
       }
     }
   }
   __syncthreads();
-  if (kind == KIND_DST1) fft_p2<T, L, 1, -1>(zl, t, B.twy);
-  else fft_p2<T, L, 1, 1>(zl, t, B.twy);
+  if (kind == KIND_DST1) fft_p2<T, L, 1, -1>(z + line * L, t, tw);
+  else fft_p2<T, L, 1, 1>(z + line * L, t, tw);
   if (vec && ncols == W) {
     for (int e = threadIdx.x; e < totv; e += blockDim.x) {
       const int n = B.fvpr.div(e), jv = e - n * vpr;
@@ -344,14 +396,14 @@ __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const
 #pragma unroll
       for (int k = 0; k < V; ++k) {
         const int j = jv * V + k;
-        comp[k] = value_inverse(z + (j >> 1) * L, kind, N, n, j & 1, B.sy);
+        comp[k] = value_inverse(z + (j >> 1) * L, kind, N, n, j & 1, B.sy, SwIx{});
       }
       *reinterpret_cast<vec_t*>(H + n * pitch + col0 + jv * V) = v;
     }
   } else {
     for (int e = threadIdx.x; e < N * W; e += blockDim.x) {
       const int n = B.fw.div(e), j = e - n * W;
-      if (j < ncols) H[n * pitch + col0 + j] = value_inverse(z + (j >> 1) * L, kind, N, n, j & 1, B.sy);
+      if (j < ncols) H[n * pitch + col0 + j] = value_inverse(z + (j >> 1) * L, kind, N, n, j & 1, B.sy, SwIx{});
     }
   }
 }

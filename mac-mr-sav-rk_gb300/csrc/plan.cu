@@ -78,6 +78,7 @@ static cudaError_t build_block(TBlockDev<T>& B, int rows, int cols, int kx, int 
   B.pitch = (cols + 31) / 32 * 32;
   B.px = pick_pairs(Lx, rows, sms);
   B.wy = pick_strip(Ly, cols, sms, int(sizeof(T)));
+  B.tpl = Lx / 8;  // each specialised launch sets its own
   B.fcols = FastDiv(cols);
   B.frows = FastDiv(rows);
   B.fw = FastDiv(B.wy);

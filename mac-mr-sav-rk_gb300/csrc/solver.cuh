@@ -323,9 +323,12 @@ inline int total_groups(const RowArgs<T>& a) { return a.blk[0].groups + (a.nblk 
 template <typename T>
 inline int total_groups(const ColArgs<T>& a) { return a.blk[0].groups + (a.nblk > 1 ? a.blk[1].groups : 0); }
 
+// Opt in to more than the default 48 KB of shared memory per CTA.  The
+// default covers static plus dynamic bytes, and the finishers' static arrays
+// take a few KB, so the opt-in starts well below 48 KB of dynamic memory.
 template <class K>
 inline void set_smem(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+  if (bytes > 40 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
 }
 
 // Row pairs per CTA of a specialised row pass (at least 64 threads per CTA).
@@ -376,13 +379,15 @@ struct Launcher {
     if (row_p2(a) && (!b || row_p2(*b))) {
       auto one = [&](int bk, cudaStream_t st) {
         const TBlockDev<T>& B = bk ? *b : a;
-        const int P = p2_pairs(B), G = B.fx.L / kE;
-        const size_t sm = size_t(P) * B.fx.L * sizeof(cplx<T>);
+        const int P = p2_pairs(B), G = p2_threads_per_line<T>(B, B.fx.L, P);
+        TBlockDev<T> Bl = B;
+        Bl.tpl = G;
+        const size_t sm = p2_smem<T>(B.fx.L, P);
 #define MACSAV_RF(LL)                                                                        \
   {                                                                                          \
     auto k = k_row_forward_p2<T, LL, Src>;                                                   \
     set_smem(k, sm);                                                                         \
-    launch_k(k, dim3(row_grid(B), cols), P * G, sm, st, B, active, src, bk);                       \
+    launch_k(k, dim3(row_grid(B), cols), P * G, sm, st, Bl, active, src, bk);                       \
   }
         MACSAV_P2_SWITCH(B.fx.L, MACSAV_RF)
 #undef MACSAV_RF
@@ -404,13 +409,15 @@ struct Launcher {
     if (row_p2(a) && (!b || row_p2(*b)) && (!partial || !b)) {
       auto one = [&](int bk, cudaStream_t st) {
         const TBlockDev<T>& B = bk ? *b : a;
-        const int P = p2_pairs(B), G = B.fx.L / kE;
-        const size_t sm = size_t(P) * B.fx.L * sizeof(cplx<T>);
+        const int P = p2_pairs(B), G = p2_threads_per_line<T>(B, B.fx.L, P);
+        TBlockDev<T> Bl = B;
+        Bl.tpl = G;
+        const size_t sm = p2_smem<T>(B.fx.L, P);
 #define MACSAV_RI(LL)                                                                        \
   {                                                                                          \
     auto k = k_row_inverse_p2<T, LL, Dst, Fin>;                                              \
     set_smem(k, sm);                                                                         \
-    launch_k(k, dim3(row_grid(B), cols), P * G, sm, st, B, active, dst, bk, partial, fin, done);   \
+    launch_k(k, dim3(row_grid(B), cols), P * G, sm, st, Bl, active, dst, bk, partial, fin, done);   \
   }
         MACSAV_P2_SWITCH(B.fx.L, MACSAV_RI)
 #undef MACSAV_RI
@@ -431,14 +438,16 @@ struct Launcher {
     if (col_p2(a) && (!b || col_p2(*b))) {
       auto one = [&](int bk, cudaStream_t st) {
         const TBlockDev<T>& B = bk ? *b : a;
-        const int NL = B.wy / 2, G = B.fy.L / kE;
-        const size_t sm = size_t(NL) * B.fy.L * sizeof(cplx<T>);
+        const int NL = B.wy / 2, G = p2_threads_per_line<T>(B, B.fy.L, NL);
+        TBlockDev<T> Bl = B;
+        Bl.tpl = G;
+        const size_t sm = p2_smem<T>(B.fy.L, NL);
         const int grid = (B.cols + B.wy - 1) / B.wy;
 #define MACSAV_CO(LL)                                                                        \
   {                                                                                          \
     auto k = k_column_p2<T, LL>;                                                             \
     set_smem(k, sm);                                                                         \
-    launch_k(k, dim3(grid, cols), NL * G, sm, st, B, active, mode, shift, thr);                    \
+    launch_k(k, dim3(grid, cols), NL * G, sm, st, Bl, active, mode, shift, thr);                    \
   }
         MACSAV_P2_SWITCH(B.fy.L, MACSAV_CO)
 #undef MACSAV_CO

@@ -46,6 +46,7 @@ struct TBlockDev {
   int px;              // row pairs per CTA in row passes
   int wy;              // columns per CTA in the column pass (even)
   int groups;          // CTAs of this block in the current pass
+  int tpl;             // threads per line of a specialised pass (set per launch)
   FastDiv fcols, frows, fw, fvpr, fhalf;  // divisors of the element loops
   T sx, sy;            // inverse normalisation of the x / y transforms
 };
@@ -53,49 +54,55 @@ struct TBlockDev {
 __device__ __forceinline__ int makhoul_pos(int n, int N) { return (n & 1) ? N - 1 - (n >> 1) : (n >> 1); }
 
 // ---------------------------------------------------------------- packing ---
-template <typename T>
-__device__ __forceinline__ void put_real(cplx<T>* z, int kind, int N, int n, int part, T val) {
+// Element k of a shared line sits at z[ix(k)]: the identity for the generic
+// kernels, a bank swizzle for the power-of-two kernels (fftp.cuh).
+struct IdIx {
+  __device__ __forceinline__ int operator()(int i) const { return i; }
+};
+
+template <typename T, class Ix = IdIx>
+__device__ __forceinline__ void put_real(cplx<T>* z, int kind, int N, int n, int part, T val, Ix ix = Ix{}) {
   // part 0 -> real component (line a), 1 -> imaginary component (line b)
   if (kind == KIND_DST1) {
     const int M = N + 1;
-    T* p = reinterpret_cast<T*>(z + n + 1) + part;
-    T* m = reinterpret_cast<T*>(z + 2 * M - 1 - n) + part;
+    T* p = reinterpret_cast<T*>(z + ix(n + 1)) + part;
+    T* m = reinterpret_cast<T*>(z + ix(2 * M - 1 - n)) + part;
     *p = val;
     *m = -val;
   } else {
     if (kind == KIND_DST2 && (n & 1)) val = -val;
-    reinterpret_cast<T*>(z + makhoul_pos(n, N))[part] = val;
+    reinterpret_cast<T*>(z + ix(makhoul_pos(n, N)))[part] = val;
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void put_pair(cplx<T>* z, int kind, int N, int n, T va, T vb) {
+template <typename T, class Ix = IdIx>
+__device__ __forceinline__ void put_pair(cplx<T>* z, int kind, int N, int n, T va, T vb, Ix ix = Ix{}) {
   if (kind == KIND_DST1) {
     const int M = N + 1;
-    z[n + 1] = mk(va, vb);
-    z[2 * M - 1 - n] = mk(-va, -vb);
+    z[ix(n + 1)] = mk(va, vb);
+    z[ix(2 * M - 1 - n)] = mk(-va, -vb);
   } else {
     if (kind == KIND_DST2 && (n & 1)) { va = -va; vb = -vb; }
-    z[makhoul_pos(n, N)] = mk(va, vb);
+    z[ix(makhoul_pos(n, N))] = mk(va, vb);
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void zero_dst1_ends(cplx<T>* z, int N) {
-  z[0] = mk(T(0), T(0));
-  z[N + 1] = mk(T(0), T(0));
+template <typename T, class Ix = IdIx>
+__device__ __forceinline__ void zero_dst1_ends(cplx<T>* z, int N, Ix ix = Ix{}) {
+  z[ix(0)] = mk(T(0), T(0));
+  z[ix(N + 1)] = mk(T(0), T(0));
 }
 
 // Forward post-processing: unnormalised coefficient k of lines a and b.
-template <typename T>
+template <typename T, class Ix = IdIx>
 __device__ __forceinline__ void coef_forward(const cplx<T>* z, int kind, int N, int k,
-                                             const cplx<T>* __restrict__ q, T& ya, T& yb) {
+                                             const cplx<T>* __restrict__ q, T& ya, T& yb, Ix ix = Ix{}) {
   if (kind == KIND_DST1) {
-    const cplx<T> Z = z[k + 1];
+    const cplx<T> Z = z[ix(k + 1)];
     ya = -Z.y * T(0.5);
     yb = Z.x * T(0.5);
   } else {
-    const cplx<T> Zk = z[k], Zm = conjg(z[k == 0 ? 0 : N - k]);
+    const cplx<T> Zk = z[ix(k)], Zm = conjg(z[ix(k == 0 ? 0 : N - k)]);
     const cplx<T> qk = q[k];
     ya = cmul(qk, Zk + Zm).x;
     yb = cmul(qk, Zk - Zm).y;
@@ -114,13 +121,14 @@ __device__ __forceinline__ cplx<T> pre_inverse(T yak, T yam, T ybk, T ybm, cplx<
 // Inverse post-processing: real value n of line a (part 0) or b (part 1),
 // after an unscaled inverse FFT (DCT kinds) or a forward FFT (DST-I); `scale`
 // is the normalisation 1/N (DCT kinds) or 1/(N+1) (DST-I), precomputed.
-template <typename T>
-__device__ __forceinline__ T value_inverse(const cplx<T>* z, int kind, int N, int n, int part, T scale) {
+template <typename T, class Ix = IdIx>
+__device__ __forceinline__ T value_inverse(const cplx<T>* z, int kind, int N, int n, int part, T scale,
+                                           Ix ix = Ix{}) {
   if (kind == KIND_DST1) {
-    const cplx<T> Z = z[n + 1];
+    const cplx<T> Z = z[ix(n + 1)];
     return part == 0 ? -Z.y * scale : Z.x * scale;
   }
-  const cplx<T> Z = z[makhoul_pos(n, N)];
+  const cplx<T> Z = z[ix(makhoul_pos(n, N))];
   T v = (part == 0 ? Z.x : Z.y) * scale;
   if (kind == KIND_DST2 && (n & 1)) v = -v;
   return v;
