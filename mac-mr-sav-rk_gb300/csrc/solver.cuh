@@ -88,6 +88,22 @@ struct DstPacked {
   }
 };
 
+// Packed FP64 velocity accumulation: x (+)= double(value) (the correction
+// of a defect-correction sweep added to the FP64 velocity).
+template <typename T>
+struct DstAccum {
+  using aux_t = int;
+  double* x;
+  long long cstride;
+  int off1, n0, n1;
+  int add;
+  __device__ aux_t load(int, int, int, int) const { return 0; }
+  __device__ void store(int b, int c, int row, int n, T v, aux_t, Acc<T> (&)[2]) const {
+    double* p = x + c * cstride + (b == 0 ? (long long)row * n0 + n : off1 + (long long)row * n1 + n);
+    *p = add ? *p + double(v) : double(v);
+  }
+};
+
 template <typename T, typename Out>
 struct DstCells {
   using aux_t = int;
@@ -373,26 +389,63 @@ struct Launcher {
     return (B.rows + 2 * P - 1) / (2 * P);
   }
 
+  // One specialised pass over block B (bk: 0 = u or the only block, 1 = v) on stream st.
+  template <class Src>
+  void row_forward_p2(const TBlockDev<T>& B, int bk, cudaStream_t st, Src src, int cols, const int* active) const {
+    const int P = p2_pairs(B), G = p2_threads_per_line<T>(B, B.fx.L, P);
+    TBlockDev<T> Bl = B;
+    Bl.tpl = G;
+    const size_t sm = p2_smem<T>(B.fx.L, P);
+#define MACSAV_RF(LL)                                                          \
+  {                                                                            \
+    auto k = k_row_forward_p2<T, LL, Src>;                                     \
+    set_smem(k, sm);                                                           \
+    launch_k(k, dim3(row_grid(B), cols), P * G, sm, st, Bl, active, src, bk);  \
+  }
+    MACSAV_P2_SWITCH(B.fx.L, MACSAV_RF)
+#undef MACSAV_RF
+    ++*counter;
+  }
+  template <class Dst, class Fin>
+  void row_inverse_p2(const TBlockDev<T>& B, int bk, cudaStream_t st, Dst dst, int cols, const int* active,
+                      double* partial, Fin fin, unsigned int* done) const {
+    const int P = p2_pairs(B), G = p2_threads_per_line<T>(B, B.fx.L, P);
+    TBlockDev<T> Bl = B;
+    Bl.tpl = G;
+    const size_t sm = p2_smem<T>(B.fx.L, P);
+#define MACSAV_RI(LL)                                                                                \
+  {                                                                                                  \
+    auto k = k_row_inverse_p2<T, LL, Dst, Fin>;                                                      \
+    set_smem(k, sm);                                                                                 \
+    launch_k(k, dim3(row_grid(B), cols), P * G, sm, st, Bl, active, dst, bk, partial, fin, done);  \
+  }
+    MACSAV_P2_SWITCH(B.fx.L, MACSAV_RI)
+#undef MACSAV_RI
+    ++*counter;
+  }
+  void column_p2(const TBlockDev<T>& B, cudaStream_t st, int cols, const int* active, int mode, const double* shift,
+                 T thr) const {
+    const int NL = B.wy / 2, G = p2_threads_per_line<T>(B, B.fy.L, NL);
+    TBlockDev<T> Bl = B;
+    Bl.tpl = G;
+    const size_t sm = p2_smem<T>(B.fy.L, NL);
+    const int grid = (B.cols + B.wy - 1) / B.wy;
+#define MACSAV_CO(LL)                                                                  \
+  {                                                                                    \
+    auto k = k_column_p2<T, LL>;                                                       \
+    set_smem(k, sm);                                                                   \
+    launch_k(k, dim3(grid, cols), NL * G, sm, st, Bl, active, mode, shift, thr);      \
+  }
+    MACSAV_P2_SWITCH(B.fy.L, MACSAV_CO)
+#undef MACSAV_CO
+    ++*counter;
+  }
+
   template <class Src>
   void row_forward(const TBlockDev<T>& a, const TBlockDev<T>* b, size_t smem, Src src, int cols,
                    const int* active) const {
     if (row_p2(a) && (!b || row_p2(*b))) {
-      auto one = [&](int bk, cudaStream_t st) {
-        const TBlockDev<T>& B = bk ? *b : a;
-        const int P = p2_pairs(B), G = p2_threads_per_line<T>(B, B.fx.L, P);
-        TBlockDev<T> Bl = B;
-        Bl.tpl = G;
-        const size_t sm = p2_smem<T>(B.fx.L, P);
-#define MACSAV_RF(LL)                                                                        \
-  {                                                                                          \
-    auto k = k_row_forward_p2<T, LL, Src>;                                                   \
-    set_smem(k, sm);                                                                         \
-    launch_k(k, dim3(row_grid(B), cols), P * G, sm, st, Bl, active, src, bk);                       \
-  }
-        MACSAV_P2_SWITCH(B.fx.L, MACSAV_RF)
-#undef MACSAV_RF
-        ++*counter;
-      };
+      auto one = [&](int bk, cudaStream_t st) { row_forward_p2(bk ? *b : a, bk, st, src, cols, active); };
       if (b) two_blocks(one);
       else one(0, s);
       return;
@@ -408,20 +461,7 @@ struct Launcher {
                    double* partial, Fin fin, unsigned int* done) const {
     if (row_p2(a) && (!b || row_p2(*b)) && (!partial || !b)) {
       auto one = [&](int bk, cudaStream_t st) {
-        const TBlockDev<T>& B = bk ? *b : a;
-        const int P = p2_pairs(B), G = p2_threads_per_line<T>(B, B.fx.L, P);
-        TBlockDev<T> Bl = B;
-        Bl.tpl = G;
-        const size_t sm = p2_smem<T>(B.fx.L, P);
-#define MACSAV_RI(LL)                                                                        \
-  {                                                                                          \
-    auto k = k_row_inverse_p2<T, LL, Dst, Fin>;                                              \
-    set_smem(k, sm);                                                                         \
-    launch_k(k, dim3(row_grid(B), cols), P * G, sm, st, Bl, active, dst, bk, partial, fin, done);   \
-  }
-        MACSAV_P2_SWITCH(B.fx.L, MACSAV_RI)
-#undef MACSAV_RI
-        ++*counter;
+        row_inverse_p2(bk ? *b : a, bk, st, dst, cols, active, partial, fin, done);
       };
       if (b) two_blocks(one);
       else one(0, s);
@@ -436,23 +476,7 @@ struct Launcher {
   void column(const TBlockDev<T>& a, const TBlockDev<T>* b, size_t smem, int cols, const int* active, int mode,
               const double* shift, T thr) const {
     if (col_p2(a) && (!b || col_p2(*b))) {
-      auto one = [&](int bk, cudaStream_t st) {
-        const TBlockDev<T>& B = bk ? *b : a;
-        const int NL = B.wy / 2, G = p2_threads_per_line<T>(B, B.fy.L, NL);
-        TBlockDev<T> Bl = B;
-        Bl.tpl = G;
-        const size_t sm = p2_smem<T>(B.fy.L, NL);
-        const int grid = (B.cols + B.wy - 1) / B.wy;
-#define MACSAV_CO(LL)                                                                        \
-  {                                                                                          \
-    auto k = k_column_p2<T, LL>;                                                             \
-    set_smem(k, sm);                                                                         \
-    launch_k(k, dim3(grid, cols), NL * G, sm, st, Bl, active, mode, shift, thr);                    \
-  }
-        MACSAV_P2_SWITCH(B.fy.L, MACSAV_CO)
-#undef MACSAV_CO
-        ++*counter;
-      };
+      auto one = [&](int bk, cudaStream_t st) { column_p2(bk ? *b : a, st, cols, active, mode, shift, thr); };
       if (b) two_blocks(one);
       else one(0, s);
       return;
@@ -462,6 +486,39 @@ struct Launcher {
     set_smem(k, smem);
     launch_k(k, dim3(total_groups(r), cols), kFFTThreads, smem, s, r);
     ++*counter;
+  }
+
+  // Velocity inverse (forward rows, column weights, inverse rows) of both
+  // blocks.  With a fork stream and specialised passes the u chain runs on s
+  // and the v chain on s2, forked and joined once, so neither waits for the
+  // other between its passes.
+  // `pre_v(stream)` launches independent work at the head of the v chain
+  // (or before the passes when there is no fork).
+  struct NoPre {
+    void operator()(cudaStream_t) const {}
+  };
+  template <class Src, class Dst, class Pre = NoPre>
+  void velocity_solve(Src src, Dst dst, int cols, const int* active, const double* shift, Pre pre_v = Pre{}) const {
+    const bool p2 = row_p2(t.u) && row_p2(t.v) && col_p2(t.u) && col_p2(t.v);
+    if (!p2 || !s2) {
+      pre_v(s);
+      row_forward_uv(src, cols, active);
+      column_uv(cols, active, shift);
+      row_inverse_uv(dst, cols, active);
+      return;
+    }
+    cudaEventRecord(ef, s);
+    cudaStreamWaitEvent(s2, ef, 0);
+    pre_v(s2);
+    for (int bk = 0; bk < 2; ++bk) {
+      const TBlockDev<T>& B = bk ? t.v : t.u;
+      const cudaStream_t st = bk ? s2 : s;
+      row_forward_p2(B, bk, st, src, cols, active);
+      column_p2(B, st, cols, active, W_HELMHOLTZ, shift, T(0));
+      row_inverse_p2(B, bk, st, dst, cols, active, nullptr, NoFin{}, nullptr);
+    }
+    cudaEventRecord(ej, s2);
+    cudaStreamWaitEvent(s, ej, 0);
   }
 
   template <class Src>

@@ -289,9 +289,7 @@ template <typename T, class Src, typename Out>
 static void velocity_inverse(Plan* P, const Launcher<T>& L, Src src, Out* dst, long long dstride, int cols,
                              const int* active) {
   const GridDev& g = P->g;
-  L.row_forward_uv(src, cols, active);
-  L.column_uv(cols, active, P->shift);
-  L.row_inverse_uv(DstPacked<T, Out>{dst, dstride, g.nu, g.nx - 1, g.nx}, cols, active);
+  L.velocity_solve(src, DstPacked<T, Out>{dst, dstride, g.nu, g.nx - 1, g.nx}, cols, active, P->shift);
 }
 
 // One PCG iteration for every active column (all kernels predicated).  With
@@ -522,9 +520,11 @@ __global__ void __launch_bounds__(kThreads) k_accumulate(const T* src, double* d
 }
 
 // One FP32 Stokes solve of (ru, rd): transforms, stencils and Krylov vectors
-// in float, reductions in double.  Leaves the velocity correction in w2 and
-// the pressure correction (x) in the float cell buffer.
-static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, int cols, float* w2) {
+// in float, reductions in double.  Its velocity is added to the FP64 `vel`
+// by the last inverse pass (set when add = 0) and its pressure x to the FP64
+// `pres` by a kernel at the head of the v chain of that velocity inverse.
+static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, int cols, double* vel, double* pres,
+                         int add) {
   const GridDev& g = P->g;
   Launcher<float> L{P->t32, X.s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
   const long long sz = g.size, np = g.np;
@@ -539,9 +539,13 @@ static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, i
   X.net = keep_net;
   if (rc != MACSAV_OK) return rc;
   const float* x = P->cells32 + 1 * np * cols;
-  velocity_inverse<float>(
-      P, L, SrcLift<float, double, float>{ru, sz, x, nullptr, P->cg, np, g.nx, g.nu, float(g.ihx), float(g.ihy)}, w2,
-      sz, cols, nullptr);
+  const int nbp = red_blocks(np);
+  auto add_pressure = [&](cudaStream_t st) {
+    launch_k(k_accumulate<float>, dim3(nbp, cols), kThreads, 0, st, x, pres, np, add);
+    ++P->launches;
+  };
+  L.velocity_solve(SrcLift<float, double, float>{ru, sz, x, nullptr, P->cg, np, g.nx, g.nu, float(g.ihx), float(g.ihy)},
+                   DstAccum<float>{vel, sz, g.nu, g.nx - 1, g.nx, add}, cols, nullptr, P->shift, add_pressure);
   return MACSAV_OK;
 }
 
@@ -553,8 +557,7 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
   const long long sz = g.size, np = g.np;
   double* ru = P->w;               // FP64 momentum defect
   double* rd = P->cells;           // FP64 continuity defect
-  float* du = reinterpret_cast<float*>(P->vel);  // velocity correction (float)
-  const int nbv = red_blocks(sz), nbp = red_blocks(np), nbm = red_blocks(sz > np ? sz : np);
+  const int nbm = red_blocks(sz > np ? sz : np);
   for (int sweep = 0; sweep <= P->corrections; ++sweep) {
     const double* rhs_u = f;
     const double* rhs_d = nullptr;
@@ -564,11 +567,8 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
       rhs_u = ru;
       rhs_d = rd;
     }
-    int rc = inner_solve32(P, X, rhs_u, rhs_d, cols, du);
+    int rc = inner_solve32(P, X, rhs_u, rhs_d, cols, vel, pres, sweep > 0);
     if (rc != MACSAV_OK) return rc;
-    launch_k(k_accumulate<float>, dim3(nbv, cols), kThreads, 0, X.s, du, vel, sz, sweep > 0);
-    launch_k(k_accumulate<float>, dim3(nbp, cols), kThreads, 0, X.s, P->cells32 + 1 * np * cols, pres, np, sweep > 0);
-    P->launches += 2;
   }
   // mean-zero pressure and the FP64 closing checks, as in the FP64 path
   finish_pressure<double>(P, X, pres, pres, cols);
