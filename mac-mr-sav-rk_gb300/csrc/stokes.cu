@@ -28,7 +28,10 @@ inline int red_blocks(long long n) {
   long long b = (n + kThreads - 1) / kThreads;
   return int(b < 1 ? 1 : (b > g_red_cap ? g_red_cap : b));
 }
-void set_reduction_cap(int sms) { g_red_cap = sms > 0 ? 2 * sms : 304; }
+#ifndef MACSAV_RED_PER_SM
+#define MACSAV_RED_PER_SM 2
+#endif
+void set_reduction_cap(int sms) { g_red_cap = sms > 0 ? MACSAV_RED_PER_SM * sms : 304; }
 
 // ------------------------------------------------------------ CG kernels ---
 // abs_key of a T value (as the key of the same value in double).
