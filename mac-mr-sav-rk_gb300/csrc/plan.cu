@@ -198,6 +198,7 @@ int plan_build(Plan* p) {
     }
     p->partial_len = size_t(C) * 8 * 4096;
     if ((e = cudaMalloc(&p->partial, sizeof(double) * p->partial_len))) goto fail;
+    if ((e = cudaMalloc(&p->partial2, sizeof(double) * p->partial_len))) goto fail;
     if ((e = cudaMalloc(&p->cg, sizeof(CGScalars) * C))) goto fail;
     if ((e = cudaMalloc(&p->checks, sizeof(SolveChecks) * C))) goto fail;
     if ((e = cudaMalloc(&p->active, sizeof(int) * C))) goto fail;
@@ -210,11 +211,12 @@ int plan_build(Plan* p) {
     if ((e = cudaMallocHost(&p->h_active, sizeof(int) * C))) goto fail;
     if ((e = cudaMallocHost(&p->h_err, sizeof(int)))) goto fail;
     if ((e = cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming))) goto fail;
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < 3; ++k) {
       if ((e = cudaStreamCreateWithFlags(&p->aux[k], cudaStreamNonBlocking))) goto fail;
       if ((e = cudaEventCreateWithFlags(&p->evf[k], cudaEventDisableTiming))) goto fail;
       if ((e = cudaEventCreateWithFlags(&p->evj[k], cudaEventDisableTiming))) goto fail;
     }
+    if ((e = cudaEventCreateWithFlags(&p->evc, cudaEventDisableTiming))) goto fail;
   }
   // Poisson zero-mode threshold: 100 eps max(lambda) (tensor_stokes.py:165-168)
   {
@@ -238,7 +240,7 @@ void plan_free(Plan* p) {
   free_transforms(p->t64);
   free_transforms(p->t32);
   cudaFree(p->w); cudaFree(p->vel); cudaFree(p->cells); cudaFree(p->cells32); cudaFree(p->w32);
-  cudaFree(p->partial); cudaFree(p->cg); cudaFree(p->checks); cudaFree(p->active); cudaFree(p->shift);
+  cudaFree(p->partial); cudaFree(p->partial2); cudaFree(p->cg); cudaFree(p->checks); cudaFree(p->active); cudaFree(p->shift);
   cudaFree(p->errword);
   cudaFree(p->done_counter);
   cudaFree(p->net_out); cudaFree(p->net_rold); cudaFree(p->net_scale);
@@ -246,14 +248,16 @@ void plan_free(Plan* p) {
   p->done_counter = nullptr;
   cudaFreeHost(p->h_cg); cudaFreeHost(p->h_checks); cudaFreeHost(p->h_active); cudaFreeHost(p->h_err);
   if (p->done) cudaEventDestroy(p->done);
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < 3; ++k) {
     if (p->aux[k]) cudaStreamDestroy(p->aux[k]);
     if (p->evf[k]) cudaEventDestroy(p->evf[k]);
     if (p->evj[k]) cudaEventDestroy(p->evj[k]);
     p->aux[k] = nullptr;
     p->evf[k] = p->evj[k] = nullptr;
   }
-  p->w = p->vel = p->cells = p->partial = p->shift = nullptr;
+  if (p->evc) cudaEventDestroy(p->evc);
+  p->evc = nullptr;
+  p->w = p->vel = p->cells = p->partial = p->partial2 = p->shift = nullptr;
   p->cells32 = p->w32 = nullptr;
   p->cg = nullptr; p->checks = nullptr; p->active = p->errword = nullptr;
   p->h_cg = nullptr; p->h_checks = nullptr; p->h_active = p->h_err = nullptr;

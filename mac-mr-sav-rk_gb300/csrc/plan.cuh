@@ -47,7 +47,8 @@ struct StageRec {
   double r, residual, scalar_residual, divergence, predictor, factor, corr[2];
   double stokes_residual, stokes_divergence, alpha, beta, coupling, scalar_rhs;
   double max_rhs, max_conv, nn, max_velocity, max_pressure;
-  int n_corr, status, iters[2], cg_info, pad;
+  int n_corr, status, iters[2], cg_info;
+  int sav_status;  // SAV failure of the stage, merged into status by k_stage_close
 };
 
 struct GraphEntry {
@@ -110,9 +111,14 @@ struct Plan {
   double* shift = nullptr;
   int* errword = nullptr;
   unsigned int* done_counter = nullptr;  // last-block counter of reductions
-  // fork streams/events for concurrent u/v passes: [0] main stream, [1] CG body
-  cudaStream_t aux[2] = {nullptr, nullptr};
-  cudaEvent_t evf[2] = {nullptr, nullptr}, evj[2] = {nullptr, nullptr};
+  // fork streams/events: [0] concurrent u/v passes of the main stream, [1] the
+  // same inside the CG body, [2] a stage's closing work (pressure centring and
+  // the Stokes check), which runs beside the stage's SAV algebra and uses
+  // partial2 and done_counter[8] for its reductions
+  cudaStream_t aux[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t evf[3] = {nullptr, nullptr, nullptr}, evj[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t evc = nullptr;
+  double* partial2 = nullptr;
   // pinned host mirrors
   CGScalars* h_cg = nullptr;
   SolveChecks* h_checks = nullptr;
@@ -153,6 +159,8 @@ struct Exec {
   cudaGraphConditionalHandle cond;
   double ktol;        // Krylov tolerance of the solve being enqueued (0: the plan's)
   int net = 0;        // use the plan's learned preconditioner (flexible CG)
+  double* partial = nullptr;       // reduction partials (null: the plan's)
+  unsigned int* counter = nullptr; // last-block counter (null: the plan's)
 };
 
 int plan_build(Plan* p);

@@ -172,38 +172,16 @@ struct CGFin {
       const int c = pr / K, k = pr - c * K;
       if (gated && !active[c]) continue;  // uniform across the warp
       const double* o = partial + size_t(c) * nb * K + k;
-      // Each lane folds partials b = lane, lane + 32, ... in that order; the
-      // loads of a batch are issued together (one L2 round trip per batch,
-      // not one per partial), the sums then taken in the same order.
-      constexpr int kBatch = 16;
       if ((mm >> k) & 1) {
         unsigned long long m = 0ull;
-        for (int b0 = 0; b0 < nb; b0 += 32 * kBatch) {
-          unsigned long long buf[kBatch];
-#pragma unroll
-          for (int i = 0; i < kBatch; ++i) {
-            const int b = b0 + lane + 32 * i;
-            buf[i] = b < nb ? (unsigned long long)__ldcg(reinterpret_cast<const long long*>(o + size_t(b) * K)) : 0ull;
-          }
-#pragma unroll
-          for (int i = 0; i < kBatch; ++i) m = max(m, buf[i]);
-        }
+        for (int b = lane; b < nb; b += 32)
+          m = max(m, (unsigned long long)__ldcg(reinterpret_cast<const long long*>(o + size_t(b) * K)));
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, off));
         if (lane == 0) vals[c][k] = key_value(m);
       } else {
         typename R::P v = R::zero();
-        for (int b0 = 0; b0 < nb; b0 += 32 * kBatch) {
-          typename R::P buf[kBatch];
-#pragma unroll
-          for (int i = 0; i < kBatch; ++i) {
-            const int b = b0 + lane + 32 * i;
-            buf[i] = b < nb ? R::load(o + size_t(b) * K) : R::zero();
-          }
-#pragma unroll
-          for (int i = 0; i < kBatch; ++i)
-            if (b0 + lane + 32 * i < nb) v = R::add(v, buf[i]);
-        }
+        for (int b = lane; b < nb; b += 32) v = R::add(v, R::load(o + size_t(b) * K));
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) v = R::add(v, R::shfl_down(v, off));
         if (lane == 0) vals[c][k] = R::value(v);
@@ -315,8 +293,9 @@ struct CGFin {
 
 template <typename T>
 inline CGFin<T> make_fin(const Plan* P, const Exec& X, int op, int nb, int K, int cols) {
-  return CGFin<T>{op, P->partial, nb, K, cols, P->cg, P->active, P->g.np, X.ktol > 0 ? X.ktol : P->ktol, P->maxit,
-                  P->checks, X.graph ? 1 : 0, X.cond, X.net && P->net ? 1 : 0, P->net_maxit, 1.0 / P->g.np};
+  return CGFin<T>{op, X.partial ? X.partial : P->partial, nb, K, cols, P->cg, P->active, P->g.np,
+                  X.ktol > 0 ? X.ktol : P->ktol, P->maxit, P->checks, X.graph ? 1 : 0, X.cond,
+                  X.net && P->net ? 1 : 0, P->net_maxit, 1.0 / P->g.np};
 }
 
 // ------------------------------------------------------------- launching ---

@@ -20,8 +20,9 @@
 
 namespace macsav {
 
-int enqueue_solve_fp64(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres);
-int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres);
+int enqueue_solve_fp64(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres, bool close);
+int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres, bool close);
+int enqueue_close(Plan* P, Exec& X, const double* f, const double* vel, double* pres, int cols, cudaEvent_t centred);
 
 namespace {
 
@@ -270,11 +271,14 @@ __global__ void __launch_bounds__(kThreads) k_stage_sav(const double* partial, i
   const double alpha = area * nv;  // + lifting work, zero for MAC
   double beta = area * nw;
   R.alpha = alpha;
+  // statuses set before the Stokes solve stop here; the solve's own status
+  // (k_stage_stokes, on the side stream) may still be unset, so this kernel
+  // records its failures in sav_status and k_stage_close merges them
   if (R.status) return;
   if (beta < 0.0) {
     const double scale = sqrt(area * R.nn * area * ww);  // Momentum.cauchy_scale
     if (beta < -1e-12 * (1.0 + scale)) {
-      R.status = ST_NEG_ENERGY;
+      R.sav_status = ST_NEG_ENERGY;
       return;
     }
   }
@@ -283,7 +287,7 @@ __global__ void __launch_bounds__(kThreads) k_stage_sav(const double* partial, i
   const int order = ix.order;
   if (!isfinite(predictor) || !isfinite(dt) || !isfinite(d) || !isfinite(srhs) || !isfinite(alpha) ||
       !isfinite(beta) || dt <= 0 || d <= 0) {
-    R.status = ST_SAV_INPUT;
+    R.sav_status = ST_SAV_INPUT;
     return;
   }
   double z = predictor, c = 1.0;
@@ -293,12 +297,12 @@ __global__ void __launch_bounds__(kThreads) k_stage_sav(const double* partial, i
     const double resp = dt * dt * c * c * beta;
     const double den = d + resp;
     if (!isfinite(den) || den <= 0) {
-      R.status = ST_SAV_DENOM;
+      R.sav_status = ST_SAV_DENOM;
       return;
     }
     z = (srhs - dt * c * alpha + resp) / den;
     if (!isfinite(z)) {
-      R.status = ST_SAV_NONFINITE;
+      R.sav_status = ST_SAV_NONFINITE;
       return;
     }
     R.corr[it] = z;
@@ -328,6 +332,7 @@ __global__ void __launch_bounds__(kThreads) k_stage_close(const double* partial,
   const double nu_dot = sav ? fold_sum(partial + kPartNu, nbn, 1, 0, red) : 0.0;
   if (threadIdx.x != 0) return;
   StageRec& R = recs[stage];
+  if (!R.status && R.sav_status) R.status = R.sav_status;  // a Stokes failure comes first
   const double dt = coef[ix.dt];
   R.max_velocity = maxu;
   R.divergence = maxdiv;
@@ -675,21 +680,46 @@ static int enqueue_step(Plan* P, Exec& X, int scheme, const StageProgram& G, boo
     launch_k(k_fold_combine, M, kThreads, 0, s, P->partial, nbs, rec);
     launch_k(k_set_shift, 1, kMaxCols, 0, s, P->shift, B.coef, G.kappa[i], cols, cols * M);
     P->launches += 3;
-    int rc = P->precision == MACSAV_FP64 ? enqueue_solve_fp64(P, X, B.F, cols * M, B.VW, B.PI)
-                                         : enqueue_solve_mixed(P, X, B.F, cols * M, B.VW, B.PI);
+    const bool fp64 = P->precision == MACSAV_FP64;
+    int rc = fp64 ? enqueue_solve_fp64(P, X, B.F, cols * M, B.VW, B.PI, false)
+                  : enqueue_solve_mixed(P, X, B.F, cols * M, B.VW, B.PI, false);
     if (rc != MACSAV_OK) return rc;
-    launch_k(k_stage_stokes, 1, kMaxMembers, 0, s, P->checks, P->cg, cols, M, P->tol, rec);
-    ++P->launches;
+    // The solve's closing work (pressure centring on the mixed path, the
+    // FP64 Stokes check and its stage record) on the side stream, with its
+    // own partials and counter, beside the SAV algebra below: the velocity
+    // is final here, the centred pressure is first needed by k_recombine
+    // and the check's record by k_stage_close.  Single-cavity plans only:
+    // a batched plan already fills the GPU, and with many plans in flight
+    // (ensembles) the extra streams cost more than they hide (measured on
+    // GB300: single cavity 512^2 -1.6% step time, 256-member ensemble +9%).
+    const bool overlap = M == 1;
+    {
+      const cudaStream_t side = overlap ? P->aux[2] : s;
+      if (overlap) {
+        cudaEventRecord(P->evf[2], s);
+        cudaStreamWaitEvent(side, P->evf[2], 0);
+      }
+      Exec Xc = X;
+      Xc.s = side;
+      Xc.partial = P->partial2;
+      Xc.counter = P->done_counter + 8;
+      enqueue_close(P, Xc, B.F, B.VW, B.PI, cols * M, fp64 || !overlap ? nullptr : P->evj[2]);
+      launch_k(k_stage_stokes, 1, kMaxMembers, 0, side, P->checks, P->cg, cols, M, P->tol, rec);
+      ++P->launches;
+      if (overlap) cudaEventRecord(P->evc, side);
+    }
     if (sav) {
       launch_k(k_dots3, dim3(nbs, M), kThreads, 0, s, B.F + sz, B.VW, sz, ms.F, P->partial);
       launch_k(k_stage_sav, M, kThreads, 0, s, P->partial, nbs, B.recs, i, B.coef, G.sav[i], area);
       P->launches += 2;
     }
+    if (overlap && !fp64) cudaStreamWaitEvent(s, P->evj[2], 0);  // centred pressure
     double* pi = B.PS + i * np;
     launch_k(k_recombine, dim3(nbn, M), kThreads, 0, s, g, B.VW, B.PI, B.F + sz, U, pi, rec, B.coef, G.dt_idx, sav ? 1 : 0,
                                                    P->partial + kPartNu, ms);
     launch_k(k_stage_defect, dim3(nbn, M), kThreads, 0, s, g, U, pi, B.F, B.KU + i * sz, rec, B.coef, G.dt_idx,
                                                       G.kappa[i], sav ? 1 : 0, P->partial, ms);
+    if (overlap) cudaStreamWaitEvent(s, P->evc, 0);  // Stokes check and its record
     const int gate = (scheme == MACSAV_SDIRK2 || scheme == MACSAV_SDIRK3) ? 0 : 1;
     launch_k(k_stage_close, M, kThreads, 0, s, P->partial, nbn, nbn, B.recs, i, B.coef, G.sav[i], area, sav ? 1 : 0, gate);
     P->launches += 3;

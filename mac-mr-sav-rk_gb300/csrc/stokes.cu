@@ -443,10 +443,12 @@ static void finish_pressure(Plan* P, const Exec& X, const T* x, double* pres, in
   const long long np = P->g.np;
   const int rb = red_blocks(np);
   const cudaStream_t s = X.s;
-  launch_k(k_center_cells<T>, dim3(rb, cols), kThreads, 0, s, P->g.np, x, np, nullptr, np, P->cg, 0, P->partial,
-                                                        make_fin<double>(P, X, OP_MEAN_X, rb, 1, cols), P->done_counter);
-  launch_k(k_center_cells<T>, dim3(rb, cols), kThreads, 0, s, P->g.np, x, np, pres, np, P->cg, 1, P->partial,
-                                                        make_fin<double>(P, X, OP_MEAN_X, rb, 1, cols), P->done_counter);
+  double* part = X.partial ? X.partial : P->partial;
+  unsigned int* done = X.counter ? X.counter : P->done_counter;
+  launch_k(k_center_cells<T>, dim3(rb, cols), kThreads, 0, s, P->g.np, x, np, nullptr, np, P->cg, 0, part,
+                                                        make_fin<double>(P, X, OP_MEAN_X, rb, 1, cols), done);
+  launch_k(k_center_cells<T>, dim3(rb, cols), kThreads, 0, s, P->g.np, x, np, pres, np, P->cg, 1, part,
+                                                        make_fin<double>(P, X, OP_MEAN_X, rb, 1, cols), done);
   launch_k(k_shift_cells, dim3(rb, cols), kThreads, 0, s, P->g.np, pres, np, P->cg);
   P->launches += 3;
 }
@@ -455,15 +457,26 @@ static void closing_checks(Plan* P, const Exec& X, const double* f, const double
                            const double* shift) {
   const long long n = P->g.size > P->g.np ? P->g.size : P->g.np;
   const int rb = red_blocks(n);
-  launch_k(k_stokes_check, dim3(rb, cols), kThreads, 0, X.s, P->g, vel, pres, f, P->g.size, P->g.np, shift, P->partial,
-                                                       make_fin<double>(P, X, OP_CHECKS, rb, 6, cols), P->done_counter);
+  launch_k(k_stokes_check, dim3(rb, cols), kThreads, 0, X.s, P->g, vel, pres, f, P->g.size, P->g.np, shift,
+           X.partial ? X.partial : P->partial, make_fin<double>(P, X, OP_CHECKS, rb, 6, cols),
+           X.counter ? X.counter : P->done_counter);
   ++P->launches;
+}
+
+// The closing work a solve enqueued with close = false left out: for the
+// mixed path the pressure centring (signalling `centred` once pres is final)
+// and for both the FP64 closing checks.  The step runs it on its side stream.
+int enqueue_close(Plan* P, Exec& X, const double* f, const double* vel, double* pres, int cols, cudaEvent_t centred) {
+  if (P->precision != MACSAV_FP64) finish_pressure<double>(P, X, pres, pres, cols);
+  if (centred) cudaEventRecord(centred, X.s);
+  closing_checks(P, X, f, vel, pres, cols, P->shift);
+  return MACSAV_OK;
 }
 
 // FP64 solve: TensorStokes.solve with every vector in double.  Shifts are
 // read from P->shift (device), so the same enqueue serves the stand-alone
 // solve and the captured stage.
-int enqueue_solve_fp64(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres) {
+int enqueue_solve_fp64(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres, bool close) {
   const GridDev& g = P->g;
   Launcher<double> L{P->t64, X.s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
   const long long sz = g.size;
@@ -475,7 +488,7 @@ int enqueue_solve_fp64(Plan* P, Exec& X, const double* f, int cols, double* vel,
   velocity_inverse<double>(
       P, L, SrcLift<double, double, double>{f, sz, pres, nullptr, P->cg, (long long)g.np, g.nx, g.nu, g.ihx, g.ihy},
       vel, sz, cols, nullptr);
-  closing_checks(P, X, f, vel, pres, cols, P->shift);
+  if (close) closing_checks(P, X, f, vel, pres, cols, P->shift);
   return MACSAV_OK;
 }
 
@@ -484,7 +497,7 @@ int solve_fp64(Plan* P, const double* f, int cols, double mass, double visc, dou
   (void)mass;
   (void)visc;
   Exec X{s, false, nullptr, 0, 0.0};
-  return enqueue_solve_fp64(P, X, f, cols, vel, pres);
+  return enqueue_solve_fp64(P, X, f, cols, vel, pres, true);
 }
 
 // ------------------------------------------------- FP32 + FP64 correction ---
@@ -555,7 +568,7 @@ static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, i
 // TensorStokes.solve with FP32 bulk: an FP32 solve, then `corrections`
 // defect-correction sweeps whose defects are formed in FP64, so the result
 // satisfies the same FP64 residual and divergence gates as the FP64 path.
-int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres) {
+int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres, bool close) {
   const GridDev& g = P->g;
   const long long sz = g.size, np = g.np;
   double* ru = P->w;               // FP64 momentum defect
@@ -574,8 +587,10 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
     if (rc != MACSAV_OK) return rc;
   }
   // mean-zero pressure and the FP64 closing checks, as in the FP64 path
-  finish_pressure<double>(P, X, pres, pres, cols);
-  closing_checks(P, X, f, vel, pres, cols, P->shift);
+  if (close) {
+    finish_pressure<double>(P, X, pres, pres, cols);
+    closing_checks(P, X, f, vel, pres, cols, P->shift);
+  }
   return MACSAV_OK;
 }
 
@@ -626,7 +641,7 @@ int solve_mixed(Plan* P, const double* f, int cols, double mass, double visc, do
   (void)visc;
   Exec X{s, false, nullptr, 0, 0.0};
   *sweeps = P->corrections;
-  return enqueue_solve_mixed(P, X, f, cols, vel, pres);
+  return enqueue_solve_mixed(P, X, f, cols, vel, pres, true);
 }
 
 }  // namespace macsav
