@@ -317,18 +317,7 @@ def learned_leg(pkg, g, w, x0_host, dev, args, x64) -> dict:
     import torch
     from importlib import import_module
     L = import_module(pkg.__name__ + ".learned")
-    t0 = time.perf_counter()
-    grid = pkg.MACGrid(256, 256)
-    helper = pkg.MACNavierStokes(grid, w["nu"])
-    rhs = []
-    for s in range(4):
-        x = pkg.fields.packed_curl_velocity(256, 256, 1.0, 1.0, w["psi_modes"], 1000 + s)
-        rhs += [x, helper.nonlinear(x).cpu().numpy() * w["dt"]]
-    pairs = L.collect_pairs(grid, rhs, 1.0, w["nu"] * w["dt"] / 4)
-    net = L.UNet(seed=0)
-    losses = L.train(net, pairs, steps=200, batch=8, lr=1e-3)
-    torch.cuda.synchronize()
-    train_sec = time.perf_counter() - t0
+    net, training = train_unet(pkg, w["nu"], w["dt"], w["psi_modes"])
     scheme = pkg.make_scheme(w["scheme"])
     stream = torch.cuda.current_stream()
 
@@ -368,11 +357,123 @@ def learned_leg(pkg, g, w, x0_host, dev, args, x64) -> dict:
             "fallbacks_per_step": c_learned["fallbacks"],
             "plain_fp32_cg_iterations_per_step": c_plain["iterations"],
             "error_vs_fp64": err,
-            "network": {"params": net.num_params, "channels": list(net.channels), "activations": "bf16",
-                        "convolutions": "direct, CUDA cores (not tensor cores)"},
-            "training": {"pairs": int(pairs.inputs.shape[0]), "grid": "256x256", "steps": len(losses),
-                         "loss_first": float(np.mean(losses[:5])), "loss_last": float(np.mean(losses[-5:])),
-                         "seconds": train_sec}}
+            "network": network_info(net), "training": training}
+
+
+def network_info(net) -> dict:
+    return {"params": net.num_params, "channels": list(net.channels), "activations": "bf16",
+            "convolutions": ("3x3 forward on tcgen05 (BF16 operands, FP32 accumulator in TMEM), backward on CUDA cores"
+                             if net.tensor_cores else "CUDA cores")}
+
+
+def train_unet(pkg, nu: float, dt: float, psi_modes: int):
+    """The U-Net of the learned preconditioner, trained on the GPU on pairs
+    logged by plain FP64 Schur CG on four 256^2 cavities with the given
+    physics (stage shift of sdirk3_mrsav: mass 1, viscosity nu*dt/4)."""
+    import torch
+    from importlib import import_module
+    L = import_module(pkg.__name__ + ".learned")
+    t0 = time.perf_counter()
+    grid = pkg.MACGrid(256, 256)
+    helper = pkg.MACNavierStokes(grid, nu)
+    rhs = []
+    for s in range(4):
+        x = pkg.fields.packed_curl_velocity(256, 256, 1.0, 1.0, psi_modes, 1000 + s)
+        rhs += [x, helper.nonlinear(x).cpu().numpy() * dt]
+    pairs = L.collect_pairs(grid, rhs, 1.0, nu * dt / 4)
+    net = L.UNet(seed=0)
+    losses = L.train(net, pairs, steps=200, batch=8, lr=1e-3)
+    torch.cuda.synchronize()
+    return net, {"pairs": int(pairs.inputs.shape[0]), "grid": "256x256", "nu": nu, "dt": dt, "steps": len(losses),
+                 "loss_first": float(np.mean(losses[:5])), "loss_last": float(np.mean(losses[-5:])),
+                 "seconds": time.perf_counter() - t0}
+
+
+LEARNED = {"workload": "learned1024_sdirk3_mrsav", "nx": 1024, "ny": 1024, "lx": 1.0, "ly": 1.0, "nu": 1e-4,
+           "dt": 1e-4, "psi_modes": 32, "seed": 20261204, "scheme": "sdirk3_mrsav", "stages_per_step": 4,
+           "steps": 100, "krylov_tolerance": 1e-10, "reference_krylov_tolerance": 1e-12,
+           "train_nu": 1e-3, "train_dt": 2.5e-4}
+
+
+def run_learned(args) -> None:
+    """The learned-preconditioner run: 1024^2, nu=1e-4, sdirk3_mrsav, dt=1e-4,
+    psi modes <= 32, 100 steps (``--steps`` other than 10 overrides), flexible
+    CG at Krylov tolerance 1e-10 with the U-Net trained on 256^2 cavities with
+    the 512^2 workload's physics (nu=1e-3, dt=2.5e-4).  Three graph-captured
+    runs from the same field: FP64 plain at 1e-12 (the reference), FP32 bulk
+    plain and FP32 bulk with the network at 1e-10; reports each one's speed
+    and its velocity error against the FP64 run after the same steps."""
+    import torch
+    import __graft_entry__
+    from importlib import import_module
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    __graft_entry__.build()
+    pkg = __graft_entry__.load_package()
+    L = import_module(pkg.__name__ + ".learned")
+    w = LEARNED
+    steps = w["steps"] if args.steps == 10 else args.steps
+    g = pkg.MACGrid(w["nx"], w["ny"], w["lx"], w["ly"])
+    dev = torch.device("cuda", local)
+    x0 = pkg.fields.packed_curl_velocity(w["nx"], w["ny"], w["lx"], w["ly"], w["psi_modes"], w["seed"])
+    net, training = train_unet(pkg, w["train_nu"], w["train_dt"], w["psi_modes"])
+    stream = torch.cuda.current_stream()
+
+    def run(precision, ktol, with_net):
+        model = pkg.MACNavierStokes(g, w["nu"], precision=precision, use_graph=True, krylov_tolerance=ktol)
+        if with_net:
+            L.attach(model, net)
+        scheme = pkg.make_scheme(w["scheme"])
+        x = torch.from_numpy(x0.copy()).to(dev)
+        y = torch.empty_like(x)
+        pres = torch.empty((4, g.np), dtype=torch.float64, device=dev)
+        t, r = 0.0, 1.0
+        for _ in range(args.warmup):
+            y, r, _, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
+            x, y, t = y, x, t + w["dt"]
+        before = L.cg_counters(model, 2) if precision == "fp32" else None
+        total = 0.0
+        for _ in range(steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            y, r, _, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
+            b.record(stream)
+            b.synchronize()
+            total += a.elapsed_time(b)
+            x, y, t = y, x, t + w["dt"]
+        iters = None
+        if before is not None:
+            after = L.cg_counters(model, 2)
+            iters = {k: (sum(after[k]) - sum(before[k])) / steps for k in after}
+        return total / steps, x, iters
+
+    with ClockSampler(local) as clk:
+        ms64, x64, _ = run("fp64", w["reference_krylov_tolerance"], False)
+        ms32, x32, it32 = run("fp32", w["krylov_tolerance"], False)
+        msl, xl, itl = run("fp32", w["krylov_tolerance"], True)
+    if rank != 0:
+        return
+    cells = w["nx"] * w["ny"] * w["stages_per_step"]
+
+    def err(x):
+        return float(torch.linalg.vector_norm(x - x64) / torch.linalg.vector_norm(x64))
+
+    line = {"metric": METRIC, "value": cells / (msl / 1e3), "unit": "cell-stage/s", "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": msl, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32+bf16 network+fp64",
+            "data": "synthetic (seeded stream-function curl field, psi modes <= 32)",
+            "config": {"workload": w["workload"], **{k: w[k] for k in ("nx", "ny", "nu", "dt", "scheme",
+                                                                       "krylov_tolerance",
+                                                                       "reference_krylov_tolerance")},
+                       "note": "value = FP32 bulk with the learned preconditioner (flexible CG in the FP32 "
+                               "inner solves; FP64 defect correction and the reference's gates unchanged)"},
+            "error_vs_fp64": err(xl), "cg_iterations_per_step": itl,
+            "plain_fp32": {"value": cells / (ms32 / 1e3), "ms_per_step": ms32, "error_vs_fp64": err(x32),
+                           "cg_iterations_per_step": it32},
+            "fp64": {"value": cells / (ms64 / 1e3), "ms_per_step": ms64, "unit": "cell-stage/s"},
+            "speedup_vs_fp64": ms64 / msl, "speedup_vs_plain_fp32": ms32 / msl,
+            "network": network_info(net), "training": training, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
 
 
 def profile_unet() -> None:
@@ -419,7 +520,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["cavity512", "ensemble256", "adaptive2048"], default="cavity512")
+    ap.add_argument("--workload", choices=["cavity512", "ensemble256", "adaptive2048", "learned1024"],
+                    default="cavity512")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner leg")
     ap.add_argument("--profile", choices=["fp32", "fp64", "unet"], default=None,
                     help="run two eager steps of the workload and exit (for ncu captures)")
@@ -440,6 +542,9 @@ def main() -> None:
         return
     if args.workload == "adaptive2048":
         run_adaptive(args)
+        return
+    if args.workload == "learned1024":
+        run_learned(args)
         return
 
     import torch
