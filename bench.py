@@ -28,6 +28,7 @@ reference's own path, all host threads) on the same workload.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import pathlib
@@ -624,16 +625,18 @@ def main() -> None:
     value = cells / (ms32 / 1e3)
     value64 = cells / (ms64 / 1e3)
 
-    # end to end through the public API with host state (H2D + D2H each step)
+    # end to end through the public API with host state (H2D + D2H each step):
+    # each step gets a State holding only the previous step's host arrays (no
+    # cached device vector), so its velocity crosses to the device and the new
+    # state comes back to host memory
     scheme = pkg.make_scheme(w["scheme"])
     st_host = pkg.State(0.0, *g.unpack(x0_host), 0.0)
     for _ in range(args.warmup):
-        st_host = scheme.step(m32, pkg.State(st_host.t, np.array(st_host.u), np.array(st_host.v), st_host.r),
-                              w["dt"]).state
+        st_host = scheme.step(m32, pkg.State(st_host.t, st_host.u, st_host.v, st_host.r), w["dt"]).state
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        fresh = pkg.State(st_host.t, np.array(st_host.u), np.array(st_host.v), st_host.r)  # no device copy
+        fresh = pkg.State(st_host.t, st_host.u, st_host.v, st_host.r)  # host arrays only
         st_host = scheme.step(m32, fresh, w["dt"]).state
     torch.cuda.synchronize()
     e2e_sec = time.perf_counter() - t0
@@ -641,9 +644,12 @@ def main() -> None:
     if world > 1:
         dist.all_reduce(et, op=dist.ReduceOp.MAX)
     e2e_value = cells / float(et[0])
+    # bytes copied per e2e step: the face arrays u (ny, nx+1) and v (ny+1, nx)
+    # each way, plus the stage records read back with the step
+    face_bytes = (g.ny * (g.nx + 1) + (g.ny + 1) * g.nx) * 8
+    rec_bytes = C.sizeof(lib.StageRecord)
 
     # dominant kernel (FP32 column pass of the velocity blocks) timed alone
-    import ctypes as C
     ms_k, bytes_k = C.c_double(), C.c_double()
     m32.plan.check(lib.load().macsav_time_pass(m32.plan.handle, 0, 50, C.byref(ms_k), C.byref(bytes_k),
                                                stokes.stream_handle()))
@@ -680,8 +686,8 @@ def main() -> None:
         "error_vs_fp64": {"rel_l2_velocity": diff, "after_steps": args.warmup + args.steps},
         "cg_iterations_mean": mean_iters,
         "clocks": clk32,
-        "e2e": {"value": e2e_value, "unit": "cell-stage/s", "h2d_bytes_per_step": g.size * 8,
-                "d2h_bytes_per_step": g.size * 8 + 4 * 160},
+        "e2e": {"value": e2e_value, "unit": "cell-stage/s", "h2d_bytes_per_step": face_bytes,
+                "d2h_bytes_per_step": face_bytes + w["stages_per_step"] * rec_bytes},
         "gpu_launches": int(l32 * args.steps),
         "roofline": {"kernel": "k_column<float> (velocity blocks, 2 RHS)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
