@@ -170,7 +170,9 @@ class Ensemble:
         unit, j = self._where[index]
         x = velocity if isinstance(velocity, torch.Tensor) else torch.from_numpy(
             np.ascontiguousarray(np.asarray(velocity, dtype=np.float64)))
-        unit.x[unit.cur, j].copy_(x.to("cuda", torch.float64).reshape(-1))
+        # one copy straight into the member's slot (a blocking copy from host
+        # memory; from a pinned buffer it runs at full link speed)
+        unit.x[unit.cur, j].copy_(x.reshape(-1).to(torch.float64))
         self.r[index] = float(r)
         self.t[index] = float(t)
 
