@@ -4,9 +4,12 @@ Each test restates one reference test (file:line in its docstring) against the
 fused device schemes and the device TensorStokes: the zero-velocity closed form
 of the SAV scalar, Laplacian reuse per stage, the discrete SAV energy balance,
 preservation of a steady state, second/third order in time against an exact
-semidiscrete solution, and second order in space of the Stokes solve on a
-manufactured solution.  The bars are the reference's.
+semidiscrete solution, second order in space of the Stokes solve on a
+manufactured solution, and the scalar-map and stage-gate failures with the
+reference's exception types and messages.  The bars are the reference's.
 """
+import re
+
 import numpy as np
 import pytest
 
@@ -188,3 +191,50 @@ def test_stokes_spatial_convergence_and_operator_structure(pkg):
                        np.sqrt(og.area * np.sum((np.asarray(solved.pressure) - p) ** 2))])
     rates = np.log2(np.array(errors[:-1]) / np.array(errors[1:]))
     assert np.min(rates) > 1.7, (errors, rates)
+
+
+def _oracle_error(name, g_args, nu, x0, t, r, dt, tol, ktol):
+    og = O.Grid(*g_args)
+    m = O.OracleModel(og, nu, backend=O.TensorStokesOracle(og, tol, ktol))
+    try:
+        O.make_scheme(name).step(m, m.state(t, x0, r), dt)
+    except Exception as error:  # the reference's exception for this step
+        return error
+    return None
+
+
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize(("name", "r"), [("sdirk2_mrsav", float("nan")), ("sdirk3_mrsav", float("inf")),
+                                         ("sdirk2_mrsav", 1e200), ("sdirk3_mrsav", -1e200),
+                                         ("imex_euler_mrsav", float("nan"))])
+def test_scalar_map_failures_raise_like_reference(pkg, name, r, graph):
+    """scalar_correction.py:29-52 guards (inputs, denominator) and the IMEX
+    Euler state check, raised with the reference's type and message."""
+    x0 = pkg.fields.packed_curl_velocity(16, 12, 1.3, 0.8, 4, 3)
+    want = _oracle_error(name, (16, 12, 1.3, 0.8), 0.05, x0, 0.1, r, 0.01, 1e-9, 1e-12)
+    assert want is not None
+    model = pkg.MACNavierStokes(pkg.MACGrid(16, 12, 1.3, 0.8), 0.05, use_graph=graph)
+    with pytest.raises(type(want)) as got:
+        pkg.make_scheme(name).step(model, model.state(0.1, x0, r), 0.01)
+    assert str(got.value) == str(want)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("name", ["sdirk2_mrsav", "sdirk3_mrsav", "imex_euler_mrsav", "imex_euler"])
+def test_stage_gate_failure_raises_like_reference(pkg, name, graph):
+    """A Stokes backend loose enough to pass its own gate (1e-2) but not the
+    stage gate (1e-8): the stage residual messages of sdirk2_mrsav.py:60-66,
+    sdirk3_mrsav.py:105-114 and imex_euler*.py, with the same divergence."""
+    x0 = pkg.fields.packed_curl_velocity(16, 12, 1.3, 0.8, 4, 3)
+    want = _oracle_error(name, (16, 12, 1.3, 0.8), 0.05, x0, 0.1, 0.2, 0.01, 1e-2, 1e-6)
+    assert isinstance(want, RuntimeError)
+    backend = pkg.TensorStokes(pkg.MACGrid(16, 12, 1.3, 0.8), tolerance=1e-2, krylov_tolerance=1e-6)
+    model = pkg.MACNavierStokes(pkg.MACGrid(16, 12, 1.3, 0.8), 0.05, backend=backend, use_graph=graph)
+    with pytest.raises(RuntimeError) as got:
+        pkg.make_scheme(name).step(model, model.state(0.1, x0, 0.2), 0.01)
+    msg, ref = str(got.value), str(want)
+    head = re.match(r"[A-Za-z ]+", ref).group(0)  # the text before the first number
+    assert head.endswith("residuals ") or head.endswith("residual ")
+    assert msg.startswith(head), (msg, ref)
+    div = float(msg.rsplit(" ", 1)[1])
+    assert div == pytest.approx(float(ref.rsplit(" ", 1)[1]), rel=1e-6)
