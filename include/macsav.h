@@ -207,7 +207,7 @@ int macsav_step_finish(macsav_plan* plan, macsav_stage_record* records, double* 
  * (Polak-Ribiere beta) in the FP32 inner solves.  A column whose learned
  * attempt has not converged after learned_max_iterations (or turned
  * non-finite) restarts plain PCG from zero, and the FP64 defect correction
- * and closing gates judge the result as before.  Grids need nx, ny
+ * and closing gates accept or reject the result as before.  Grids need nx, ny
  * multiples of 8.  Inputs/outputs of the network calls are device FP32
  * [batch][ny][nx]; parameters are host FP32 in layer order, each layer
  * [c_out][c_in][k][k]. */

@@ -14,7 +14,7 @@ plain FP64 Schur CG itself: for every iteration k of a logged solve, the
 residual r_k and the exact error p* - p_k of the iterate (which solves
 S e = r_k); the target is that error minus M r_k, in the units above.
 
-Plain PCG stays the fallback and the judge: a column whose learned attempt
+Plain PCG stays the fallback and the gates stay in charge: a column whose learned attempt
 does not converge within ``learned_max_iterations`` restarts plain PCG from
 zero, and the FP64 defect correction and the reference's closing gates decide
 as before, so the network never changes the answer beyond the tolerance.

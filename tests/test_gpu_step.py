@@ -1,8 +1,8 @@
 """The fused device step, the GPU model seam and the integrate driver against
 the reference (golden fixtures) and the oracle.
 
-Bars: <= 1e-11 relative L2 on the stepped velocity and pressures (north-star
-parity for the FP64 path), SAV scalars to 1e-12, identical CG iterations.
+Bars: <= 1e-11 relative L2 on the stepped velocity and pressures (the parity
+bar of the FP64 path), SAV scalars to 1e-12, identical CG iterations.
 """
 import numpy as np
 import pytest
