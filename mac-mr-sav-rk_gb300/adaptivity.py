@@ -233,13 +233,21 @@ def integrate_adaptive(model, scheme, initial, T: float, initial_step: float, *,
             trial = scheme.step(model, result.final, step)
             if trial.embedded_velocity is None:
                 raise ValueError("Scheme does not provide an embedded velocity")
-            high = model.vector(trial.state)
-            if terminal:
-                trial.state = model.state(end, high, trial.state.r)
             # a fused GPU step brings the embedded-error inner products with it
             norms = getattr(trial, "embedded_norms", None) if error_norm is None else None
+            device = getattr(trial.state, "device", None) if norms is not None else None
+            if device is not None:
+                # finiteness of the new state on the device (the maximum of
+                # |x| propagates NaN and Inf), not on a host copy of it
+                high = device
+                high_finite = bool(np.isfinite(model.max_abs(device)))
+            else:
+                high = model.vector(trial.state)
+                high_finite = bool(np.isfinite(high).all())
+            if terminal:
+                trial.state = model.state(end, high, trial.state.r)
             emb_finite = (norms[3] == 0.0) if norms is not None else _finite(model, trial.embedded_velocity)
-            if not np.isfinite(high).all() or not emb_finite or not np.isfinite(trial.state.r):
+            if not high_finite or not emb_finite or not np.isfinite(trial.state.r):
                 raise FloatingPointError("Nonfinite trial state")
             if norms is not None:
                 error_u = _error_from_norms(norms, controller)
