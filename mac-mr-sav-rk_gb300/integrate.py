@@ -78,6 +78,16 @@ def step_sizes(T: float, *, dt: float | None = None, steps: list | None = None) 
     return np.r_[np.full(count, dt), T - count * dt]
 
 
+def state_finite(model, state) -> bool:
+    """Every velocity entry of ``state`` is finite (integrate.py:67).  A state
+    that carries its packed device vector is checked on the device (the
+    maximum of |x| propagates NaN and Inf), without a host copy."""
+    device = getattr(state, "device", None)
+    if device is not None and hasattr(model, "max_abs"):
+        return bool(np.isfinite(model.max_abs(device)))
+    return bool(np.isfinite(model.vector(state)).all())
+
+
 def integrate(model, scheme, initial: State, steps, snapshots: list | None = None,
               progress: Callable[[int, float, float], None] | None = None, *,
               on_accept: Callable[[State], None] | None = None) -> Result:
@@ -99,7 +109,7 @@ def integrate(model, scheme, initial: State, steps, snapshots: list | None = Non
     for k, dt in enumerate(seq):
         try:
             trial = scheme.step(model, history.state, float(dt))
-            if not np.isfinite(model.vector(trial.state)).all() or not np.isfinite(trial.state.r):
+            if not state_finite(model, trial.state) or not np.isfinite(trial.state.r):
                 raise FloatingPointError("Nonfinite trial state")
             diagnostic = model.diagnostics(trial.state)
             if not all(np.isfinite(v) for v in diagnostic.values()):
