@@ -36,6 +36,7 @@ namespace {
 using cd = cplx<double>;
 constexpr int kKL = 3, kKU = 3, kLD = 2 * kKL + kKU + 1;  // band storage rows
 constexpr int kChThreads = 256;
+constexpr int kChSolveThreads = 8;  // threads per CTA of the per-mode recurrences
 
 struct ChanGrid {
   int nx, ny, nu, nv, size, np, nm;  // nm = nx/2 + 1 x modes
@@ -275,9 +276,13 @@ __device__ ModeCoef mode_coef(const ChanGrid& g, int m) {
   return r;
 }
 
-// band element (i, j) of mode m's factor array (LAPACK band layout: column
-// j holds rows j-KU-KL .. j+KL at offsets 0 .. LD-1)
-__device__ __forceinline__ cd& band(cd* ab, int i, int j) { return ab[(long long)j * kLD + (kKL + kKU + i - j)]; }
+// Band element (i, j) of the factor of mode m1 + 1 (LAPACK band layout:
+// column j holds rows j-KU-KL .. j+KL at offsets 0 .. LD-1).  The modes are
+// interleaved (element e of every mode contiguous, nmodes apart), so the
+// threads of a warp, one mode each, read and write coalesced.
+__device__ __forceinline__ long long band_index(int i, int j, int nmodes, int m1) {
+  return ((long long)j * kLD + (kKL + kKU + i - j)) * nmodes + m1;
+}
 
 // Assemble and factor the saddle system of every mode m >= 1 (one thread per
 // mode); mode 0 stores the Thomas factors of hu0 = m I + k Ly(ny, wall).
@@ -301,30 +306,30 @@ __global__ void k_ch_factor(ChanGrid g, double mass, double visc, cd* lu, int* p
     return;
   }
   const int n = 3 * ny - 1;
-  cd* ab = lu + (long long)(m - 1) * n * kLD;
-  int* pv = piv + (long long)(m - 1) * n;
-  for (long long e = 0; e < (long long)n * kLD; ++e) ab[e] = mk(0.0, 0.0);
+  const int nmodes = g.nm - 1, m1 = m - 1;
+  auto band = [&](int i, int j) -> cd& { return lu[band_index(i, j, nmodes, m1)]; };
+  for (long long e = 0; e < (long long)n * kLD; ++e) lu[e * nmodes + m1] = mk(0.0, 0.0);
   const ModeCoef mc = mode_coef(g, m);
   const double a0 = mass + visc * mc.lam;
   const cd d = mc.d, dc = conjg(d);
   for (int j = 0; j < ny; ++j) {
     const int ru = 3 * j, rp = 3 * j + 1, rv = 3 * j + 2;
     // u_j momentum: hu, -conj(d) p_j
-    band(ab, ru, ru) = mk(a0 + visc * ((j == 0 || j == ny - 1) ? 3.0 : 2.0) * iy2, 0.0);
-    if (j > 0) band(ab, ru, ru - 3) = mk(-visc * iy2, 0.0);
-    if (j < ny - 1) band(ab, ru, ru + 3) = mk(-visc * iy2, 0.0);
-    band(ab, ru, rp) = mk(-dc.x, -dc.y);
+    band(ru, ru) = mk(a0 + visc * ((j == 0 || j == ny - 1) ? 3.0 : 2.0) * iy2, 0.0);
+    if (j > 0) band(ru, ru - 3) = mk(-visc * iy2, 0.0);
+    if (j < ny - 1) band(ru, ru + 3) = mk(-visc * iy2, 0.0);
+    band(ru, rp) = mk(-dc.x, -dc.y);
     // continuity j (negated): -d u_j - (v_j - v_{j-1})/hy
-    band(ab, rp, ru) = mk(-d.x, -d.y);
-    if (j < ny - 1) band(ab, rp, rv) = mk(-g.ihy, 0.0);
-    if (j > 0) band(ab, rp, rv - 3) = mk(g.ihy, 0.0);
+    band(rp, ru) = mk(-d.x, -d.y);
+    if (j < ny - 1) band(rp, rv) = mk(-g.ihy, 0.0);
+    if (j > 0) band(rp, rv - 3) = mk(g.ihy, 0.0);
     // v_j momentum (face j+1): hv, -(p_j - p_{j+1})/hy
     if (j < ny - 1) {
-      band(ab, rv, rv) = mk(a0 + 2.0 * visc * iy2, 0.0);
-      if (j > 0) band(ab, rv, rv - 3) = mk(-visc * iy2, 0.0);
-      if (j < ny - 2) band(ab, rv, rv + 3) = mk(-visc * iy2, 0.0);
-      band(ab, rv, rp) = mk(-g.ihy, 0.0);
-      band(ab, rv, rp + 3) = mk(g.ihy, 0.0);
+      band(rv, rv) = mk(a0 + 2.0 * visc * iy2, 0.0);
+      if (j > 0) band(rv, rv - 3) = mk(-visc * iy2, 0.0);
+      if (j < ny - 2) band(rv, rv + 3) = mk(-visc * iy2, 0.0);
+      band(rv, rp) = mk(-g.ihy, 0.0);
+      band(rv, rp + 3) = mk(g.ihy, 0.0);
     }
   }
   // banded LU with partial pivoting (the elimination order of gbtf2)
@@ -334,14 +339,14 @@ __global__ void k_ch_factor(ChanGrid g, double mass, double visc, cd* lu, int* p
     int p = 0;
     double best = -1.0;
     for (int r = 0; r <= km; ++r) {
-      const cd v = band(ab, k + r, k);
+      const cd v = band(k + r, k);
       const double a = fabs(v.x) + fabs(v.y);  // |re| + |im|, as izamax
       if (a > best) {
         best = a;
         p = r;
       }
     }
-    pv[k] = k + p;
+    piv[(long long)k * nmodes + m1] = k + p;
     if (!(best > 0.0)) {
       status[0] = 2;
       continue;
@@ -349,30 +354,48 @@ __global__ void k_ch_factor(ChanGrid g, double mass, double visc, cd* lu, int* p
     ju = max(ju, min(k + kKU + p, n - 1));
     if (p != 0)
       for (int j = k; j <= ju; ++j) {
-        const cd t = band(ab, k, j);
-        band(ab, k, j) = band(ab, k + p, j);
-        band(ab, k + p, j) = t;
+        const cd t = band(k, j);
+        band(k, j) = band(k + p, j);
+        band(k + p, j) = t;
       }
-    const cd piv_v = band(ab, k, k);
+    const cd piv_v = band(k, k);
     const double den = piv_v.x * piv_v.x + piv_v.y * piv_v.y;
     const cd inv = mk(piv_v.x / den, -piv_v.y / den);
-    for (int r = 1; r <= km; ++r) band(ab, k + r, k) = cmul(band(ab, k + r, k), inv);
+    for (int r = 1; r <= km; ++r) band(k + r, k) = cmul(band(k + r, k), inv);
     for (int j = k + 1; j <= ju; ++j) {
-      const cd akj = band(ab, k, j);
+      const cd akj = band(k, j);
       if (akj.x == 0.0 && akj.y == 0.0) continue;
       for (int r = 1; r <= km; ++r) {
-        cd& t = band(ab, k + r, j);
-        t = t - cmul(band(ab, k + r, k), akj);
+        cd& t = band(k + r, j);
+        t = t - cmul(band(k + r, k), akj);
       }
     }
   }
+  // the solve multiplies by 1/U(k,k): store the reciprocal pivots
+  for (int k = 0; k < n; ++k) {
+    const cd d = band(k, k);
+    const double den = d.x * d.x + d.y * d.y;
+    band(k, k) = mk(d.x / den, -d.y / den);
+  }
 }
 
-// One thread per (mode, column): right-hand side in the interleaved order,
-// gbtrs-style forward and back substitution, scatter to u/v/p spectra.
-__global__ void k_ch_solve(ChanGrid g, const cd* fu, const cd* fv, long long fstride, const cd* lu, const int* piv,
-                           const double* zero, cd* uo, cd* vo, cd* po, long long vstride, long long pstride, cd* work,
-                           int cols, double mass, double visc) {
+// One thread per (mode, column): gbtrs-style forward and back substitution
+// of the mode's factored saddle system, right-hand side in the interleaved
+// order (u_j, continuity_j, v_j), results scattered to the u/v/p spectra.
+// Both sweeps keep the active part of the vector in registers: the forward
+// sweep a window of KL+1 entries (the pivot swap and the updates of step k
+// stay inside b[k..k+KL]), the back sweep the last KL+KU solved entries, so
+// the only dependence between steps is through registers; the factor and the
+// forward results are streamed (mode-interleaved, coalesced).  Divisions by
+// pivots become multiplications by reciprocals formed off the recurrence,
+// and the back sweep subtracts the newest unknown last, so each step adds
+// about five dependent FP64 operations to the chain (GB300's FP64 latency is
+// about 67 cycles and a division about 640).  The mode 0 thread solves
+// hu0 u = fu by Thomas with the same register chaining.
+__global__ void k_ch_solve(ChanGrid g, const cd* __restrict__ fu, const cd* __restrict__ fv, long long fstride,
+                           const cd* __restrict__ lu, const int* __restrict__ piv, const double* __restrict__ zero,
+                           cd* __restrict__ uo, cd* __restrict__ vo, cd* __restrict__ po, long long vstride,
+                           long long pstride, cd* __restrict__ work, int cols, double mass, double visc) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int m = t % g.nm, c = t / g.nm;
   if (c >= cols) return;
@@ -382,86 +405,217 @@ __global__ void k_ch_solve(ChanGrid g, const cd* fu, const cd* fv, long long fst
   cd* uc = uo + c * vstride;
   cd* vc = vo + c * vstride;
   cd* pc = po + c * pstride;
+  // Loads are issued in chunks (U entries of the factor, pivots and inputs
+  // at once, all independent of the recurrence), then the chunk's steps run
+  // on registers: one memory round trip per chunk instead of one per step.
+  const cd z0 = mk(0.0, 0.0);
   if (m == 0) {
+    constexpr int U = 8;
     const double* cp = zero;
     const double* dn = zero + ny;
     const double off = -visc * g.ihy2;
     // hu0 u = fu (Thomas), v = 0, p_{k+1} = p_k + hy fv_k, mean removed
-    cd prev = mk(0.0, 0.0);
-    for (int j = 0; j < ny; ++j) {
-      const cd f = fuc[(long long)j * nm];
-      const cd y = j == 0 ? mk(f.x / dn[0], f.y / dn[0])
-                          : mk((f.x - off * prev.x) / dn[j], (f.y - off * prev.y) / dn[j]);
-      uc[(long long)j * nm] = y;
-      prev = y;
-    }
-    for (int j = ny - 2; j >= 0; --j) {
-      const cd nx1 = uc[(long long)(j + 1) * nm];
-      const cd y = uc[(long long)j * nm];
-      uc[(long long)j * nm] = mk(y.x - cp[j] * nx1.x, y.y - cp[j] * nx1.y);
-    }
-    for (int k = 0; k < ny - 1; ++k) vc[(long long)k * nm] = mk(0.0, 0.0);
-    cd p = mk(0.0, 0.0), sum = mk(0.0, 0.0);
-    for (int j = 0; j < ny; ++j) {
-      if (j > 0) {
-        const cd f = fvc[(long long)(j - 1) * nm];
-        p = mk(p.x + g.hy * f.x, p.y + g.hy * f.y);
+    cd prev = z0;
+    for (int j0 = 0; j0 < ny; j0 += U) {
+      cd f[U];
+      double d[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int j = j0 + u;
+        f[u] = j < ny ? fuc[(long long)j * nm] : z0;
+        d[u] = j < ny ? dn[j] : 1.0;
       }
-      pc[(long long)j * nm] = p;
-      sum = sum + p;
+      double rd[U];  // reciprocal pivots, off the recurrence
+#pragma unroll
+      for (int u = 0; u < U; ++u) rd[u] = 1.0 / d[u];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int j = j0 + u;
+        if (j < ny) {
+          const cd y = j == 0 ? mk(f[u].x * rd[u], f[u].y * rd[u])
+                              : mk((f[u].x - off * prev.x) * rd[u], (f[u].y - off * prev.y) * rd[u]);
+          uc[(long long)j * nm] = y;
+          prev = y;
+        }
+      }
+    }
+    cd next = prev;  // u_{ny-1} = y_{ny-1}
+    for (int j0 = ny - 2; j0 >= 0; j0 -= U) {
+      cd yv[U];
+      double e[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int j = j0 - u;
+        yv[u] = j >= 0 ? uc[(long long)j * nm] : z0;
+        e[u] = j >= 0 ? cp[j] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int j = j0 - u;
+        if (j >= 0) {
+          next = mk(yv[u].x - e[u] * next.x, yv[u].y - e[u] * next.y);
+          uc[(long long)j * nm] = next;
+        }
+      }
+    }
+    for (int k = 0; k < ny - 1; ++k) vc[(long long)k * nm] = z0;
+    cd p = z0, sum = z0;
+    for (int j0 = 0; j0 < ny; j0 += U) {
+      cd f[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int j = j0 + u;
+        f[u] = (j > 0 && j < ny) ? fvc[(long long)(j - 1) * nm] : z0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int j = j0 + u;
+        if (j < ny) {
+          if (j > 0) p = mk(p.x + g.hy * f[u].x, p.y + g.hy * f[u].y);
+          pc[(long long)j * nm] = p;
+          sum = sum + p;
+        }
+      }
     }
     const cd mean = mk(sum.x / ny, sum.y / ny);
+#pragma unroll 8
     for (int j = 0; j < ny; ++j) pc[(long long)j * nm] = pc[(long long)j * nm] - mean;
     return;
   }
+  static_assert(kKL == 3 && kKL + kKU == 6 && kLD == 10, "register windows below are written for KL = KU = 3");
   const int n = 3 * ny - 1;
-  const cd* ab = lu + (long long)(m - 1) * n * kLD;
-  const int* pv = piv + (long long)(m - 1) * n;
-  cd* b = work + ((long long)c * nm + m) * n;
-  for (int j = 0; j < ny; ++j) {
-    b[3 * j] = fuc[(long long)j * nm + m];
-    b[3 * j + 1] = mk(0.0, 0.0);
-    if (j < ny - 1) b[3 * j + 2] = fvc[(long long)j * nm + m];
-  }
-  auto A = [&](int i, int j) { return ab[(long long)j * kLD + (kKL + kKU + i - j)]; };
-  for (int k = 0; k < n; ++k) {
-    const int p = pv[k];
-    if (p != k) {
-      const cd tmp = b[k];
-      b[k] = b[p];
-      b[p] = tmp;
+  const int nmodes = nm - 1, m1 = m - 1;
+  const long long wstride = (long long)cols * nmodes;  // forward results, interleaved over (column, mode)
+  cd* y = work + (long long)c * nmodes + m1;
+  // column k of the factor starts at lu + k * cstep + m1; within it row i
+  // sits at (KL + KU + i - k) * nmodes (band_index)
+  const long long cstep = (long long)kLD * nmodes;
+  const cd* lum = lu + m1;
+  const int* pvm = piv + m1;
+  const int oL1 = 7 * nmodes, oL2 = 8 * nmodes, oL3 = 9 * nmodes;  // L(k+r, k), r = 1..3
+  const int oD = 6 * nmodes;                                          // 1 / U(k, k)
+  const long long fj = nm;                                            // spectrum row stride
+  // forward: L with row interchanges; window w0..w3 = b[k..k+3]
+  auto rhs = [&](int j, int r) -> cd {
+    return r == 0 ? fuc[(long long)j * fj + m] : (r == 1 ? z0 : fvc[(long long)j * fj + m]);
+  };
+  cd w0 = rhs(0, 0), w1 = rhs(0, 1), w2 = n > 2 ? rhs(0, 2) : z0, w3 = n > 3 ? rhs(1, 0) : z0;
+  int jr = 1, rr = 1;  // (j, r) of entry k + 4 = 3 j + r, for k = 0
+  constexpr int UF = 8;
+  for (int k0 = 0; k0 < n; k0 += UF) {
+    int pp[UF];
+    cd l1[UF], l2[UF], l3[UF], in[UF];
+    const cd* col = lum + k0 * cstep;
+#pragma unroll
+    for (int u = 0; u < UF; ++u) {
+      const int k = k0 + u;
+      pp[u] = k < n ? pvm[(long long)k * nmodes] - k : 0;  // 0..KL
+      l1[u] = k + 1 < n ? col[oL1] : z0;
+      l2[u] = k + 2 < n ? col[oL2] : z0;
+      l3[u] = k + 3 < n ? col[oL3] : z0;
+      in[u] = k + 4 < n ? rhs(jr, rr) : z0;
+      col += cstep;
+      if (++rr == 3) {
+        rr = 0;
+        ++jr;
+      }
     }
-    const int km = min(kKL, n - 1 - k);
-    const cd bk = b[k];
-    for (int r = 1; r <= km; ++r) b[k + r] = b[k + r] - cmul(A(k + r, k), bk);
+#pragma unroll
+    for (int u = 0; u < UF; ++u) {
+      const int k = k0 + u;
+      if (k < n) {
+        const int p = pp[u];
+        if (p == 1) { const cd tmp = w0; w0 = w1; w1 = tmp; }
+        else if (p == 2) { const cd tmp = w0; w0 = w2; w2 = tmp; }
+        else if (p == 3) { const cd tmp = w0; w0 = w3; w3 = tmp; }
+        const cd bk = w0;
+        y[(long long)k * wstride] = bk;
+        if (k + 1 < n) w1 = w1 - cmul(l1[u], bk);
+        if (k + 2 < n) w2 = w2 - cmul(l2[u], bk);
+        if (k + 3 < n) w3 = w3 - cmul(l3[u], bk);
+        w0 = w1;
+        w1 = w2;
+        w2 = w3;
+        w3 = in[u];
+      }
+    }
   }
-  for (int k = n - 1; k >= 0; --k) {
-    cd s = b[k];
-    const int last = min(n - 1, k + kKL + kKU);
-    for (int j = k + 1; j <= last; ++j) s = s - cmul(A(k, j), b[j]);
-    const cd pk = A(k, k);
-    const double den = pk.x * pk.x + pk.y * pk.y;
-    b[k] = mk((s.x * pk.x + s.y * pk.y) / den, (s.y * pk.x - s.x * pk.y) / den);
-  }
-  for (int j = 0; j < ny; ++j) {
-    uc[(long long)j * nm + m] = b[3 * j];
-    pc[(long long)j * nm + m] = b[3 * j + 1];
-    if (j < ny - 1) vc[(long long)j * nm + m] = b[3 * j + 2];
+  // back: U (bandwidth KL+KU); window x1..x6 = x[k+1..k+6] (zero past n-1).
+  // U(k, k+1+i) sits at column k's base + (15 + 9 i) * nmodes.
+  cd x1 = z0, x2 = z0, x3 = z0, x4 = z0, x5 = z0, x6 = z0;
+  int jo = (n - 1) / 3, ro = (n - 1) - 3 * ((n - 1) / 3);  // (j, r) of entry k, for k = n - 1
+  constexpr int UB = 4;
+  for (int k0 = n - 1; k0 >= 0; k0 -= UB) {
+    cd yy[UB], rp[UB], a[UB][6];
+    const cd* col = lum + k0 * cstep;
+#pragma unroll
+    for (int u = 0; u < UB; ++u) {
+      const int k = k0 - u;
+      yy[u] = k >= 0 ? y[(long long)k * wstride] : z0;
+      rp[u] = k >= 0 ? col[oD] : z0;
+#pragma unroll
+      for (int i = 0; i < 6; ++i) a[u][i] = (k >= 0 && k + 1 + i < n) ? col[(15 + 9 * i) * nmodes] : z0;
+      col -= cstep;
+    }
+#pragma unroll
+    for (int u = 0; u < UB; ++u) {
+      const int k = k0 - u;
+      if (k >= 0) {
+        // the older entries first, the newest (x_{k+1}) last: one complex
+        // multiply-subtract and the pivot multiply are all that each step
+        // adds to the dependent chain
+        cd s = yy[u];
+        if (k + 6 < n) s = s - cmul(a[u][5], x6);
+        if (k + 5 < n) s = s - cmul(a[u][4], x5);
+        if (k + 4 < n) s = s - cmul(a[u][3], x4);
+        if (k + 3 < n) s = s - cmul(a[u][2], x3);
+        if (k + 2 < n) s = s - cmul(a[u][1], x2);
+        if (k + 1 < n) s = s - cmul(a[u][0], x1);
+        const cd xk = cmul(s, rp[u]);
+        x6 = x5;
+        x5 = x4;
+        x4 = x3;
+        x3 = x2;
+        x2 = x1;
+        x1 = xk;
+        const long long o = (long long)jo * fj + m;
+        if (ro == 0) uc[o] = xk;
+        else if (ro == 1) pc[o] = xk;
+        else vc[o] = xk;
+        if (--ro < 0) {
+          ro = 2;
+          --jo;
+        }
+      }
+    }
   }
   (void)mass;
 }
 
-// pressure -= mean over all cells, per column (fft_stokes.py:122)
-__global__ void k_ch_center(double* p, int np, double* partial) {
+// pressure -= mean over all cells, per column (fft_stokes.py:122), in two
+// launches over (kChCenterBlocks, column): block sums, then every block folds
+// the column's block sums in the same fixed order and shifts its part.
+constexpr int kChCenterBlocks = 128;
+__global__ void k_ch_center_sums(const double* p, int np, double* partial) {
   __shared__ double red[32];
-  const int c = blockIdx.x;
+  const int c = blockIdx.y;
   double s[1] = {0.0};
-  for (int i = threadIdx.x; i < np; i += blockDim.x) s[0] += p[(long long)c * np + i];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
+    s[0] += p[(long long)c * np + i];
   block_sum<1>(s, red);
+  if (threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = s[0];
+}
+__global__ void k_ch_center_shift(double* p, int np, const double* partial) {
   __shared__ double mean;
-  if (threadIdx.x == 0) mean = s[0] / np;
+  const int c = blockIdx.y;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int b = 0; b < gridDim.x; ++b) t += partial[c * gridDim.x + b];
+    mean = t / np;
+  }
   __syncthreads();
-  for (int i = threadIdx.x; i < np; i += blockDim.x) p[(long long)c * np + i] -= mean;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
+    p[(long long)c * np + i] -= mean;
 }
 
 // Closing checks (fft_stokes.py:124-131): max|defect|, max|f|, max|u|,
@@ -757,8 +911,9 @@ int macsav_channel_solve(macsav_channel* h, const double* rhs, int cols, double 
         return ch_cuda(&C);
     }
     cudaMemsetAsync(C.status, 0, sizeof(int), s);
-    macsav::k_ch_factor<<<(g.nm + 63) / 64, 64, 0, s>>>(g, mass, viscosity, fresh.lu, fresh.piv, fresh.zero,
-                                                        C.status);
+    const int tpb = macsav::kChSolveThreads;
+    macsav::k_ch_factor<<<(g.nm + tpb - 1) / tpb, tpb, 0, s>>>(g, mass, viscosity, fresh.lu, fresh.piv, fresh.zero,
+                                                              C.status);
     cudaMemcpyAsync(C.h_status, C.status, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return ch_cuda(&C);
     if (C.h_status[0] != 0) {
@@ -777,14 +932,21 @@ int macsav_channel_solve(macsav_channel* h, const double* rhs, int cols, double 
   // forward FFTs of the loads (u rows then v rows: one (2ny-1) x nx matrix)
   launch_fft(&C, false, rhs, g.size, rows, C.fspec, fstride, cols, s);
   // mode solves into u/v spectra (uspec: u rows then v rows) and pspec
+  // Each thread is one long sequential recurrence on the narrow FP64 pipe:
+  // few threads per CTA spread them over as many SMs as possible.
   const int threads = g.nm * cols;
-  macsav::k_ch_solve<<<(threads + 63) / 64, 64, 0, s>>>(g, C.fspec, C.fspec + (long long)g.ny * g.nm, fstride,
+  const int tpb = macsav::kChSolveThreads;
+  macsav::k_ch_solve<<<(threads + tpb - 1) / tpb, tpb, 0, s>>>(g, C.fspec, C.fspec + (long long)g.ny * g.nm, fstride,
                                                         slot->lu, slot->piv, slot->zero, C.uspec,
                                                         C.uspec + (long long)g.ny * g.nm, C.pspec, fstride,
                                                         (long long)g.ny * g.nm, C.work, cols, mass, viscosity);
   launch_fft(&C, true, C.uspec, fstride, rows, vel, g.size, cols, s);
   launch_fft(&C, true, C.pspec, (long long)g.ny * g.nm, g.ny, pres, g.np, cols, s);
-  macsav::k_ch_center<<<cols, macsav::kChThreads, 0, s>>>(pres, g.np, nullptr);
+  {
+    const int nbc = std::max(1, std::min(macsav::kChCenterBlocks, 2048 / cols));  // C.partial holds 2048 sums
+    macsav::k_ch_center_sums<<<dim3(nbc, cols), macsav::kChThreads, 0, s>>>(pres, g.np, C.partial);
+    macsav::k_ch_center_shift<<<dim3(nbc, cols), macsav::kChThreads, 0, s>>>(pres, g.np, C.partial);
+  }
   cudaMemsetAsync(C.keys, 0, sizeof(unsigned long long) * 5 * cols, s);
   const int n = g.size > g.np ? g.size : g.np;
   macsav::k_ch_check<<<dim3(ch_grid_blocks(n), cols), macsav::kChThreads, 0, s>>>(g, vel, pres, rhs, mass,
