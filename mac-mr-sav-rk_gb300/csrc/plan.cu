@@ -195,6 +195,7 @@ int plan_build(Plan* p) {
     if (p->precision == MACSAV_FP32_MIXED) {
       if ((e = cudaMalloc(&p->cells32, sizeof(float) * np * C * 6))) goto fail;
       if ((e = cudaMalloc(&p->w32, sizeof(float) * size * C))) goto fail;
+      if ((e = cudaMalloc(&p->wacc32, sizeof(float) * size * C))) goto fail;
     }
     p->partial_len = size_t(C) * 8 * 4096;
     if ((e = cudaMalloc(&p->partial, sizeof(double) * p->partial_len))) goto fail;
@@ -239,7 +240,7 @@ void plan_free(Plan* p) {
   step_free(p);
   free_transforms(p->t64);
   free_transforms(p->t32);
-  cudaFree(p->w); cudaFree(p->vel); cudaFree(p->cells); cudaFree(p->cells32); cudaFree(p->w32);
+  cudaFree(p->w); cudaFree(p->vel); cudaFree(p->cells); cudaFree(p->cells32); cudaFree(p->w32); cudaFree(p->wacc32);
   cudaFree(p->partial); cudaFree(p->partial2); cudaFree(p->cg); cudaFree(p->checks); cudaFree(p->active); cudaFree(p->shift);
   cudaFree(p->errword);
   cudaFree(p->done_counter);
@@ -258,7 +259,7 @@ void plan_free(Plan* p) {
   if (p->evc) cudaEventDestroy(p->evc);
   p->evc = nullptr;
   p->w = p->vel = p->cells = p->partial = p->partial2 = p->shift = nullptr;
-  p->cells32 = p->w32 = nullptr;
+  p->cells32 = p->w32 = p->wacc32 = nullptr;
   p->cg = nullptr; p->checks = nullptr; p->active = p->errword = nullptr;
   p->h_cg = nullptr; p->h_checks = nullptr; p->h_active = p->h_err = nullptr;
   p->done = nullptr;

@@ -103,6 +103,7 @@ struct Plan {
   double* cells = nullptr;  // 6 cell-sized vectors per column: b x r z p q
   float* cells32 = nullptr; // float CG vectors (mixed path)
   float* w32 = nullptr;
+  float* wacc32 = nullptr;  // velocity of an FP32 inner solve, accumulated inside its CG (mixed path)
   double* partial = nullptr;
   size_t partial_len = 0;
   CGScalars* cg = nullptr;

@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(kThreads) k_div_q(GridDev g, const WIn* w, lon
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_cg_update(int np, T* x, T* r, T* p, const T* z, const T* q, T* r_old,
                                                         long long cs, const CGScalars* cg, const int* active,
-                                                        double* partial, CGFin<T> fin, unsigned int* done) {
+                                                        double* partial, CGFin<T> fin, unsigned int* done,
+                                                        const T* wv, T* wacc, long long vsz) {
   pdl_wait();
   const int c = blockIdx.y;
   Acc<T> acc[1];
@@ -138,6 +139,12 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int np, T* x, T* r, T* p
       const T rv = ro - alpha * (q[k] - mq);
       r[k] = rv;
       acc[0].add(rv * rv);
+    }
+    // the velocity follows x: wacc += alpha (mI+kK)^{-1} D^T pdir (wv holds
+    // that velocity for this iteration's direction)
+    if (wacc) {
+      for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vsz; i += (long long)gridDim.x * blockDim.x)
+        wacc[c * vsz + i] += alpha * wv[c * vsz + i];
     }
   }
   write_sums<T, 1>(acc, partial, 1);
@@ -299,7 +306,7 @@ static void velocity_inverse(Plan* P, const Launcher<T>& L, Src src, Out* dst, l
 // the learned preconditioner (X.net, FP32 only) z = M r + net(r), projected to
 // mean zero, and beta is the Polak-Ribiere form of flexible CG.
 template <typename T>
-static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* cells, int cols) {
+static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* cells, int cols, T* wacc) {
   const GridDev& g = P->g;
   const long long np = g.np, sz = g.size;
   T* b = cells;
@@ -343,7 +350,8 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
   launch_k(k_div_q<T, T>, dim3(rb, cols), kThreads, 0, s, g, w, sz, q, z, pd, np, P->cg, P->active, P->partial,
                                                     make_fin<T>(P, X, OP_ALPHA, rb, 3, cols), P->done_counter);
   launch_k(k_cg_update<T>, dim3(rb, cols), kThreads, 0, s, g.np, x, r, pd, z, q, r_old, np, P->cg, P->active, P->partial,
-                                                     make_fin<T>(P, X, OP_CHECK, rb, 1, cols), P->done_counter);
+                                                     make_fin<T>(P, X, OP_CHECK, rb, 1, cols), P->done_counter,
+                                                     static_cast<const T*>(w), wacc, sz);
   P->launches += 2;
 }
 
@@ -351,7 +359,8 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
 // On entry w holds (mI+kK)^{-1} f in T; on exit x holds the pressure iterate
 // and P->cg the per-column counters.
 template <typename T>
-static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int cols, const double* rd = nullptr) {
+static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int cols, const double* rd = nullptr,
+                     T* wacc = nullptr) {
   const GridDev& g = P->g;
   const long long np = g.np, sz = g.size;
   T* b = cells;
@@ -359,7 +368,8 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
   T* r = cells + 2 * np * cols;
   const int rb = red_blocks(np);
   const cudaStream_t s = X.s;
-  launch_k(k_pressure_rhs<T, T>, dim3(rb, cols), kThreads, 0, s, g, w, sz, b, np, rd, P->partial,
+  launch_k(k_pressure_rhs<T, T>, dim3(rb, cols), kThreads, 0, s, g, static_cast<const T*>(wacc ? wacc : w), sz, b, np,
+           rd, P->partial,
                                                            make_fin<T>(P, X, OP_MEAN_B, rb, 1, cols), P->done_counter);
   ++P->launches;
   if (!X.graph) {
@@ -384,7 +394,7 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
                           cudaMemcpyDeviceToDevice, s);
         }
       }
-      cg_iteration<T>(P, X, L, w, cells, cols);
+      cg_iteration<T>(P, X, L, w, cells, cols, wacc);
       if constexpr (std::is_same<T, double>::value) {
         if (log) {
           cudaMemcpyAsync(P->log_z + P->log_n * np, cells + 3 * np * cols, sizeof(double) * np,
@@ -431,7 +441,7 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
   Launcher<T> Ls{L.t, X.side, L.counter, P->aux[1], P->evf[1], P->evj[1]};
   Exec Xs = X;
   Xs.s = X.side;
-  cg_iteration<T>(P, Xs, Ls, w, cells, cols);
+  cg_iteration<T>(P, Xs, Ls, w, cells, cols, wacc);
   cudaGraph_t captured;
   if (cudaStreamEndCapture(X.side, &captured) != cudaSuccess) return MACSAV_ERR_CUDA;
   return MACSAV_OK;
@@ -524,6 +534,23 @@ __global__ void __launch_bounds__(kThreads) k_defect64(GridDev g, const double* 
   }
 }
 
+// vel (+)= double(u) over sz and pres (+)= double(x) over np elements per
+// column: the closing accumulation of an FP32 inner solve.
+__global__ void __launch_bounds__(kThreads) k_accumulate_sweep(const float* u, double* vel, long long sz, const float* x,
+                                                               double* pres, long long np, int add) {
+  pdl_wait();
+  const int c = blockIdx.y;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < sz; i += stride) {
+    const long long k = c * sz + i;
+    vel[k] = add ? vel[k] + double(u[k]) : double(u[k]);
+  }
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += stride) {
+    const long long k = c * np + i;
+    pres[k] = add ? pres[k] + double(x[k]) : double(x[k]);
+  }
+}
+
 // dst (+)= double(src) over n elements per column.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_accumulate(const T* src, double* dst, long long n, int add) {
@@ -536,25 +563,43 @@ __global__ void __launch_bounds__(kThreads) k_accumulate(const T* src, double* d
 }
 
 // One FP32 Stokes solve of (ru, rd): transforms, stencils and Krylov vectors
-// in float, reductions in double.  Its velocity is added to the FP64 `vel`
-// by the last inverse pass (set when add = 0) and its pressure x to the FP64
-// `pres` by a kernel at the head of the v chain of that velocity inverse.
+// in float, reductions in double.  Its velocity and pressure are added to
+// the FP64 `vel` and `pres` (set when add = 0).
+//
+// Plain PCG: the velocity is accumulated inside the CG, u = (mI+kK)^{-1} ru
+// + sum_k alpha_k (mI+kK)^{-1} D^T pdir_k, from the velocity each iteration
+// computes anyway (k_cg_update), so no closing velocity inverse
+// (mI+kK)^{-1}(ru + D^T x) is needed; one kernel adds u and x to the FP64
+// fields.  The same vector in exact arithmetic; in float it differs at
+// rounding level, which the FP64 defect correction absorbs like any other
+// inner-solve error.  With the learned preconditioner (flexible CG, whose
+// columns may restart) the closing velocity inverse is kept.
 static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, int cols, double* vel, double* pres,
                          int add) {
   const GridDev& g = P->g;
   Launcher<float> L{P->t32, X.s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
   const long long sz = g.size, np = g.np;
   float* w = P->w32;
-  velocity_inverse<float>(P, L, SrcPacked<float, double>{ru, sz, g.nu, g.nx - 1, g.nx}, w, sz, cols, nullptr);
+  const bool net = P->net != nullptr;
+  float* wacc = net ? nullptr : P->wacc32;
+  velocity_inverse<float>(P, L, SrcPacked<float, double>{ru, sz, g.nu, g.nx - 1, g.nx}, wacc ? wacc : w, sz, cols,
+                          nullptr);
   const double keep = X.ktol;
   const int keep_net = X.net;
   X.ktol = P->inner_ktol;
-  X.net = P->net ? 1 : 0;
-  int rc = schur_pcg<float>(P, X, L, w, P->cells32, cols, rd);
+  X.net = net ? 1 : 0;
+  int rc = schur_pcg<float>(P, X, L, w, P->cells32, cols, rd, wacc);
   X.ktol = keep;
   X.net = keep_net;
   if (rc != MACSAV_OK) return rc;
   const float* x = P->cells32 + 1 * np * cols;
+  if (wacc) {
+    const int nb = red_blocks(sz);
+    launch_k(k_accumulate_sweep, dim3(nb, cols), kThreads, 0, X.s, static_cast<const float*>(wacc), vel, sz, x, pres,
+             np, add);
+    ++P->launches;
+    return MACSAV_OK;
+  }
   const int nbp = red_blocks(np);
   auto add_pressure = [&](cudaStream_t st) {
     launch_k(k_accumulate<float>, dim3(nbp, cols), kThreads, 0, st, x, pres, np, add);
