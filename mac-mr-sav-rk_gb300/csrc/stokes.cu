@@ -424,6 +424,12 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
   launch_k(k_cg_start<T>, dim3(rb, cols), kThreads, 0, s, g.np, b, x, r, np, P->cg, P->partial,
                                                     make_fin<T>(P, X, OP_START, rb, 2, cols), P->done_counter);
   ++P->launches;
+  // The first iteration outside the loop: its kernels are predicated on the
+  // columns' flags like the loop body's (a column that is already converged,
+  // e.g. a zero right-hand side, does nothing), its convergence check sets
+  // the loop condition, and nearly every solve needs it, so one conditional
+  // body launch per solve is saved.
+  cg_iteration<T>(P, X, L, w, cells, cols, wacc);
   if (cudaStreamGetCaptureInfo(s, &st, nullptr, &graph, &deps, nullptr, &ndeps) != cudaSuccess)
     return MACSAV_ERR_CUDA;
   cudaGraphNodeParams cp = {};
