@@ -496,14 +496,16 @@ int enqueue_solve_fp64(Plan* P, Exec& X, const double* f, int cols, double* vel,
   const GridDev& g = P->g;
   Launcher<double> L{P->t64, X.s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
   const long long sz = g.size;
-  velocity_inverse<double>(P, L, SrcPacked<double, double>{f, sz, g.nu, g.nx - 1, g.nx}, P->w, sz, cols, nullptr);
-  int rc = schur_pcg<double>(P, X, L, P->w, P->cells, cols);
+  // u = (mI + kK)^{-1} (f + D^T p) (tensor_stokes.py:331-336), accumulated
+  // alongside p inside the CG: vel starts as (mI+kK)^{-1} f and each update
+  // adds alpha (mI+kK)^{-1} D^T pdir, the velocity the iteration computed for
+  // its direction.  The same vector as the reference's closing inverse, to
+  // rounding (D^T of the pressure mean is zero, so the centring does not
+  // enter), without its three transform passes.
+  velocity_inverse<double>(P, L, SrcPacked<double, double>{f, sz, g.nu, g.nx - 1, g.nx}, vel, sz, cols, nullptr);
+  int rc = schur_pcg<double>(P, X, L, P->w, P->cells, cols, nullptr, vel);
   if (rc != MACSAV_OK) return rc;
   finish_pressure<double>(P, X, P->cells + 1LL * g.np * cols, pres, cols);
-  // u = (mI + kK)^{-1} (f + D^T p)
-  velocity_inverse<double>(
-      P, L, SrcLift<double, double, double>{f, sz, pres, nullptr, P->cg, (long long)g.np, g.nx, g.nu, g.ihx, g.ihy},
-      vel, sz, cols, nullptr);
   if (close) closing_checks(P, X, f, vel, pres, cols, P->shift);
   return MACSAV_OK;
 }
