@@ -756,7 +756,7 @@ def main() -> None:
         "e2e": {"value": e2e_value, "unit": "cell-stage/s", "h2d_bytes_per_step": face_bytes,
                 "d2h_bytes_per_step": face_bytes + w["stages_per_step"] * rec_bytes},
         "gpu_launches": int(l32 * args.steps),
-        "roofline": {"kernel": "k_column<float> (velocity blocks, 2 RHS)", "bound": "hbm",
+        "roofline": {"kernel": "k_column_p2<float> (velocity blocks, 2 RHS)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": "measured" if pk.exists() else "fallback",
                      "traffic": traffic, "bytes_per_launch": bytes_k.value, "ms_per_launch": ms_k.value},

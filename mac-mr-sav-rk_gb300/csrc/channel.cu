@@ -395,7 +395,7 @@ __global__ void k_ch_factor(ChanGrid g, double mass, double visc, cd* lu, int* p
 __global__ void k_ch_solve(ChanGrid g, const cd* __restrict__ fu, const cd* __restrict__ fv, long long fstride,
                            const cd* __restrict__ lu, const int* __restrict__ piv, const double* __restrict__ zero,
                            cd* __restrict__ uo, cd* __restrict__ vo, cd* __restrict__ po, long long vstride,
-                           long long pstride, cd* __restrict__ work, int cols, double mass, double visc) {
+                           long long pstride, cd* __restrict__ work, int cols, double visc) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int m = t % g.nm, c = t / g.nm;
   if (c >= cols) return;
@@ -589,7 +589,6 @@ __global__ void k_ch_solve(ChanGrid g, const cd* __restrict__ fu, const cd* __re
       }
     }
   }
-  (void)mass;
 }
 
 // pressure -= mean over all cells, per column (fft_stokes.py:122), in two
@@ -939,7 +938,7 @@ int macsav_channel_solve(macsav_channel* h, const double* rhs, int cols, double 
   macsav::k_ch_solve<<<(threads + tpb - 1) / tpb, tpb, 0, s>>>(g, C.fspec, C.fspec + (long long)g.ny * g.nm, fstride,
                                                         slot->lu, slot->piv, slot->zero, C.uspec,
                                                         C.uspec + (long long)g.ny * g.nm, C.pspec, fstride,
-                                                        (long long)g.ny * g.nm, C.work, cols, mass, viscosity);
+                                                        (long long)g.ny * g.nm, C.work, cols, viscosity);
   launch_fft(&C, true, C.uspec, fstride, rows, vel, g.size, cols, s);
   launch_fft(&C, true, C.pspec, (long long)g.ny * g.nm, g.ny, pres, g.np, cols, s);
   {

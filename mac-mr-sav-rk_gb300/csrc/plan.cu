@@ -190,7 +190,6 @@ int plan_build(Plan* p) {
     const int C = p->maxcols;
     const size_t size = g.size, np = g.np;
     if ((e = cudaMalloc(&p->w, sizeof(double) * size * C))) goto fail;
-    if ((e = cudaMalloc(&p->vel, sizeof(double) * size * C))) goto fail;
     if ((e = cudaMalloc(&p->cells, sizeof(double) * np * C * 6))) goto fail;
     if (p->precision == MACSAV_FP32_MIXED) {
       if ((e = cudaMalloc(&p->cells32, sizeof(float) * np * C * 6))) goto fail;
@@ -240,7 +239,7 @@ void plan_free(Plan* p) {
   step_free(p);
   free_transforms(p->t64);
   free_transforms(p->t32);
-  cudaFree(p->w); cudaFree(p->vel); cudaFree(p->cells); cudaFree(p->cells32); cudaFree(p->w32); cudaFree(p->wacc32);
+  cudaFree(p->w); cudaFree(p->cells); cudaFree(p->cells32); cudaFree(p->w32); cudaFree(p->wacc32);
   cudaFree(p->partial); cudaFree(p->partial2); cudaFree(p->cg); cudaFree(p->checks); cudaFree(p->active); cudaFree(p->shift);
   cudaFree(p->errword);
   cudaFree(p->done_counter);
@@ -258,7 +257,7 @@ void plan_free(Plan* p) {
   }
   if (p->evc) cudaEventDestroy(p->evc);
   p->evc = nullptr;
-  p->w = p->vel = p->cells = p->partial = p->partial2 = p->shift = nullptr;
+  p->w = p->cells = p->partial = p->partial2 = p->shift = nullptr;
   p->cells32 = p->w32 = p->wacc32 = nullptr;
   p->cg = nullptr; p->checks = nullptr; p->active = p->errword = nullptr;
   p->h_cg = nullptr; p->h_checks = nullptr; p->h_active = p->h_err = nullptr;

@@ -99,7 +99,6 @@ struct Plan {
 
   // work buffers (column-blocked, maxcols columns)
   double* w = nullptr;      // packed velocity scratch
-  double* vel = nullptr;    // packed velocity scratch 2
   double* cells = nullptr;  // 6 cell-sized vectors per column: b x r z p q
   float* cells32 = nullptr; // float CG vectors (mixed path)
   float* w32 = nullptr;
