@@ -683,6 +683,27 @@ def main() -> None:
     # both trajectories start from the same field and take the same steps
     diff = float(torch.linalg.vector_norm(x32 - x64) / torch.linalg.vector_norm(x64))
 
+    # the workload's full run (200 steps) in both forms, the FP32-bulk error
+    # against FP64 every 20 steps (outside the timed region)
+    def trajectory_errors(steps: int = 200, every: int = 20) -> list:
+        ms = {p: pkg.MACNavierStokes(g, w["nu"], precision=p, use_graph=True) for p in ("fp32", "fp64")}
+        sch = pkg.make_scheme(w["scheme"])
+        xs = {p: torch.from_numpy(x0_host.copy()).to(dev) for p in ms}
+        ys = {p: torch.empty_like(xs[p]) for p in ms}
+        ps = torch.empty((4, g.np), dtype=torch.float64, device=dev)
+        rs = {p: 0.0 for p in ms}
+        out = []
+        for k in range(1, steps + 1):
+            for p in ms:
+                ys[p], rs[p], _, _, _ = sch.step_device(ms[p], xs[p], (k - 1) * w["dt"], rs[p], w["dt"], x1=ys[p],
+                                                        pres=ps, want_embedded=False)
+                xs[p], ys[p] = ys[p], xs[p]
+            if k % every == 0:
+                out.append(float(torch.linalg.vector_norm(xs["fp32"] - xs["fp64"]) / torch.linalg.vector_norm(xs["fp64"])))
+        return out
+
+    traj = trajectory_errors() if rank == 0 else []
+
     # max over ranks of the timed totals
     tot = torch.tensor([ms32, ms64], dtype=torch.float64, device=dev)
     if world > 1:
@@ -750,7 +771,8 @@ def main() -> None:
                    "l2": "flushed (256 MiB write) before every timed step", "graph": "one CUDA graph per step"},
         "fp64": {"value": value64, "ms_per_step": ms64 / args.steps, "unit": "cell-stage/s"},
         "speedup_vs_fp64": value / value64,
-        "error_vs_fp64": {"rel_l2_velocity": diff, "after_steps": args.warmup + args.steps},
+        "error_vs_fp64": {"rel_l2_velocity": diff, "after_steps": args.warmup + args.steps,
+                          "trajectory_200_steps_every_20": traj},
         "cg_iterations_mean": mean_iters,
         "clocks": clk32,
         "e2e": {"value": e2e_value, "unit": "cell-stage/s", "h2d_bytes_per_step": face_bytes,
