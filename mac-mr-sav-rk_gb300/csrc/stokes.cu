@@ -648,22 +648,29 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
 }
 
 // Average device time of `reps` launches of one transform pass over the
-// velocity blocks (two right-hand sides), with its algorithmic bytes per
-// launch (each element of the pass's input read once and output written once).
+// velocity blocks (two right-hand sides, u and v concurrently), replayed from
+// a captured graph, with its algorithmic bytes per launch (each element of the
+// pass's input read once and output written once).
 //   pass 0: FP32 column pass; 1: FP32 forward row pass (FP64 packed input);
 //   2: FP32 inverse row pass; 3: FP64 column pass.
-int time_pass(Plan* P, int pass, int reps, cudaStream_t s, double* ms, double* bytes) {
+int time_pass(Plan* P, int pass, int reps, cudaStream_t user, double* ms, double* bytes) {
   const GridDev& g = P->g;
   const int cols = 2;
   if (P->maxcols < 2 || reps < 1 || pass < 0 || pass > 3) return MACSAV_ERR_VALUE;
   if (pass < 3 && P->precision != MACSAV_FP32_MIXED) return MACSAV_ERR_VALUE;
-  const double shift[4] = {1.0, 1e-6, 1.0, 1e-6};
-  cudaMemcpyAsync(P->shift, shift, sizeof shift, cudaMemcpyHostToDevice, s);
+  // a capturable stream of our own (the caller's may be the legacy stream),
+  // ordered after the caller's work
+  cudaStream_t s;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return MACSAV_ERR_CUDA;
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
+  cudaEventRecord(a, user);
+  cudaStreamWaitEvent(s, a, 0);
+  const double shift[4] = {1.0, 1e-6, 1.0, 1e-6};
+  cudaMemcpyAsync(P->shift, shift, sizeof shift, cudaMemcpyHostToDevice, s);
   const double n = double(g.size) * cols;
-  auto run = [&](int k) {
+  auto run = [&]() {
     if (pass == 0) Launcher<float>{P->t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.column_uv(cols, nullptr, P->shift);
     else if (pass == 1)
       Launcher<float>{P->t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.row_forward_uv(SrcPacked<float, double>{P->w, g.size, g.nu, g.nx - 1,
@@ -672,17 +679,33 @@ int time_pass(Plan* P, int pass, int reps, cudaStream_t s, double* ms, double* b
       Launcher<float>{P->t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.row_inverse_uv(DstPacked<float, float>{P->w32, g.size, g.nu,
                                                                                       g.nx - 1, g.nx}, cols, nullptr);
     else Launcher<double>{P->t64, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.column_uv(cols, nullptr, P->shift);
-    (void)k;
   };
-  run(0);  // warm-up
-  cudaEventRecord(a, s);
-  for (int k = 0; k < reps; ++k) run(k);
-  cudaEventRecord(b, s);
-  cudaError_t e = cudaEventSynchronize(b);
+  run();  // warm-up
+  // the reps are captured into one graph and replayed, as the pass runs
+  // inside the captured step (u and v blocks concurrently, no host gaps)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    for (int k = 0; k < reps; ++k) run();
+    e = cudaStreamEndCapture(s, &graph);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);  // warm
+  if (e == cudaSuccess) {
+    cudaEventRecord(a, s);
+    e = cudaGraphLaunch(exec, s);
+    cudaEventRecord(b, s);
+  }
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
   float t = 0;
-  cudaEventElapsedTime(&t, a, b);
+  if (e == cudaSuccess) cudaEventElapsedTime(&t, a, b);
+  cudaStreamSynchronize(s);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
   cudaEventDestroy(a);
   cudaEventDestroy(b);
+  cudaStreamDestroy(s);
   *ms = double(t) / reps;
   *bytes = pass == 0 ? 2 * 4 * n : (pass == 1 ? (8 + 4) * n : (pass == 2 ? (4 + 4) * n : 2 * 8 * n));
   return e == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
