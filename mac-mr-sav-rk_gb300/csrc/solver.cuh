@@ -44,6 +44,24 @@ struct SrcCells {
   __device__ T operator()(int, int c, int row, int n) const { return load_as<T>(x + c * cstride + (long long)row * nx + n); }
 };
 
+// r = b - mean(b) for the first CG iteration of a fused start (the source of
+// the preconditioner's row pass, which reads every element once, also
+// stores r).
+template <typename T>
+struct SrcCellsStart {
+  const T* b;
+  T* r;
+  const CGScalars* cg;
+  long long cstride;
+  int nx;
+  __device__ T operator()(int, int c, int row, int n) const {
+    const long long k = c * cstride + (long long)row * nx + n;
+    const T v = b[k] - cg_mean_b<T>(cg[c]);
+    r[k] = v;
+    return v;
+  }
+};
+
 // f + D^T P with P = p1 (+ beta p2 after the first CG iteration), on u/v rows.
 template <typename T, typename FIn, typename PIn>
 struct SrcLift {
@@ -132,7 +150,7 @@ struct DstCellsDot {
 };
 
 // ------------------------------------------------------- Krylov scalars ---
-enum ScalarOp : int { OP_MEAN_B, OP_START, OP_RHO, OP_ALPHA, OP_CHECK, OP_MEAN_X, OP_CHECKS, OP_FCG };
+enum ScalarOp : int { OP_MEAN_B, OP_START, OP_RHO, OP_ALPHA, OP_CHECK, OP_MEAN_X, OP_CHECKS, OP_FCG, OP_START_RHS };
 
 // Block-wide fold of the K-slot partials of `nb` blocks per column in a
 // fixed order, then thread 0 updates each column's scalars.  Sum slots hold
@@ -156,7 +174,9 @@ struct CGFin {
   int use_net, net_maxit;
   double inv_np;
 
-  __device__ int maxmask() const { return op == OP_START ? 0x2 : (op == OP_CHECKS ? 0x3f : 0); }
+  __device__ int maxmask() const {
+    return op == OP_START ? 0x2 : (op == OP_CHECKS ? 0x3f : (op == OP_START_RHS ? 0x4 : 0));
+  }
 
   // One warp per (column, slot) folds that slot's nb block partials (lane
   // stride, then a shuffle tree: a fixed order), so all columns and slots are
@@ -192,7 +212,7 @@ struct CGFin {
       const int c = threadIdx.x;
       if (!(gated && !active[c])) update(c, vals[c], vals[c]);
     }
-    if (use_cond && (op == OP_START || op == OP_CHECK)) {
+    if (use_cond && (op == OP_START || op == OP_CHECK || op == OP_START_RHS)) {
       __syncthreads();
       if (threadIdx.x == 0) {
         int a = 0;
@@ -200,6 +220,23 @@ struct CGFin {
         cudaGraphSetConditional(cond, a ? 1u : 0u);
       }
     }
+  }
+
+  // CG start from ||b||^2 = rr (bnorm and max_b set)
+  __device__ void start(int c, CGScalars& g, double rr) const {
+    g.atol = ktol * g.bnorm;  // _get_atol_rtol: max(atol=0, rtol*||b||)
+    g.atol2 = g.atol * g.atol;
+    g.iters = 0;
+    g.info = 0;
+    g.rho_prev = 0;
+    g.beta = 0;
+    g.beta_t = 0.0f;
+    g.rr = rr;
+    g.net_on = use_net;
+    g.restart = 0;
+    // zero RHS (tensor_stokes.py:309-311) or already converged: no update
+    const bool go = (g.max_b != 0.0) && !(sqrt(g.rr) < g.atol) && (g.bnorm == g.bnorm);
+    active[c] = go ? 1 : 0;
   }
 
   // s[k] / m[k]: the folded sum / maximum of slot k (one array, per maxmask)
@@ -210,22 +247,18 @@ struct CGFin {
         g.mean_b = s[0] * inv_np;
         g.mean_b_t = float(g.mean_b);
         break;
+      case OP_START_RHS:  // fused pressure right-hand side and start (FP32 inner solves):
+        // sums of b and b^2 and max|b| of the uncentred b; ||b - mean|| from them
+        g.mean_b = s[0] * inv_np;
+        g.mean_b_t = float(g.mean_b);
+        g.bnorm = sqrt(fmax(s[1] - s[0] * g.mean_b, 0.0));
+        g.max_b = m[2];
+        start(c, g, g.bnorm * g.bnorm);
+        break;
       case OP_START: {
         g.bnorm = sqrt(s[0]);
         g.max_b = m[1];
-        g.atol = ktol * g.bnorm;  // _get_atol_rtol: max(atol=0, rtol*||b||)
-        g.atol2 = g.atol * g.atol;
-        g.iters = 0;
-        g.info = 0;
-        g.rho_prev = 0;
-        g.beta = 0;
-        g.beta_t = 0.0f;
-        g.rr = s[0];
-        g.net_on = use_net;
-        g.restart = 0;
-        // zero RHS (tensor_stokes.py:309-311) or already converged: no update
-        const bool go = (g.max_b != 0.0) && !(sqrt(g.rr) < g.atol) && (g.bnorm == g.bnorm);
-        active[c] = go ? 1 : 0;
+        start(c, g, s[0]);
         break;
       }
       case OP_RHO:

@@ -89,6 +89,38 @@ __global__ void __launch_bounds__(kThreads) k_cg_start(int np, T* b, T* x, T* r,
   last_block_finish(fin, done);
 }
 
+// Fused start of an FP32 inner solve: b = rd - D w (stored uncentred);
+// last block: mean, ||b - mean|| and max|b| and the CG start (OP_START_RHS).
+// The first iteration's preconditioner pass forms r = b - mean (SrcCellsStart),
+// so no separate start kernel runs.
+template <typename T, typename WIn>
+__global__ void __launch_bounds__(kThreads) k_pressure_rhs_start(GridDev g, const WIn* w, long long ws, T* b, T* x,
+                                                                 long long cs, const double* rd, double* partial,
+                                                                 CGFin<T> fin, unsigned int* done) {
+  pdl_wait();
+  const int c = blockIdx.y;
+  const T ihx = T(g.ihx), ihy = T(g.ihy);
+  Acc<T> acc[2];
+  T mt = T(0);
+  bool bad = false;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < g.np; idx += gridDim.x * blockDim.x) {
+    const int j = idx / g.nx, i = idx - j * g.nx;
+    T v = -D_atT<T>(w + c * ws, g, j, i, ihx, ihy);
+    if (rd) v += load_as<T>(rd + c * (long long)g.np + idx);
+    b[c * cs + idx] = v;
+    x[c * cs + idx] = T(0);  // x0 = 0 (also the answer of a column that never starts)
+    acc[0].add(v);
+    acc[1].add(v * v);
+    const T av = v < T(0) ? -v : v;
+    bad |= !(av == av);
+    mt = av > mt ? av : mt;
+  }
+  unsigned long long key[1] = {bad ? 0x7ff8000000000000ull : abs_key_t<T>(mt)};
+  write_sums<T, 2>(acc, partial, 3);
+  write_keys<1>(key, partial, 3, 2);
+  last_block_finish(fin, done);
+}
+
 // q = D w; last block: alpha from p.q, sum q, sum p (OP_ALPHA), p = z + beta p.
 template <typename T, typename WIn>
 __global__ void __launch_bounds__(kThreads) k_div_q(GridDev g, const WIn* w, long long ws, T* q, const T* z, const T* p,
@@ -306,7 +338,8 @@ static void velocity_inverse(Plan* P, const Launcher<T>& L, Src src, Out* dst, l
 // the learned preconditioner (X.net, FP32 only) z = M r + net(r), projected to
 // mean zero, and beta is the Polak-Ribiere form of flexible CG.
 template <typename T>
-static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* cells, int cols, T* wacc) {
+static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* cells, int cols, T* wacc,
+                         bool fused_first = false) {
   const GridDev& g = P->g;
   const long long np = g.np, sz = g.size;
   T* b = cells;
@@ -329,7 +362,8 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
   }
   (void)b;
   // z = M r = IDCT(g * DCT(r)); last block: rho = r . z, beta
-  L.row_forward_p(SrcCells<T, T>{r, np, g.nx}, cols, P->active);
+  if (fused_first) L.row_forward_p(SrcCellsStart<T>{b, r, P->cg, np, g.nx}, cols, P->active);
+  else L.row_forward_p(SrcCells<T, T>{r, np, g.nx}, cols, P->active);
   L.column_p(cols, P->active, P->shift, T(P->pthr));
   L.row_inverse_p(DstCellsDot<T>{z, r, np, g.nx}, cols, P->active, P->partial,
                   make_fin<T>(P, X, OP_RHO, L.groups_row_p(), 2, cols), P->done_counter);
@@ -368,14 +402,33 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
   T* r = cells + 2 * np * cols;
   const int rb = red_blocks(np);
   const cudaStream_t s = X.s;
-  launch_k(k_pressure_rhs<T, T>, dim3(rb, cols), kThreads, 0, s, g, static_cast<const T*>(wacc ? wacc : w), sz, b, np,
-           rd, P->partial,
-                                                           make_fin<T>(P, X, OP_MEAN_B, rb, 1, cols), P->done_counter);
+  const T* w0 = static_cast<const T*>(wacc ? wacc : w);
+  // FP32 inner solves with an accumulated velocity start in one kernel; the
+  // FP64 path keeps the reference's centring then start (SciPy semantics)
+  const bool fused = std::is_same<T, float>::value && wacc != nullptr;
+  if (X.graph) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t graph;
+    if (cudaStreamGetCaptureInfo(s, &st, nullptr, &graph, nullptr, nullptr, nullptr) != cudaSuccess ||
+        st != cudaStreamCaptureStatusActive)
+      return MACSAV_ERR_CUDA;
+    if (cudaGraphConditionalHandleCreate(&X.cond, graph, 0, cudaGraphCondAssignDefault) != cudaSuccess)
+      return MACSAV_ERR_CUDA;
+  }
+  if (fused) {
+    launch_k(k_pressure_rhs_start<T, T>, dim3(rb, cols), kThreads, 0, s, g, w0, sz, b, x, np, rd, P->partial,
+             make_fin<T>(P, X, OP_START_RHS, rb, 3, cols), P->done_counter);
+  } else {
+    launch_k(k_pressure_rhs<T, T>, dim3(rb, cols), kThreads, 0, s, g, w0, sz, b, np, rd, P->partial,
+             make_fin<T>(P, X, OP_MEAN_B, rb, 1, cols), P->done_counter);
+  }
   ++P->launches;
   if (!X.graph) {
-    launch_k(k_cg_start<T>, dim3(rb, cols), kThreads, 0, s, g.np, b, x, r, np, P->cg, P->partial,
-                                                      make_fin<T>(P, X, OP_START, rb, 2, cols), P->done_counter);
-    ++P->launches;
+    if (!fused) {
+      launch_k(k_cg_start<T>, dim3(rb, cols), kThreads, 0, s, g.np, b, x, r, np, P->cg, P->partial,
+               make_fin<T>(P, X, OP_START, rb, 2, cols), P->done_counter);
+      ++P->launches;
+    }
     const int limit = P->maxit + (X.net && P->net ? P->net_maxit : 0);
     for (int it = 0; it < limit; ++it) {
       cudaMemcpyAsync(P->h_active, P->active, sizeof(int) * cols, cudaMemcpyDeviceToHost, s);
@@ -394,7 +447,7 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
                           cudaMemcpyDeviceToDevice, s);
         }
       }
-      cg_iteration<T>(P, X, L, w, cells, cols, wacc);
+      cg_iteration<T>(P, X, L, w, cells, cols, wacc, fused && it == 0);
       if constexpr (std::is_same<T, double>::value) {
         if (log) {
           cudaMemcpyAsync(P->log_z + P->log_n * np, cells + 3 * np * cols, sizeof(double) * np,
@@ -415,21 +468,18 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
   cudaGraph_t graph;
   const cudaGraphNode_t* deps = nullptr;
   size_t ndeps = 0;
-  if (cudaStreamGetCaptureInfo(s, &st, nullptr, &graph, &deps, nullptr, &ndeps) != cudaSuccess ||
-      st != cudaStreamCaptureStatusActive)
-    return MACSAV_ERR_CUDA;
-  if (cudaGraphConditionalHandleCreate(&X.cond, graph, 0, cudaGraphCondAssignDefault) != cudaSuccess)
-    return MACSAV_ERR_CUDA;
-  // k_cg_start's last block sets the loop condition
-  launch_k(k_cg_start<T>, dim3(rb, cols), kThreads, 0, s, g.np, b, x, r, np, P->cg, P->partial,
-                                                    make_fin<T>(P, X, OP_START, rb, 2, cols), P->done_counter);
-  ++P->launches;
+  // the start kernel's last block sets the loop condition
+  if (!fused) {
+    launch_k(k_cg_start<T>, dim3(rb, cols), kThreads, 0, s, g.np, b, x, r, np, P->cg, P->partial,
+             make_fin<T>(P, X, OP_START, rb, 2, cols), P->done_counter);
+    ++P->launches;
+  }
   // The first iteration outside the loop: its kernels are predicated on the
   // columns' flags like the loop body's (a column that is already converged,
   // e.g. a zero right-hand side, does nothing), its convergence check sets
   // the loop condition, and nearly every solve needs it, so one conditional
   // body launch per solve is saved.
-  cg_iteration<T>(P, X, L, w, cells, cols, wacc);
+  cg_iteration<T>(P, X, L, w, cells, cols, wacc, fused);
   if (cudaStreamGetCaptureInfo(s, &st, nullptr, &graph, &deps, nullptr, &ndeps) != cudaSuccess)
     return MACSAV_ERR_CUDA;
   cudaGraphNodeParams cp = {};
