@@ -754,6 +754,40 @@ def main() -> None:
 
     learned = None if args.no_learned else learned_leg(pkg, g, w, x0_host, dev, args, x64)
 
+    # FP64 path: its dominant kernel (the FP64 velocity column pass) against
+    # the FP64 rate and against HBM.  The FP64 peak is not in the measured
+    # peaks file, so it is measured here: a float64 matmul 4096^3, best of 3.
+    ms_k64, bytes_k64 = C.c_double(), C.c_double()
+    m64.plan.check(lib.load().macsav_time_pass(m64.plan.handle, 3, 20, C.byref(ms_k64), C.byref(bytes_k64),
+                                               stokes.stream_handle()))
+
+    def column_flops(block_cols: int, m: int) -> float:
+        # forward and inverse transform of every column, 2.5 m log2(m) each
+        return block_cols * 2 * 2.5 * m * np.log2(m)
+    lu, lv = int(2 ** np.ceil(np.log2(g.ny))), int(2 ** np.ceil(np.log2(2 * g.ny)))  # DST-II, DST-I lengths
+    flops64 = 2 * (column_flops(g.nx - 1, lu) + column_flops(g.nx, lv))  # two right-hand sides
+    a_m = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    best = float("inf")
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a_m, a_m)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a_m
+    fp64_peak = 2 * 4096 ** 3 / (best * 1e-3) / 1e12
+    fp64_achieved = flops64 / (ms_k64.value * 1e-3) / 1e12
+    roofline64 = {"kernel": "k_column_p2<double> (velocity blocks, 2 RHS)", "bound": "fp64",
+                  "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": fp64_achieved / fp64_peak,
+                  "peak_source": "measured here: float64 matmul 4096^3 (torch), best of 4",
+                  "flops_per_launch": flops64, "flop_convention": "2.5 m log2(m) per line and direction",
+                  "ms_per_launch": ms_k64.value,
+                  "bytes": {"achieved": bytes_k64.value / (ms_k64.value * 1e-3) / 1e9, "unit": "GB/s",
+                            "frac_of_hbm": bytes_k64.value / (ms_k64.value * 1e-3) / 1e9
+                            / float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs", 6800.0))
+                            if (ROOT / "MEASURED_PEAKS.json").exists() else None}}
+
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -782,6 +816,7 @@ def main() -> None:
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": "measured" if pk.exists() else "fallback",
                      "traffic": traffic, "bytes_per_launch": bytes_k.value, "ms_per_launch": ms_k.value},
+        "roofline_fp64": roofline64,
     }
     if learned is not None:
         line["learned"] = learned
