@@ -392,13 +392,11 @@ __global__ void k_ch_factor(ChanGrid g, double mass, double visc, cd* lu, int* p
 // about five dependent FP64 operations to the chain (GB300's FP64 latency is
 // about 67 cycles and a division about 640).  The mode 0 thread solves
 // hu0 u = fu by Thomas with the same register chaining.
-__global__ void k_ch_solve(ChanGrid g, const cd* __restrict__ fu, const cd* __restrict__ fv, long long fstride,
-                           const cd* __restrict__ lu, const int* __restrict__ piv, const double* __restrict__ zero,
-                           cd* __restrict__ uo, cd* __restrict__ vo, cd* __restrict__ po, long long vstride,
-                           long long pstride, cd* __restrict__ work, int cols, double visc) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int m = t % g.nm, c = t / g.nm;
-  if (c >= cols) return;
+__device__ __forceinline__ void ch_solve_one(const ChanGrid& g, const cd* __restrict__ fu, const cd* __restrict__ fv,
+                                             long long fstride, const cd* __restrict__ lu, const int* __restrict__ piv,
+                                             const double* __restrict__ zero, cd* __restrict__ uo, cd* __restrict__ vo,
+                                             cd* __restrict__ po, long long vstride, long long pstride,
+                                             cd* __restrict__ work, int cols, double visc, int m, int c) {
   const int ny = g.ny, nm = g.nm;
   const cd* fuc = fu + c * fstride;
   const cd* fvc = fv + c * fstride;
@@ -587,6 +585,289 @@ __global__ void k_ch_solve(ChanGrid g, const cd* __restrict__ fu, const cd* __re
           --jo;
         }
       }
+    }
+  }
+}
+
+// One thread per (mode, column), each running ch_solve_one.
+__global__ void k_ch_solve(ChanGrid g, const cd* __restrict__ fu, const cd* __restrict__ fv, long long fstride,
+                           const cd* __restrict__ lu, const int* __restrict__ piv, const double* __restrict__ zero,
+                           cd* __restrict__ uo, cd* __restrict__ vo, cd* __restrict__ po, long long vstride,
+                           long long pstride, cd* __restrict__ work, int cols, double visc) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = t % g.nm, c = t / g.nm;
+  if (c >= cols) return;
+  ch_solve_one(g, fu, fv, fstride, lu, piv, zero, uo, vo, po, vstride, pstride, work, cols, visc, m, c);
+}
+
+// Partitioned (spike) substitution: one warp per (mode >= 1, column).  The
+// n = 3 ny - 1 steps of each sweep are split into 32 chunks, one per lane.
+// A sweep step is an affine map of its register window (forward: the 4
+// pending entries; back: the last 6 unknowns), so a lane (1) runs its chunk
+// on the unit windows and on the zero window with the chunk's inputs, which
+// gives the chunk's map W_out = T W_in + t; (2) the lanes pass the windows
+// along (W_in of chunk c+1 = T_c W_in(c) + t_c, 31 shuffle steps); (3) each
+// lane reruns its chunk from its true window.  The dependent chain per lane
+// is about 2 n / 32 + 31 steps instead of 2 n.  Mode 0 (Thomas) runs on lane 0
+// of one extra warp per column.
+// Mode 0 of column c by one warp: hu0 u = fu by Thomas, v = 0, and
+// p_{j+1} = p_j + hy fv_j with the mean removed.  The three recurrences are
+// affine in their carried value (y_j = a_j y_{j-1} + b_j), so each lane
+// composes its chunk's map, the lanes pass the carried value along (31
+// shuffle steps), and each lane reruns its chunk from the true value.
+__device__ __forceinline__ void ch_mode0_warp(const ChanGrid& g, const cd* __restrict__ fu, const cd* __restrict__ fv,
+                                              long long fstride, const double* __restrict__ zero, cd* __restrict__ uo,
+                                              cd* __restrict__ vo, cd* __restrict__ po, long long vstride,
+                                              long long pstride, double visc, int c, int lane) {
+  const int ny = g.ny, nm = g.nm;
+  const cd* fuc = fu + c * fstride;
+  const cd* fvc = fv + c * fstride;
+  cd* uc = uo + c * vstride;
+  cd* vc = vo + c * vstride;
+  cd* pc = po + c * pstride;
+  const double* cp = zero;
+  const double* dn = zero + ny;
+  const double off = -visc * g.ihy2;
+  const cd z0 = mk(0.0, 0.0);
+  const int S = (ny + 31) / 32;
+  const int j0 = min(lane * S, ny), j1 = min(j0 + S, ny);
+  // carry v across lanes: lane it+1 receives lane it's map applied to its carry
+  auto pass = [&](double a, cd b, cd first) -> cd {  // returns this lane's incoming carry
+    cd v = first;
+    for (int it = 0; it < 31; ++it) {
+      const cd cand = mk(a * v.x + b.x, a * v.y + b.y);
+      const double re = __shfl_sync(0xffffffffu, cand.x, it), im = __shfl_sync(0xffffffffu, cand.y, it);
+      if (lane == it + 1) v = mk(re, im);
+    }
+    return v;
+  };
+  // forward Thomas: y_j = (f_j - off y_{j-1}) / dn_j  (y_{-1} = 0)
+  double A = 1.0;
+  cd B = z0;
+  for (int j = j0; j < j1; ++j) {
+    const double a = -off / dn[j];
+    const cd f = fuc[(long long)j * nm];
+    const cd b = mk(f.x / dn[j], f.y / dn[j]);
+    A = a * A;
+    B = mk(a * B.x + b.x, a * B.y + b.y);
+  }
+  cd yin = pass(A, B, z0);
+  for (int j = j0; j < j1; ++j) {
+    const cd f = fuc[(long long)j * nm];
+    yin = mk((f.x - off * yin.x) / dn[j], (f.y - off * yin.y) / dn[j]);
+    uc[(long long)j * nm] = yin;
+  }
+  __syncwarp();
+  // back: u_j = y_j - cp_j u_{j+1} (u_{ny} = 0 reproduces u_{ny-1} = y_{ny-1});
+  // chunks from the top: lane l covers j = ny-1-l S down to ny-(l+1) S
+  const int bt = ny - 1 - min(lane * S, ny), bb = max(ny - (lane + 1) * S, 0);
+  A = 1.0;
+  B = z0;
+  for (int j = bt; j >= bb; --j) {
+    const double a = j < ny - 1 ? -cp[j] : 0.0;
+    const cd yj = uc[(long long)j * nm];
+    A = a * A;
+    B = mk(a * B.x + yj.x, a * B.y + yj.y);
+  }
+  cd uin = pass(A, B, z0);
+  __syncwarp();  // every lane has read its y before any overwrites them
+  for (int j = bt; j >= bb; --j) {
+    const cd yj = uc[(long long)j * nm];
+    uin = j < ny - 1 ? mk(yj.x - cp[j] * uin.x, yj.y - cp[j] * uin.y) : yj;
+    uc[(long long)j * nm] = uin;
+  }
+  for (int k = lane; k < ny - 1; k += 32) vc[(long long)k * nm] = z0;
+  // pressure: p_0 = 0, p_j = p_{j-1} + hy fv_{j-1}; then the mean removed
+  cd P = z0;
+  for (int j = j0; j < j1; ++j)
+    if (j > 0) {
+      const cd f = fvc[(long long)(j - 1) * nm];
+      P = mk(P.x + g.hy * f.x, P.y + g.hy * f.y);
+    }
+  cd pin = pass(1.0, P, z0);
+  cd sum = z0;
+  for (int j = j0; j < j1; ++j) {
+    if (j > 0) {
+      const cd f = fvc[(long long)(j - 1) * nm];
+      pin = mk(pin.x + g.hy * f.x, pin.y + g.hy * f.y);
+    }
+    pc[(long long)j * nm] = pin;
+    sum = sum + pin;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sum.x += __shfl_xor_sync(0xffffffffu, sum.x, o);
+    sum.y += __shfl_xor_sync(0xffffffffu, sum.y, o);
+  }
+  const cd mean = mk(sum.x / ny, sum.y / ny);
+  for (int j = j0; j < j1; ++j) pc[(long long)j * nm] = pc[(long long)j * nm] - mean;
+}
+
+constexpr int kSpikeThreads = 256;
+__global__ void __launch_bounds__(kSpikeThreads) k_ch_solve_spike(
+    ChanGrid g, const cd* __restrict__ fu, const cd* __restrict__ fv, long long fstride, const cd* __restrict__ lu,
+    const int* __restrict__ piv, const double* __restrict__ zero, cd* __restrict__ uo, cd* __restrict__ vo,
+    cd* __restrict__ po, long long vstride, long long pstride, cd* __restrict__ work, int cols, double visc) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nm = g.nm, ny = g.ny, nmodes = nm - 1;
+  if (warp < cols) {
+    ch_mode0_warp(g, fu, fv, fstride, zero, uo, vo, po, vstride, pstride, visc, warp, lane);
+    return;
+  }
+  const int wm = warp - cols;
+  if (wm >= nmodes * cols) return;  // whole warp
+  const int c = wm / nmodes, m1 = wm - c * nmodes, m = m1 + 1;
+  const cd z0 = mk(0.0, 0.0), one = mk(1.0, 0.0);
+  const cd* fuc = fu + c * fstride;
+  const cd* fvc = fv + c * fstride;
+  cd* uc = uo + c * vstride;
+  cd* vc = vo + c * vstride;
+  cd* pc = po + c * pstride;
+  const int n = 3 * ny - 1;
+  const long long wstride = (long long)cols * nmodes;
+  cd* y = work + (long long)c * nmodes + m1;
+  const long long cstep = (long long)kLD * nmodes;
+  const cd* lum = lu + m1;
+  const int* pvm = piv + m1;
+  const int oL1 = 7 * nmodes, oL2 = 8 * nmodes, oL3 = 9 * nmodes, oD = 6 * nmodes;
+  const long long fj = nm;
+  auto rhs = [&](int k) -> cd {  // entry k < n of the interleaved right-hand side
+    const int j = k / 3, r = k - 3 * j;
+    return r == 0 ? fuc[(long long)j * fj + m] : (r == 1 ? z0 : fvc[(long long)j * fj + m]);
+  };
+  const int S = (n + 31) / 32;
+  // ---- forward: window (w0..w3) = b[k..k+3] before step k -------------------
+  const int f0 = min(lane * S, n), f1 = min(f0 + S, n);
+  // one forward step of NV windows; the last one (if aff) takes b[k+4]
+  auto fwd = [&](auto& W, int nv, int k, bool aff, cd* out) {
+    const cd* col = lum + k * cstep;
+    const int p = pvm[(long long)k * nmodes] - k;
+    const cd l1 = k + 1 < n ? col[oL1] : z0, l2 = k + 2 < n ? col[oL2] : z0, l3 = k + 3 < n ? col[oL3] : z0;
+    const cd bn = (aff && k + 4 < n) ? rhs(k + 4) : z0;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      if (v >= nv) break;
+      cd w0 = W[v][0], w1 = W[v][1], w2 = W[v][2], w3 = W[v][3];
+      if (p == 1) { const cd tmp = w0; w0 = w1; w1 = tmp; }
+      else if (p == 2) { const cd tmp = w0; w0 = w2; w2 = tmp; }
+      else if (p == 3) { const cd tmp = w0; w0 = w3; w3 = tmp; }
+      if (out && v == nv - 1) *out = w0;
+      if (k + 1 < n) w1 = w1 - cmul(l1, w0);
+      if (k + 2 < n) w2 = w2 - cmul(l2, w0);
+      if (k + 3 < n) w3 = w3 - cmul(l3, w0);
+      W[v][0] = w1;
+      W[v][1] = w2;
+      W[v][2] = w3;
+      W[v][3] = (aff && v == nv - 1) ? bn : z0;
+    }
+  };
+  cd T[5][4];  // columns 0..3: responses to the unit windows; 4: the affine part
+#pragma unroll
+  for (int v = 0; v < 5; ++v)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) T[v][i] = (v == i) ? one : z0;
+  for (int k = f0; k < f1; ++k) fwd(T, 5, k, true, nullptr);
+  // pass the windows along the chunks
+  cd win[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) win[i] = (lane == 0 && i < n) ? rhs(i) : z0;
+  for (int it = 0; it < 31; ++it) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      cd cand = T[4][i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) cand = cand + cmul(T[j][i], win[j]);
+      const double re = __shfl_sync(0xffffffffu, cand.x, it), im = __shfl_sync(0xffffffffu, cand.y, it);
+      if (lane == it + 1) win[i] = mk(re, im);
+    }
+  }
+  {
+    cd W1[1][4] = {{win[0], win[1], win[2], win[3]}};
+    for (int k = f0; k < f1; ++k) {
+      cd yk;
+      fwd(W1, 1, k, true, &yk);
+      y[(long long)k * wstride] = yk;
+    }
+  }
+  __syncwarp();
+  // ---- back: window (x1..x6) = x[k+1..k+6] before step k (descending) -------
+  const int bt = n - 1 - min(lane * S, n), bb = max(n - (lane + 1) * S, 0);  // chunk k = bt .. bb
+  auto bwd = [&](auto& X, int nv, int k, bool aff, cd* out) {
+    const cd* col = lum + k * cstep;
+    cd a[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) a[i] = k + 1 + i < n ? col[(15 + 9 * i) * nmodes] : z0;
+    const cd rp = col[oD];
+    const cd yk = aff ? y[(long long)k * wstride] : z0;
+#pragma unroll
+    for (int v = 0; v < 7; ++v) {
+      if (v >= nv) break;
+      cd sacc = (aff && v == nv - 1) ? yk : z0;
+      if (k + 6 < n) sacc = sacc - cmul(a[5], X[v][5]);
+      if (k + 5 < n) sacc = sacc - cmul(a[4], X[v][4]);
+      if (k + 4 < n) sacc = sacc - cmul(a[3], X[v][3]);
+      if (k + 3 < n) sacc = sacc - cmul(a[2], X[v][2]);
+      if (k + 2 < n) sacc = sacc - cmul(a[1], X[v][1]);
+      if (k + 1 < n) sacc = sacc - cmul(a[0], X[v][0]);
+      const cd xk = cmul(sacc, rp);
+      if (out && v == nv - 1) *out = xk;
+      X[v][5] = X[v][4];
+      X[v][4] = X[v][3];
+      X[v][3] = X[v][2];
+      X[v][2] = X[v][1];
+      X[v][1] = X[v][0];
+      X[v][0] = xk;
+    }
+  };
+  // the chunk's map in two batches (registers): unit windows 0..3, then 4, 5 and the affine part
+  cd R[7][6];
+  {
+    cd XA[4][6];
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+#pragma unroll
+      for (int i = 0; i < 6; ++i) XA[v][i] = (v == i) ? one : z0;
+    for (int k = bt; k >= bb; --k) bwd(XA, 4, k, false, nullptr);
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+#pragma unroll
+      for (int i = 0; i < 6; ++i) R[v][i] = XA[v][i];
+  }
+  {
+    cd XB[3][6];
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+#pragma unroll
+      for (int i = 0; i < 6; ++i) XB[v][i] = (v < 2 && v + 4 == i) ? one : z0;
+    for (int k = bt; k >= bb; --k) bwd(XB, 3, k, true, nullptr);
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+#pragma unroll
+      for (int i = 0; i < 6; ++i) R[4 + v][i] = XB[v][i];
+  }
+  cd xin[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) xin[i] = z0;  // above the top chunk: x[n..n+5] = 0
+  for (int it = 0; it < 31; ++it) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      cd cand = R[6][i];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) cand = cand + cmul(R[j][i], xin[j]);
+      const double re = __shfl_sync(0xffffffffu, cand.x, it), im = __shfl_sync(0xffffffffu, cand.y, it);
+      if (lane == it + 1) xin[i] = mk(re, im);
+    }
+  }
+  {
+    cd X1[1][6] = {{xin[0], xin[1], xin[2], xin[3], xin[4], xin[5]}};
+    for (int k = bt; k >= bb; --k) {
+      cd xk;
+      bwd(X1, 1, k, true, &xk);
+      const int j = k / 3, r = k - 3 * j;
+      const long long o = (long long)j * fj + m;
+      if (r == 0) uc[o] = xk;
+      else if (r == 1) pc[o] = xk;
+      else vc[o] = xk;
     }
   }
 }
@@ -931,14 +1212,13 @@ int macsav_channel_solve(macsav_channel* h, const double* rhs, int cols, double 
   // forward FFTs of the loads (u rows then v rows: one (2ny-1) x nx matrix)
   launch_fft(&C, false, rhs, g.size, rows, C.fspec, fstride, cols, s);
   // mode solves into u/v spectra (uspec: u rows then v rows) and pspec
-  // Each thread is one long sequential recurrence on the narrow FP64 pipe:
-  // few threads per CTA spread them over as many SMs as possible.
-  const int threads = g.nm * cols;
-  const int tpb = macsav::kChSolveThreads;
-  macsav::k_ch_solve<<<(threads + tpb - 1) / tpb, tpb, 0, s>>>(g, C.fspec, C.fspec + (long long)g.ny * g.nm, fstride,
-                                                        slot->lu, slot->piv, slot->zero, C.uspec,
-                                                        C.uspec + (long long)g.ny * g.nm, C.pspec, fstride,
-                                                        (long long)g.ny * g.nm, C.work, cols, viscosity);
+  // one warp per (mode >= 1, column) in the partitioned form, plus one warp
+  // per column for mode 0
+  const long long threads = 32LL * (cols + (long long)(g.nm - 1) * cols);
+  const int tpb = macsav::kSpikeThreads;
+  macsav::k_ch_solve_spike<<<int((threads + tpb - 1) / tpb), tpb, 0, s>>>(
+      g, C.fspec, C.fspec + (long long)g.ny * g.nm, fstride, slot->lu, slot->piv, slot->zero, C.uspec,
+      C.uspec + (long long)g.ny * g.nm, C.pspec, fstride, (long long)g.ny * g.nm, C.work, cols, viscosity);
   launch_fft(&C, true, C.uspec, fstride, rows, vel, g.size, cols, s);
   launch_fft(&C, true, C.pspec, (long long)g.ny * g.nm, g.ny, pres, g.np, cols, s);
   {
