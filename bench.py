@@ -56,17 +56,66 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle samples during the timed region."""
+    """SM clock and throttle-reason samples taken during the timed region.
+
+    Reads NVML through ctypes (read-only queries: clocks, maximum clocks and
+    the active clock-event reasons) every 10 ms on a background thread, so a
+    timed region of a few tens of milliseconds still gets several samples;
+    falls back to ``nvidia-smi -lms 200`` where NVML cannot be loaded.
+    """
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits (nvml.h)
+    REASON_BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20,
+                   "hw_thermal_slowdown": 0x40}
+    PERIOD_S = 0.010
 
     def __init__(self, index: int) -> None:
         self.index = index
         self.proc = None
+        self.thread = None
+        self.samples = []   # (sm_mhz, max_mhz, reasons bitmask)
+        self.lines = []
+
+    def _nvml(self):
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return None
+        if lib.nvmlInit_v2() != 0:
+            return None
+        dev = C.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.index), C.byref(dev)) != 0:
+            lib.nvmlShutdown()
+            return None
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons", None)
+        if reasons is None:
+            lib.nvmlShutdown()
+            return None
+        return lib, dev, reasons
+
+    def _loop(self, lib, dev, reasons):
+        sm, mx, rs = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        while not self.stop.is_set():
+            ok = (lib.nvmlDeviceGetClockInfo(dev, 1, C.byref(sm)) == 0          # NVML_CLOCK_SM
+                  and lib.nvmlDeviceGetMaxClockInfo(dev, 1, C.byref(mx)) == 0
+                  and reasons(dev, C.byref(rs)) == 0)
+            if ok:
+                self.samples.append((float(sm.value), float(mx.value), int(rs.value)))
+            self.stop.wait(self.PERIOD_S)
 
     def __enter__(self):
+        import threading
+        h = self._nvml()
+        if h is not None:
+            self.nvml = h
+            self.stop = threading.Event()
+            self.thread = threading.Thread(target=self._loop, args=h, daemon=True)
+            self.thread.start()
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -76,7 +125,11 @@ class ClockSampler:
         return self
 
     def __exit__(self, *exc):
-        self.lines = []
+        if self.thread is not None:
+            self.stop.set()
+            self.thread.join(timeout=5)
+            self.nvml[0].nvmlShutdown()
+            return
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -88,8 +141,12 @@ class ClockSampler:
 
     def summary(self) -> dict:
         sm, mx, reasons = [], [], set()
+        for s, m, bits in self.samples:
+            sm.append(s)
+            mx.append(m)
+            reasons.update(name for name, bit in self.REASON_BITS.items() if bits & bit)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in getattr(self, "lines", []):
+        for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -104,7 +161,7 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvml" if self.samples else "nvidia-smi"}
 
 
 def initial_state(pkg):

@@ -134,6 +134,17 @@ int macsav_inner_max_static(const double* a, const double* b, long long n, doubl
  * as plain copies. */
 int macsav_layout(macsav_plan* plan, int direction, double* packed, double* u, double* v, void* stream);
 
+/* *mapped = 1 when the first and last byte of [p, p + bytes) are page-locked
+ * host memory that the current device dereferences at the same address (the
+ * pinned memory of cudaHostAlloc under unified addressing), else 0; never
+ * an error for ordinary pageable or foreign pointers.  A caller that knows
+ * the range lies in one allocation may then pass p to macsav_layout as u or
+ * v: the pack kernel reads, and the unpack kernel writes, the host arrays
+ * over the host link directly, with no staging copy (the host arrays of
+ * MACGrid.pack / unpack, solver/mac/grid.py:52-65).  NULL mapped or
+ * bytes < 0: MACSAV_ERR_VALUE. */
+int macsav_host_mapped(const void* p, long long bytes, int* mapped);
+
 /* MACNavierStokes.diagnostics (solver/mac_ns.py:95-107) of a packed velocity x
  * with scalar r: out[0..7] = kinetic, modified_energy, divergence_inf,
  * h1_seminorm_squared, r, angular_momentum, power, dissipation.  force may be

@@ -250,6 +250,23 @@ int macsav_layout(macsav_plan* plan, int direction, double* packed, double* u, d
   return rc == MACSAV_OK ? MACSAV_OK : cuda_status(&plan->p);
 }
 
+int macsav_host_mapped(const void* p, long long bytes, int* mapped) {
+  if (!mapped || bytes < 0) return MACSAV_ERR_VALUE;
+  *mapped = 0;
+  if (!p || bytes == 0) return MACSAV_OK;
+  const char* ends[2] = {static_cast<const char*>(p), static_cast<const char*>(p) + (bytes - 1)};
+  for (const char* q : ends) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return MACSAV_OK;
+    }
+    if (at.type != cudaMemoryTypeHost || at.devicePointer != q || at.hostPointer != q) return MACSAV_OK;
+  }
+  *mapped = 1;
+  return MACSAV_OK;
+}
+
 int macsav_diagnostics(macsav_plan* plan, const double* x, double r, double nu, const double* force, double* out,
                        void* stream) {
   if (!plan || !x || !out) return MACSAV_ERR_VALUE;

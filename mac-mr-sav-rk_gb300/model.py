@@ -93,6 +93,14 @@ class MACNavierStokes:
             raise ValueError("Incorrect MAC array shapes")
         if np.any(u[:, [0, -1]] != 0) or np.any(v[[0, -1], :] != 0):
             raise ValueError("Normal boundary velocities must be zero")
+        if self._host_mapped(u) and self._host_mapped(v):
+            # pinned face arrays (those of a State this model built): the pack
+            # kernel reads them over the host link, no staging copy or sync
+            x = torch.empty(g.size, dtype=torch.float64, device=self.device)
+            self.plan.check(self.plan.lib.macsav_layout(self.plan.handle, 1, dptr(x), u.ctypes.data, v.ctypes.data,
+                                                        stream_handle()))
+            x._host_faces = (u, v)  # keeps the pinned blocks alive while the kernel may read them
+            return x
         with warnings.catch_warnings():
             # States hold read-only arrays; these host views are only read (copied to the device)
             warnings.filterwarnings("ignore", message="The given NumPy array is not writable")
@@ -103,26 +111,53 @@ class MACNavierStokes:
                                                     stream_handle()))
         return x
 
+    def _mapped_range(self, ptr: int, nbytes: int) -> bool:
+        ok = C.c_int()
+        self.plan.check(self.plan.lib.macsav_host_mapped(ptr, nbytes, C.byref(ok)))
+        return bool(ok.value)
+
+    def _host_mapped(self, a: np.ndarray) -> bool:
+        """True when host array ``a`` lies inside one pinned torch storage (its
+        numpy base) that the device maps at the same address, so the layout
+        kernels may read it directly; pageable and foreign arrays take the
+        copy path."""
+        base = a.base
+        if not (isinstance(base, torch.Tensor) and a.flags.c_contiguous and a.dtype == np.float64
+                and base.device.type == "cpu" and base.is_pinned()):
+            return False
+        st = base.untyped_storage()
+        lo, p = st.data_ptr(), a.ctypes.data
+        if not (lo <= p and p + a.nbytes <= lo + st.nbytes()):
+            return False
+        return self._mapped_range(p, a.nbytes)
+
     def state(self, t: float, velocity, r: float = 0.0) -> State:
-        """A host State (face arrays unpacked on the device, then copied) that
-        also keeps the packed device vector.  The host arrays live in pinned
-        memory from torch's caching host allocator: the copies run at full
-        link speed, a later H2D of the same arrays does too, and the blocks of
-        dropped states are reused instead of faulting in fresh pages (on the
-        Grace host a GPU write into fresh pageable pages of this size cost
-        about 2.5 ms, against about 30 us into resident ones)."""
+        """A host State (face arrays unpacked on the device) that also keeps
+        the packed device vector.  The host arrays live in pinned memory from
+        torch's caching host allocator, which the device maps: the unpack
+        kernel writes them over the host link (NVLink-C2C on a Grace host)
+        and a later ``device_vector`` of the same arrays packs from them
+        directly, with no staging copies; the blocks of dropped states are
+        reused instead of faulting in fresh pages (on the Grace host a GPU
+        write into fresh pageable pages of this size cost about 2.5 ms).
+        Where the pinned blocks are not mapped, the arrays are copied."""
         dv = self._dev(velocity).contiguous()
         g = self.grid
         if dv.numel() != g.size:
             raise ValueError("Incorrect free-vector shape")
-        ud = torch.empty((g.ny, g.nx + 1), dtype=torch.float64, device=self.device)
-        vd = torch.empty((g.ny + 1, g.nx), dtype=torch.float64, device=self.device)
-        self.plan.check(self.plan.lib.macsav_layout(self.plan.handle, 0, dptr(dv), dptr(ud), dptr(vd),
-                                                    stream_handle()))
-        hu = torch.empty(ud.shape, dtype=torch.float64, pin_memory=True)
-        hv = torch.empty(vd.shape, dtype=torch.float64, pin_memory=True)
-        hu.copy_(ud, non_blocking=True)
-        hv.copy_(vd, non_blocking=True)
+        hu = torch.empty((g.ny, g.nx + 1), dtype=torch.float64, pin_memory=True)
+        hv = torch.empty((g.ny + 1, g.nx), dtype=torch.float64, pin_memory=True)
+        if self._mapped_range(hu.data_ptr(), hu.nbytes) and self._mapped_range(hv.data_ptr(), hv.nbytes):
+            # the unpack kernel writes the pinned host arrays over the host link
+            self.plan.check(self.plan.lib.macsav_layout(self.plan.handle, 0, dptr(dv), hu.data_ptr(), hv.data_ptr(),
+                                                        stream_handle()))
+        else:
+            ud = torch.empty(hu.shape, dtype=torch.float64, device=self.device)
+            vd = torch.empty(hv.shape, dtype=torch.float64, device=self.device)
+            self.plan.check(self.plan.lib.macsav_layout(self.plan.handle, 0, dptr(dv), dptr(ud), dptr(vd),
+                                                        stream_handle()))
+            hu.copy_(ud, non_blocking=True)
+            hv.copy_(vd, non_blocking=True)
         torch.cuda.current_stream().synchronize()
         u, v = hu.numpy(), hv.numpy()
         u.flags.writeable = False

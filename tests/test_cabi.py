@@ -33,3 +33,17 @@ def test_plan_create_rejects_bad_arguments_without_gpu():
     assert so.macsav_plan_create(ctypes.byref(h), 8, 8, 1.0, 1.0, 0, -1.0, 1e-12, 100, 2) == lib.ERR_VALUE
     assert b"Invalid solver controls" in so.macsav_plan_error(None)
     assert not h.value
+
+
+def test_host_mapped_rejects_bad_arguments_and_pageable_memory():
+    import numpy as np
+    lib = _lib_module()
+    so = lib.load()
+    a = np.zeros(1024)
+    ok = ctypes.c_int(7)
+    assert so.macsav_host_mapped(a.ctypes.data, a.nbytes, None) == lib.ERR_VALUE
+    assert so.macsav_host_mapped(a.ctypes.data, -1, ctypes.byref(ok)) == lib.ERR_VALUE
+    assert so.macsav_host_mapped(None, 8, ctypes.byref(ok)) == lib.OK and ok.value == 0
+    # ordinary (pageable) host memory is never reported as mapped pinned memory
+    ok.value = 7
+    assert so.macsav_host_mapped(a.ctypes.data, a.nbytes, ctypes.byref(ok)) == lib.OK and ok.value == 0

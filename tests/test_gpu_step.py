@@ -164,3 +164,37 @@ def test_embedded_norms_match_host_inner_products(pkg, name, graph):
     for got, want in zip(trial.embedded_norms[:3], expect):
         assert got == pytest.approx(want, rel=1e-12, abs=1e-300)
     assert trial.embedded_norms[3] == 0.0
+
+
+def test_host_state_layout_over_mapped_pinned_memory(pkg):
+    """The pinned host arrays of a State built by the model are read and
+    written by the layout kernels directly; the result is bitwise the copy
+    path's (MACGrid.pack / unpack, solver/mac/grid.py:52-65), pageable arrays
+    take the copy path, and a step from either gives the same state."""
+    import torch
+    g = pkg.MACGrid(48, 40, 1.2, 1.0)
+    model = pkg.MACNavierStokes(g, 1e-2)
+    x = np.random.default_rng(7).standard_normal(g.size)
+    st = model.state(0.0, x, 0.5)
+    u_ref, v_ref = g.unpack(x)
+    np.testing.assert_array_equal(st.u, u_ref)   # unpack: exact copies, zero walls
+    np.testing.assert_array_equal(st.v, v_ref)
+    assert isinstance(st.u.base, torch.Tensor) and st.u.base.is_pinned()
+    mapped = model.device_vector(pkg.State(st.t, st.u, st.v, st.r))
+    assert hasattr(mapped, "_host_faces")          # packed from the pinned arrays directly
+    pageable = model.device_vector(pkg.State(st.t, np.array(st.u), np.array(st.v), st.r))
+    assert not hasattr(pageable, "_host_faces")    # copied
+    np.testing.assert_array_equal(mapped.cpu().numpy(), x)
+    np.testing.assert_array_equal(pageable.cpu().numpy(), x)
+    scheme = pkg.make_scheme("sdirk2_mrsav")
+    a = scheme.step(model, pkg.State(st.t, st.u, st.v, st.r), 1e-3).state
+    b = scheme.step(model, pkg.State(st.t, np.array(st.u), np.array(st.v), st.r), 1e-3).state
+    np.testing.assert_array_equal(a.u, b.u)
+    np.testing.assert_array_equal(a.v, b.v)
+    assert a.r == b.r
+    # wall checks still apply to pinned arrays
+    bad = model.state(0.0, x, 0.5)
+    with pytest.raises(ValueError, match="Normal boundary velocities must be zero"):
+        u_bad = torch.from_numpy(np.array(bad.u)).pin_memory()
+        u_bad[0, 0] = 1.0
+        model.device_vector(pkg.State(0.0, u_bad.numpy(), bad.v, 0.5))
