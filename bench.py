@@ -267,20 +267,18 @@ def run_ensemble(args) -> None:
     del eager
     err = max(float(torch.linalg.vector_norm(e32.velocity(i) - e64.velocity(i))
                     / torch.linalg.vector_norm(e64.velocity(i))) for i in range(len(mine)))
-    # end to end: host states in, host states out, every step, through
-    # pinned host buffers (one per member, allocated once)
-    hosts = [torch.empty(e32.velocity(i).numel(), dtype=torch.float64, pin_memory=True) for i in range(len(mine))]
-    for i, h in enumerate(hosts):
-        h.copy_(e32.velocity(i))
+    # end to end: host states in, host states out, every step, through the
+    # ensemble's pinned host block (one array per member, allocated once):
+    # every member's state uploaded by one kernel, stepped, and downloaded by
+    # one kernel, each reading or writing the pinned block over the host link
+    e32.host_buffers()
+    e32.download()
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for i, x in enumerate(hosts):
-            e32.set_state(i, x, r=e32.r[i], t=e32.t[i])
+        e32.upload()
         e32.step(w["dt"])
-        for i, h in enumerate(hosts):
-            h.copy_(e32.velocity(i), non_blocking=True)
-        torch.cuda.current_stream().synchronize()
+        e32.download()
     e2e_sec = time.perf_counter() - t0
     tot = torch.tensor([ms32, ms64, e2e_sec, err], dtype=torch.float64, device="cuda")
     if world > 1:

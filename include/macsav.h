@@ -145,6 +145,18 @@ int macsav_layout(macsav_plan* plan, int direction, double* packed, double* u, d
  * bytes < 0: MACSAV_ERR_VALUE. */
 int macsav_host_mapped(const void* p, long long bytes, int* mapped);
 
+/* Copies `count` vectors in one kernel on `stream`: src[k] -> dst[k], n[k]
+ * doubles each (max_n >= every n[k] sizes the grid).  The arrays src, dst, n
+ * and every src[k], dst[k] must be device-accessible: device memory, or
+ * pinned host memory that the device maps (macsav_host_mapped), which the
+ * kernel then reads or writes over the host link.  This is the ensemble's
+ * host boundary: all members' packed velocities in or out in one launch
+ * instead of one copy per member (no reference counterpart: the reference
+ * steps one model at a time).  count < 0, max_n < 0 or NULL arrays:
+ * MACSAV_ERR_VALUE; count == 0: MACSAV_OK, nothing launched. */
+int macsav_copy_vectors(int count, const double* const* src, double* const* dst, const long long* n, long long max_n,
+                        void* stream);
+
 /* MACNavierStokes.diagnostics (solver/mac_ns.py:95-107) of a packed velocity x
  * with scalar r: out[0..7] = kinetic, modified_energy, divergence_inf,
  * h1_seminorm_squared, r, angular_momentum, power, dissipation.  force may be

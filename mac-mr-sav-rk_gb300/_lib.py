@@ -89,6 +89,7 @@ _SIGNATURES = {
     "macsav_set_programmatic_launch": (_I, [_I]),
     "macsav_layout": (_I, [_P, _I, _P, _P, _P, _P]),
     "macsav_host_mapped": (_I, [_P, _LL, C.POINTER(_I)]),
+    "macsav_copy_vectors": (_I, [_I, _P, _P, _P, _LL, _P]),
     "macsav_step_enqueue": (_I, [_P, _I, _D, _D, _D, _D, _P, _D, _P, _P, _P, _P, _P]),
     "macsav_step_finish": (_I, [_P, C.POINTER(StageRecord), C.POINTER(_D)]),
     "macsav_time_pass": (_I, [_P, _I, _I, C.POINTER(_D), C.POINTER(_D), _P]),

@@ -21,6 +21,8 @@ int solve_mixed(Plan* P, const double* f, int cols, double mass, double visc, do
                 cudaStream_t s, int* sweeps);
 int op_apply(Plan* P, int which, const double* in, double* out, int cols, cudaStream_t s);
 int op_layout(Plan* P, int direction, double* packed, double* u, double* v, cudaStream_t s);
+int op_copy_vectors(int count, const double* const* src, double* const* dst, const long long* n, long long max_n,
+                    cudaStream_t s);
 int op_combine(Plan* P, int nterms, const double* coeffs, const double* const* fields, double* out, long long n,
                cudaStream_t s);
 int op_dot_max(Plan* P, const double* a, const double* b, long long n, double* result, cudaStream_t s);
@@ -265,6 +267,13 @@ int macsav_host_mapped(const void* p, long long bytes, int* mapped) {
   }
   *mapped = 1;
   return MACSAV_OK;
+}
+
+int macsav_copy_vectors(int count, const double* const* src, double* const* dst, const long long* n, long long max_n,
+                        void* stream) {
+  if (count < 0 || max_n < 0 || (count > 0 && (!src || !dst || !n))) return MACSAV_ERR_VALUE;
+  if (count == 0 || max_n == 0) return MACSAV_OK;
+  return macsav::op_copy_vectors(count, src, dst, n, max_n, static_cast<cudaStream_t>(stream));
 }
 
 int macsav_diagnostics(macsav_plan* plan, const double* x, double r, double nu, const double* force, double* out,

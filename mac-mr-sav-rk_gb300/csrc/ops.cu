@@ -219,6 +219,29 @@ int op_layout(Plan* P, int direction, double* packed, double* u, double* v, cuda
   return cudaGetLastError() == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
 }
 
+// Copies `count` vectors, src[k] -> dst[k] (n[k] doubles each), in one
+// launch: blockIdx.y strides over the vectors, blockIdx.x and the threads over
+// each vector's elements.  The ensemble's host boundary: src or dst are then
+// pinned host arrays that the device maps, read or written over the host link.
+__global__ void __launch_bounds__(kThreads) k_copy_vectors(int count, const double* const* src, double* const* dst,
+                                                           const long long* n) {
+  for (int k = blockIdx.y; k < count; k += gridDim.y) {
+    const double* s = src[k];
+    double* d = dst[k];
+    const long long m = n[k];
+    for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < m; i += (long long)gridDim.x * kThreads)
+      d[i] = s[i];
+  }
+}
+
+int op_copy_vectors(int count, const double* const* src, double* const* dst, const long long* n, long long max_n,
+                    cudaStream_t s) {
+  const long long per = (max_n + 8LL * kThreads - 1) / (8LL * kThreads);  // about 8 elements per thread
+  const dim3 grid(unsigned(std::min<long long>(std::max<long long>(per, 1), 1024)), unsigned(std::min(count, 65535)));
+  k_copy_vectors<<<grid, kThreads, 0, s>>>(count, src, dst, n);
+  return cudaGetLastError() == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
+}
+
 void launch_convection(Plan* P, const double* x, double* out, cudaStream_t s) {
   k_convection<<<dim3(op_blocks(P->g.size), 1), kThreads, 0, s>>>(P->g, x, out);
   ++P->launches;

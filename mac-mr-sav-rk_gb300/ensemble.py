@@ -158,6 +158,8 @@ class Ensemble:
         self.t = np.zeros(len(self.members))
         self.r = np.zeros(len(self.members))
         self.last_records: list[list[StageRecord]] = []
+        self._host = None      # (pinned block, per-member views, mapped)
+        self._tables = {}      # device pointer tables of the host copies, by slot parity
 
     def __len__(self) -> int:
         return len(self.members)
@@ -183,6 +185,81 @@ class Ensemble:
         for i, m in enumerate(self.members):
             g = m.grid()
             self.set_state(i, fields.packed_curl_velocity(m.nx, m.ny, g.lx, g.ly, modes, m.seed), r0)
+
+    # ------------------------------------------------------ host boundary ---
+    def host_buffers(self) -> list[np.ndarray]:
+        """One host array per member (its packed velocity, float64), in one
+        pinned block allocated on first use and owned by the ensemble.
+        ``upload()`` moves every buffer into its member's state and
+        ``download()`` fills every buffer from it, each as one kernel that
+        reads or writes the pinned block over the host link
+        (``macsav_copy_vectors``); where the device does not map the block,
+        as one copy per member.  Either way the call returns once the data
+        have arrived."""
+        if self._host is None:
+            sizes = [m.grid().size for m in self.members]
+            block = torch.empty(sum(sizes), dtype=torch.float64, pin_memory=True)
+            offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+            views = [block[int(offs[i]):int(offs[i + 1])].numpy() for i in range(len(sizes))]
+            ok = C.c_int()
+            _lib.check(self.lib.macsav_host_mapped(block.data_ptr(), block.nbytes, C.byref(ok)), None)
+            self._host = (block, views, bool(ok.value))
+        return self._host[1]
+
+    def _copy_tables(self) -> tuple[torch.Tensor, torch.Tensor, int]:
+        """Device pointer tables (src, dst, n) for host -> states and
+        states -> host at the current slot parity of every plan."""
+        key = tuple(u.cur for u in self.units)
+        hit = self._tables.get(key)
+        if hit is None:
+            block, views, _ = self._host
+            host = [v.ctypes.data for v in views]
+            slots = [0] * len(self.members)
+            for u in self.units:
+                for j, i in enumerate(u.indices):
+                    slots[i] = u.x[u.cur, j].data_ptr()
+            n = [v.size for v in views]
+            t_in = torch.tensor([host, slots, n], dtype=torch.int64).to("cuda")
+            t_out = torch.tensor([slots, host, n], dtype=torch.int64).to("cuda")
+            hit = self._tables[key] = (t_in, t_out, max(n))
+        return hit
+
+    def _copy_all(self, upload: bool) -> None:
+        if self._host is None:
+            self.host_buffers()
+        block, views, mapped = self._host
+        if mapped:
+            t_in, t_out, max_n = self._copy_tables()
+            t = t_in if upload else t_out
+            row = t.stride(0) * t.element_size()
+            p = t.data_ptr()
+            _lib.check(self.lib.macsav_copy_vectors(len(views), p, p + row, p + 2 * row, max_n, stream_handle()),
+                       None)
+        else:
+            for i, v in enumerate(views):
+                slot, h = self.velocity(i), torch.from_numpy(v)
+                if upload:
+                    slot.copy_(h, non_blocking=True)
+                else:
+                    h.copy_(slot, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    def upload(self, r=None, t=None) -> None:
+        """Every member's state from its host buffer (``host_buffers``), with
+        optional per-member SAV scalars ``r`` and times ``t``."""
+        if r is not None and len(r) != len(self.members) or t is not None and len(t) != len(self.members):
+            raise ValueError("need one r and one t per member")
+        self._copy_all(True)
+        if r is not None:
+            self.r[:] = np.asarray(r, dtype=np.float64)
+        if t is not None:
+            self.t[:] = np.asarray(t, dtype=np.float64)
+
+    def download(self) -> list[np.ndarray]:
+        """Every member's packed velocity into its host buffer; returns the
+        buffers."""
+        self._copy_all(False)
+        return self._host[1]
 
     def velocity(self, index: int) -> torch.Tensor:
         unit, j = self._where[index]

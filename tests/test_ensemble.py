@@ -100,6 +100,40 @@ def test_ensemble_step_equals_lone_steps(precision, batched):
 
 
 @pytest.mark.gpu
+def test_host_buffers_upload_download_round_trip():
+    """All members' states in and out through the ensemble's pinned host
+    block (one kernel each way): bitwise the per-member copies, at both slot
+    parities, and a step from uploaded states equals one from set_state."""
+    import torch
+    E = _ens()
+    members = [E.Member(64, 96, 3e-3, 11), E.Member(96, 64, 2e-4, 12), E.Member(64, 96, 9e-4, 14)]
+    a = E.Ensemble(members, "sdirk2_mrsav", precision="fp64")
+    b = E.Ensemble(members, "sdirk2_mrsav", precision="fp64")
+    a.seed_fields(modes=6)
+    bufs = a.host_buffers()
+    assert [v.size for v in bufs] == [m.grid().size for m in members]
+    assert a.host_buffers()[0] is bufs[0]                     # allocated once
+    assert torch.from_numpy(bufs[0]).is_pinned()
+    for parity in range(2):
+        out = a.download()
+        for i in range(len(members)):
+            np.testing.assert_array_equal(out[i], a.velocity(i).cpu().numpy())
+        rng = np.random.default_rng(parity)
+        for v in bufs:
+            v[:] = rng.standard_normal(v.size) * 1e-2
+        a.upload(r=[1.0] * 3, t=[0.0] * 3)
+        for i in range(len(members)):
+            np.testing.assert_array_equal(a.velocity(i).cpu().numpy(), bufs[i])
+            b.set_state(i, bufs[i].copy(), r=1.0, t=0.0)
+        a.step(5e-4)
+        b.step(5e-4)
+        for i in range(len(members)):
+            assert torch.equal(a.velocity(i), b.velocity(i))
+    with pytest.raises(ValueError):
+        a.upload(r=[1.0])
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("scheme", ["sdirk3_mrsav", "sdirk2"])
 def test_batched_plan_matches_single_member_plans(scheme):
     """Members sharing a plan (one launch per kernel for all of them) give
