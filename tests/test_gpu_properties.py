@@ -238,3 +238,69 @@ def test_stage_gate_failure_raises_like_reference(pkg, name, graph):
     assert msg.startswith(head), (msg, ref)
     div = float(msg.rsplit(" ", 1)[1])
     assert div == pytest.approx(float(ref.rsplit(" ", 1)[1]), rel=1e-6)
+
+
+FULL = [("cavity512", (512, 512, 1.0, 1.0), 1e-3, 2.5e-4, 16),
+        ("cavity2048x1024", (2048, 1024, 2.0, 1.0), 5e-5, 1e-4, 64)]
+
+
+@pytest.mark.parametrize(("shape", "nu", "dt", "modes"), [f[1:] for f in FULL], ids=[f[0] for f in FULL])
+def test_full_size_fp32_bulk_tracks_fp64_and_gates_hold(pkg, shape, nu, dt, modes):
+    """The single-cavity workloads at full size (512^2 and 2048 x 1024,
+    sdirk3_mrsav, seeded curl fields): over two graph-captured steps every
+    stage passes the reference's stage gates (solver/schemes/sdirk3_mrsav.py:
+    18-65: residuals <= 1e-8, max |D u| <= 1e-8 (1 + max |u|)), and the
+    FP32-bulk form stays within 1e-12 of the FP64 path in velocity and SAV
+    scalar.  The last stage's pressures are compared through what they do to
+    the velocity: dt |grad(p32 - p64)| <= 1e-9 |u| (the pressure enters the
+    momentum balance only through its gradient, and with a weak pressure,
+    norm 5e-4 here, its own relative difference is no measure)."""
+    g = pkg.MACGrid(*shape)
+    x0 = pkg.fields.packed_curl_velocity(shape[0], shape[1], shape[2], shape[3], modes, 20261203)
+    out = {}
+    for prec in ("fp64", "fp32"):
+        model = pkg.MACNavierStokes(g, nu, precision=prec, use_graph=True)
+        state = model.state(0.0, x0, 1.0)
+        scheme = pkg.make_scheme("sdirk3_mrsav")
+        for _ in range(2):
+            trial = scheme.step(model, state, dt)
+            state = trial.state
+            umax = float(np.abs(model.vector(state)).max())
+            for st in trial.stages:
+                assert st.residual <= 1e-8 and st.scalar_residual <= 1e-8
+                assert st.divergence_inf <= 1e-8 * (1.0 + umax)
+        out[prec] = (model.vector(state), np.asarray(trial.stages[-1].pressure), state.r)
+        del model
+    (u64, p64, r64), (u32, p32, r32) = out["fp64"], out["fp32"]
+    assert np.linalg.norm(u32 - u64) <= 1e-12 * np.linalg.norm(u64)
+    dp = p32 - p64
+    grad = np.sqrt(np.sum((np.diff(dp, axis=1) / g.hx) ** 2) + np.sum((np.diff(dp, axis=0) / g.hy) ** 2))
+    assert dt * grad <= 1e-9 * np.linalg.norm(u64)
+    assert abs(r32 - r64) <= 1e-12
+
+
+def test_sav_discrete_energy_balance_at_512(pkg):
+    """The discrete modified-energy identity of tests/core/test_numerics.py:40-55
+    at the 512^2 workload size (sdirk2_mrsav, nu=1e-3, dt=2.5e-4); the bar is
+    relative to the kinetic energy, as the identity's terms scale with it."""
+    og = O.Grid(512, 512)
+    g = pkg.MACGrid(512, 512)
+    model = pkg.MACNavierStokes(g, 1e-3, use_graph=True)
+    old = vortex(og, 0.8)
+    dt, r0, eta = 2.5e-4, 0.9, 1 - 1 / np.sqrt(2)
+    n0 = O.nonlinear(og, old)
+    trial = pkg.make_scheme("sdirk2_mrsav", 2.0).step(model, model.state(0.0, old, r0), dt)
+    s1, s2 = trial.stages
+    first = np.asarray(model.backend.solve(old - dt * eta * (1 + r0) * (1 - s1.r) * n0, mass=1.0,
+                                           viscosity=model.nu * eta * dt).velocity)
+    second = model.vector(trial.state)
+    velocities, scalars = [old, first, second], [r0, s1.r, s2.r]
+    balance = 0.0
+    for i in (1, 2):
+        balance += og.inner(velocities[i] - velocities[i - 1], velocities[i]) \
+            + (scalars[i] - scalars[i - 1]) * (scalars[i] - 1)
+        for j in range(1, i + 1):
+            a = eta if i == j else 1 - 2 * eta
+            balance += dt * a * (model.nu * og.inner(O.apply_K(og, velocities[j]), velocities[i])
+                                 + 2.0 * scalars[j] * (scalars[i] - 1))
+    assert abs(balance) < 1e-11 * max(og.inner(old, old), 1.0)
