@@ -703,7 +703,12 @@ __device__ __forceinline__ void ch_mode0_warp(const ChanGrid& g, const cd* __res
   for (int j = j0; j < j1; ++j) pc[(long long)j * nm] = pc[(long long)j * nm] - mean;
 }
 
-constexpr int kSpikeThreads = 256;
+// One warp per CTA: the kernel is warp-synchronous (shuffles only), and
+// with 8-warp CTAs the 514 warps of a 512-mode, two-column solve packed into
+// 65 CTAs, so 65 of GB300's 152 SMs did all the FP64 work (ncu: FP64 pipe 86%
+// busy on the active SMs, 36% over the GPU).  Single-warp CTAs spread the
+// recurrences over every SM (3-4 warps each).
+constexpr int kSpikeThreads = 32;
 __global__ void __launch_bounds__(kSpikeThreads) k_ch_solve_spike(
     ChanGrid g, const cd* __restrict__ fu, const cd* __restrict__ fv, long long fstride, const cd* __restrict__ lu,
     const int* __restrict__ piv, const double* __restrict__ zero, cd* __restrict__ uo, cd* __restrict__ vo,
