@@ -93,9 +93,11 @@ class MACNavierStokes:
             raise ValueError("Incorrect MAC array shapes")
         if np.any(u[:, [0, -1]] != 0) or np.any(v[[0, -1], :] != 0):
             raise ValueError("Normal boundary velocities must be zero")
-        if self._host_mapped(u) and self._host_mapped(v):
-            # pinned face arrays (those of a State this model built): the pack
-            # kernel reads them over the host link, no staging copy or sync
+        if not (u.flags.writeable or v.flags.writeable) and self._host_mapped(u) and self._host_mapped(v):
+            # read-only pinned face arrays (those of a State this model built):
+            # the pack kernel reads them over the host link, no staging copy or
+            # sync.  Writable arrays take the blocking copy, so a caller may
+            # overwrite them as soon as this returns, as after MACGrid.pack.
             x = torch.empty(g.size, dtype=torch.float64, device=self.device)
             self.plan.check(self.plan.lib.macsav_layout(self.plan.handle, 1, dptr(x), u.ctypes.data, v.ctypes.data,
                                                         stream_handle()))

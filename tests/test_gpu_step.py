@@ -184,8 +184,14 @@ def test_host_state_layout_over_mapped_pinned_memory(pkg):
     assert hasattr(mapped, "_host_faces")          # packed from the pinned arrays directly
     pageable = model.device_vector(pkg.State(st.t, np.array(st.u), np.array(st.v), st.r))
     assert not hasattr(pageable, "_host_faces")    # copied
+    # writable pinned arrays are copied (blocking), so callers may reuse them at once
+    writable = torch.from_numpy(np.array(st.u)).pin_memory().numpy()
+    assert writable.flags.writeable
+    copied = model.device_vector(pkg.State(st.t, writable, st.v, st.r))
+    assert not hasattr(copied, "_host_faces")
     np.testing.assert_array_equal(mapped.cpu().numpy(), x)
     np.testing.assert_array_equal(pageable.cpu().numpy(), x)
+    np.testing.assert_array_equal(copied.cpu().numpy(), x)
     scheme = pkg.make_scheme("sdirk2_mrsav")
     a = scheme.step(model, pkg.State(st.t, st.u, st.v, st.r), 1e-3).state
     b = scheme.step(model, pkg.State(st.t, np.array(st.u), np.array(st.v), st.r), 1e-3).state
