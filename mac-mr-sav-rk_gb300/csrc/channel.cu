@@ -36,7 +36,7 @@ namespace {
 using cd = cplx<double>;
 constexpr int kKL = 3, kKU = 3, kLD = 2 * kKL + kKU + 1;  // band storage rows
 constexpr int kChThreads = 256;
-constexpr int kChSolveThreads = 8;  // threads per CTA of the per-mode recurrences
+constexpr int kChFactorThreads = 8;  // threads per CTA of the per-mode band factorisations
 
 struct ChanGrid {
   int nx, ny, nu, nv, size, np, nm;  // nm = nx/2 + 1 x modes
@@ -379,227 +379,6 @@ __global__ void k_ch_factor(ChanGrid g, double mass, double visc, cd* lu, int* p
   }
 }
 
-// One thread per (mode, column): gbtrs-style forward and back substitution
-// of the mode's factored saddle system, right-hand side in the interleaved
-// order (u_j, continuity_j, v_j), results scattered to the u/v/p spectra.
-// Both sweeps keep the active part of the vector in registers: the forward
-// sweep a window of KL+1 entries (the pivot swap and the updates of step k
-// stay inside b[k..k+KL]), the back sweep the last KL+KU solved entries, so
-// the only dependence between steps is through registers; the factor and the
-// forward results are streamed (mode-interleaved, coalesced).  Divisions by
-// pivots become multiplications by reciprocals formed off the recurrence,
-// and the back sweep subtracts the newest unknown last, so each step adds
-// about five dependent FP64 operations to the chain (GB300's FP64 latency is
-// about 67 cycles and a division about 640).  The mode 0 thread solves
-// hu0 u = fu by Thomas with the same register chaining.
-__device__ __forceinline__ void ch_solve_one(const ChanGrid& g, const cd* __restrict__ fu, const cd* __restrict__ fv,
-                                             long long fstride, const cd* __restrict__ lu, const int* __restrict__ piv,
-                                             const double* __restrict__ zero, cd* __restrict__ uo, cd* __restrict__ vo,
-                                             cd* __restrict__ po, long long vstride, long long pstride,
-                                             cd* __restrict__ work, int cols, double visc, int m, int c) {
-  const int ny = g.ny, nm = g.nm;
-  const cd* fuc = fu + c * fstride;
-  const cd* fvc = fv + c * fstride;
-  cd* uc = uo + c * vstride;
-  cd* vc = vo + c * vstride;
-  cd* pc = po + c * pstride;
-  // Loads are issued in chunks (U entries of the factor, pivots and inputs
-  // at once, all independent of the recurrence), then the chunk's steps run
-  // on registers: one memory round trip per chunk instead of one per step.
-  const cd z0 = mk(0.0, 0.0);
-  if (m == 0) {
-    constexpr int U = 8;
-    const double* cp = zero;
-    const double* dn = zero + ny;
-    const double off = -visc * g.ihy2;
-    // hu0 u = fu (Thomas), v = 0, p_{k+1} = p_k + hy fv_k, mean removed
-    cd prev = z0;
-    for (int j0 = 0; j0 < ny; j0 += U) {
-      cd f[U];
-      double d[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int j = j0 + u;
-        f[u] = j < ny ? fuc[(long long)j * nm] : z0;
-        d[u] = j < ny ? dn[j] : 1.0;
-      }
-      double rd[U];  // reciprocal pivots, off the recurrence
-#pragma unroll
-      for (int u = 0; u < U; ++u) rd[u] = 1.0 / d[u];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int j = j0 + u;
-        if (j < ny) {
-          const cd y = j == 0 ? mk(f[u].x * rd[u], f[u].y * rd[u])
-                              : mk((f[u].x - off * prev.x) * rd[u], (f[u].y - off * prev.y) * rd[u]);
-          uc[(long long)j * nm] = y;
-          prev = y;
-        }
-      }
-    }
-    cd next = prev;  // u_{ny-1} = y_{ny-1}
-    for (int j0 = ny - 2; j0 >= 0; j0 -= U) {
-      cd yv[U];
-      double e[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int j = j0 - u;
-        yv[u] = j >= 0 ? uc[(long long)j * nm] : z0;
-        e[u] = j >= 0 ? cp[j] : 0.0;
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int j = j0 - u;
-        if (j >= 0) {
-          next = mk(yv[u].x - e[u] * next.x, yv[u].y - e[u] * next.y);
-          uc[(long long)j * nm] = next;
-        }
-      }
-    }
-    for (int k = 0; k < ny - 1; ++k) vc[(long long)k * nm] = z0;
-    cd p = z0, sum = z0;
-    for (int j0 = 0; j0 < ny; j0 += U) {
-      cd f[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int j = j0 + u;
-        f[u] = (j > 0 && j < ny) ? fvc[(long long)(j - 1) * nm] : z0;
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int j = j0 + u;
-        if (j < ny) {
-          if (j > 0) p = mk(p.x + g.hy * f[u].x, p.y + g.hy * f[u].y);
-          pc[(long long)j * nm] = p;
-          sum = sum + p;
-        }
-      }
-    }
-    const cd mean = mk(sum.x / ny, sum.y / ny);
-#pragma unroll 8
-    for (int j = 0; j < ny; ++j) pc[(long long)j * nm] = pc[(long long)j * nm] - mean;
-    return;
-  }
-  static_assert(kKL == 3 && kKL + kKU == 6 && kLD == 10, "register windows below are written for KL = KU = 3");
-  const int n = 3 * ny - 1;
-  const int nmodes = nm - 1, m1 = m - 1;
-  const long long wstride = (long long)cols * nmodes;  // forward results, interleaved over (column, mode)
-  cd* y = work + (long long)c * nmodes + m1;
-  // column k of the factor starts at lu + k * cstep + m1; within it row i
-  // sits at (KL + KU + i - k) * nmodes (band_index)
-  const long long cstep = (long long)kLD * nmodes;
-  const cd* lum = lu + m1;
-  const int* pvm = piv + m1;
-  const int oL1 = 7 * nmodes, oL2 = 8 * nmodes, oL3 = 9 * nmodes;  // L(k+r, k), r = 1..3
-  const int oD = 6 * nmodes;                                          // 1 / U(k, k)
-  const long long fj = nm;                                            // spectrum row stride
-  // forward: L with row interchanges; window w0..w3 = b[k..k+3]
-  auto rhs = [&](int j, int r) -> cd {
-    return r == 0 ? fuc[(long long)j * fj + m] : (r == 1 ? z0 : fvc[(long long)j * fj + m]);
-  };
-  cd w0 = rhs(0, 0), w1 = rhs(0, 1), w2 = n > 2 ? rhs(0, 2) : z0, w3 = n > 3 ? rhs(1, 0) : z0;
-  int jr = 1, rr = 1;  // (j, r) of entry k + 4 = 3 j + r, for k = 0
-  constexpr int UF = 8;
-  for (int k0 = 0; k0 < n; k0 += UF) {
-    int pp[UF];
-    cd l1[UF], l2[UF], l3[UF], in[UF];
-    const cd* col = lum + k0 * cstep;
-#pragma unroll
-    for (int u = 0; u < UF; ++u) {
-      const int k = k0 + u;
-      pp[u] = k < n ? pvm[(long long)k * nmodes] - k : 0;  // 0..KL
-      l1[u] = k + 1 < n ? col[oL1] : z0;
-      l2[u] = k + 2 < n ? col[oL2] : z0;
-      l3[u] = k + 3 < n ? col[oL3] : z0;
-      in[u] = k + 4 < n ? rhs(jr, rr) : z0;
-      col += cstep;
-      if (++rr == 3) {
-        rr = 0;
-        ++jr;
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < UF; ++u) {
-      const int k = k0 + u;
-      if (k < n) {
-        const int p = pp[u];
-        if (p == 1) { const cd tmp = w0; w0 = w1; w1 = tmp; }
-        else if (p == 2) { const cd tmp = w0; w0 = w2; w2 = tmp; }
-        else if (p == 3) { const cd tmp = w0; w0 = w3; w3 = tmp; }
-        const cd bk = w0;
-        y[(long long)k * wstride] = bk;
-        if (k + 1 < n) w1 = w1 - cmul(l1[u], bk);
-        if (k + 2 < n) w2 = w2 - cmul(l2[u], bk);
-        if (k + 3 < n) w3 = w3 - cmul(l3[u], bk);
-        w0 = w1;
-        w1 = w2;
-        w2 = w3;
-        w3 = in[u];
-      }
-    }
-  }
-  // back: U (bandwidth KL+KU); window x1..x6 = x[k+1..k+6] (zero past n-1).
-  // U(k, k+1+i) sits at column k's base + (15 + 9 i) * nmodes.
-  cd x1 = z0, x2 = z0, x3 = z0, x4 = z0, x5 = z0, x6 = z0;
-  int jo = (n - 1) / 3, ro = (n - 1) - 3 * ((n - 1) / 3);  // (j, r) of entry k, for k = n - 1
-  constexpr int UB = 4;
-  for (int k0 = n - 1; k0 >= 0; k0 -= UB) {
-    cd yy[UB], rp[UB], a[UB][6];
-    const cd* col = lum + k0 * cstep;
-#pragma unroll
-    for (int u = 0; u < UB; ++u) {
-      const int k = k0 - u;
-      yy[u] = k >= 0 ? y[(long long)k * wstride] : z0;
-      rp[u] = k >= 0 ? col[oD] : z0;
-#pragma unroll
-      for (int i = 0; i < 6; ++i) a[u][i] = (k >= 0 && k + 1 + i < n) ? col[(15 + 9 * i) * nmodes] : z0;
-      col -= cstep;
-    }
-#pragma unroll
-    for (int u = 0; u < UB; ++u) {
-      const int k = k0 - u;
-      if (k >= 0) {
-        // the older entries first, the newest (x_{k+1}) last: one complex
-        // multiply-subtract and the pivot multiply are all that each step
-        // adds to the dependent chain
-        cd s = yy[u];
-        if (k + 6 < n) s = s - cmul(a[u][5], x6);
-        if (k + 5 < n) s = s - cmul(a[u][4], x5);
-        if (k + 4 < n) s = s - cmul(a[u][3], x4);
-        if (k + 3 < n) s = s - cmul(a[u][2], x3);
-        if (k + 2 < n) s = s - cmul(a[u][1], x2);
-        if (k + 1 < n) s = s - cmul(a[u][0], x1);
-        const cd xk = cmul(s, rp[u]);
-        x6 = x5;
-        x5 = x4;
-        x4 = x3;
-        x3 = x2;
-        x2 = x1;
-        x1 = xk;
-        const long long o = (long long)jo * fj + m;
-        if (ro == 0) uc[o] = xk;
-        else if (ro == 1) pc[o] = xk;
-        else vc[o] = xk;
-        if (--ro < 0) {
-          ro = 2;
-          --jo;
-        }
-      }
-    }
-  }
-}
-
-// One thread per (mode, column), each running ch_solve_one.
-__global__ void k_ch_solve(ChanGrid g, const cd* __restrict__ fu, const cd* __restrict__ fv, long long fstride,
-                           const cd* __restrict__ lu, const int* __restrict__ piv, const double* __restrict__ zero,
-                           cd* __restrict__ uo, cd* __restrict__ vo, cd* __restrict__ po, long long vstride,
-                           long long pstride, cd* __restrict__ work, int cols, double visc) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int m = t % g.nm, c = t / g.nm;
-  if (c >= cols) return;
-  ch_solve_one(g, fu, fv, fstride, lu, piv, zero, uo, vo, po, vstride, pstride, work, cols, visc, m, c);
-}
-
 // Partitioned (spike) substitution: one warp per (mode >= 1, column).  The
 // n = 3 ny - 1 steps of each sweep are split into 32 chunks, one per lane.
 // A sweep step is an affine map of its register window (forward: the 4
@@ -608,8 +387,8 @@ __global__ void k_ch_solve(ChanGrid g, const cd* __restrict__ fu, const cd* __re
 // gives the chunk's map W_out = T W_in + t; (2) the lanes pass the windows
 // along (W_in of chunk c+1 = T_c W_in(c) + t_c, 31 shuffle steps); (3) each
 // lane reruns its chunk from its true window.  The dependent chain per lane
-// is about 2 n / 32 + 31 steps instead of 2 n.  Mode 0 (Thomas) runs on lane 0
-// of one extra warp per column.
+// is about 2 n / 32 + 31 steps instead of 2 n.  Mode 0 runs on one extra
+// warp per column (ch_mode0_warp).
 // Mode 0 of column c by one warp: hu0 u = fu by Thomas, v = 0, and
 // p_{j+1} = p_j + hy fv_j with the mean removed.  The three recurrences are
 // affine in their carried value (y_j = a_j y_{j-1} + b_j), so each lane
@@ -1196,7 +975,7 @@ int macsav_channel_solve(macsav_channel* h, const double* rhs, int cols, double 
         return ch_cuda(&C);
     }
     cudaMemsetAsync(C.status, 0, sizeof(int), s);
-    const int tpb = macsav::kChSolveThreads;
+    const int tpb = macsav::kChFactorThreads;
     macsav::k_ch_factor<<<(g.nm + tpb - 1) / tpb, tpb, 0, s>>>(g, mass, viscosity, fresh.lu, fresh.piv, fresh.zero,
                                                               C.status);
     cudaMemcpyAsync(C.h_status, C.status, sizeof(int), cudaMemcpyDeviceToHost, s);
