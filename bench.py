@@ -1,24 +1,31 @@
 """Benchmark of the MAC mr-SAV stage hot path on one or more GB300s.
 
-Metric (cell-stage updates/s): nx*ny*(stages completed)/second for the
-512^2 sdirk3_mrsav cavity (nu=1e-3, dt=2.5e-4, psi modes k,l<=16, seeded
-synthetic field), the single-case precision configuration.  ``value`` is the
-FP32-bulk form (FP32 transforms/stencils/Krylov vectors, FP64 reductions,
-FP64 defect correction so the reference's 1e-9 Stokes and 1e-8 stage gates
-hold) with the state resident in HBM; the plain FP64 path is timed beside it
-(``fp64``) and the relative L2 difference of the two trajectories is reported.
-``e2e`` is the same metric through the public API (``scheme.step(model,
-state, dt)`` with a host ``State``: the velocity goes host->device and the new
-state device->host every step).
+Metric (cell-stage updates/s): nx*ny*(stages completed)/second.  The default
+workload is the learned-preconditioner case: the 1024^2 unit-square cavity,
+nu=1e-4, sdirk3_mrsav, dt=1e-4, stream-function modes k,l <= 32 (seeded
+synthetic field).  ``value`` is FP32 bulk with the learned preconditioner
+(FP32 transforms/stencils/Krylov vectors, FP64 reductions, FP64 defect
+correction so the reference's 1e-9 Stokes and 1e-8 stage gates hold;
+flexible CG at Krylov tolerance 1e-10 whose first search direction per Stokes
+solve comes from the trained U-Net), with the state resident in HBM.  Beside
+it: the plain FP64 path at 1e-12 (``fp64``, ``speedup_vs_fp64``), plain FP32
+bulk (``plain_fp32``), the errors against the FP64 run and, for the first
+step, against the CPU oracle; ``e2e`` is the same metric through the public
+API (``scheme.step(model, state, dt)`` with host states), ``roofline`` the
+dominant kernel against the measured HBM bandwidth, ``cpu_baseline`` the
+oracle on one step.  The network is trained and judged before the timed
+region.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload cavity512|ensemble256|adaptive2048]
+                  [--workload learned1024|cavity512|ensemble256|adaptive2048|channel512]
 
-``--workload ensemble256`` measures the mixed-size ensemble instead: 256
-cavities (nx, ny drawn from {64, 96, 128, 192, 256}, domain [0, nx/ny] x
-[0, 1], nu log-uniform in [1e-4, 1e-2], psi modes k,l <= 8, sdirk2_mrsav,
-dt=5e-4), all members' steps in flight at once (``Ensemble``); with N ranks
-the members are sharded by cell count (``scaling: strong``).
+``--workload cavity512`` is the 512^2 precision case (nu=1e-3, dt=2.5e-4,
+modes <= 16) with the FP32-vs-FP64 trajectory errors over its 200 steps;
+``ensemble256`` the mixed-size ensemble: 256 cavities (nx, ny drawn from
+{64, 96, 128, 192, 256}, domain [0, nx/ny] x [0, 1], nu log-uniform in
+[1e-4, 1e-2], psi modes k,l <= 8, sdirk2_mrsav, dt=5e-4), all members' steps
+in flight at once (``Ensemble``); with N ranks the members are sharded by
+cell count (``scaling: strong``).
 
 Multi-GPU: independent replicas of the cavity, one per rank (a single cavity
 does not shard; the reference has no distributed path), ``scaling: weak``.
@@ -169,16 +176,19 @@ def initial_state(pkg):
     return pkg.fields.packed_curl_velocity(w["nx"], w["ny"], w["lx"], w["ly"], w["psi_modes"], w["seed"])
 
 
-def cpu_baseline(steps: int = 2, threads: int = 1) -> dict:
-    """The CPU oracle (restatement of the reference path) on a bounded sample."""
+def cpu_baseline(w=None, steps: int = 2, threads: int = 1) -> dict:
+    """The CPU oracle (restatement of the reference path) on a bounded sample:
+    ``steps`` steps of workload ``w`` from its seeded field, Krylov tolerance
+    1e-12 (the reference's own)."""
     import __graft_entry__
     pkg = __graft_entry__.load_package()
     import oracle
-    w = WORKLOAD
+    w = w or WORKLOAD
     g = oracle.Grid(w["nx"], w["ny"], w["lx"], w["ly"])
     model = oracle.OracleModel(g, w["nu"], backend=oracle.TensorStokesOracle(g, 1e-9, 1e-12, workers=threads))
     scheme = oracle.make_scheme(w["scheme"])
-    state = model.state(0.0, initial_state(pkg), 0.0)
+    x0 = pkg.fields.packed_curl_velocity(w["nx"], w["ny"], w["lx"], w["ly"], w["psi_modes"], w["seed"])
+    state = model.state(0.0, x0, 1.0)
     t0 = time.perf_counter()
     for _ in range(steps):
         state = scheme.step(model, state, w["dt"]).state
@@ -190,19 +200,25 @@ def cpu_baseline(steps: int = 2, threads: int = 1) -> dict:
 
 
 def run_reference(args) -> None:
+    """The reference arm: the oracle (the reference's CPU path restated in
+    NumPy/SciPy; the reference itself is Python and cannot travel here) on
+    the same workload and metric, with every host thread for SciPy's FFTs, a
+    bounded sample of min(K, 3) steps.  Under torchrun only rank 0 runs."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    w = WORKLOAD
-    base = cpu_baseline(steps=max(1, args.steps), threads=threads)
+    w = WORKLOAD if args.workload == "cavity512" else HEADLINE
+    steps = max(1, min(args.steps, 3))
+    base = cpu_baseline(w, steps=steps, threads=threads)
     value = base["value"]
-    sec_per_step = base["seconds"] / max(1, args.steps)
-    line = {"metric": METRIC, "value": value, "unit": "cell-stage/s", "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * sec_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+    line = {"metric": METRIC, "value": value, "unit": "cell-stage/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * base["seconds"] / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded stream-function curl field)",
             "config": {"workload": w["workload"], **{k: w[k] for k in ("nx", "ny", "nu", "dt", "scheme",
-                                                                       "psi_modes")}},
+                                                                       "psi_modes")},
+                       "krylov_tolerance": 1e-12, "sample": f"{steps} steps per run"},
             "cpu_baseline": {"value": value, "unit": "cell-stage/s", "cores": threads, "kind": "port",
                              "sample": base["sample"]},
             "e2e": {"value": value, "unit": "cell-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -318,9 +334,9 @@ ADAPTIVE = {"workload": "adaptive2048x1024_sdirk3_mrsav", "nx": 2048, "ny": 1024
 def run_adaptive(args) -> None:
     """The adaptive run: 2048x1024 on [0,2]x[0,1], nu=5e-5, psi modes <= 64,
     sdirk3_mrsav with SDIRK3(2) PI control (rtol 1e-5), dt0=1e-4 to t=0.05
-    through ``integrate_adaptive`` (every attempt one fused step), FP32 bulk
-    and FP64; reports accepted / rejected attempts and the FP32 run's error
-    against the FP64 run at t_end."""
+    through the package's device-resident loop ``run_adaptive`` (every attempt
+    one fused step), FP32 bulk and FP64; reports accepted / rejected attempts
+    and the FP32 run's error against the FP64 run at t_end."""
     import torch
     import __graft_entry__
     rank, world, local = dist_env()
@@ -335,11 +351,11 @@ def run_adaptive(args) -> None:
         for precision in ("fp32", "fp64"):
             model = pkg.MACNavierStokes(g, w["nu"], precision=precision, use_graph=True)
             scheme = pkg.make_scheme(w["scheme"])
-            ctl = pkg.PIController(rtol=w["rtol"])
+            ctl = pkg.StepControl(rtol=w["rtol"], pi=(0.7, 0.4))  # the reference PIController's defaults
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            res = pkg.integrate_adaptive(model, scheme, model.state(0.0, x0, 1.0), w["t_end"], w["dt0"],
-                                         controller=ctl, retain_history=False)
+            res = pkg.run_adaptive(model, scheme, model.state(0.0, x0, 1.0), w["t_end"], w["dt0"], ctl,
+                                   keep_attempts=False)
             torch.cuda.synchronize()
             runs[precision] = (res, time.perf_counter() - t0, model.vector(res.final))
     if rank != 0:
@@ -356,8 +372,8 @@ def run_adaptive(args) -> None:
             "data": "synthetic (seeded stream-function curl field, psi modes <= 64)",
             "config": {"workload": w["workload"], **{k: w[k] for k in ("nx", "ny", "lx", "ly", "nu", "t_end", "dt0",
                                                                        "rtol", "scheme")},
-                       "controller": "PIController (SDIRK3(2) embedded error)",
-                       "note": "wall time of the whole integrate_adaptive call (host decisions included)"},
+                       "controller": "PI control (SDIRK3(2) embedded error), the reference PIController's constants",
+                       "note": "wall time of the whole run_adaptive call (host decisions included)"},
             "status": res32.status, "t_end_reached": float(res32.final.t),
             "accepted": acc32, "rejected": attempts32 - acc32,
             "fp64": {"value": cells * attempts64 / sec64, "seconds": sec64, "accepted": acc64,
@@ -369,172 +385,355 @@ def run_adaptive(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def learned_leg(pkg, g, w, x0_host, dev, args, x64) -> dict:
-    """FP32 bulk with the learned preconditioner on the same steps as ``value``:
-    the U-Net is trained here, on the GPU, on pairs logged by plain FP64 Schur
-    CG on 256^2 cavities with this workload's physics (stage shift of
-    sdirk3_mrsav: mass 1, viscosity nu*dt/4), then attached to a fresh FP32
-    model whose graph-captured steps are timed like ``value``."""
-    import torch
-    from importlib import import_module
-    L = import_module(pkg.__name__ + ".learned")
-    net, training = train_unet(pkg, w["nu"], w["dt"], w["psi_modes"])
-    scheme = pkg.make_scheme(w["scheme"])
-    stream = torch.cuda.current_stream()
-
-    def run(net_or_none):
-        model = pkg.MACNavierStokes(g, w["nu"], precision="fp32", use_graph=True)
-        if net_or_none is not None:
-            L.attach(model, net_or_none)
-        x = torch.from_numpy(x0_host.copy()).to(dev)
-        y = torch.empty_like(x)
-        pres = torch.empty((4, g.np), dtype=torch.float64, device=dev)
-        t, r = 0.0, 0.0
-        for _ in range(args.warmup):
-            y, r, _, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
-            x, y, t = y, x, t + w["dt"]
-        before = L.cg_counters(model, 2)
-        total = 0.0
-        for _ in range(args.steps):
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            y, r, _, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
-            b.record(stream)
-            b.synchronize()
-            total += a.elapsed_time(b)
-            x, y, t = y, x, t + w["dt"]
-        after = L.cg_counters(model, 2)
-        delta = {k: (sum(after[k]) - sum(before[k])) / args.steps for k in after}
-        return total / args.steps, delta, x
-
-    ms_plain, c_plain, _ = run(None)
-    ms_learned, c_learned, x = run(net)
-    cells = w["nx"] * w["ny"] * w["stages_per_step"]
-    err = float(torch.linalg.vector_norm(x - x64) / torch.linalg.vector_norm(x64))
-    return {"value": cells / (ms_learned / 1e3), "unit": "cell-stage/s", "ms_per_step": ms_learned,
-            "plain_fp32_ms_per_step": ms_plain, "speedup_vs_plain_fp32": ms_plain / ms_learned,
-            "cg_iterations_per_step": c_learned["iterations"],
-            "learned_iterations_per_step": c_learned["learned_iterations"],
-            "fallbacks_per_step": c_learned["fallbacks"],
-            "plain_fp32_cg_iterations_per_step": c_plain["iterations"],
-            "error_vs_fp64": err,
-            "network": network_info(net), "training": training}
-
-
 def network_info(net) -> dict:
     return {"params": net.num_params, "channels": list(net.channels), "activations": "bf16",
             "convolutions": ("3x3 forward on tcgen05 (BF16 operands, FP32 accumulator in TMEM), backward on CUDA cores"
                              if net.tensor_cores else "CUDA cores")}
 
 
-def train_unet(pkg, nu: float, dt: float, psi_modes: int):
-    """The U-Net of the learned preconditioner, trained on the GPU on pairs
-    logged by plain FP64 Schur CG on four 256^2 cavities with the given
-    physics (stage shift of sdirk3_mrsav: mass 1, viscosity nu*dt/4)."""
+def stage_rhs_columns(pkg, g, w, seeds, model):
+    """Two-column stage-like Stokes right-hand sides [x, dt N(x)] of seeded
+    curl fields with the workload's modes (host (size, 2) arrays)."""
+    out = []
+    for s in seeds:
+        x = pkg.fields.packed_curl_velocity(g.nx, g.ny, g.lx, g.ly, w["psi_modes"], s)
+        out.append(np.column_stack([x, w["dt"] * model.nonlinear(x).cpu().numpy()]))
+    return out
+
+
+def train_first_direction(pkg, g, w) -> tuple:
+    """The learned preconditioner of the headline workload, trained on the GPU
+    with the library's own BF16 forward/backward kernels: pairs (pressure
+    right-hand side -> error of the spectral first direction) logged by plain
+    FP64 Schur CG on the workload's grid and stage shift (mass 1, viscosity
+    nu dt / 4, the sdirk3 stage diagonal) for seeded stage-like right-hand
+    sides, restricted to the network's grid; then its output gain is set with
+    plain PCG as the judge on held-out right-hand sides."""
     import torch
     from importlib import import_module
     L = import_module(pkg.__name__ + ".learned")
     t0 = time.perf_counter()
-    grid = pkg.MACGrid(256, 256)
-    helper = pkg.MACNavierStokes(grid, nu)
-    rhs = []
-    for s in range(4):
-        x = pkg.fields.packed_curl_velocity(256, 256, 1.0, 1.0, psi_modes, 1000 + s)
-        rhs += [x, helper.nonlinear(x).cpu().numpy() * dt]
-    pairs = L.collect_pairs(grid, rhs, 1.0, nu * dt / 4)
+    helper = pkg.MACNavierStokes(g, w["nu"])
+    mass, visc = 1.0, w["nu"] * w["dt"] / 4
+    train_cols = stage_rhs_columns(pkg, g, w, range(1000, 1000 + w["train_fields"]), helper)
+    rhs = [c[:, k] for c in train_cols for k in range(2)]
+    pairs = L.collect_first_direction_pairs(g, rhs, mass, visc, restriction=w["restriction"])
     net = L.UNet(seed=0)
-    losses = L.train(net, pairs, steps=200, batch=8, lr=1e-3)
+    losses = L.train(net, pairs, steps=w["train_steps"], batch=8, lr=1e-3)
     torch.cuda.synchronize()
-    return net, {"pairs": int(pairs.inputs.shape[0]), "grid": "256x256", "nu": nu, "dt": dt, "steps": len(losses),
-                 "loss_first": float(np.mean(losses[:5])), "loss_last": float(np.mean(losses[-5:])),
-                 "seconds": time.perf_counter() - t0}
+    t_train = time.perf_counter() - t0
+    held = stage_rhs_columns(pkg, g, w, range(2000, 2000 + w["judge_fields"]), helper)
+    judge = L.calibrate_gain(net, g, held, mass, visc, restriction=w["restriction"],
+                             krylov_tolerance=w["krylov_tolerance"])
+    info = {"pairs": int(pairs.inputs.shape[0]), "logged_on": f"{g.nx}x{g.ny}",
+            "network_grid": f"{g.nx // w['restriction']}x{g.ny // w['restriction']}",
+            "shift": {"mass": mass, "viscosity": visc}, "steps": len(losses),
+            "loss_first": float(np.mean(losses[:5])), "loss_last": float(np.mean(losses[-5:])),
+            "seconds": t_train, "judge": {"held_out_solves": len(held),
+                                          "inner_iterations_per_gain": judge["iterations_per_gain"],
+                                          "gain": judge["gain"]}}
+    return net, info
 
 
-LEARNED = {"workload": "learned1024_sdirk3_mrsav", "nx": 1024, "ny": 1024, "lx": 1.0, "ly": 1.0, "nu": 1e-4,
-           "dt": 1e-4, "psi_modes": 32, "seed": 20261204, "scheme": "sdirk3_mrsav", "stages_per_step": 4,
-           "steps": 100, "krylov_tolerance": 1e-10, "reference_krylov_tolerance": 1e-12,
-           "train_nu": 1e-3, "train_dt": 2.5e-4}
-
-
-def run_learned(args) -> None:
-    """The learned-preconditioner run: 1024^2, nu=1e-4, sdirk3_mrsav, dt=1e-4,
-    psi modes <= 32, 100 steps (``--steps`` other than 10 overrides), flexible
-    CG at Krylov tolerance 1e-10 with the U-Net trained on 256^2 cavities with
-    the 512^2 workload's physics (nu=1e-3, dt=2.5e-4).  Three graph-captured
-    runs from the same field: FP64 plain at 1e-12 (the reference), FP32 bulk
-    plain and FP32 bulk with the network at 1e-10; reports each one's speed
-    and its velocity error against the FP64 run after the same steps."""
+def timed_steps(pkg, g, w, x0_host, dev, args, precision, ktol, net=None, flush=None, count_launches=False):
+    """W warm-up + K timed steps of one form on device-resident state, one CUDA
+    graph per step, per-step CUDA events on the launching stream, L2 flushed
+    (256 MiB write) before every timed step, outside the events.  Returns the
+    model, the state after W + K steps, per-step ms, inner CG iterations per
+    step and (optionally) the kernel launches of one eager step."""
     import torch
-    import __graft_entry__
     from importlib import import_module
+    L = import_module(pkg.__name__ + ".learned")
+    model = pkg.MACNavierStokes(g, w["nu"], precision=precision, use_graph=True, krylov_tolerance=ktol)
+    if net is not None:
+        L.attach(model, net)
+        L.placement(model, every_iteration=False, restriction=w["restriction"])
+    scheme = pkg.make_scheme(w["scheme"])
+    stream = torch.cuda.current_stream()
+    x = torch.from_numpy(x0_host.copy()).to(dev)
+    y = torch.empty_like(x)
+    pres = torch.empty((4, g.np), dtype=torch.float64, device=dev)
+    t, r = 0.0, 1.0
+    for _ in range(args.warmup):
+        y, r, _, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
+        x, y, t = y, x, t + w["dt"]
+    launches = None
+    if count_launches:
+        eager = pkg.MACNavierStokes(g, w["nu"], precision=precision, use_graph=False, krylov_tolerance=ktol)
+        if net is not None:
+            L.attach(eager, net)
+            L.placement(eager, every_iteration=False, restriction=w["restriction"])
+        before = eager.plan.launches
+        scheme.step_device(eager, x, t, r, w["dt"], pres=torch.empty_like(pres), want_embedded=False)
+        launches = eager.plan.launches - before
+        del eager
+    torch.cuda.synchronize()
+    before = L.cg_counters(model, 2) if precision == "fp32" else None
+    events = []
+    for _ in range(args.steps):
+        if flush is not None:
+            flush.fill_(1.0)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        y, r, _, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
+        b.record(stream)
+        events.append((a, b))
+        x, y, t = y, x, t + w["dt"]
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in events]
+    iters = None
+    if before is not None:
+        after = L.cg_counters(model, 2)
+        iters = {k: (sum(after[k]) - sum(before[k])) / args.steps for k in after}
+    return {"model": model, "x": x, "r": r, "t": t, "ms": ms, "iterations": iters, "launches": launches}
+
+
+def column_roofline(pkg, model, pass_id, reps, hbm, pk_exists, traffic_file):
+    """The dominant kernel (a transform column pass over both velocity
+    blocks, two right-hand sides) timed alone from a captured graph of
+    ``reps`` launches, against the measured HBM bandwidth."""
+    from importlib import import_module
+    lib = import_module(pkg.__name__ + "._lib")
+    stokes = import_module(pkg.__name__ + ".stokes")
+    ms_k, bytes_k = C.c_double(), C.c_double()
+    model.plan.check(lib.load().macsav_time_pass(model.plan.handle, pass_id, reps, C.byref(ms_k), C.byref(bytes_k),
+                                                 stokes.stream_handle()))
+    achieved = bytes_k.value / (ms_k.value * 1e-3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / traffic_file
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("traffic_bytes_per_launch")
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "peak_source": "measured" if pk_exists else "fallback", "traffic": traffic,
+            "bytes_per_launch": bytes_k.value, "ms_per_launch": ms_k.value}
+
+
+def fp64_roofline(pkg, g, model64, dev, hbm):
+    """The FP64 path's dominant kernel (the FP64 velocity column pass) against
+    the FP64 rate (measured here: float64 matmul 4096^3, best of 4; the FP64
+    peak is not in the measured peaks file) and against HBM."""
+    import torch
+    from importlib import import_module
+    lib = import_module(pkg.__name__ + "._lib")
+    stokes = import_module(pkg.__name__ + ".stokes")
+    ms_k64, bytes_k64 = C.c_double(), C.c_double()
+    model64.plan.check(lib.load().macsav_time_pass(model64.plan.handle, 3, 20, C.byref(ms_k64), C.byref(bytes_k64),
+                                                   stokes.stream_handle()))
+
+    def column_flops(block_cols: int, m: int) -> float:
+        # forward and inverse transform of every column, 2.5 m log2(m) each
+        return block_cols * 2 * 2.5 * m * np.log2(m)
+    lu, lv = int(2 ** np.ceil(np.log2(g.ny))), int(2 ** np.ceil(np.log2(2 * g.ny)))  # DST-II, DST-I lengths
+    flops64 = 2 * (column_flops(g.nx - 1, lu) + column_flops(g.nx, lv))  # two right-hand sides
+    a_m = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    best = float("inf")
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a_m, a_m)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a_m
+    fp64_peak = 2 * 4096 ** 3 / (best * 1e-3) / 1e12
+    fp64_achieved = flops64 / (ms_k64.value * 1e-3) / 1e12
+    gbs = bytes_k64.value / (ms_k64.value * 1e-3) / 1e9
+    return {"kernel": "k_column_p2<double> (velocity blocks, 2 RHS)", "bound": "fp64",
+            "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": fp64_achieved / fp64_peak,
+            "peak_source": "measured here: float64 matmul 4096^3 (torch), best of 4",
+            "flops_per_launch": flops64, "flop_convention": "2.5 m log2(m) per line and direction",
+            "ms_per_launch": ms_k64.value, "bytes": {"achieved": gbs, "unit": "GB/s", "frac_of_hbm": gbs / hbm}}
+
+
+def e2e_steps(pkg, model, w, x0_host, args, pageable: bool) -> float:
+    """Seconds for K steps through the public API, ``scheme.step(model,
+    state, dt)``, with host states: every step its velocity goes host ->
+    device and the new state device -> host.  pinned: each step gets the
+    previous step's host face arrays (the library's pinned, device-mapped
+    arrays); pageable: fresh NumPy copies of them (the staging-copy path a
+    caller's own arrays take)."""
+    import torch
+    g = model.grid
+    scheme = pkg.make_scheme(w["scheme"])
+    st = pkg.State(0.0, *g.unpack(x0_host), 1.0)
+
+    def fresh(s):
+        if pageable:
+            return pkg.State(s.t, np.array(s.u), np.array(s.v), s.r)
+        return pkg.State(s.t, s.u, s.v, s.r)  # host arrays only, no cached device vector
+    for _ in range(args.warmup):
+        st = scheme.step(model, fresh(st), w["dt"]).state
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = scheme.step(model, fresh(st), w["dt"]).state
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0
+
+
+HEADLINE = {"workload": "learned1024_sdirk3_mrsav", "nx": 1024, "ny": 1024, "lx": 1.0, "ly": 1.0, "nu": 1e-4,
+            "dt": 1e-4, "psi_modes": 32, "seed": 20261204, "scheme": "sdirk3_mrsav", "stages_per_step": 4,
+            "krylov_tolerance": 1e-10, "reference_krylov_tolerance": 1e-12, "restriction": 4,
+            "train_fields": 32, "train_steps": 400, "judge_fields": 3}
+
+
+def oracle_step(w, x0, threads: int):
+    """One step of the workload by the CPU oracle (the reference's path
+    restated in NumPy/SciPy) from x0; returns (seconds, new velocity)."""
+    import oracle
+    g = oracle.Grid(w["nx"], w["ny"], w["lx"], w["ly"])
+    model = oracle.OracleModel(g, w["nu"], backend=oracle.TensorStokesOracle(
+        g, 1e-9, w.get("reference_krylov_tolerance", 1e-12), workers=threads))
+    scheme = oracle.make_scheme(w["scheme"])
+    state = model.state(0.0, x0, 1.0)
+    t0 = time.perf_counter()
+    state = scheme.step(model, state, w["dt"]).state
+    return time.perf_counter() - t0, model.vector(state)
+
+
+def run_headline(args) -> None:
+    """The headline workload: 1024^2 unit-square cavity, nu=1e-4,
+    sdirk3_mrsav, dt=1e-4, psi modes k,l <= 32.  ``value`` is FP32 bulk with
+    the learned preconditioner (flexible CG, Krylov tolerance 1e-10); beside
+    it the plain FP64 path at 1e-12 (the reference's own setting, the only one
+    at which its gates hold here), plain FP32 bulk at 1e-10, their errors
+    against the FP64 run after the same steps and, for the first step, against
+    the CPU oracle itself."""
+    import torch
+    import torch.distributed as dist
+    import __graft_entry__
     rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     __graft_entry__.build()
     pkg = __graft_entry__.load_package()
-    L = import_module(pkg.__name__ + ".learned")
-    w = LEARNED
-    steps = w["steps"] if args.steps == 10 else args.steps
+    from importlib import import_module
+    lib = import_module(pkg.__name__ + "._lib")
+    w = HEADLINE
     g = pkg.MACGrid(w["nx"], w["ny"], w["lx"], w["ly"])
     dev = torch.device("cuda", local)
-    x0 = pkg.fields.packed_curl_velocity(w["nx"], w["ny"], w["lx"], w["ly"], w["psi_modes"], w["seed"])
-    net, training = train_unet(pkg, w["train_nu"], w["train_dt"], w["psi_modes"])
-    stream = torch.cuda.current_stream()
+    x0_host = pkg.fields.packed_curl_velocity(w["nx"], w["ny"], w["lx"], w["ly"], w["psi_modes"], w["seed"])
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
 
-    def run(precision, ktol, with_net):
-        model = pkg.MACNavierStokes(g, w["nu"], precision=precision, use_graph=True, krylov_tolerance=ktol)
-        if with_net:
-            L.attach(model, net)
-        scheme = pkg.make_scheme(w["scheme"])
-        x = torch.from_numpy(x0.copy()).to(dev)
-        y = torch.empty_like(x)
-        pres = torch.empty((4, g.np), dtype=torch.float64, device=dev)
-        t, r = 0.0, 1.0
-        for _ in range(args.warmup):
-            y, r, _, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
-            x, y, t = y, x, t + w["dt"]
-        before = L.cg_counters(model, 2) if precision == "fp32" else None
-        total = 0.0
-        for _ in range(steps):
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            y, r, _, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
-            b.record(stream)
-            b.synchronize()
-            total += a.elapsed_time(b)
-            x, y, t = y, x, t + w["dt"]
-        iters = None
-        if before is not None:
-            after = L.cg_counters(model, 2)
-            iters = {k: (sum(after[k]) - sum(before[k])) / steps for k in after}
-        return total / steps, x, iters
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
 
+    net, training = train_first_direction(pkg, g, w)
+    barrier()
     with ClockSampler(local) as clk:
-        ms64, x64, _ = run("fp64", w["reference_krylov_tolerance"], False)
-        ms32, x32, it32 = run("fp32", w["krylov_tolerance"], False)
-        msl, xl, itl = run("fp32", w["krylov_tolerance"], True)
-    if rank != 0:
-        return
-    cells = w["nx"] * w["ny"] * w["stages_per_step"]
+        learned = timed_steps(pkg, g, w, x0_host, dev, args, "fp32", w["krylov_tolerance"], net, flush, True)
+    barrier()
+    plain = timed_steps(pkg, g, w, x0_host, dev, args, "fp32", w["krylov_tolerance"], None, flush)
+    barrier()
+    fp64 = timed_steps(pkg, g, w, x0_host, dev, args, "fp64", w["reference_krylov_tolerance"], None, flush)
+    barrier()
+    tot = torch.tensor([sum(learned["ms"]), sum(plain["ms"]), sum(fp64["ms"])], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(tot, op=dist.ReduceOp.MAX)
+    ms_l, ms_p, ms_64 = (float(v) for v in tot)
+    cells = w["nx"] * w["ny"] * w["stages_per_step"] * args.steps * world
 
     def err(x):
-        return float(torch.linalg.vector_norm(x - x64) / torch.linalg.vector_norm(x64))
+        return float(torch.linalg.vector_norm(x - fp64["x"]) / torch.linalg.vector_norm(fp64["x"]))
 
-    line = {"metric": METRIC, "value": cells / (msl / 1e3), "unit": "cell-stage/s", "n_gpus": world,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": msl, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "fp32+bf16 network+fp64",
-            "data": "synthetic (seeded stream-function curl field, psi modes <= 32)",
-            "config": {"workload": w["workload"], **{k: w[k] for k in ("nx", "ny", "nu", "dt", "scheme",
-                                                                       "krylov_tolerance",
-                                                                       "reference_krylov_tolerance")},
-                       "note": "value = FP32 bulk with the learned preconditioner (flexible CG in the FP32 "
-                               "inner solves; FP64 defect correction and the reference's gates unchanged)"},
-            "error_vs_fp64": err(xl), "cg_iterations_per_step": itl,
-            "plain_fp32": {"value": cells / (ms32 / 1e3), "ms_per_step": ms32, "error_vs_fp64": err(x32),
-                           "cg_iterations_per_step": it32},
-            "fp64": {"value": cells / (ms64 / 1e3), "ms_per_step": ms64, "unit": "cell-stage/s"},
-            "speedup_vs_fp64": ms64 / msl, "speedup_vs_plain_fp32": ms32 / msl,
-            "network": network_info(net), "training": training, "clocks": clk.summary()}
+    # end to end through scheme.step with host states (learned form)
+    e2e_pinned = e2e_steps(pkg, learned["model"], w, x0_host, args, pageable=False)
+    e2e_pageable = e2e_steps(pkg, learned["model"], w, x0_host, args, pageable=True)
+    et = torch.tensor([e2e_pinned, e2e_pageable], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(et, op=dist.ReduceOp.MAX)
+    face_bytes = (g.ny * (g.nx + 1) + (g.ny + 1) * g.nx) * 8
+    rec_bytes = C.sizeof(lib.StageRecord)
+
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    roof = column_roofline(pkg, plain["model"], 0, 50, hbm, pk.exists(), "column_pass_traffic_1024.json")
+    roof["kernel"] = "k_column_p2<float,1024> (velocity blocks, 2 RHS)"
+    roof64 = fp64_roofline(pkg, g, fp64["model"], dev, hbm)
+
+    # the first step of each GPU form against the CPU oracle's first step
+    first = {}
+    for name, prec, ktol, with_net in (("fp64", "fp64", w["reference_krylov_tolerance"], False),
+                                       ("fp32_learned", "fp32", w["krylov_tolerance"], True)):
+        class _One:
+            steps, warmup = 1, 0
+        first[name] = timed_steps(pkg, g, w, x0_host, dev, _One, prec, ktol, net if with_net else None)["x"]
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    threads = 1
+    oracle_sec, oracle_x = (None, None) if args.no_cpu_baseline else oracle_step(w, x0_host, threads)
+    vs_oracle = None
+    if oracle_x is not None:
+        ox = torch.from_numpy(oracle_x).to(dev)
+        vs_oracle = {k: float(torch.linalg.vector_norm(v - ox) / torch.linalg.vector_norm(ox))
+                     for k, v in first.items()}
+    cav = quick_cavity512(pkg, dev, args, flush)
+    line = {
+        "metric": METRIC, "value": cells / (ms_l / 1e3), "unit": "cell-stage/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_l / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+bf16 network+fp64",
+        "data": "synthetic (seeded stream-function curl field, psi modes <= 32)",
+        "config": {"workload": w["workload"], **{k: w[k] for k in ("nx", "ny", "nu", "dt", "scheme", "psi_modes",
+                                                                   "krylov_tolerance", "reference_krylov_tolerance")},
+                   "parallelism": f"replicas{world}",
+                   "form": "fp32 transforms/stencils/Krylov + fp64 reductions + fp64 defect correction; "
+                           "flexible CG with the learned first direction",
+                   "learned_placement": f"first search direction of each Stokes solve, network on the "
+                                        f"{w['restriction']}x{w['restriction']}-restricted residual",
+                   "l2": "flushed (256 MiB write) before every timed step", "graph": "one CUDA graph per step"},
+        "speedup_vs_fp64": ms_64 / ms_l,
+        "error_vs_fp64": {"rel_l2_velocity": err(learned["x"]), "after_steps": args.warmup + args.steps},
+        "error_vs_oracle_first_step": vs_oracle,
+        "cg_iterations_per_step": learned["iterations"],
+        "plain_fp32": {"value": cells / (ms_p / 1e3), "ms_per_step": ms_p / args.steps,
+                       "error_vs_fp64": err(plain["x"]), "cg_iterations_per_step": plain["iterations"]},
+        "fp64": {"value": cells / (ms_64 / 1e3), "ms_per_step": ms_64 / args.steps, "unit": "cell-stage/s",
+                 "krylov_tolerance": w["reference_krylov_tolerance"]},
+        "learned_vs_plain_fp32": ms_p / ms_l,
+        "network": network_info(net), "training": training,
+        "clocks": clk.summary(),
+        "e2e": {"value": cells / float(et[0]), "unit": "cell-stage/s", "h2d_bytes_per_step": face_bytes,
+                "d2h_bytes_per_step": face_bytes + w["stages_per_step"] * rec_bytes,
+                "host_memory": "the library's pinned, device-mapped state arrays fed back each step",
+                "pageable": {"value": cells / float(et[1]),
+                             "host_memory": "fresh pageable NumPy copies of the face arrays each step"}},
+        "gpu_launches": int(learned["launches"] * args.steps),
+        "roofline": roof,
+        "roofline_fp64": roof64,
+        "cavity512_sdirk3_mrsav": cav,
+    }
+    if oracle_sec is not None:
+        line["cpu_baseline"] = {"value": w["nx"] * w["ny"] * w["stages_per_step"] / oracle_sec,
+                                "unit": "cell-stage/s", "cores": threads, "kind": "port",
+                                "sample": f"one step of the {w['workload']} workload (NumPy/SciPy oracle, "
+                                          f"{threads} thread, Krylov 1e-12)"}
     print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def quick_cavity512(pkg, dev, args, flush) -> dict:
+    """The 512^2 precision case (nu=1e-3, dt=2.5e-4, modes <= 16, sdirk3_mrsav):
+    FP32 bulk (plain preconditioner) and FP64 on the same K steps."""
+    w = dict(WORKLOAD, restriction=1)
+    g = pkg.MACGrid(w["nx"], w["ny"], w["lx"], w["ly"])
+    x0 = initial_state(pkg)
+    a = timed_steps(pkg, g, w, x0, dev, args, "fp32", 1e-12, None, flush)
+    b = timed_steps(pkg, g, w, x0, dev, args, "fp64", 1e-12, None, flush)
+    import torch
+    cells = w["nx"] * w["ny"] * w["stages_per_step"] * args.steps
+    return {"value": cells / (sum(a["ms"]) / 1e3), "ms_per_step": sum(a["ms"]) / args.steps,
+            "fp64": {"value": cells / (sum(b["ms"]) / 1e3), "ms_per_step": sum(b["ms"]) / args.steps},
+            "error_vs_fp64": float(torch.linalg.vector_norm(a["x"] - b["x"]) / torch.linalg.vector_norm(b["x"])),
+            "unit": "cell-stage/s"}
 
 
 def profile_unet() -> None:
@@ -553,25 +752,57 @@ def profile_unet() -> None:
     print(json.dumps({"profile": "unet", "out_norm": float(y.norm())}))
 
 
-def profile_steps(precision: str) -> None:
-    """Two eager steps of the bench workload (the launch list and kernel
-    captures of profiles/ come from this)."""
+def profile_steps(precision: str, workload: str) -> None:
+    """Two eager steps of a workload (the launch lists and kernel captures of
+    profiles/ come from this).  precision "learned": the headline's FP32 form
+    with an (untrained) network in its first-direction placement, so that no
+    training kernels precede the steps."""
     import torch
     import __graft_entry__
+    from importlib import import_module
     __graft_entry__.build()
     pkg = __graft_entry__.load_package()
-    w = WORKLOAD
+    w = HEADLINE if workload == "learned1024" else WORKLOAD
     g = pkg.MACGrid(w["nx"], w["ny"], w["lx"], w["ly"])
-    model = pkg.MACNavierStokes(g, w["nu"], precision=precision, use_graph=False)
+    ktol = w.get("krylov_tolerance", 1e-12) if precision != "fp64" else 1e-12
+    model = pkg.MACNavierStokes(g, w["nu"], precision="fp64" if precision == "fp64" else "fp32", use_graph=False,
+                                krylov_tolerance=ktol)
+    if precision == "learned":
+        L = import_module(pkg.__name__ + ".learned")
+        net = L.UNet(seed=0)
+        L.attach(model, net)
+        L.placement(model, every_iteration=False, restriction=w["restriction"])
     scheme = pkg.make_scheme(w["scheme"])
-    x = torch.from_numpy(initial_state(pkg)).to("cuda")
-    t, r = 0.0, 0.0
+    x = torch.from_numpy(pkg.fields.packed_curl_velocity(w["nx"], w["ny"], w["lx"], w["ly"], w["psi_modes"],
+                                                         w["seed"])).to("cuda")
+    t, r = 0.0, 1.0
     for _ in range(2):
         x, r, recs, _, _ = scheme.step_device(model, x, t, r, w["dt"], want_embedded=False)
         t += w["dt"]
     torch.cuda.synchronize()
-    print(json.dumps({"profile": precision, "launches": model.plan.launches,
+    print(json.dumps({"profile": precision, "workload": w["workload"], "launches": model.plan.launches,
                       "iterations": [list(rc.iterations[:2]) for rc in recs]}))
+
+
+def profile_pass(workload: str, pass_id: int) -> None:
+    """Three launches of one transform pass (macsav_time_pass: 0 the FP32
+    velocity column pass, 3 the FP64 one) on the workload's grid, after one
+    warm-up launch, for a DRAM-traffic capture of that kernel."""
+    import torch
+    import __graft_entry__
+    from importlib import import_module
+    __graft_entry__.build()
+    pkg = __graft_entry__.load_package()
+    lib = import_module(pkg.__name__ + "._lib")
+    stokes = import_module(pkg.__name__ + ".stokes")
+    w = HEADLINE if workload == "learned1024" else WORKLOAD
+    g = pkg.MACGrid(w["nx"], w["ny"], w["lx"], w["ly"])
+    model = pkg.MACNavierStokes(g, w["nu"], precision="fp64" if pass_id == 3 else "fp32")
+    ms_k, bytes_k = C.c_double(), C.c_double()
+    model.plan.check(lib.load().macsav_time_pass(model.plan.handle, pass_id, 3, C.byref(ms_k), C.byref(bytes_k),
+                                                 stokes.stream_handle()))
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "pass", "pass": pass_id, "workload": w["workload"], "bytes": bytes_k.value}))
 
 
 CHANNEL = {"workload": "channel512_fft_stokes", "nx": 512, "ny": 512, "lx": 6.283185307179586, "ly": 1.0,
@@ -608,6 +839,11 @@ def run_channel(args) -> None:
             vel, pres, res, div = solver.solve_device(f, w["mass"], visc)
             torch.cuda.synchronize()
             times.append(time.perf_counter() - t0)
+    # the solve's own gate (FFTStokes: residual and divergence <= tolerance):
+    # a timing of a wrong solve is no timing
+    umax = float(vel.abs().max())
+    if not (res <= 1e-9 and div <= 1e-9 * (1.0 + umax)):
+        raise RuntimeError(f"channel solve failed its gate: residual {res:.3e}, divergence {div:.3e}")
     if rank != 0:
         return
     sec = statistics.median(times)
@@ -640,11 +876,11 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["cavity512", "ensemble256", "adaptive2048", "learned1024", "channel512"],
-                    default="cavity512")
-    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner leg")
-    ap.add_argument("--profile", choices=["fp32", "fp64", "unet"], default=None,
-                    help="run two eager steps of the workload and exit (for ncu captures)")
+    ap.add_argument("--workload", choices=["learned1024", "cavity512", "ensemble256", "adaptive2048", "channel512"],
+                    default="learned1024")
+    ap.add_argument("--profile", choices=["fp32", "fp64", "learned", "unet", "pass0", "pass3"], default=None,
+                    help="run two eager steps of the workload (or launches of one transform pass) and exit, "
+                         "for ncu captures")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -652,8 +888,11 @@ def main() -> None:
     if args.profile == "unet":
         profile_unet()
         return
+    if args.profile in ("pass0", "pass3"):
+        profile_pass(args.workload, int(args.profile[-1]))
+        return
     if args.profile:
-        profile_steps(args.profile)
+        profile_steps(args.profile, args.workload)
         return
     if args.warmup < 3:
         args.warmup = 3
@@ -664,7 +903,7 @@ def main() -> None:
         run_adaptive(args)
         return
     if args.workload == "learned1024":
-        run_learned(args)
+        run_headline(args)
         return
     if args.workload == "channel512":
         run_channel(args)
@@ -817,7 +1056,6 @@ def main() -> None:
     if tf.exists():
         traffic = json.loads(tf.read_text()).get("traffic_bytes_per_launch")
 
-    learned = None if args.no_learned else learned_leg(pkg, g, w, x0_host, dev, args, x64)
 
     # FP64 path: its dominant kernel (the FP64 velocity column pass) against
     # the FP64 rate and against HBM.  The FP64 peak is not in the measured
@@ -857,7 +1095,7 @@ def main() -> None:
         if world > 1:
             dist.destroy_process_group()
         return
-    base = None if args.no_cpu_baseline else cpu_baseline(steps=2, threads=1)
+    base = None if args.no_cpu_baseline else cpu_baseline(WORKLOAD, steps=2, threads=1)
     mean_iters = float(np.mean([[a, b] for stage in it32 for (a, b) in stage]))
     line = {
         "metric": METRIC, "value": value, "unit": "cell-stage/s", "n_gpus": world, "steps": args.steps,
@@ -883,8 +1121,6 @@ def main() -> None:
                      "traffic": traffic, "bytes_per_launch": bytes_k.value, "ms_per_launch": ms_k.value},
         "roofline_fp64": roofline64,
     }
-    if learned is not None:
-        line["learned"] = learned
     if base is not None:
         line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line), flush=True)

@@ -122,8 +122,11 @@ int macsav_max_abs(macsav_plan* plan, const double* a, long long n, double* resu
  * (larger n: MACSAV_ERR_UNSUPPORTED, before any device work; NULL a/result or
  * n < 0: MACSAV_ERR_VALUE).  The first call on each device finds the array's
  * address (this may load the module) and clears its completion counter:
- * make it outside any stream capture.  Calls share that array, so calls
- * that overlap on the device race: order them (e.g. one stream). */
+ * make it outside any stream capture.  The address is kept per device
+ * context: after cudaDeviceReset (or any new context on the device) the next
+ * call repeats that set-up, and is again a first call.  Calls share that
+ * array, so calls that overlap on the device race: order them (e.g. one
+ * stream). */
 #define MACSAV_STATIC_REDUCE_MAX_N 16777216LL
 int macsav_inner_max_static(const double* a, const double* b, long long n, double weight, double* result,
                             void* stream);
@@ -256,6 +259,16 @@ int macsav_unet_train_step(macsav_unet* net, const float* in, const float* targe
 /* Attach (net != NULL) or detach the learned preconditioner of an FP32_MIXED
  * plan.  The plan keeps a pointer: destroy the plan (or detach) first. */
 int macsav_plan_set_preconditioner(macsav_plan* plan, macsav_unet* net, int learned_max_iterations);
+/* Where the attached network is evaluated.  every_iteration = 0 (the
+ * default): only in the first CG iteration of the first FP32 inner solve of
+ * each Stokes solve, i.e. it shapes the first search direction of the solve
+ * of the stage's own right-hand side, and the remaining iterations are
+ * flexible CG with the spectral preconditioner; 1: in every iteration of
+ * every inner solve.  restriction f = 1, 2 or 4: the network sees the residual
+ * averaged over f x f cells (nx / f, ny / f multiples of 8) and its output is
+ * prolonged bilinearly to the cells, which makes one evaluation f^2 times
+ * cheaper.  No reference counterpart (see macsav_unet above). */
+int macsav_plan_set_learned_placement(macsav_plan* plan, int every_iteration, int restriction);
 /* Per-column CG counters since the start of the last macsav_stokes_solve:
  * iterations of every inner solve, those run with the network, and plain-PCG
  * restarts. */

@@ -57,12 +57,6 @@ class Trial:
     embedded_velocity: Any | None = None
 
 
-@dataclass
-class History:
-    state: State
-    accepted_steps: int = 0
-
-
 class DeviceArray:
     """A device-resident field that turns into a NumPy array on demand
     (``np.asarray(x)``); ``.tensor`` is the CUDA tensor itself."""

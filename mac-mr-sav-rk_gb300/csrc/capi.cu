@@ -467,6 +467,36 @@ int macsav_unet_train_step(macsav_unet* net, const float* in, const float* targe
   return cudaGetLastError() == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
 }
 
+// The plan's buffers for a network that works on the cells restricted by f:
+// the network workspace (batch = the plan's columns), the full-resolution
+// output, the previous residual and the scales, and the restricted input and
+// output when f > 1.
+static int net_buffers(Plan* P, macsav::UNet* net, int f) {
+  const int ny = P->g.ny, nx = P->g.nx;
+  if (ny % f || nx % f)
+    return fail(P, MACSAV_ERR_UNSUPPORTED, "the restriction factor must divide nx and ny");
+  const int rc = macsav::net_work_ensure(net, &P->netw, P->maxcols, ny / f, nx / f, false);
+  if (rc == MACSAV_ERR_UNSUPPORTED)
+    return fail(P, rc, "the learned preconditioner needs nx / f and ny / f multiples of 8 (f: restriction)");
+  if (rc != MACSAV_OK) return cuda_status(P);
+  const size_t cells = size_t(P->maxcols) * P->g.np;
+  if (!P->net_out) {
+    if (cudaMalloc(&P->net_out, cells * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&P->net_rold, cells * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&P->net_scale, 2 * macsav::kMaxCols * sizeof(float)) != cudaSuccess)
+      return cuda_status(P);
+    cudaMemset(P->net_rold, 0, cells * sizeof(float));
+  }
+  if (f > 1 && !P->net_cin) {
+    // sized for the finest restriction (f = 2) so a later change of f reuses them
+    const size_t coarse = size_t(P->maxcols) * (ny / 2) * (nx / 2);
+    if (cudaMalloc(&P->net_cin, coarse * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&P->net_cout, coarse * sizeof(float)) != cudaSuccess)
+      return cuda_status(P);
+  }
+  return MACSAV_OK;
+}
+
 int macsav_plan_set_preconditioner(macsav_plan* plan, macsav_unet* net, int learned_max_iterations) {
   if (!plan) return MACSAV_ERR_VALUE;
   Plan* P = &plan->p;
@@ -481,20 +511,28 @@ int macsav_plan_set_preconditioner(macsav_plan* plan, macsav_unet* net, int lear
     return fail(P, MACSAV_ERR_UNSUPPORTED, "the learned preconditioner runs in the FP32 inner solves (FP32_MIXED)");
   if (learned_max_iterations < 1 || learned_max_iterations > 1000)
     return fail(P, MACSAV_ERR_VALUE, "learned_max_iterations must be in 1..1000");
-  const int rc = macsav::net_work_ensure(&net->net, &P->netw, P->maxcols, P->g.ny, P->g.nx, false);
-  if (rc == MACSAV_ERR_UNSUPPORTED) return fail(P, rc, "the learned preconditioner needs nx, ny multiples of 8");
-  if (rc != MACSAV_OK) return cuda_status(P);
-  const size_t cells = size_t(P->maxcols) * P->g.np;
-  if (!P->net_out) {
-    if (cudaMalloc(&P->net_out, cells * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&P->net_rold, cells * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&P->net_scale, 2 * macsav::kMaxCols * sizeof(float)) != cudaSuccess)
-      return cuda_status(P);
-    cudaMemset(P->net_rold, 0, cells * sizeof(float));
-  }
+  const int rc = net_buffers(P, &net->net, P->net_restrict);
+  if (rc != MACSAV_OK) return rc;
   P->net = &net->net;
   P->net_maxit = learned_max_iterations;
   return cudaDeviceSynchronize() == cudaSuccess ? MACSAV_OK : cuda_status(P);
+}
+
+int macsav_plan_set_learned_placement(macsav_plan* plan, int every_iteration, int restriction) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  if (restriction != 1 && restriction != 2 && restriction != 4)
+    return fail(P, MACSAV_ERR_VALUE, "restriction must be 1, 2 or 4");
+  cudaDeviceSynchronize();
+  for (auto& kv : P->st.graphs) cudaGraphExecDestroy(kv.exec);  // captured with the old placement
+  P->st.graphs.clear();
+  if (P->net) {
+    const int rc = net_buffers(P, P->net, restriction);
+    if (rc != MACSAV_OK) return rc;
+  }
+  P->net_every = every_iteration ? 1 : 0;
+  P->net_restrict = restriction;
+  return MACSAV_OK;
 }
 
 int macsav_plan_cg_counters(macsav_plan* plan, int columns, int* iterations, int* learned_iterations,

@@ -141,6 +141,15 @@ struct Plan {
   float* net_rold = nullptr;   // previous residual (Polak-Ribiere beta), [maxcols][np]
   float* net_scale = nullptr;  // per-column input and output scales, [2][maxcols]
   int net_maxit = 20;          // learned iterations before the plain-PCG restart
+  // placement: every_iter = 0 evaluates the network only in the first CG
+  // iteration of the first inner solve of each Stokes solve (its first search
+  // direction); 1 in every iteration of every inner solve.  The network works
+  // on the residual restricted by `restrict_f` (1, 2 or 4: f x f cell means)
+  // and its output is prolonged bilinearly back to the cells.
+  int net_every = 0;
+  int net_restrict = 1;
+  float* net_cin = nullptr;    // restricted network input,  [maxcols][np / f^2]
+  float* net_cout = nullptr;   // restricted network output, [maxcols][np / f^2]
 
   // residual / preconditioned residual / iterate log of eager FP64 solves
   double* log_r = nullptr;

@@ -26,10 +26,17 @@
 // thread) looks up the array's device address with cudaGetSymbolAddress and
 // clears the counter with cudaMemsetAsync on the caller's stream.  The lookup
 // may load the module, so make that first call outside any stream capture.
+// The address belongs to the device's context: a call that finds a different
+// context current (after cudaDeviceReset, or after the primary context was
+// released and made again) repeats the set-up for the new context, so it never
+// hands the kernel an address of a context that is gone.  Such a call is again
+// a first call, to be made outside any stream capture.
 //
 // Calls share the one array per device: two calls whose kernels overlap (on
 // different streams, or from different threads without ordering) race on the
 // partials, the counter and the result.  Order them, e.g. on one stream.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "common.cuh"
@@ -91,18 +98,49 @@ __global__ void __launch_bounds__(kSRThreads) k_inner_max_static(const double* a
 
 std::mutex g_setup_lock;
 double* g_scratch_ptr[kSRMaxDevices] = {};
+unsigned long long g_scratch_ctx[kSRMaxDevices] = {};  // context id the address belongs to
 
-// Device address of the scratch on the current device; set-up on first use.
+// The driver's id of the context current on this thread (0 when none is
+// current yet).  The two driver entry points are looked up through the
+// runtime once, so the library does not link the driver library itself.
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+    void *f1 = nullptr, *f2 = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess) {
+      get_current = reinterpret_cast<GetCurrent>(f1);
+      get_id = reinterpret_cast<GetId>(f2);
+    }
+    looked_up = true;
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
+
+// Device address of the scratch on the current device; set-up on the first
+// use in each context of that device.
 int scratch_for_current_device(double** out, cudaStream_t s) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (dev < 0 || dev >= kSRMaxDevices) return MACSAV_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> hold(g_setup_lock);
-  if (!g_scratch_ptr[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_scratch_ptr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
     double* ptr = nullptr;
     if (cudaGetSymbolAddress((void**)&ptr, g_reduce_scratch) != cudaSuccess || !ptr) return MACSAV_ERR_CUDA;
     if (cudaMemsetAsync(ptr + kSRCounter, 0, sizeof(double), s) != cudaSuccess) return MACSAV_ERR_CUDA;
     g_scratch_ptr[dev] = ptr;
+    g_scratch_ctx[dev] = current_context_id();  // the lookup made the context current if none was
   }
   *out = g_scratch_ptr[dev];
   return MACSAV_OK;

@@ -212,7 +212,8 @@ __global__ void k_net_scales(const CGScalars* cg, const int* active, int cols, i
   scale[cols + c] = on ? float(rms * g.rho / g.rr) : 0.0f;
 }
 
-// z += net output; partial sums of z, r.z, r_old.z, r, r_old (OP_FCG).
+// z += net output (add null: z unchanged); partial sums of z, r.z, r_old.z,
+// r, r_old (OP_FCG).
 __global__ void __launch_bounds__(kThreads) k_fcg_z(int np, float* z, const float* add, const float* r,
                                                     const float* r_old, long long cs, const CGScalars* cg,
                                                     const int* active, double* partial, CGFin<float> fin,
@@ -223,7 +224,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_z(int np, float* z, const floa
   if (active[c]) {
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
       const long long k = c * cs + idx;
-      const float zn = z[k] + add[k];
+      const float zn = add ? z[k] + add[k] : z[k];
       z[k] = zn;
       const float rv = r[k], ro = r_old[k];
       a[0].add(zn);
@@ -245,6 +246,47 @@ __global__ void __launch_bounds__(kThreads) k_fcg_center(int np, float* z, long 
   if (!active[c]) return;
   const float m = cg[c].mean_z_t;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) z[c * cs + idx] -= m;
+}
+
+// Restricted network input: the mean of each f x f block of cells of r, times
+// the column's input scale.  One thread per coarse cell and column.
+__global__ void __launch_bounds__(kThreads) k_net_restrict(int ny, int nx, int f, const float* r, long long cs,
+                                                           const float* scale, float* out) {
+  pdl_wait();
+  const int c = blockIdx.y;
+  const int nyc = ny / f, nxc = nx / f;
+  const float w = scale[c] / float(f * f);
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nyc * nxc; idx += gridDim.x * blockDim.x) {
+    const int jc = idx / nxc, ic = idx - jc * nxc;
+    const float* src = r + c * cs + (long long)(jc * f) * nx + ic * f;
+    float acc = 0.0f;
+    for (int a = 0; a < f; ++a)
+      for (int b = 0; b < f; ++b) acc += src[(long long)a * nx + b];
+    out[(long long)c * nyc * nxc + idx] = w * acc;
+  }
+}
+
+// Bilinear prolongation of the restricted network output to the cells: cell
+// (j, i) sits at coarse position ((j + 1/2)/f - 1/2, (i + 1/2)/f - 1/2);
+// beyond the outermost coarse centres the value is held constant.
+__global__ void __launch_bounds__(kThreads) k_net_prolong(int ny, int nx, int f, const float* in, float* out,
+                                                          long long cs) {
+  pdl_wait();
+  const int c = blockIdx.y;
+  const int nyc = ny / f, nxc = nx / f;
+  const float* src = in + (long long)c * nyc * nxc;
+  const float inv = 1.0f / float(f);
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < ny * nx; idx += gridDim.x * blockDim.x) {
+    const int j = idx / nx, i = idx - j * nx;
+    const float yc = fminf(fmaxf((j + 0.5f) * inv - 0.5f, 0.0f), float(nyc - 1));
+    const float xc = fminf(fmaxf((i + 0.5f) * inv - 0.5f, 0.0f), float(nxc - 1));
+    const int j0 = min(int(yc), nyc - 1), i0 = min(int(xc), nxc - 1);
+    const int j1 = min(j0 + 1, nyc - 1), i1 = min(i0 + 1, nxc - 1);
+    const float ty = yc - float(j0), tx = xc - float(i0);
+    const float a = src[j0 * nxc + i0] + tx * (src[j0 * nxc + i1] - src[j0 * nxc + i0]);
+    const float b = src[j1 * nxc + i0] + tx * (src[j1 * nxc + i1] - src[j1 * nxc + i0]);
+    out[c * cs + idx] = a + ty * (b - a);
+  }
 }
 
 __global__ void k_reset_counters(CGScalars* cg, int cols) {
@@ -335,11 +377,12 @@ static void velocity_inverse(Plan* P, const Launcher<T>& L, Src src, Out* dst, l
 }
 
 // One PCG iteration for every active column (all kernels predicated).  With
-// the learned preconditioner (X.net, FP32 only) z = M r + net(r), projected to
-// mean zero, and beta is the Polak-Ribiere form of flexible CG.
+// the learned preconditioner (X.net, FP32 only) beta is the Polak-Ribiere form
+// of flexible CG and, in iterations that evaluate the network (eval_net),
+// z = M r + net(r), projected to mean zero; otherwise z = M r.
 template <typename T>
 static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* cells, int cols, T* wacc,
-                         bool fused_first = false) {
+                         bool fused_first = false, bool eval_net = true) {
   const GridDev& g = P->g;
   const long long np = g.np, sz = g.size;
   T* b = cells;
@@ -369,10 +412,28 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
                   make_fin<T>(P, X, OP_RHO, L.groups_row_p(), 2, cols), P->done_counter);
   if constexpr (std::is_same<T, float>::value) {
     if (net) {
-      launch_k(k_net_scales, 1, 32, 0, s, P->cg, P->active, cols, g.np, P->net_scale);
-      ++P->launches;
-      unet_forward(P->net, &P->netw, r, P->net_scale, cols, g.ny, g.nx, P->net_out, P->net_scale + cols, s);
-      launch_k(k_fcg_z, dim3(rb, cols), kThreads, 0, s, g.np, z, P->net_out, r, r_old, np, P->cg, P->active, P->partial,
+      const float* add = nullptr;
+      if (eval_net) {
+        launch_k(k_net_scales, 1, 32, 0, s, P->cg, P->active, cols, g.np, P->net_scale);
+        ++P->launches;
+        const int f = P->net_restrict;
+        const long long net_before = P->net->launches;
+        if (f == 1) {
+          unet_forward(P->net, &P->netw, r, P->net_scale, cols, g.ny, g.nx, P->net_out, P->net_scale + cols, s);
+        } else {
+          const int npc = (g.ny / f) * (g.nx / f);
+          launch_k(k_net_restrict, dim3(red_blocks(npc), cols), kThreads, 0, s, g.ny, g.nx, f,
+                   static_cast<const float*>(r), np, static_cast<const float*>(P->net_scale), P->net_cin);
+          unet_forward(P->net, &P->netw, P->net_cin, nullptr, cols, g.ny / f, g.nx / f, P->net_cout,
+                       P->net_scale + cols, s);
+          launch_k(k_net_prolong, dim3(rb, cols), kThreads, 0, s, g.ny, g.nx, f,
+                   static_cast<const float*>(P->net_cout), P->net_out, np);
+          P->launches += 2;
+        }
+        P->launches += P->net->launches - net_before;  // the network's own kernels count as the plan's
+        add = P->net_out;
+      }
+      launch_k(k_fcg_z, dim3(rb, cols), kThreads, 0, s, g.np, z, add, r, r_old, np, P->cg, P->active, P->partial,
                                                   make_fin<float>(P, X, OP_FCG, rb, 5, cols), P->done_counter);
       launch_k(k_fcg_center, dim3(rb, cols), kThreads, 0, s, g.np, z, np, P->cg, P->active);
       P->launches += 2;
@@ -447,7 +508,7 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
                           cudaMemcpyDeviceToDevice, s);
         }
       }
-      cg_iteration<T>(P, X, L, w, cells, cols, wacc, fused && it == 0);
+      cg_iteration<T>(P, X, L, w, cells, cols, wacc, fused && it == 0, P->net_every || it == 0);
       if constexpr (std::is_same<T, double>::value) {
         if (log) {
           cudaMemcpyAsync(P->log_z + P->log_n * np, cells + 3 * np * cols, sizeof(double) * np,
@@ -497,7 +558,7 @@ static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int
   Launcher<T> Ls{L.t, X.side, L.counter, P->aux[1], P->evf[1], P->evj[1]};
   Exec Xs = X;
   Xs.s = X.side;
-  cg_iteration<T>(P, Xs, Ls, w, cells, cols, wacc);
+  cg_iteration<T>(P, Xs, Ls, w, cells, cols, wacc, false, P->net_every != 0);
   cudaGraph_t captured;
   if (cudaStreamEndCapture(X.side, &captured) != cudaSuccess) return MACSAV_ERR_CUDA;
   return MACSAV_OK;
@@ -630,15 +691,19 @@ __global__ void __launch_bounds__(kThreads) k_accumulate(const T* src, double* d
 // (mI+kK)^{-1}(ru + D^T x) is needed; one kernel adds u and x to the FP64
 // fields.  The same vector in exact arithmetic; in float it differs at
 // rounding level, which the FP64 defect correction absorbs like any other
-// inner-solve error.  With the learned preconditioner (flexible CG, whose
-// columns may restart) the closing velocity inverse is kept.
+// inner-solve error.  The learned preconditioner (flexible CG, whose columns
+// may restart) runs in the first inner solve of a Stokes solve only (add = 0:
+// its right-hand side is the stage's own, a smooth field; the correction
+// sweeps solve for rounding-level defects), and that solve keeps the closing
+// velocity inverse.  With the every-iteration placement it runs in all inner
+// solves.
 static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, int cols, double* vel, double* pres,
                          int add) {
   const GridDev& g = P->g;
   Launcher<float> L{P->t32, X.s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
   const long long sz = g.size, np = g.np;
   float* w = P->w32;
-  const bool net = P->net != nullptr;
+  const bool net = P->net != nullptr && (P->net_every || add == 0);
   float* wacc = net ? nullptr : P->wacc32;
   velocity_inverse<float>(P, L, SrcPacked<float, double>{ru, sz, g.nu, g.nx - 1, g.nx}, wacc ? wacc : w, sz, cols,
                           nullptr);

@@ -18,6 +18,21 @@ Plain PCG stays the fallback and the gates stay in charge: a column whose learne
 does not converge within ``learned_max_iterations`` restarts plain PCG from
 zero, and the FP64 defect correction and the reference's closing gates decide
 as before, so the network never changes the answer beyond the tolerance.
+
+Placement (``placement``): by default the network shapes only the first
+search direction of each Stokes solve (the first iteration of its first FP32
+inner solve, whose right-hand side is the stage's own); the other iterations
+are flexible CG with the spectral preconditioner.  It may work on the
+residual restricted to a coarser grid (f x f cell means), its output
+prolonged bilinearly.  ``calibrate_gain`` sets the network's output gain with
+plain PCG as the judge, on held-out solves.
+
+What it can gain is bounded by what the spectral preconditioner leaves: at
+the workloads' shifts (k / h^2 of order 1e-3) one PCG iteration already
+takes a smooth right-hand side to a relative residual near 2e-5, below the
+inner solves' tolerance, and a correction only shortens a solve if its own
+error (in the Schur norm) is below that, which a BF16 network with 8-bit
+mantissas does not reach.
 """
 from __future__ import annotations
 
@@ -187,6 +202,95 @@ def train(net: UNet, pairs: Pairs, *, steps: int = 200, batch: int = 8, lr: floa
         idx = torch.randint(0, n, (min(batch, n),), generator=gen).to("cuda")
         losses.append(net.train_step(pairs.inputs[idx].contiguous(), pairs.targets[idx].contiguous(), lr))
     return losses
+
+
+def collect_first_direction_pairs(grid: MACGrid, rhs_columns, mass: float, viscosity: float, *,
+                                  restriction: int = 1, krylov_tolerance: float = 1e-12) -> Pairs:
+    """Pairs for the first-direction placement: for each right-hand side, the
+    pressure right-hand side b of plain FP64 Schur CG (its first residual) and
+    the error of the spectral preconditioner's first direction, p* - M b, in
+    the units of ``collect_pairs``; both restricted by f x f cell means when
+    ``restriction`` f > 1 (the network then works on the restricted grid)."""
+    plan = Plan(grid, "fp64", 1e-9, krylov_tolerance, 100, 2)
+    lib = plan.lib
+    np_ = grid.np
+    logs = [torch.empty(2 * np_, dtype=torch.float64, device="cuda") for _ in range(3)]
+    inputs, targets, iters = [], [], []
+    for rhs in rhs_columns:
+        f = torch.as_tensor(np.ascontiguousarray(rhs, dtype=np.float64), device="cuda")
+        n = C.c_int()
+        # the log keeps one pair (k = 0) and the converged iterate (row 1 of x)
+        plan.check(lib.macsav_stokes_log(plan.handle, dptr(f), float(mass), float(viscosity), 1,
+                                         dptr(logs[0]), dptr(logs[1]), dptr(logs[2]), C.byref(n), stream_handle()))
+        k = int(n.value)
+        iters.append(k)
+        if k < 1:
+            continue
+        b, mb, xs = logs[0][:np_], logs[1][:np_], logs[2][np_:2 * np_]
+        rr = float((b * b).sum())
+        rms = (rr / np_) ** 0.5
+        scale = rms * float((b * mb).sum()) / rr
+        t = xs - mb
+        t = t - t.mean()
+        inputs.append((b / rms).reshape(1, 1, grid.ny, grid.nx))
+        targets.append((t / scale).reshape(1, 1, grid.ny, grid.nx))
+    x, y = torch.cat(inputs), torch.cat(targets)
+    if restriction > 1:
+        x = torch.nn.functional.avg_pool2d(x, restriction)
+        y = torch.nn.functional.avg_pool2d(y, restriction)
+    return Pairs(x[:, 0].float().contiguous(), y[:, 0].float().contiguous(), iters)
+
+
+def scale_output(net: UNet, gain: float) -> None:
+    """Multiply the network's output by ``gain`` (the bias-free network is
+    linear in its last layer's weights)."""
+    p = net.params()
+    co, ci, k = layer_shapes(net.channels)[-1]
+    n_last = co * ci * k * k
+    p[-n_last:] *= np.float32(gain)
+    net.set_params(p)
+
+
+def calibrate_gain(net: UNet, grid: MACGrid, rhs_columns, mass: float, viscosity: float, *,
+                   gains=(0.0, 0.25, 0.5, 1.0), restriction: int = 1, krylov_tolerance: float = 1e-10,
+                   max_columns: int = 2) -> dict:
+    """Choose the output gain of the network with plain PCG as the judge: for
+    every candidate gain, the FP32 Stokes solves of the held-out right-hand
+    sides (two columns per solve) with the network in the first-direction
+    placement, counting all inner CG iterations; the gain kept is the largest
+    one that needs no more iterations than the smallest count (gain 0 is plain
+    PCG's count).  The network's last layer is scaled by that gain; returns
+    the counts per gain and the choice."""
+    from .stokes import TensorStokes
+    base = net.params()
+    counts = {}
+    for gain in gains:
+        net.set_params(base)
+        scale_output(net, gain)
+        ts = TensorStokes(grid, precision="fp32", krylov_tolerance=krylov_tolerance, max_columns=max_columns)
+        attach(ts, net)
+        placement(ts, every_iteration=False, restriction=restriction)
+        total = 0
+        for cols in rhs_columns:
+            ts.solve(cols, mass=mass, viscosity=viscosity)
+            total += sum(cg_counters(ts, cols.shape[1])["iterations"])
+        counts[float(gain)] = total
+        attach(ts, None)
+    best = min(counts.values())
+    chosen = max(g for g, c in counts.items() if c == best)
+    net.set_params(base)
+    scale_output(net, chosen)
+    return {"iterations_per_gain": counts, "gain": chosen}
+
+
+def placement(backend, *, every_iteration: bool = False, restriction: int = 1) -> None:
+    """Where the attached network runs: the first search direction of each
+    Stokes solve (default) or every CG iteration; on the residual restricted
+    by f x f cell means (``restriction`` 1, 2 or 4)."""
+    backend = getattr(backend, "backend", backend)
+    plan = backend.plan
+    plan.check(plan.lib.macsav_plan_set_learned_placement(plan.handle, 1 if every_iteration else 0,
+                                                          int(restriction)))
 
 
 def attach(backend, net: UNet | None, learned_max_iterations: int = 20) -> None:

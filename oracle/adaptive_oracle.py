@@ -1,11 +1,15 @@
-"""Adaptive SDIRK3(2) / SDIRK2(1) driver with I and PI step control.
+"""Restatement of the reference's adaptive driver -- TEST INFRASTRUCTURE ONLY.
 
-Host-side restatement of the reference's ``solver/adaptivity/controller.py``
-(I/PI controllers :14-70, scalar error control :73-90, continuation :93-100,
-error estimate :112-123, driver :126-398).  Every trial is one fused device
-step; the embedded velocity stays on the device and the error norms are
-reduced there (``model.combine`` / ``model.inner``), so a trial costs one
-device step plus three scalar read-backs.
+``integrate_adaptive`` with its I and PI controllers as in the reference's
+``solver/adaptivity/controller.py`` (I/PI controllers :14-70, scalar error
+control :73-90, continuation :93-100, error estimate :112-123, driver
+:126-398).  The tests drive the GPU model and the fused GPU schemes with it,
+as a user drives them with the reference's own driver (the reference's Python
+cannot travel to the GPU machine), and pin it to the reference's adaptive runs
+(tests/golden/adaptive.npz).  It takes the fused step's device-formed
+embedded-error inner products when a trial carries them (``_error_from_norms``)
+and checks a device state's finiteness on the device; otherwise it works on
+host vectors like the reference.  The product package never imports it.
 """
 from __future__ import annotations
 
@@ -16,8 +20,7 @@ from typing import Any, Literal
 
 import numpy as np
 
-from .core import stage_diagnostics
-from .integrate import Result
+from .integrate_oracle import Result, stage_diagnostics
 
 
 @dataclass(frozen=True)

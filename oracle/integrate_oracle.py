@@ -1,7 +1,12 @@
-"""Fixed/prescribed-step driver (the reference's solver/integrate.py:47-100 and
-solver/schedule.py:7-29), unchanged in behaviour: finiteness checks on the
-host state, per-step diagnostics, snapshots at the nearest nodes, the failed
-prefix kept on an exception, observer time excluded from ``seconds``."""
+"""Restatement of the reference's fixed-step driver -- TEST INFRASTRUCTURE ONLY.
+
+``integrate`` as in the reference's ``solver/integrate.py:47-100`` with
+``solver/schedule.py:7-29``: finiteness checks on the state, per-step
+diagnostics, snapshots at the nearest nodes, the failed prefix kept on an
+exception, observer time excluded from ``seconds``.  The tests drive the GPU
+model and the fused GPU schemes with it, as a user drives them with the
+reference's own driver.  The product package never imports it.
+"""
 from __future__ import annotations
 
 from collections.abc import Callable
@@ -10,13 +15,19 @@ from time import perf_counter, process_time
 
 import numpy as np
 
-from .core import History, Stage, State, stage_diagnostics
+from .mac_oracle import stage_diagnostics
+
+
+@dataclass
+class History:
+    state: object
+    accepted_steps: int = 0
 
 
 @dataclass
 class Result:
     """``solver/integrate.py:12-25``."""
-    final: State
+    final: object
     times: list
     diagnostics: list
     stages: list = field(default_factory=list)
@@ -88,9 +99,9 @@ def state_finite(model, state) -> bool:
     return bool(np.isfinite(model.vector(state)).all())
 
 
-def integrate(model, scheme, initial: State, steps, snapshots: list | None = None,
+def integrate(model, scheme, initial, steps, snapshots: list | None = None,
               progress: Callable[[int, float, float], None] | None = None, *,
-              on_accept: Callable[[State], None] | None = None) -> Result:
+              on_accept: Callable | None = None) -> Result:
     """``solver/integrate.py:47-100``."""
     seq = np.asarray(steps, dtype=float)
     if seq.ndim != 1 or seq.size == 0 or np.any(seq <= 0) or not np.isfinite(seq).all():
@@ -100,7 +111,7 @@ def integrate(model, scheme, initial: State, steps, snapshots: list | None = Non
     if any(not np.isfinite(t) or t < initial.t or t > nodes[-1] + 1e-12 for t in requests):
         raise ValueError("Snapshot time outside integration interval")
     indices = nearest_node_indices(nodes, requests)
-    kept: dict[int, State] = {}
+    kept: dict = {}
     if 0 in indices:
         kept[0] = initial
     history = History(initial)

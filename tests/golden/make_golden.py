@@ -1,9 +1,9 @@
 """Generate the golden fixtures by running the reference itself.
 
-Run from the repository root, in a container where the reference tree is
-mounted at /root/reference:
+Run from the repository root with the path of the reference's source tree,
+given as the first argument or in the environment variable MACSAV_REFERENCE:
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/reference
 
 It imports the reference's own ``solver`` package (numba is absent, so the
 identity ``njit`` stand-in from ``oracle/reference_shim`` is put first on the
@@ -24,7 +24,10 @@ import numpy as np
 sys.dont_write_bytecode = True
 HERE = pathlib.Path(__file__).resolve().parent
 REPO = HERE.parent.parent
-REF = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+_ref_arg = sys.argv[1] if len(sys.argv) > 1 else __import__("os").environ.get("MACSAV_REFERENCE")
+if not _ref_arg:
+    sys.exit("usage: make_golden.py REFERENCE_DIR (or set MACSAV_REFERENCE)")
+REF = pathlib.Path(_ref_arg)
 sys.path.insert(0, str(REPO / "oracle" / "reference_shim"))
 sys.path.insert(0, str(REF))
 

@@ -165,3 +165,24 @@ def test_reference_scheme_code_runs_on_gpu_channel(ch, d, name):
     keys = [str(k) for k in d[f"run_{name}_diag_keys"]]
     got = np.array([res.diagnostics[-1][k] for k in keys])
     np.testing.assert_allclose(got, d[f"run_{name}_diag"], rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.parametrize("nx,ny", [(24, 40), (16, 77)])
+def test_spike_solve_multi_step_chunks_match_oracle(ch, nx, ny):
+    """Random loads on grids whose banded systems (n = 3 ny - 1 = 119 and 230
+    unknowns per mode) span several steps per lane of the warp-partitioned
+    substitution, with n not a multiple of 32, and every x mode carrying
+    data: velocity and pressure against the oracle's dense per-mode solves."""
+    import oracle.channel_oracle as CO
+    grid = ch.ChannelGrid(nx, ny, 2.1, .9)
+    og = CO.ChannelGridOracle(nx, ny, 2.1, .9)
+    model = ch.ChannelModel(grid, .1, backend="fft")
+    rng = np.random.default_rng(nx * 1000 + ny)
+    loads = rng.normal(size=(grid.size, 2))
+    for mass, visc in ((1.0, 2.5e-4), (1.0, .05)):
+        sol = model.backend.solve(loads, mass=mass, viscosity=visc)
+        vel, pres = CO.fft_solve(og, loads, mass, visc)
+        for c in range(2):
+            assert np.linalg.norm(sol.velocity[:, c] - vel[:, c]) <= 1e-11 * np.linalg.norm(vel[:, c])
+            assert np.linalg.norm(sol.pressure[:, :, c] - pres[:, :, c]) <= 1e-11 * np.linalg.norm(pres[:, :, c])
+        assert sol.residual < 1e-10 and sol.divergence_inf < 1e-10

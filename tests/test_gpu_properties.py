@@ -165,7 +165,7 @@ def test_order_against_exact_semidiscrete_solution(pkg, name, horizon, counts, r
     model.force = force
     errors = []
     for count in counts:
-        result = pkg.integrate(model, pkg.make_scheme(name, 1.0), model.state(0.0, base), [horizon / count] * count)
+        result = pkg.run_fixed(model, pkg.make_scheme(name, 1.0), model.state(0.0, base), [horizon / count] * count)
         assert result.status == "complete", result.error
         errors.append(og.norm(model.vector(result.final) - np.exp(-horizon) * base))
     assert min(np.log2(np.array(errors[:-1]) / errors[1:])) > rate, errors

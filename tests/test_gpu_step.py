@@ -1,5 +1,8 @@
-"""The fused device step, the GPU model seam and the integrate driver against
-the reference (golden fixtures) and the oracle.
+"""The fused device step and the GPU model seam against the reference (golden
+fixtures) and the oracle, driven as a user drives them: one step at a time,
+under the reference's fixed-step driver (its restatement in
+oracle/integrate_oracle.py, since the reference cannot travel to the GPU
+machine), and by the package's device-resident loop ``run_fixed``.
 
 Bars: <= 1e-11 relative L2 on the stepped velocity and pressures (the parity
 bar of the FP64 path), SAV scalars to 1e-12, identical CG iterations.
@@ -8,6 +11,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+import oracle.integrate_oracle as DRV
 from helpers import golden, load_package
 
 pytestmark = pytest.mark.gpu
@@ -57,13 +61,18 @@ def test_config1_trajectory_matches_reference(pkg):
     d = golden("config1_64")
     g = pkg.MACGrid(64, 64)
     model = pkg.MACNavierStokes(g, 1e-2, use_graph=True)
-    res = pkg.integrate(model, pkg.make_scheme("sdirk2_mrsav"), model.state(0.0, d["x0"], 0.0), [1e-3] * 100)
+    res = DRV.integrate(model, pkg.make_scheme("sdirk2_mrsav"), model.state(0.0, d["x0"], 0.0), [1e-3] * 100)
     assert res.status == "complete", res.error
     assert _rel(model.vector(res.final), d["x_final"]) < 1e-11
     assert abs(res.final.r - float(d["r_final"])) < 1e-12
     keys = [str(k) for k in d["diag_keys"]]
     got = np.array([[row[k] for k in keys] for row in res.diagnostics])
     np.testing.assert_allclose(got, d["diagnostics"], rtol=1e-10, atol=1e-12)
+    # the package's device-resident loop over the same 100 steps
+    fixed = pkg.run_fixed(model, pkg.make_scheme("sdirk2_mrsav"), model.state(0.0, d["x0"], 0.0), [1e-3] * 100)
+    assert fixed.status == "complete" and len(fixed.times) == 101
+    assert _rel(model.vector(fixed.final), d["x_final"]) < 1e-11
+    assert abs(fixed.final.r - float(d["r_final"])) < 1e-12
 
 
 def test_generic_scheme_code_runs_on_gpu_model(pkg):
@@ -104,7 +113,7 @@ def test_forced_step_matches_oracle(pkg):
 
 def test_step_failure_is_reported_like_reference(pkg):
     """A NaN body force fails the step with the reference's exception and
-    integrate keeps the accepted prefix (integrate.py:90-93)."""
+    the reference's integrate keeps the accepted prefix (integrate.py:90-93)."""
     g = pkg.MACGrid(8, 6)
     model = pkg.MACNavierStokes(g, 0.1)
     x0 = pkg.fields.packed_curl_velocity(8, 6, 1.0, 1.0, 2, 1)
@@ -114,10 +123,16 @@ def test_step_failure_is_reported_like_reference(pkg):
         calls.append(t)
         return np.full(g.size, np.nan) if t > 0.012 else np.zeros(g.size)
     model.force = force
-    res = pkg.integrate(model, pkg.make_scheme("sdirk2_mrsav"), model.state(0.0, x0), [0.01, 0.01, 0.01])
+    res = DRV.integrate(model, pkg.make_scheme("sdirk2_mrsav"), model.state(0.0, x0), [0.01, 0.01, 0.01])
     assert res.status == "failed"
     assert res.error.startswith("ValueError: Invalid Stokes RHS")
     assert len(res.times) == 2
+    # the device-resident loop: a failing stage check ends the run with its prefix
+    backend = pkg.TensorStokes(g, max_iterations=1)
+    bad = pkg.MACNavierStokes(g, 0.1, backend=backend)
+    fixed = pkg.run_fixed(bad, pkg.make_scheme("sdirk2_mrsav"), bad.state(0.0, x0), [0.01, 0.01])
+    assert fixed.status == "failed" and fixed.error.startswith("RuntimeError: Pressure Schur CG failed")
+    assert fixed.times == [0.0] and fixed.final.t == 0.0
 
 
 def test_cg_failure_inside_step(pkg):
