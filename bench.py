@@ -784,6 +784,49 @@ def profile_steps(precision: str, workload: str) -> None:
                       "iterations": [list(rc.iterations[:2]) for rc in recs]}))
 
 
+def profile_transform32() -> None:
+    """The autotuner's measurements for the FP32 row transforms at the
+    solver's lengths (n = 64..512 and 1023/1024, rows = 2n: two right-hand
+    sides of a square block)."""
+    import torch
+    import __graft_entry__
+    from importlib import import_module
+    __graft_entry__.build()
+    pkg = __graft_entry__.load_package()
+    stokes = import_module(pkg.__name__ + ".stokes")
+    plan = stokes.Plan(pkg.MACGrid(8, 8))
+    table = []
+    for kind, name in ((0, "dct2"), (1, "dst2"), (2, "dst1")):
+        for n in (64, 127, 128, 255, 256, 511, 512, 1023, 1024):
+            for inverse in (0, 1):
+                m, tf, tt = C.c_int(), C.c_double(), C.c_double()
+                plan.check(plan.lib.macsav_transform32_autotune(plan.handle, kind, inverse, 2 * n, n, C.byref(m),
+                                                                C.byref(tf), C.byref(tt), stokes.stream_handle()))
+                table.append({"kind": name, "n": n, "rows": 2 * n, "inverse": inverse, "fft_us": 1e3 * tf.value,
+                              "tc6_us": 1e3 * tt.value if tt.value > 0 else None,
+                              "chosen": "tc6" if m.value == 2 else "fft"})
+    print(json.dumps({"profile": "transform32", "autotune": table}))
+
+
+def profile_tgemm() -> None:
+    """Three launches of the tensor-core row transform (DCT-II, 6 products)
+    at n = 512 on 1024 rows, after one warm-up (for a kernel capture)."""
+    import torch
+    import __graft_entry__
+    from importlib import import_module
+    __graft_entry__.build()
+    pkg = __graft_entry__.load_package()
+    stokes = import_module(pkg.__name__ + ".stokes")
+    plan = stokes.Plan(pkg.MACGrid(8, 8))
+    x = torch.randn(1024, 512, device="cuda", dtype=torch.float32)
+    y = torch.empty_like(x)
+    for _ in range(4):
+        plan.check(plan.lib.macsav_transform32(plan.handle, 0, 0, 1024, 512, 2, stokes.dptr(x), stokes.dptr(y),
+                                               stokes.stream_handle()))
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "tgemm", "n": 512, "rows": 1024}))
+
+
 def profile_pass(workload: str, pass_id: int) -> None:
     """Three launches of one transform pass (macsav_time_pass: 0 the FP32
     velocity column pass, 3 the FP64 one) on the workload's grid, after one
@@ -878,7 +921,9 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["learned1024", "cavity512", "ensemble256", "adaptive2048", "channel512"],
                     default="learned1024")
-    ap.add_argument("--profile", choices=["fp32", "fp64", "learned", "unet", "pass0", "pass3"], default=None,
+    ap.add_argument("--profile", choices=["fp32", "fp64", "learned", "unet", "pass0", "pass3", "transform32",
+                                          "tgemm"],
+                    default=None,
                     help="run two eager steps of the workload (or launches of one transform pass) and exit, "
                          "for ncu captures")
     args = ap.parse_args()
@@ -887,6 +932,12 @@ def main() -> None:
         return
     if args.profile == "unet":
         profile_unet()
+        return
+    if args.profile == "transform32":
+        profile_transform32()
+        return
+    if args.profile == "tgemm":
+        profile_tgemm()
         return
     if args.profile in ("pass0", "pass3"):
         profile_pass(args.workload, int(args.profile[-1]))

@@ -89,6 +89,31 @@ int macsav_convection(macsav_plan* plan, const double* x, double* n, int columns
 int macsav_transform(macsav_plan* plan, int kind, int inverse, int rows, int n, const double* in,
                      double* out, void* stream);
 
+/* FP32 form of macsav_transform: the same orthonormal transforms along each
+ * row of a (rows, n) row-major FP32 array, computed by
+ *   MACSAV_TRANSFORM_FFT  the shared-memory FFT kernels of the solver (FP32);
+ *   MACSAV_TRANSFORM_TC3  a transform-matrix product on the tcgen05 tensor
+ *                         cores, operands split into 2 BF16 pieces, 3 products
+ *                         (relative error about 1e-5);
+ *   MACSAV_TRANSFORM_TC6  the same with 3 BF16 pieces, 6 products (FP32 accuracy);
+ *   MACSAV_TRANSFORM_AUTO the autotuner's choice for this (kind, direction,
+ *                         rows, n), measured on first use.
+ * The tensor-core forms take n <= 512 (MACSAV_ERR_UNSUPPORTED beyond).  The
+ * reference applies these transforms with scipy.fft (_transform_axis,
+ * solver/mac/tensor_stokes.py:58-82); synchronises `stream`. */
+#define MACSAV_TRANSFORM_FFT 0
+#define MACSAV_TRANSFORM_TC3 1
+#define MACSAV_TRANSFORM_TC6 2
+#define MACSAV_TRANSFORM_AUTO 3
+int macsav_transform32(macsav_plan* plan, int kind, int inverse, int rows, int n, int method, const float* in,
+                       float* out, void* stream);
+/* The autotuner: times the FFT and the TC6 form for this (kind, direction,
+ * rows, n) (10 launches each after a warm-up, CUDA events on `stream`),
+ * keeps the faster one as the plan's choice for MACSAV_TRANSFORM_AUTO and
+ * returns it with both average times (ms; ms_tensor = -1 when n > 512). */
+int macsav_transform32_autotune(macsav_plan* plan, int kind, int inverse, int rows, int n, int* method,
+                                double* ms_fft, double* ms_tensor, void* stream);
+
 /* Shifted Stokes solve (mass I + viscosity K) u - D^T p = f, D u = 0 by
  * DST/DCT velocity inverses inside a pressure Schur PCG
  * (TensorStokes.solve, solver/mac/tensor_stokes.py:245-364).
@@ -367,6 +392,12 @@ int macsav_time_pass(macsav_plan* plan, int pass, int reps, double* ms, double* 
  * (default 1e-4).  The closing FP64 gates are unchanged, so too few sweeps
  * surface as the reference's Stokes-gate error, never as a silent loss. */
 int macsav_plan_set_refinement(macsav_plan* plan, int corrections, double inner_krylov_tolerance);
+/* Krylov tolerance of the first FP32 solve of each FP32_MIXED Stokes solve
+ * (the one that starts from zero); the correction sweeps keep the inner
+ * tolerance above.  0 (the default) means the inner tolerance.  A tighter
+ * first solve leaves a smaller defect, so fewer sweeps reach the gates; like
+ * the sweep count, a bad choice surfaces as the Stokes-gate error. */
+int macsav_plan_set_first_solve_tolerance(macsav_plan* plan, double first_krylov_tolerance);
 
 /* Run macsav_step as one captured CUDA graph per (scheme, force, embedded)
  * (the pressure CG loop becomes a conditional WHILE node).  Default: off. */

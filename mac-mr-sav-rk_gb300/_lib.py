@@ -72,6 +72,9 @@ _SIGNATURES = {
     "macsav_unet_train_step": (_I, [_P, _P, _P, _I, _I, _I, C.c_float, C.POINTER(_D), _P]),
     "macsav_plan_set_preconditioner": (_I, [_P, _P, _I]),
     "macsav_plan_set_learned_placement": (_I, [_P, _I, _I]),
+    "macsav_plan_set_first_solve_tolerance": (_I, [_P, _D]),
+    "macsav_transform32": (_I, [_P, _I, _I, _I, _I, _I, _P, _P, _P]),
+    "macsav_transform32_autotune": (_I, [_P, _I, _I, _I, _I, C.POINTER(_I), C.POINTER(_D), C.POINTER(_D), _P]),
     "macsav_plan_cg_counters": (_I, [_P, _I, _P, _P, _P]),
     "macsav_stokes_log": (_I, [_P, _P, _D, _D, _I, _P, _P, _P, C.POINTER(_I), _P]),
     "macsav_step_embedded_norms": (_I, [_P, C.POINTER(_D)]),

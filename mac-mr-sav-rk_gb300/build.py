@@ -16,7 +16,7 @@ ROOT = PKG.parent
 SRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = PKG / "libmacsav.so"
-UNITS = ["plan", "stokes", "ops", "step", "capi", "static_reduce", "unet", "channel"]
+UNITS = ["plan", "stokes", "ops", "step", "capi", "static_reduce", "unet", "channel", "tgemm"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--diag-suppress=177",
          f"-I{ROOT / 'include'}"]

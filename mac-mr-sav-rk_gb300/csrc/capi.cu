@@ -30,6 +30,10 @@ int op_diagnostics(Plan* P, const double* x, double r, double nu, const double* 
                    cudaStream_t s);
 int op_transform(Plan* P, int kind, int inverse, int rows, int n, const double* in, double* out, cudaStream_t s);
 int time_pass(Plan* P, int pass, int reps, cudaStream_t s, double* ms, double* bytes);
+int op_transform32(Plan* P, int kind, int inverse, int rows, int n, int method, const float* in, float* out,
+                   cudaStream_t s);
+int op_transform32_autotune(Plan* P, int kind, int inverse, int rows, int n, int* method, double* ms_fft,
+                            double* ms_tensor, cudaStream_t s);
 void reset_cg_counters(Plan* P, int cols, cudaStream_t s);
 }  // namespace macsav
 
@@ -608,6 +612,16 @@ int macsav_plan_set_refinement(macsav_plan* plan, int corrections, double inner_
   return MACSAV_OK;
 }
 
+int macsav_plan_set_first_solve_tolerance(macsav_plan* plan, double first_krylov_tolerance) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  if (!(first_krylov_tolerance >= 0) || !(first_krylov_tolerance < 1))
+    return fail(&plan->p, MACSAV_ERR_VALUE, "0 <= first-solve tolerance < 1");
+  plan->p.first_ktol = first_krylov_tolerance;
+  for (auto& kv : plan->p.st.graphs) cudaGraphExecDestroy(kv.exec);  // captured with the old tolerance
+  plan->p.st.graphs.clear();
+  return MACSAV_OK;
+}
+
 int macsav_plan_set_graph(macsav_plan* plan, int enable) {
   if (!plan) return MACSAV_ERR_VALUE;
   plan->p.use_graph = enable ? 1 : 0;
@@ -615,3 +629,20 @@ int macsav_plan_set_graph(macsav_plan* plan, int enable) {
 }
 
 }  // extern "C"
+
+int macsav_transform32(macsav_plan* plan, int kind, int inverse, int rows, int n, int method, const float* in,
+                       float* out, void* stream) {
+  if (!plan || !in || !out) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  const int rc = macsav::op_transform32(P, kind, inverse, rows, n, method, in, out, static_cast<cudaStream_t>(stream));
+  return rc == MACSAV_ERR_CUDA ? cuda_status(P) : rc;
+}
+
+int macsav_transform32_autotune(macsav_plan* plan, int kind, int inverse, int rows, int n, int* method,
+                                double* ms_fft, double* ms_tensor, void* stream) {
+  if (!plan || !method || !ms_fft || !ms_tensor) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  const int rc = macsav::op_transform32_autotune(P, kind, inverse, rows, n, method, ms_fft, ms_tensor,
+                                                 static_cast<cudaStream_t>(stream));
+  return rc == MACSAV_ERR_CUDA ? cuda_status(P) : rc;
+}

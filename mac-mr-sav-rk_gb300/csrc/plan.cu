@@ -121,6 +121,7 @@ cudaError_t build_line_block(TBlockDev<T>& B, int rows, int cols, int kx, int sm
   return build_block(B, rows, cols, kx, KIND_DCT2, 1.0, 1.0, sms, allocs);
 }
 template cudaError_t build_line_block<double>(TBlockDev<double>&, int, int, int, int, std::vector<void*>&);
+template cudaError_t build_line_block<float>(TBlockDev<float>&, int, int, int, int, std::vector<void*>&);
 
 template <typename T>
 size_t row_smem(const TBlockDev<T>& B) {
@@ -235,8 +236,11 @@ fail:
 
 void step_free(Plan* P);
 
+void free_transform32_cache(Plan* P);
+
 void plan_free(Plan* p) {
   step_free(p);
+  free_transform32_cache(p);
   free_transforms(p->t64);
   free_transforms(p->t32);
   cudaFree(p->w); cudaFree(p->cells); cudaFree(p->cells32); cudaFree(p->w32); cudaFree(p->wacc32);

@@ -90,6 +90,7 @@ struct Plan {
   int members = 1;  // equal-shape cavities stepped together (2 Stokes columns each)
   // FP32_MIXED: inner FP32 Krylov tolerance and defect-correction sweeps
   double inner_ktol = 1e-4;
+  double first_ktol = 0.0;  // tolerance of a Stokes solve's first FP32 solve (0: inner_ktol)
   int corrections = 2;
   int num_sms;
   std::string err;
@@ -150,6 +151,10 @@ struct Plan {
   int net_restrict = 1;
   float* net_cin = nullptr;    // restricted network input,  [maxcols][np / f^2]
   float* net_cout = nullptr;   // restricted network output, [maxcols][np / f^2]
+
+  // FP32 row transforms of macsav_transform32: tensor-core matrices, FFT
+  // line blocks and the autotuner's choices (tgemm.cu)
+  struct Transform32Cache* tcache = nullptr;
 
   // residual / preconditioned residual / iterate log of eager FP64 solves
   double* log_r = nullptr;

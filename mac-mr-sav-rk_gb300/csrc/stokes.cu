@@ -709,7 +709,7 @@ static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, i
                           nullptr);
   const double keep = X.ktol;
   const int keep_net = X.net;
-  X.ktol = P->inner_ktol;
+  X.ktol = (add == 0 && P->first_ktol > 0.0) ? P->first_ktol : P->inner_ktol;
   X.net = net ? 1 : 0;
   int rc = schur_pcg<float>(P, X, L, w, P->cells32, cols, rd, wacc);
   X.ktol = keep;

@@ -29,6 +29,7 @@ struct ConvArgs {
   int ca, cb, co;
   const float* dy;          // backward: masked output gradient [B][co][H][W]
   const __nv_bfloat16* w;   // [co][ca+cb][ks*ks]
+  const __nv_bfloat16* wp;  // the tensor-core operand copy of w (k_conv3_tc), per chunk
   __nv_bfloat16* yb;        // forward output (BF16) or
   float* yf;                // forward output (FP32)
   float* ga;                // backward: input gradient of channels [0, ca)
@@ -170,7 +171,7 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
   return false;
 }
 
-__global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs q, int* err) {
+__global__ void __launch_bounds__(128, 5) k_conv3_tc(ConvArgs q, int* err) {
   extern __shared__ __align__(1024) unsigned char tcsm[];
   __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(tcsm);
   unsigned char* Bs = tcsm + kTcSmemHalo;
@@ -182,7 +183,9 @@ __global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs q, int* err) {
   const int H = q.H, W = q.W;
   const long long HW = (long long)H * W;
   const int b = blockIdx.z, x0 = blockIdx.x * 8, y0 = blockIdx.y * 16;
-  constexpr uint32_t kCols = 64;  // tensor-memory columns (N <= 64)
+  // tensor-memory columns: the accumulator's N (a power of two, at least 32),
+  // so that more CTAs of a small layer fit an SM's 512 columns
+  const uint32_t kCols = N <= 32 ? 32u : 64u;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
                  "r"(kCols));
@@ -206,28 +209,39 @@ __global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs q, int* err) {
   const __nv_bfloat16 zero = __float2bfloat16_rn(0.f);
   for (int ch = 0; ch < nchunks; ++ch) {
     const int ci0 = ch * kTcC;
-    // halo [c/8][pixel][c%8] of the chunk's channels (zero outside the image / cin)
-    for (int e = tid; e < kTcC * kTcHalo; e += 128) {
-      const int c = e / kTcHalo, pix = e - c * kTcHalo, hy = pix / kTcHx, hx = pix - hy * kTcHx;
-      const int ci = ci0 + c, gy = y0 + hy - 1, gx = x0 + hx - 1;
-      __nv_bfloat16 v = zero;
-      if (ci < cin && gy >= 0 && gy < H && gx >= 0 && gx < W) {
-        const long long off = (long long)gy * W + gx;
-        v = ci < q.ca ? q.xa[((long long)b * q.ca + ci) * HW + off] : q.xb[((long long)b * q.cb + (ci - q.ca)) * HW + off];
-      }
-      halo[((c >> 3) * kTcHalo + pix) * 8 + (c & 7)] = v;
-    }
-    // B_t[co][c] = w[co][ci0 + c][t], 8 channels per 16-byte store
-    for (int e = tid; e < 9 * N * 2; e += 128) {
-      const int t = e / (N * 2), r = e - t * N * 2, row = r >> 1, kg = r & 1;
-      __align__(16) __nv_bfloat16 v[8];
+    // halo [c/8][pixel][c%8] of the chunk's channels (zero outside the image /
+    // cin), in two halves whose loads are all issued before their stores
+    constexpr int kHaloPer = (kTcC * kTcHalo + 127) / 128, kHalf = (kHaloPer + 1) / 2;
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int ci = ci0 + kg * 8 + j;
-        v[j] = ci < cin ? q.w[((long long)row * cin + ci) * 9 + t] : zero;
+    for (int h0 = 0; h0 < kHaloPer; h0 += kHalf) {
+      __nv_bfloat16 hv[kHalf];
+#pragma unroll
+      for (int k = 0; k < kHalf; ++k) {
+        const int e = tid + (h0 + k) * 128;
+        const int c = e / kTcHalo, pix = e - c * kTcHalo, hy = pix / kTcHx, hx = pix - hy * kTcHx;
+        const int ci = ci0 + c, gy = y0 + hy - 1, gx = x0 + hx - 1;
+        hv[k] = zero;
+        if (h0 + k < kHaloPer && e < kTcC * kTcHalo && ci < cin && gy >= 0 && gy < H && gx >= 0 && gx < W) {
+          const long long off = (long long)gy * W + gx;
+          hv[k] = ci < q.ca ? __ldg(q.xa + ((long long)b * q.ca + ci) * HW + off)
+                            : __ldg(q.xb + ((long long)b * q.cb + (ci - q.ca)) * HW + off);
+        }
       }
-      *reinterpret_cast<uint4*>(Bs + t * btap + (row >> 3) * kTcBSBO + kg * kTcBLBO + (row & 7) * 16) =
-          *reinterpret_cast<const uint4*>(v);
+#pragma unroll
+      for (int k = 0; k < kHalf; ++k) {
+        const int e = tid + (h0 + k) * 128;
+        if (h0 + k < kHaloPer && e < kTcC * kTcHalo) {
+          const int c = e / kTcHalo, pix = e - c * kTcHalo;
+          halo[((c >> 3) * kTcHalo + pix) * 8 + (c & 7)] = hv[k];
+        }
+      }
+    }
+    // B_t[co][c] = w[co][ci0 + c][t]: the chunk's operand copy, already in
+    // the [tap][co/8][2][8 rows][8 channels] layout, 16 bytes per copy
+    {
+      const uint4* src = reinterpret_cast<const uint4*>(q.wp) + (long long)ch * 9 * N * 2;
+      uint4* dst = reinterpret_cast<uint4*>(Bs);
+      for (int e = tid; e < 9 * N * 2; e += 128) dst[e] = __ldg(src + e);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
@@ -442,6 +456,22 @@ __global__ void k_adam(float* w, float* g, float* m1, float* m2, __nv_bfloat16* 
     g[e] = 0.f;
   }
 }
+// The tensor-core operand copy of one 3x3 layer: element e of chunk ch, tap
+// t, row group rg, channel group kg, row r8, channel c8 is
+// w[row = 8 rg + r8][ci = 16 ch + 8 kg + c8][t] (zero beyond cin).
+__global__ void k_pack_w3(const __nv_bfloat16* w, __nv_bfloat16* wp, int co, int cin, long long total) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int c8 = int(e & 7), r8 = int((e >> 3) & 7), kg = int((e >> 6) & 1);
+    long long rest = e >> 7;
+    const int rg = int(rest % (co / 8));
+    rest /= (co / 8);
+    const int t = int(rest % 9), ch = int(rest / 9);
+    const int row = rg * 8 + r8, ci = ch * 16 + kg * 8 + c8;
+    wp[e] = ci < cin ? w[((long long)row * cin + ci) * 9 + t] : __float2bfloat16_rn(0.f);
+  }
+}
+
 __global__ void k_sync_bf16(const float* w, __nv_bfloat16* wb, long long n) {
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
     wb[e] = f2bf(w[e]);
@@ -509,6 +539,7 @@ void conv_fwd(UNet* N, int li, const __nv_bfloat16* xa, const __nv_bfloat16* xb,
   q.cb = L.cb;
   q.co = L.co;
   q.w = N->wb + L.w_off;
+  q.wp = L.p_off >= 0 ? N->wpack + L.p_off : nullptr;
   q.yb = yb;
   q.yf = yf;
   q.out_scale = oscale;
@@ -516,7 +547,7 @@ void conv_fwd(UNet* N, int li, const __nv_bfloat16* xa, const __nv_bfloat16* xb,
   q.B = B;
   q.H = H;
   q.W = W;
-  if (N->tensor_cores && L.ks == 3 && yb && (L.co == 16 || L.co == 32 || L.co == 64)) {
+  if (N->tensor_cores && L.ks == 3 && yb && L.p_off >= 0) {
     const dim3 tgrid((W + 7) / 8, (H + 15) / 16, B);
     static bool attr = false;
     if (!attr) {
@@ -614,9 +645,12 @@ int unet_init(UNet* N, const int* channels) {
     }
   const int* c = N->ch;
   long long off = 0;
+  long long poff = 0;
   auto add = [&](int idx, int ca, int cb, int co, int ks, int relu) {
-    N->layer[idx] = ConvLayer{ca, cb, co, ks, relu, off};
+    const bool tc = ks == 3 && (co == 16 || co == 32 || co == 64);
+    N->layer[idx] = ConvLayer{ca, cb, co, ks, relu, off, tc ? poff : -1};
     off += (long long)co * (ca + cb) * ks * ks;
+    if (tc) poff += (long long)((ca + cb + 15) / 16) * 9 * co * 16;
   };
   add(0, 1, 0, c[0], 3, 1);
   add(1, c[0], 0, c[0], 3, 1);
@@ -630,7 +664,10 @@ int unet_init(UNet* N, const int* channels) {
   add(10, c[1], c[0], c[0], 3, 1);
   add(11, c[0], 0, 1, 1, 0);
   N->nparams = off;
+  N->npack = poff;
   const size_t n = size_t(off);
+  if (cudaMalloc(&N->wpack, size_t(poff) * sizeof(__nv_bfloat16)) != cudaSuccess) return MACSAV_ERR_CUDA;
+  cudaMemset(N->wpack, 0, size_t(poff) * sizeof(__nv_bfloat16));
   if (cudaMalloc(&N->w32, n * sizeof(float)) != cudaSuccess || cudaMalloc(&N->grad, n * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&N->m1, n * sizeof(float)) != cudaSuccess || cudaMalloc(&N->m2, n * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&N->wb, n * sizeof(__nv_bfloat16)) != cudaSuccess ||
@@ -652,6 +689,8 @@ void unet_free(UNet* N) {
   cudaFree(N->m1);
   cudaFree(N->m2);
   cudaFree(N->wb);
+  cudaFree(N->wpack);
+  N->wpack = nullptr;
   cudaFree(N->loss);
   cudaFree(N->tc_err);
   N->tc_err = nullptr;
@@ -744,6 +783,18 @@ int unet_backward(UNet* N, NetWork* W, const float* in, const float* target, int
   return cudaGetLastError() == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
 }
 
+// Refresh the tensor-core operand copies from the BF16 weights.
+static void pack_weights(UNet* N, cudaStream_t s) {
+  for (int li = 0; li < kNetLayers; ++li) {
+    const ConvLayer& L = N->layer[li];
+    if (L.p_off < 0) continue;
+    const int cin = L.ca + L.cb;
+    const long long total = (long long)((cin + 15) / 16) * 9 * L.co * 16;
+    k_pack_w3<<<grid1(total), 256, 0, s>>>(N->wb + L.w_off, N->wpack + L.p_off, L.co, cin, total);
+    ++N->launches;
+  }
+}
+
 int unet_adam(UNet* N, float lr, cudaStream_t s) {
   const double b1 = 0.9, b2 = 0.999;
   N->adam_t += 1;
@@ -751,12 +802,14 @@ int unet_adam(UNet* N, float lr, cudaStream_t s) {
   k_adam<<<grid1(N->nparams), 256, 0, s>>>(N->w32, N->grad, N->m1, N->m2, N->wb, N->nparams, lr, float(b1), float(b2),
                                            float(c1), float(c2), 1e-8f);
   ++N->launches;
+  pack_weights(N, s);
   return cudaGetLastError() == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
 }
 
 int unet_sync_bf16(UNet* N, cudaStream_t s) {
   k_sync_bf16<<<grid1(N->nparams), 256, 0, s>>>(N->w32, N->wb, N->nparams);
   ++N->launches;
+  pack_weights(N, s);
   return cudaGetLastError() == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
 }
 

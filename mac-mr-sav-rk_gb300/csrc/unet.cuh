@@ -26,6 +26,7 @@ constexpr int kNetLayers = 12;
 struct ConvLayer {
   int ca, cb, co, ks, relu;
   long long w_off;  // offset of the layer's [co][ca+cb][ks*ks] weights in the parameter vector
+  long long p_off;  // offset of its tensor-core operand copy in UNet::wpack (-1: none)
 };
 
 struct UNet {
@@ -34,6 +35,12 @@ struct UNet {
   long long nparams = 0;
   float* w32 = nullptr;                 // master weights
   __nv_bfloat16* wb = nullptr;          // BF16 copy read by the kernels
+  // BF16 weights of the 3x3 layers in the shared-memory operand layout of
+  // the tensor-core convolution, per 16-channel chunk [chunk][tap][co/8][2][8][8],
+  // refreshed whenever the weights change, so a CTA stages them with
+  // contiguous 16-byte copies
+  __nv_bfloat16* wpack = nullptr;
+  long long npack = 0;
   float* grad = nullptr;                // weight gradients
   float *m1 = nullptr, *m2 = nullptr;   // Adam moments
   long long adam_t = 0;

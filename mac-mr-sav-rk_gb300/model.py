@@ -36,14 +36,16 @@ class MACNavierStokes:
     def __init__(self, grid: MACGrid, nu: float, force: Callable[[float], Any] | None = None,
                  backend: TensorStokes | None = None, cache_size: int = 4, *, precision: str = "fp64",
                  krylov_tolerance: float = 1e-12, tolerance: float = 1e-9, use_graph: bool = False,
-                 corrections: int | None = None, inner_krylov_tolerance: float | None = None) -> None:
+                 corrections: int | None = None, inner_krylov_tolerance: float | None = None,
+                 first_krylov_tolerance: float | None = None) -> None:
         if not np.isfinite(nu) or nu <= 0:
             raise ValueError("nu must be positive and finite")
         self.grid = grid
         self.nu = nu
         self.backend = backend if backend is not None else TensorStokes(
             grid, tolerance=tolerance, krylov_tolerance=krylov_tolerance, precision=precision,
-            corrections=corrections, inner_krylov_tolerance=inner_krylov_tolerance)
+            corrections=corrections, inner_krylov_tolerance=inner_krylov_tolerance,
+            first_krylov_tolerance=first_krylov_tolerance)
         self.force = force if force is not None else _zero_force(grid)
         self.use_graph = use_graph
         self.device = torch.device("cuda")

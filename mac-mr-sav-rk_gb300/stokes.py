@@ -99,7 +99,8 @@ class TensorStokes:
     def __init__(self, operators, tolerance: float = 1e-9, krylov_tolerance: float = 1e-12,
                  max_iterations: int = 100, matrix_free_operators: bool = True,
                  reuse_transform_buffers: bool = True, *, precision: str = "fp64", max_columns: int = 2,
-                 corrections: int | None = None, inner_krylov_tolerance: float | None = None) -> None:
+                 corrections: int | None = None, inner_krylov_tolerance: float | None = None,
+                 first_krylov_tolerance: float | None = None) -> None:
         # tensor_stokes.py:137-147
         if (tolerance <= 0 or krylov_tolerance <= 0 or not np.isfinite([tolerance, krylov_tolerance]).all()
                 or max_iterations < 1):
@@ -127,6 +128,9 @@ class TensorStokes:
             self.plan.check(self.plan.lib.macsav_plan_set_refinement(
                 self.plan.handle, 2 if corrections is None else int(corrections),
                 1e-4 if inner_krylov_tolerance is None else float(inner_krylov_tolerance)))
+        if first_krylov_tolerance is not None:
+            self.plan.check(self.plan.lib.macsav_plan_set_first_solve_tolerance(self.plan.handle,
+                                                                               float(first_krylov_tolerance)))
         self.setup_seconds = perf_counter() - start
         self.solve_seconds = 0.0
         self.solves = 0

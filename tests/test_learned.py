@@ -37,7 +37,8 @@ def test_forward_matches_torch_oracle(env):
     got = net.forward(x).cpu()
     ref = unet_torch.forward(unet_torch.split_params(net.params(), L.layer_shapes()), x).detach()
     err = float((got - ref).norm() / ref.norm())
-    assert err < 2e-2, err
+    print("forward relative error against the oracle: %.1e" % err)
+    assert err < 1e-2, err
     # positive homogeneity of the bias-free ReLU network
     got2 = net.forward(4.0 * x).cpu()
     assert float((got2 - 4.0 * got).norm() / got.norm().mul(4)) < 2e-2
@@ -54,17 +55,21 @@ def test_gradients_match_torch_autograd(env):
     ref_loss = ((unet_torch.forward(ws, x) - t) ** 2).mean()
     ref_loss.backward()
     ref = torch.cat([w.grad.reshape(-1) for w in ws]).numpy()
-    assert loss == pytest.approx(float(ref_loss.detach()), rel=2e-2)
+    assert loss == pytest.approx(float(ref_loss.detach()), rel=1e-2)
     rel = np.linalg.norm(grads - ref) / np.linalg.norm(ref)
     cos = float(grads @ ref / (np.linalg.norm(grads) * np.linalg.norm(ref)))
-    assert rel < 5e-2 and cos > 0.998, (rel, cos)
-    # every layer receives a gradient of the right size
-    off = 0
+    # every layer's gradient: the oracle rounds the same activations to BF16,
+    # so what is left is FP32 summation order and the odd activation that
+    # rounds to the other BF16 neighbour
+    off, per_layer = 0, []
     for co, ci, k in L.layer_shapes():
         n = co * ci * k * k
         g, r = grads[off:off + n], ref[off:off + n]
-        assert np.linalg.norm(g - r) <= 0.1 * np.linalg.norm(r) + 1e-12
+        per_layer.append(float(np.linalg.norm(g - r) / max(np.linalg.norm(r), 1e-30)))
         off += n
+    print("gradient relative error per layer:", ["%.1e" % e for e in per_layer], "overall %.1e" % rel)
+    assert rel < 1e-2 and cos > 0.9999, (rel, cos)
+    assert max(per_layer) < 1e-2, per_layer
 
 
 def _stage_rhs(pkg, grid, seeds, torch):
