@@ -676,6 +676,7 @@ def run_headline(args) -> None:
         vs_oracle = {k: float(torch.linalg.vector_norm(v - ox) / torch.linalg.vector_norm(ox))
                      for k, v in first.items()}
     cav = quick_cavity512(pkg, dev, args, flush)
+    autotune = transform_choices(pkg)
     line = {
         "metric": METRIC, "value": cells / (ms_l / 1e3), "unit": "cell-stage/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_l / args.steps, "higher_is_better": True,
@@ -709,6 +710,7 @@ def run_headline(args) -> None:
         "roofline": roof,
         "roofline_fp64": roof64,
         "cavity512_sdirk3_mrsav": cav,
+        "transform_autotune": autotune,
     }
     if oracle_sec is not None:
         line["cpu_baseline"] = {"value": w["nx"] * w["ny"] * w["stages_per_step"] / oracle_sec,
@@ -718,6 +720,24 @@ def run_headline(args) -> None:
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def transform_choices(pkg) -> dict:
+    """The autotuner's choice between the shared-memory FFT and the tcgen05
+    transform-matrix product (6 BF16 products) for FP32 forward transforms of
+    2n rows of length n, with both times (us)."""
+    from importlib import import_module
+    stokes = import_module(pkg.__name__ + ".stokes")
+    plan = stokes.Plan(pkg.MACGrid(8, 8))
+    out = {}
+    for kind, name in ((0, "dct2"), (1, "dst2"), (2, "dst1")):
+        for n in (64, 128, 256, 511, 512):
+            m, tf, tt = C.c_int(), C.c_double(), C.c_double()
+            plan.check(plan.lib.macsav_transform32_autotune(plan.handle, kind, 0, 2 * n, n, C.byref(m), C.byref(tf),
+                                                            C.byref(tt), stokes.stream_handle()))
+            out[f"{name}_{n}"] = {"choice": "tensor" if m.value == 2 else "fft", "fft_us": round(1e3 * tf.value, 1),
+                                  "tensor_us": round(1e3 * tt.value, 1)}
+    return out
 
 
 def quick_cavity512(pkg, dev, args, flush) -> dict:
