@@ -487,7 +487,8 @@ static int net_buffers(Plan* P, macsav::UNet* net, int f) {
   if (!P->net_out) {
     if (cudaMalloc(&P->net_out, cells * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&P->net_rold, cells * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&P->net_scale, 2 * macsav::kMaxCols * sizeof(float)) != cudaSuccess)
+        cudaMalloc(&P->net_scale, 2 * macsav::kMaxCols * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&P->net_wacc0, size_t(P->maxcols) * P->g.size * sizeof(float)) != cudaSuccess)
       return cuda_status(P);
     cudaMemset(P->net_rold, 0, cells * sizeof(float));
   }

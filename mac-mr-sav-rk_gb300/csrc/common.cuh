@@ -89,6 +89,17 @@ __device__ __forceinline__ df32 df_add(df32 a, df32 b) {
   return {h, e - (h - s.hi)};
 }
 __device__ __forceinline__ double df_value(df32 a) { return double(a.hi) + double(a.lo); }
+__device__ __forceinline__ df32 df_neg(df32 a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ df32 df_sub(df32 a, df32 b) { return df_add(a, df_neg(b)); }
+// Product of two double-floats (Dekker's product with an FMA for the exact
+// low part of hi*hi), renormalised.
+__device__ __forceinline__ df32 df_mul(df32 a, df32 b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  const float h = p + e;
+  return {h, e - (h - p)};
+}
 
 // Conversions between double and float without the FP64 pipe: the binary64
 // fields are re-packed with integer instructions, rounding to nearest even.
@@ -118,6 +129,30 @@ __device__ __forceinline__ double f2d_bits(float f) {
   if (e == 0xff) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull | (m << 29)));
   return __longlong_as_double((long long)(sign | ((unsigned long long)(e - 127 + 1023) << 52) | (m << 29)));
 }
+// A double as a double-float hi + lo without the FP64 pipe: hi is x rounded
+// to float (d2f_bits), lo the rest x - hi (exact in binary64, at most 30
+// significant bits) rounded to float, so hi + lo carries about 48 bits.
+// Zero, subnormal, infinite and NaN inputs, and parts beyond the float range,
+// give lo = 0 (hi carries the special value).
+__device__ __forceinline__ df32 d2df(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const float hi = d2f_bits(x);
+  const int e = int((b >> 52) & 0x7ff);
+  const unsigned int hb = __float_as_uint(hi);
+  const int he = int((hb >> 23) & 0xffu);
+  const int se = e - 1075 + 127;  // biased float exponent of 2^(e - 1075)
+  if (e == 0 || e == 0x7ff || he == 0 || he == 0xff || se + 64 <= 0 || se >= 255) return {hi, 0.0f};
+  const long long m = (long long)((b & 0xfffffffffffffull) | (1ull << 52));  // |x| = m 2^(e-1075)
+  const long long hm = (long long)((hb & 0x7fffffu) | 0x800000u);              // |hi| = hm 2^(he-150)
+  const int sh = he - e + 925;  // 29, or 30 when the rounding carried into the exponent
+  const int r = int(m - (hm << sh));  // |r| <= 2^29
+  // r 2^(e-1075) as a float, scaled in two steps when 2^(e-1075) is below
+  // the normal float range (|x| below about 2^-75)
+  const float lo = se > 0 ? float(r) * __uint_as_float((unsigned int)se << 23)
+                          : (float(r) * __uint_as_float((unsigned int)(se + 64) << 23)) * 5.421010862427522e-20f;
+  return {hi, (b >> 63) ? -lo : lo};
+}
+
 // Load a double into T without touching the FP64 pipe when T is float.
 template <typename T>
 __device__ __forceinline__ T load_as(const double* p) {

@@ -248,7 +248,7 @@ void plan_free(Plan* p) {
   cudaFree(p->errword);
   cudaFree(p->done_counter);
   cudaFree(p->net_out); cudaFree(p->net_rold); cudaFree(p->net_scale);
-  cudaFree(p->net_cin); cudaFree(p->net_cout);
+  cudaFree(p->net_cin); cudaFree(p->net_cout); cudaFree(p->net_wacc0);
   net_work_free(&p->netw);
   p->done_counter = nullptr;
   cudaFreeHost(p->h_cg); cudaFreeHost(p->h_checks); cudaFreeHost(p->h_active); cudaFreeHost(p->h_err);

@@ -140,6 +140,7 @@ struct Plan {
   NetWork netw;
   float* net_out = nullptr;    // network output, [maxcols][np]
   float* net_rold = nullptr;   // previous residual (Polak-Ribiere beta), [maxcols][np]
+  float* net_wacc0 = nullptr;  // start of the accumulated velocity, for restarts, [maxcols][size]
   float* net_scale = nullptr;  // per-column input and output scales, [2][maxcols]
   int net_maxit = 20;          // learned iterations before the plain-PCG restart
   // placement: every_iter = 0 evaluates the network only in the first CG

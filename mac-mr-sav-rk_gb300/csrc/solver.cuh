@@ -106,22 +106,6 @@ struct DstPacked {
   }
 };
 
-// Packed FP64 velocity accumulation: x (+)= double(value) (the correction
-// of a defect-correction sweep added to the FP64 velocity).
-template <typename T>
-struct DstAccum {
-  using aux_t = int;
-  double* x;
-  long long cstride;
-  int off1, n0, n1;
-  int add;
-  __device__ aux_t load(int, int, int, int) const { return 0; }
-  __device__ void store(int b, int c, int row, int n, T v, aux_t, Acc<T> (&)[2]) const {
-    double* p = x + c * cstride + (b == 0 ? (long long)row * n0 + n : off1 + (long long)row * n1 + n);
-    *p = add ? *p + double(v) : double(v);
-  }
-};
-
 template <typename T, typename Out>
 struct DstCells {
   using aux_t = int;

@@ -184,9 +184,12 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int np, T* x, T* r, T* p
 }
 
 // ------------------------------------------- learned preconditioner (FCG) ---
-// Columns whose learned attempt failed restart plain PCG from zero: x = 0, r = b.
+// Columns whose learned attempt failed restart plain PCG from zero: x = 0,
+// r = b, and the accumulated velocity back to its start (mI+kK)^{-1} ru,
+// kept in wacc0 (sz elements per column).
 __global__ void __launch_bounds__(kThreads) k_fcg_restart(int np, const float* b, float* x, float* r, long long cs,
-                                                          const CGScalars* cg) {
+                                                          const CGScalars* cg, float* wacc, const float* wacc0,
+                                                          long long sz) {
   pdl_wait();
   const int c = blockIdx.y;
   if (!cg[c].restart) return;
@@ -195,6 +198,10 @@ __global__ void __launch_bounds__(kThreads) k_fcg_restart(int np, const float* b
     x[k] = 0.0f;
     r[k] = b[k];
   }
+  if (wacc && wacc0)
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < sz;
+         idx += (long long)gridDim.x * blockDim.x)
+      wacc[c * sz + idx] = wacc0[c * sz + idx];
 }
 
 // Network input scale 1/rms(r) and output scale rms(r) rho/rr (rho = r.Mr of
@@ -399,7 +406,8 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
     net = X.net && P->net;
     if (net) {
       r_old = P->net_rold;
-      launch_k(k_fcg_restart, dim3(rb, cols), kThreads, 0, s, g.np, b, x, r, np, P->cg);
+      launch_k(k_fcg_restart, dim3(rb, cols), kThreads, 0, s, g.np, b, x, r, np, P->cg, wacc,
+               static_cast<const float*>(P->net_wacc0), sz);
       ++P->launches;
     }
   }
@@ -630,25 +638,64 @@ int solve_fp64(Plan* P, const double* f, int cols, double mass, double visc, dou
 }
 
 // ------------------------------------------------- FP32 + FP64 correction ---
-// FP64 defect of the accumulated solution: ru = f - (m u + k K u - D^T p),
-// rd = -D u (the continuity defect).
-__global__ void __launch_bounds__(kThreads) k_defect64(GridDev g, const double* f, const double* vel,
-                                                       const double* pres, const double* shift, double* ru,
-                                                       double* rd) {
+// Defect of the accumulated solution: ru = f - (m u + k K u - D^T p),
+// rd = -D u (the continuity defect), for the next correction sweep.  It is
+// computed in double-float arithmetic on the FP32 pipe (about 48 bits, no
+// FP64 instruction): its consumer, the next FP32 inner solve, reads it
+// rounded to float, so the float nearest to the defect is what is stored;
+// computing it in double-float keeps the cancellation between f and
+// m u + k K u - D^T p (the defect is 1e-4 .. 1e-9 of f) exact to far below
+// that rounding.  GB300 runs FP64 at about 1/70 of FP32, and the FP64 form of
+// this kernel issued about 20 FP64 operations per face.
+__global__ void __launch_bounds__(kThreads) k_defect_df(GridDev g, const double* f, const double* vel,
+                                                        const double* pres, const double* shift, double* ru,
+                                                        double* rd) {
   pdl_wait();
   const int c = blockIdx.y;
-  const double mass = shift[2 * c], visc = shift[2 * c + 1];
+  const df32 mass = d2df(shift[2 * c]), visc = d2df(shift[2 * c + 1]);
+  const df32 ihx = d2df(g.ihx), ihy = d2df(g.ihy), ihx2 = d2df(g.ihx2), ihy2 = d2df(g.ihy2);
   const double* u = vel + c * (long long)g.size;
   const double* pp = pres + c * (long long)g.np;
   const int n = g.size > g.np ? g.size : g.np;
+  const df32 zero{0.0f, 0.0f};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     if (i < g.size) {
-      const long long k = c * (long long)g.size + i;
-      ru[k] = f[k] - (mass * u[i] + visc * K_at(u, g, i) - Dt_at(pp, g, i));
+      // (K u)_i with the wall rows of K_at: neighbours beyond a normal wall
+      // are 0, beyond a tangential wall -u_i (diagonal 3/h^2)
+      df32 cc, l, r, s, nn, dt;
+      if (i < g.nu) {
+        const int w = g.nx - 1, j = i / w, q = i - j * w;
+        cc = d2df(u[i]);
+        l = q > 0 ? d2df(u[i - 1]) : zero;
+        r = q < w - 1 ? d2df(u[i + 1]) : zero;
+        s = j > 0 ? d2df(u[i - w]) : df_neg(cc);
+        nn = j < g.ny - 1 ? d2df(u[i + w]) : df_neg(cc);
+        const int lc = j * g.nx + q;
+        dt = df_mul(df_sub(d2df(pp[lc]), d2df(pp[lc + 1])), ihx);
+      } else {
+        const int fi = i - g.nu, j = fi / g.nx, q = fi - j * g.nx;
+        cc = d2df(u[i]);
+        l = q > 0 ? d2df(u[i - 1]) : df_neg(cc);
+        r = q < g.nx - 1 ? d2df(u[i + 1]) : df_neg(cc);
+        s = j > 0 ? d2df(u[i - g.nx]) : zero;
+        nn = j < g.ny - 2 ? d2df(u[i + g.nx]) : zero;
+        const int lc = j * g.nx + q;
+        dt = df_mul(df_sub(d2df(pp[lc]), d2df(pp[lc + g.nx])), ihy);
+      }
+      const df32 c2{2.0f * cc.hi, 2.0f * cc.lo};
+      const df32 kx = df_mul(df_sub(df_sub(c2, l), r), ihx2);
+      const df32 ky = df_mul(df_sub(df_sub(c2, s), nn), ihy2);
+      const df32 op = df_sub(df_add(df_mul(mass, cc), df_mul(visc, df_add(kx, ky))), dt);
+      ru[c * (long long)g.size + i] = f2d_bits(df_sub(d2df(f[c * (long long)g.size + i]), op).hi);
     }
     if (i < g.np) {
       const int j = i / g.nx, q = i - j * g.nx;
-      rd[c * (long long)g.np + i] = -D_at(u, g, j, q);
+      df32 d = zero;
+      if (q < g.nx - 1) d = df_add(d, df_mul(d2df(u[j * (g.nx - 1) + q]), ihx));
+      if (q > 0) d = df_sub(d, df_mul(d2df(u[j * (g.nx - 1) + q - 1]), ihx));
+      if (j < g.ny - 1) d = df_add(d, df_mul(d2df(u[g.nu + j * g.nx + q]), ihy));
+      if (j > 0) d = df_sub(d, df_mul(d2df(u[g.nu + (j - 1) * g.nx + q]), ihy));
+      rd[c * (long long)g.np + i] = f2d_bits(-d.hi);
     }
   }
 }
@@ -670,17 +717,6 @@ __global__ void __launch_bounds__(kThreads) k_accumulate_sweep(const float* u, d
   }
 }
 
-// dst (+)= double(src) over n elements per column.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_accumulate(const T* src, double* dst, long long n, int add) {
-  pdl_wait();
-  const int c = blockIdx.y;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const long long k = c * n + i;
-    dst[k] = add ? dst[k] + double(src[k]) : double(src[k]);
-  }
-}
-
 // One FP32 Stokes solve of (ru, rd): transforms, stencils and Krylov vectors
 // in float, reductions in double.  Its velocity and pressure are added to
 // the FP64 `vel` and `pres` (set when add = 0).
@@ -694,9 +730,9 @@ __global__ void __launch_bounds__(kThreads) k_accumulate(const T* src, double* d
 // inner-solve error.  The learned preconditioner (flexible CG, whose columns
 // may restart) runs in the first inner solve of a Stokes solve only (add = 0:
 // its right-hand side is the stage's own, a smooth field; the correction
-// sweeps solve for rounding-level defects), and that solve keeps the closing
-// velocity inverse.  With the every-iteration placement it runs in all inner
-// solves.
+// sweeps solve for rounding-level defects), or in all of them with the
+// every-iteration placement.  A column that restarts from zero also takes its
+// accumulated velocity back to the start, kept in net_wacc0.
 static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, int cols, double* vel, double* pres,
                          int add) {
   const GridDev& g = P->g;
@@ -704,9 +740,9 @@ static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, i
   const long long sz = g.size, np = g.np;
   float* w = P->w32;
   const bool net = P->net != nullptr && (P->net_every || add == 0);
-  float* wacc = net ? nullptr : P->wacc32;
-  velocity_inverse<float>(P, L, SrcPacked<float, double>{ru, sz, g.nu, g.nx - 1, g.nx}, wacc ? wacc : w, sz, cols,
-                          nullptr);
+  float* wacc = P->wacc32;
+  velocity_inverse<float>(P, L, SrcPacked<float, double>{ru, sz, g.nu, g.nx - 1, g.nx}, wacc, sz, cols, nullptr);
+  if (net) cudaMemcpyAsync(P->net_wacc0, wacc, sizeof(float) * size_t(sz) * cols, cudaMemcpyDeviceToDevice, X.s);
   const double keep = X.ktol;
   const int keep_net = X.net;
   X.ktol = (add == 0 && P->first_ktol > 0.0) ? P->first_ktol : P->inner_ktol;
@@ -716,26 +752,17 @@ static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, i
   X.net = keep_net;
   if (rc != MACSAV_OK) return rc;
   const float* x = P->cells32 + 1 * np * cols;
-  if (wacc) {
-    const int nb = red_blocks(sz);
-    launch_k(k_accumulate_sweep, dim3(nb, cols), kThreads, 0, X.s, static_cast<const float*>(wacc), vel, sz, x, pres,
-             np, add);
-    ++P->launches;
-    return MACSAV_OK;
-  }
-  const int nbp = red_blocks(np);
-  auto add_pressure = [&](cudaStream_t st) {
-    launch_k(k_accumulate<float>, dim3(nbp, cols), kThreads, 0, st, x, pres, np, add);
-    ++P->launches;
-  };
-  L.velocity_solve(SrcLift<float, double, float>{ru, sz, x, nullptr, P->cg, np, g.nx, g.nu, float(g.ihx), float(g.ihy)},
-                   DstAccum<float>{vel, sz, g.nu, g.nx - 1, g.nx, add}, cols, nullptr, P->shift, add_pressure);
+  const int nb = red_blocks(sz);
+  launch_k(k_accumulate_sweep, dim3(nb, cols), kThreads, 0, X.s, static_cast<const float*>(wacc), vel, sz, x, pres, np,
+           add);
+  ++P->launches;
   return MACSAV_OK;
 }
 
 // TensorStokes.solve with FP32 bulk: an FP32 solve, then `corrections`
-// defect-correction sweeps whose defects are formed in FP64, so the result
-// satisfies the same FP64 residual and divergence gates as the FP64 path.
+// defect-correction sweeps whose defects are formed from the FP64 fields in
+// double-float arithmetic, so the result satisfies the same FP64 residual and
+// divergence gates (checked in FP64) as the FP64 path.
 int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres, bool close) {
   const GridDev& g = P->g;
   const long long sz = g.size, np = g.np;
@@ -746,7 +773,7 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
     const double* rhs_u = f;
     const double* rhs_d = nullptr;
     if (sweep > 0) {
-      launch_k(k_defect64, dim3(nbm, cols), kThreads, 0, X.s, g, f, vel, pres, P->shift, ru, rd);
+      launch_k(k_defect_df, dim3(nbm, cols), kThreads, 0, X.s, g, f, vel, pres, P->shift, ru, rd);
       ++P->launches;
       rhs_u = ru;
       rhs_d = rd;
