@@ -105,4 +105,45 @@ __device__ __forceinline__ double conv_at(const double* x, const GridDev& g, int
   return r;
 }
 
+// The same convection in double-float arithmetic on the FP32 pipe (about 48
+// bits; no FP64 instruction but the final hi + lo).  The FP32-bulk form uses
+// it: GB300 runs FP64 at about 1/70 of FP32, and conv_at issues about 35 FP64
+// operations per face.
+__device__ __forceinline__ df32 df_half(df32 a) { return {0.5f * a.hi, 0.5f * a.lo}; }
+__device__ __forceinline__ df32 U_df(const double* x, const GridDev& g, int j, int I) {
+  return (I <= 0 || I >= g.nx) ? df32{0.0f, 0.0f} : d2df(x[j * (g.nx - 1) + I - 1]);
+}
+__device__ __forceinline__ df32 V_df(const double* x, const GridDev& g, int J, int i) {
+  return (J <= 0 || J >= g.ny) ? df32{0.0f, 0.0f} : d2df(x[g.nu + (J - 1) * g.nx + i]);
+}
+__device__ __forceinline__ double conv_at_df(const double* x, const GridDev& g, int e, df32 ihx, df32 ihy) {
+  df32 r;
+  if (e < g.nu) {
+    const int w = g.nx - 1, j = e / w, I = e - j * w + 1;
+    const df32 uc = U_df(x, g, j, I);
+    const df32 ue = U_df(x, g, j, I + 1), uw = U_df(x, g, j, I - 1);
+    const df32 un = j < g.ny - 1 ? U_df(x, g, j + 1, I) : df_neg(uc);
+    const df32 us = j > 0 ? U_df(x, g, j - 1, I) : df_neg(uc);
+    const df32 fe = df_half(df_add(uc, ue)), fw = df_half(df_add(uc, uw));
+    const df32 fn = df_half(df_add(V_df(x, g, j + 1, I - 1), V_df(x, g, j + 1, I)));
+    const df32 fs = df_half(df_add(V_df(x, g, j, I - 1), V_df(x, g, j, I)));
+    r = df_add(df_mul(df_sub(df_mul(fe, fe), df_mul(fw, fw)), ihx),
+               df_mul(df_sub(df_mul(fn, df_half(df_add(uc, un))), df_mul(fs, df_half(df_add(uc, us)))), ihy));
+    r = df_sub(r, df_mul(df_half(uc), df_add(df_mul(df_sub(fe, fw), ihx), df_mul(df_sub(fn, fs), ihy))));
+  } else {
+    const int f = e - g.nu, J = f / g.nx + 1, i = f - (J - 1) * g.nx;
+    const df32 vc = V_df(x, g, J, i);
+    const df32 vn = V_df(x, g, J + 1, i), vs = V_df(x, g, J - 1, i);
+    const df32 ve = i < g.nx - 1 ? V_df(x, g, J, i + 1) : df_neg(vc);
+    const df32 vw = i > 0 ? V_df(x, g, J, i - 1) : df_neg(vc);
+    const df32 ge = df_half(df_add(U_df(x, g, J - 1, i + 1), U_df(x, g, J, i + 1)));
+    const df32 gw = df_half(df_add(U_df(x, g, J - 1, i), U_df(x, g, J, i)));
+    const df32 gn = df_half(df_add(vc, vn)), gs = df_half(df_add(vc, vs));
+    r = df_add(df_mul(df_sub(df_mul(ge, df_half(df_add(vc, ve))), df_mul(gw, df_half(df_add(vc, vw)))), ihx),
+               df_mul(df_sub(df_mul(gn, gn), df_mul(gs, gs)), ihy));
+    r = df_sub(r, df_mul(df_half(vc), df_add(df_mul(df_sub(ge, gw), ihx), df_mul(df_sub(gn, gs), ihy))));
+  }
+  return f2d_bits(r.hi) + f2d_bits(r.lo);
+}
+
 }  // namespace macsav

@@ -189,13 +189,23 @@ __global__ void __launch_bounds__(kThreads) k_stage_defect(GridDev g, const doub
   }
 }
 
-// Skew convection of every member's stage velocity (kernels.py:6-35).
+// Skew convection of every member's stage velocity (kernels.py:6-35); DF:
+// in double-float arithmetic on the FP32 pipe (the FP32-bulk form; the FP64
+// path keeps conv_at in FP64).
+template <bool DF>
 __global__ void k_conv_members(GridDev g, const double* x, long long xstr, double* out, long long ostr) {
   pdl_wait();
   const int mem = blockIdx.y;
   x += mem * xstr;
   out += mem * ostr;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < g.size; e += gridDim.x * blockDim.x) out[e] = conv_at(x, g, e);
+  if constexpr (DF) {
+    const df32 ihx = d2df(g.ihx), ihy = d2df(g.ihy);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < g.size; e += gridDim.x * blockDim.x)
+      out[e] = conv_at_df(x, g, e, ihx, ihy);
+  } else {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < g.size; e += gridDim.x * blockDim.x)
+      out[e] = conv_at(x, g, e);
+  }
 }
 
 __device__ double fold_sum(const double* partial, int nb, int K, int k, double* red) {
@@ -669,7 +679,8 @@ static int enqueue_step(Plan* P, Exec& X, int scheme, const StageProgram& G, boo
   const MemberStrides ms{5 * sz, 4 * sz, 4 * sz, cols * sz, cols * sz, cols * np, 4 * np};
   launch_k(k_clear_recs, 1, 128, 0, s, B.recs, kRecStride * M);
   // N(U_0)
-  launch_k(k_conv_members, dim3(red_nb(sz), M), kThreads, 0, s, g, B.X, ms.X, B.NN, ms.NN);
+  auto conv = P->precision == MACSAV_FP64 ? k_conv_members<false> : k_conv_members<true>;
+  launch_k(conv, dim3(red_nb(sz), M), kThreads, 0, s, g, B.X, ms.X, B.NN, ms.NN);
   P->launches += 2;
   for (int i = 0; i < G.nstages; ++i) {
     StageRec* rec = B.recs + i;
@@ -724,7 +735,7 @@ static int enqueue_step(Plan* P, Exec& X, int scheme, const StageProgram& G, boo
     launch_k(k_stage_close, M, kThreads, 0, s, P->partial, nbn, nbn, B.recs, i, B.coef, G.sav[i], area, sav ? 1 : 0, gate);
     P->launches += 3;
     if (i + 1 < G.nstages) {
-      launch_k(k_conv_members, dim3(red_nb(sz), M), kThreads, 0, s, g, U, ms.X, B.NN + (i + 1) * sz, ms.NN);
+      launch_k(conv, dim3(red_nb(sz), M), kThreads, 0, s, g, U, ms.X, B.NN + (i + 1) * sz, ms.NN);
       ++P->launches;
     }
   }

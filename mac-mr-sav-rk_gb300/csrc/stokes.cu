@@ -45,7 +45,7 @@ __device__ __forceinline__ unsigned long long abs_key_t(T v) {
 // last block: mean of b (OP_MEAN_B).
 template <typename T, typename WIn>
 __global__ void __launch_bounds__(kThreads) k_pressure_rhs(GridDev g, const WIn* w, long long ws, T* b, long long cs,
-                                                           const double* rd, double* partial, CGFin<T> fin,
+                                                           const float* rd, double* partial, CGFin<T> fin,
                                                            unsigned int* done) {
   pdl_wait();
   const int c = blockIdx.y;
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_start(int np, T* b, T* x, T* r,
 // so no separate start kernel runs.
 template <typename T, typename WIn>
 __global__ void __launch_bounds__(kThreads) k_pressure_rhs_start(GridDev g, const WIn* w, long long ws, T* b, T* x,
-                                                                 long long cs, const double* rd, double* partial,
+                                                                 long long cs, const float* rd, double* partial,
                                                                  CGFin<T> fin, unsigned int* done) {
   pdl_wait();
   const int c = blockIdx.y;
@@ -462,7 +462,7 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
 // On entry w holds (mI+kK)^{-1} f in T; on exit x holds the pressure iterate
 // and P->cg the per-column counters.
 template <typename T>
-static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int cols, const double* rd = nullptr,
+static int schur_pcg(Plan* P, Exec& X, const Launcher<T>& L, T* w, T* cells, int cols, const float* rd = nullptr,
                      T* wacc = nullptr) {
   const GridDev& g = P->g;
   const long long np = g.np, sz = g.size;
@@ -638,64 +638,78 @@ int solve_fp64(Plan* P, const double* f, int cols, double mass, double visc, dou
 }
 
 // ------------------------------------------------- FP32 + FP64 correction ---
-// Defect of the accumulated solution: ru = f - (m u + k K u - D^T p),
-// rd = -D u (the continuity defect), for the next correction sweep.  It is
-// computed in double-float arithmetic on the FP32 pipe (about 48 bits, no
-// FP64 instruction): its consumer, the next FP32 inner solve, reads it
-// rounded to float, so the float nearest to the defect is what is stored;
-// computing it in double-float keeps the cancellation between f and
-// m u + k K u - D^T p (the defect is 1e-4 .. 1e-9 of f) exact to far below
-// that rounding.  GB300 runs FP64 at about 1/70 of FP32, and the FP64 form of
-// this kernel issued about 20 FP64 operations per face.
-__global__ void __launch_bounds__(kThreads) k_defect_df(GridDev g, const double* f, const double* vel,
-                                                        const double* pres, const double* shift, double* ru,
-                                                        double* rd) {
+// Defect for the next correction sweep, updated from the last FP32 solve:
+// with the accumulated solution (vel, pres) = sum of the solves' (u_k, x_k),
+// the momentum defect f - (m vel + k K vel - D^T pres) after solve k is the
+// one after solve k-1 minus (m u_k + k K u_k - D^T x_k), and the continuity
+// defect -D vel is the last one minus D u_k (both start from f and 0).  u_k
+// and x_k are exactly the floats added to the FP64 fields, so the update needs
+// no FP64 input but f once: it runs in double-float arithmetic on the FP32
+// pipe (about 48 bits, no FP64 instruction) and keeps each defect as a float
+// pair (hi, lo) in place.  The next FP32 solve reads the hi parts, the float
+// nearest to the defect; the pairs keep the cancellation between f and the
+// operator (the defect is 1e-4 .. 1e-9 of f) exact to far below that
+// rounding.  The closing FP64 check of the solve measures the true defect of
+// (vel, pres) in FP64.  GB300 runs FP64 at about 1/70 of FP32, and the FP64
+// form of this kernel read the FP64 fields and issued about 20 FP64
+// operations per face.
+//   f: the Stokes right-hand side (first sweep) or null (the pairs hold the
+//   previous defect); u, x: the last solve's velocity and pressure (float).
+__global__ void __launch_bounds__(kThreads) k_defect_update(GridDev g, const double* f, const float* u,
+                                                            const float* x, const double* shift, float* ru_hi,
+                                                            float* ru_lo, float* rd_hi, float* rd_lo) {
   pdl_wait();
   const int c = blockIdx.y;
   const df32 mass = d2df(shift[2 * c]), visc = d2df(shift[2 * c + 1]);
   const df32 ihx = d2df(g.ihx), ihy = d2df(g.ihy), ihx2 = d2df(g.ihx2), ihy2 = d2df(g.ihy2);
-  const double* u = vel + c * (long long)g.size;
-  const double* pp = pres + c * (long long)g.np;
+  const long long su = c * (long long)g.size, sp = c * (long long)g.np;
+  const float* uc = u + su;
+  const float* xc = x + sp;
   const int n = g.size > g.np ? g.size : g.np;
-  const df32 zero{0.0f, 0.0f};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     if (i < g.size) {
-      // (K u)_i with the wall rows of K_at: neighbours beyond a normal wall
-      // are 0, beyond a tangential wall -u_i (diagonal 3/h^2)
-      df32 cc, l, r, s, nn, dt;
+      // K u_k with the wall rows of K_at: neighbours beyond a normal wall are
+      // 0, beyond a tangential wall -u (diagonal 3/h^2)
+      const float cc = uc[i];
+      float l, r, s, nn;
+      df32 dt;
       if (i < g.nu) {
         const int w = g.nx - 1, j = i / w, q = i - j * w;
-        cc = d2df(u[i]);
-        l = q > 0 ? d2df(u[i - 1]) : zero;
-        r = q < w - 1 ? d2df(u[i + 1]) : zero;
-        s = j > 0 ? d2df(u[i - w]) : df_neg(cc);
-        nn = j < g.ny - 1 ? d2df(u[i + w]) : df_neg(cc);
+        l = q > 0 ? uc[i - 1] : 0.0f;
+        r = q < w - 1 ? uc[i + 1] : 0.0f;
+        s = j > 0 ? uc[i - w] : -cc;
+        nn = j < g.ny - 1 ? uc[i + w] : -cc;
         const int lc = j * g.nx + q;
-        dt = df_mul(df_sub(d2df(pp[lc]), d2df(pp[lc + 1])), ihx);
+        dt = df_mul(df_two_sum(xc[lc], -xc[lc + 1]), ihx);
       } else {
         const int fi = i - g.nu, j = fi / g.nx, q = fi - j * g.nx;
-        cc = d2df(u[i]);
-        l = q > 0 ? d2df(u[i - 1]) : df_neg(cc);
-        r = q < g.nx - 1 ? d2df(u[i + 1]) : df_neg(cc);
-        s = j > 0 ? d2df(u[i - g.nx]) : zero;
-        nn = j < g.ny - 2 ? d2df(u[i + g.nx]) : zero;
+        l = q > 0 ? uc[i - 1] : -cc;
+        r = q < g.nx - 1 ? uc[i + 1] : -cc;
+        s = j > 0 ? uc[i - g.nx] : 0.0f;
+        nn = j < g.ny - 2 ? uc[i + g.nx] : 0.0f;
         const int lc = j * g.nx + q;
-        dt = df_mul(df_sub(d2df(pp[lc]), d2df(pp[lc + g.nx])), ihy);
+        dt = df_mul(df_two_sum(xc[lc], -xc[lc + g.nx]), ihy);
       }
-      const df32 c2{2.0f * cc.hi, 2.0f * cc.lo};
-      const df32 kx = df_mul(df_sub(df_sub(c2, l), r), ihx2);
-      const df32 ky = df_mul(df_sub(df_sub(c2, s), nn), ihy2);
-      const df32 op = df_sub(df_add(df_mul(mass, cc), df_mul(visc, df_add(kx, ky))), dt);
-      ru[c * (long long)g.size + i] = f2d_bits(df_sub(d2df(f[c * (long long)g.size + i]), op).hi);
+      const df32 kx = df_mul(df_add(df_two_sum(cc, -l), df_two_sum(cc, -r)), ihx2);
+      const df32 ky = df_mul(df_add(df_two_sum(cc, -s), df_two_sum(cc, -nn)), ihy2);
+      const df32 op = df_sub(df_add(df_mul(mass, df32{cc, 0.0f}), df_mul(visc, df_add(kx, ky))), dt);
+      const long long k = su + i;
+      const df32 prev = f ? d2df(f[k]) : df32{ru_hi[k], ru_lo[k]};
+      const df32 now = df_sub(prev, op);
+      ru_hi[k] = now.hi;
+      ru_lo[k] = now.lo;
     }
     if (i < g.np) {
       const int j = i / g.nx, q = i - j * g.nx;
-      df32 d = zero;
-      if (q < g.nx - 1) d = df_add(d, df_mul(d2df(u[j * (g.nx - 1) + q]), ihx));
-      if (q > 0) d = df_sub(d, df_mul(d2df(u[j * (g.nx - 1) + q - 1]), ihx));
-      if (j < g.ny - 1) d = df_add(d, df_mul(d2df(u[g.nu + j * g.nx + q]), ihy));
-      if (j > 0) d = df_sub(d, df_mul(d2df(u[g.nu + (j - 1) * g.nx + q]), ihy));
-      rd[c * (long long)g.np + i] = f2d_bits(-d.hi);
+      df32 d{0.0f, 0.0f};
+      const float ue = q < g.nx - 1 ? uc[j * (g.nx - 1) + q] : 0.0f, uw = q > 0 ? uc[j * (g.nx - 1) + q - 1] : 0.0f;
+      const float vn = j < g.ny - 1 ? uc[g.nu + j * g.nx + q] : 0.0f, vs = j > 0 ? uc[g.nu + (j - 1) * g.nx + q] : 0.0f;
+      d = df_add(df_mul(df_two_sum(ue, -uw), ihx), df_mul(df_two_sum(vn, -vs), ihy));
+      const long long k = sp + i;
+      const df32 prev = f ? df32{0.0f, 0.0f} : df32{rd_hi[k], rd_lo[k]};
+      const df32 now = df_sub(prev, d);
+      rd_hi[k] = now.hi;
+      rd_lo[k] = now.lo;
     }
   }
 }
@@ -717,7 +731,8 @@ __global__ void __launch_bounds__(kThreads) k_accumulate_sweep(const float* u, d
   }
 }
 
-// One FP32 Stokes solve of (ru, rd): transforms, stencils and Krylov vectors
+// One FP32 Stokes solve of (f, 0) or of the defect (ru, rd): transforms,
+// stencils and Krylov vectors
 // in float, reductions in double.  Its velocity and pressure are added to
 // the FP64 `vel` and `pres` (set when add = 0).
 //
@@ -733,15 +748,16 @@ __global__ void __launch_bounds__(kThreads) k_accumulate_sweep(const float* u, d
 // sweeps solve for rounding-level defects), or in all of them with the
 // every-iteration placement.  A column that restarts from zero also takes its
 // accumulated velocity back to the start, kept in net_wacc0.
-static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, int cols, double* vel, double* pres,
-                         int add) {
+static int inner_solve32(Plan* P, Exec& X, const double* f, const float* ru, const float* rd, int cols, double* vel,
+                         double* pres, int add) {
   const GridDev& g = P->g;
   Launcher<float> L{P->t32, X.s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
   const long long sz = g.size, np = g.np;
   float* w = P->w32;
   const bool net = P->net != nullptr && (P->net_every || add == 0);
   float* wacc = P->wacc32;
-  velocity_inverse<float>(P, L, SrcPacked<float, double>{ru, sz, g.nu, g.nx - 1, g.nx}, wacc, sz, cols, nullptr);
+  if (f) velocity_inverse<float>(P, L, SrcPacked<float, double>{f, sz, g.nu, g.nx - 1, g.nx}, wacc, sz, cols, nullptr);
+  else velocity_inverse<float>(P, L, SrcPacked<float, float>{ru, sz, g.nu, g.nx - 1, g.nx}, wacc, sz, cols, nullptr);
   if (net) cudaMemcpyAsync(P->net_wacc0, wacc, sizeof(float) * size_t(sz) * cols, cudaMemcpyDeviceToDevice, X.s);
   const double keep = X.ktol;
   const int keep_net = X.net;
@@ -766,19 +782,21 @@ static int inner_solve32(Plan* P, Exec& X, const double* ru, const double* rd, i
 int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel, double* pres, bool close) {
   const GridDev& g = P->g;
   const long long sz = g.size, np = g.np;
-  double* ru = P->w;               // FP64 momentum defect
-  double* rd = P->cells;           // FP64 continuity defect
+  // the defect pairs live in the FP64 work buffers, unused on this path
+  float* ru_hi = reinterpret_cast<float*>(P->w);
+  float* ru_lo = ru_hi + sz * cols;
+  float* rd_hi = reinterpret_cast<float*>(P->cells);
+  float* rd_lo = rd_hi + np * cols;
   const int nbm = red_blocks(sz > np ? sz : np);
   for (int sweep = 0; sweep <= P->corrections; ++sweep) {
-    const double* rhs_u = f;
-    const double* rhs_d = nullptr;
     if (sweep > 0) {
-      launch_k(k_defect_df, dim3(nbm, cols), kThreads, 0, X.s, g, f, vel, pres, P->shift, ru, rd);
+      launch_k(k_defect_update, dim3(nbm, cols), kThreads, 0, X.s, g, sweep == 1 ? f : nullptr,
+               static_cast<const float*>(P->wacc32), static_cast<const float*>(P->cells32 + np * cols), P->shift,
+               ru_hi, ru_lo, rd_hi, rd_lo);
       ++P->launches;
-      rhs_u = ru;
-      rhs_d = rd;
     }
-    int rc = inner_solve32(P, X, rhs_u, rhs_d, cols, vel, pres, sweep > 0);
+    int rc = inner_solve32(P, X, sweep == 0 ? f : nullptr, ru_hi, sweep == 0 ? nullptr : rd_hi, cols, vel, pres,
+                           sweep > 0);
     if (rc != MACSAV_OK) return rc;
   }
   // mean-zero pressure and the FP64 closing checks, as in the FP64 path
