@@ -4,6 +4,7 @@
 // in shared memory and each thread accumulates 16 output channels of one
 // pixel.  The data gradient is the same kernel on the flipped, transposed
 // weights; the weight gradient reduces tile products and adds them atomically.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <vector>
@@ -36,6 +37,7 @@ struct ConvArgs {
   float* gb;                // backward: input gradient of channels [ca, ca+cb)
   const float* out_scale;   // forward: per-sample output factor (or null)
   int relu, B, H, W;
+  int tc_group;             // k_conv3_tc: input-channel chunks staged together (shared memory per group)
 };
 
 // FWD: out[o](p) = sum_i sum_k w[o][i][k] x[i](p + d_k)
@@ -129,9 +131,13 @@ __global__ void __launch_bounds__(256) k_conv(ConvArgs q) {
 // starting at halo pixel (dy, dx): 8 consecutive pixels of a tile row form a
 // core matrix (16 B rows), SBO = 10 pixels * 16 B = 160 B steps one tile row,
 // LBO = 180 pixels * 16 B = 2880 B steps to the next 8 channels.  B_t is
-// staged as [tap][co/8][2][8 rows x 16 B] (SBO 256 B, LBO 128 B).  One elected
-// thread issues the nine MMAs and commits them to an mbarrier; all threads
-// wait (bounded) before the tiles are reused.  The epilogue reads accumulator
+// staged as [tap][co/8][2][8 rows x 16 B] (SBO 256 B, LBO 128 B).  The chunks
+// are staged in groups (as many as the opt-in shared memory holds, all of
+// this network's layers in one group): every load of a group is in flight
+// together, then one elected thread issues the group's 9 x chunks MMAs and
+// commits them to one mbarrier, and all threads wait (bounded) before the
+// tiles are reused, so a deep layer pays one load latency and one wait
+// instead of one per chunk.  The epilogue reads accumulator
 // rows with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = tile pixels),
 // applies ReLU and stores BF16.  On a wait that runs out the kernel sets
 // *err, waits (bounded) once more, frees its tensor memory and returns.
@@ -142,8 +148,6 @@ constexpr uint32_t kTcALBO = kTcHalo * 16;        // 2880: next 8 channels
 constexpr uint32_t kTcASBO = kTcHx * 16;          // 160: next tile row
 constexpr uint32_t kTcBLBO = 128, kTcBSBO = 256;  // B: next 8 channels / next 8 rows
 constexpr size_t kTcSmemHalo = size_t(2) * kTcHalo * 16;  // 5760
-constexpr size_t kTcSmemB = size_t(9) * 8 * kTcBSBO;      // 18432 (co <= 64)
-constexpr size_t kTcSmem = kTcSmemHalo + kTcSmemB;
 constexpr long long kTcSpin = 1LL << 22;          // mbarrier poll limit
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -173,8 +177,6 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
 
 __global__ void __launch_bounds__(128, 5) k_conv3_tc(ConvArgs q, int* err) {
   extern __shared__ __align__(1024) unsigned char tcsm[];
-  __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(tcsm);
-  unsigned char* Bs = tcsm + kTcSmemHalo;
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ uint32_t tmem_slot;
   __shared__ int failed;
@@ -203,60 +205,72 @@ __global__ void __launch_bounds__(128, 5) k_conv3_tc(ConvArgs q, int* err) {
   const uint32_t mb = smem_u32(&mbar);
   // instruction descriptor: FP32 accumulator, BF16 A and B, K-major, M=128, N
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(128 >> 4) << 24);
-  const uint32_t halo_s = smem_u32(halo), b_s = smem_u32(Bs);
   const uint32_t btap = uint32_t(N >> 3) * kTcBSBO;  // bytes of one tap's B tile
+  // the chunks of a group are all staged (every load of the group in flight
+  // at once), then all their MMAs issued under one commit and one wait
+  const int per_chunk = int(kTcSmemHalo) + 9 * int(btap);
+  const int group = q.tc_group;
   uint32_t phase = 0;
   const __nv_bfloat16 zero = __float2bfloat16_rn(0.f);
-  for (int ch = 0; ch < nchunks; ++ch) {
-    const int ci0 = ch * kTcC;
-    // halo [c/8][pixel][c%8] of the chunk's channels (zero outside the image /
-    // cin), in two halves whose loads are all issued before their stores
-    constexpr int kHaloPer = (kTcC * kTcHalo + 127) / 128, kHalf = (kHaloPer + 1) / 2;
-#pragma unroll
-    for (int h0 = 0; h0 < kHaloPer; h0 += kHalf) {
-      __nv_bfloat16 hv[kHalf];
-#pragma unroll
-      for (int k = 0; k < kHalf; ++k) {
-        const int e = tid + (h0 + k) * 128;
-        const int c = e / kTcHalo, pix = e - c * kTcHalo, hy = pix / kTcHx, hx = pix - hy * kTcHx;
-        const int ci = ci0 + c, gy = y0 + hy - 1, gx = x0 + hx - 1;
-        hv[k] = zero;
-        if (h0 + k < kHaloPer && e < kTcC * kTcHalo && ci < cin && gy >= 0 && gy < H && gx >= 0 && gx < W) {
-          const long long off = (long long)gy * W + gx;
-          hv[k] = ci < q.ca ? __ldg(q.xa + ((long long)b * q.ca + ci) * HW + off)
-                            : __ldg(q.xb + ((long long)b * q.cb + (ci - q.ca)) * HW + off);
+  for (int g0 = 0; g0 < nchunks; g0 += group) {
+    const int gn = min(group, nchunks - g0);
+    for (int cc = 0; cc < gn; ++cc) {
+      const int ch = g0 + cc;
+      const int ci0 = ch * kTcC;
+      __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(tcsm + cc * per_chunk);
+      unsigned char* Bs = tcsm + cc * per_chunk + kTcSmemHalo;
+      // halo [c/8][pixel][c%8] of the chunk's channels (zero outside the image /
+      // cin), in two halves whose loads are all issued before their stores
+      constexpr int kHaloPer = (kTcC * kTcHalo + 127) / 128, kHalf = (kHaloPer + 1) / 2;
+  #pragma unroll
+      for (int h0 = 0; h0 < kHaloPer; h0 += kHalf) {
+        __nv_bfloat16 hv[kHalf];
+  #pragma unroll
+        for (int k = 0; k < kHalf; ++k) {
+          const int e = tid + (h0 + k) * 128;
+          const int c = e / kTcHalo, pix = e - c * kTcHalo, hy = pix / kTcHx, hx = pix - hy * kTcHx;
+          const int ci = ci0 + c, gy = y0 + hy - 1, gx = x0 + hx - 1;
+          hv[k] = zero;
+          if (h0 + k < kHaloPer && e < kTcC * kTcHalo && ci < cin && gy >= 0 && gy < H && gx >= 0 && gx < W) {
+            const long long off = (long long)gy * W + gx;
+            hv[k] = ci < q.ca ? __ldg(q.xa + ((long long)b * q.ca + ci) * HW + off)
+                              : __ldg(q.xb + ((long long)b * q.cb + (ci - q.ca)) * HW + off);
+          }
+        }
+  #pragma unroll
+        for (int k = 0; k < kHalf; ++k) {
+          const int e = tid + (h0 + k) * 128;
+          if (h0 + k < kHaloPer && e < kTcC * kTcHalo) {
+            const int c = e / kTcHalo, pix = e - c * kTcHalo;
+            halo[((c >> 3) * kTcHalo + pix) * 8 + (c & 7)] = hv[k];
+          }
         }
       }
-#pragma unroll
-      for (int k = 0; k < kHalf; ++k) {
-        const int e = tid + (h0 + k) * 128;
-        if (h0 + k < kHaloPer && e < kTcC * kTcHalo) {
-          const int c = e / kTcHalo, pix = e - c * kTcHalo;
-          halo[((c >> 3) * kTcHalo + pix) * 8 + (c & 7)] = hv[k];
-        }
+      // B_t[co][c] = w[co][ci0 + c][t]: the chunk's operand copy, already in
+      // the [tap][co/8][2][8 rows][8 channels] layout, 16 bytes per copy
+      {
+        const uint4* src = reinterpret_cast<const uint4*>(q.wp) + (long long)ch * 9 * N * 2;
+        uint4* dst = reinterpret_cast<uint4*>(Bs);
+        for (int e = tid; e < 9 * N * 2; e += 128) dst[e] = __ldg(src + e);
       }
-    }
-    // B_t[co][c] = w[co][ci0 + c][t]: the chunk's operand copy, already in
-    // the [tap][co/8][2][8 rows][8 channels] layout, 16 bytes per copy
-    {
-      const uint4* src = reinterpret_cast<const uint4*>(q.wp) + (long long)ch * 9 * N * 2;
-      uint4* dst = reinterpret_cast<uint4*>(Bs);
-      for (int e = tid; e < 9 * N * 2; e += 128) dst[e] = __ldg(src + e);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int cc = 0; cc < gn; ++cc) {
+        const uint32_t halo_s = smem_u32(tcsm + cc * per_chunk), b_s = halo_s + uint32_t(kTcSmemHalo);
 #pragma unroll
-      for (int t = 0; t < 9; ++t) {
-        const uint32_t a_start = halo_s + uint32_t((t / 3) * kTcHx + (t % 3)) * 16;
-        const uint64_t ad = tc_desc(a_start, kTcALBO, kTcASBO);
-        const uint64_t bd = tc_desc(b_s + t * btap, kTcBLBO, kTcBSBO);
-        const uint32_t acc = (ch > 0 || t > 0) ? 1u : 0u;
-        asm volatile(
-            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+        for (int t = 0; t < 9; ++t) {
+          const uint32_t a_start = halo_s + uint32_t((t / 3) * kTcHx + (t % 3)) * 16;
+          const uint64_t ad = tc_desc(a_start, kTcALBO, kTcASBO);
+          const uint64_t bd = tc_desc(b_s + t * btap, kTcBLBO, kTcBSBO);
+          const uint32_t acc = (g0 + cc > 0 || t > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+        }
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
                    : "memory");
@@ -549,12 +563,19 @@ void conv_fwd(UNet* N, int li, const __nv_bfloat16* xa, const __nv_bfloat16* xb,
   q.W = W;
   if (N->tensor_cores && L.ks == 3 && yb && L.p_off >= 0) {
     const dim3 tgrid((W + 7) / 8, (H + 15) / 16, B);
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTcSmem));
-      attr = true;
+    // as many input-channel chunks per group as the opt-in shared memory holds
+    static int smem_max = 0;
+    if (!smem_max) {
+      int dev = 0, optin = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      smem_max = optin - 2048;  // room for the kernel's static shared memory
+      cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
     }
-    k_conv3_tc<<<tgrid, 128, kTcSmem, s>>>(q, N->tc_err);
+    const int cin = L.ca + L.cb, nchunks = (cin + kTcC - 1) / kTcC;
+    const int per_chunk = int(kTcSmemHalo) + 9 * (L.co / 8) * int(kTcBSBO);
+    q.tc_group = std::max(1, std::min(nchunks, smem_max / per_chunk));
+    k_conv3_tc<<<tgrid, 128, size_t(q.tc_group) * per_chunk, s>>>(q, N->tc_err);
     ++N->launches;
     return;
   }
