@@ -606,6 +606,21 @@ int macsav_plan_set_refinement(macsav_plan* plan, int corrections, double inner_
   if (!plan) return MACSAV_ERR_VALUE;
   if (corrections < 0 || corrections > 8 || !(inner_krylov_tolerance > 0) || !(inner_krylov_tolerance < 1))
     return fail(&plan->p, MACSAV_ERR_VALUE, "corrections must be in 0..8 and 0 < inner tolerance < 1");
+  Plan* P = &plan->p;
+  if (P->precision == MACSAV_FP32_MIXED && corrections + 1 > P->pieces) {
+    // one velocity and pressure piece per FP32 solve of a Stokes solve
+    cudaDeviceSynchronize();
+    cudaFree(P->wacc32);
+    cudaFree(P->xpieces);
+    P->wacc32 = nullptr;
+    P->xpieces = nullptr;
+    P->pieces = 0;
+    const size_t C = size_t(P->maxcols), n = size_t(corrections + 1);
+    if (cudaMalloc(&P->wacc32, sizeof(float) * P->g.size * C * n) != cudaSuccess ||
+        cudaMalloc(&P->xpieces, sizeof(float) * P->g.np * C * n) != cudaSuccess)
+      return cuda_status(P);
+    P->pieces = corrections + 1;
+  }
   plan->p.corrections = corrections;
   plan->p.inner_ktol = inner_krylov_tolerance;
   for (auto& kv : plan->p.st.graphs) cudaGraphExecDestroy(kv.exec);  // captured with the old sweep count

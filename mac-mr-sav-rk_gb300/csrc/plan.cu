@@ -195,7 +195,9 @@ int plan_build(Plan* p) {
     if (p->precision == MACSAV_FP32_MIXED) {
       if ((e = cudaMalloc(&p->cells32, sizeof(float) * np * C * 6))) goto fail;
       if ((e = cudaMalloc(&p->w32, sizeof(float) * size * C))) goto fail;
-      if ((e = cudaMalloc(&p->wacc32, sizeof(float) * size * C))) goto fail;
+      p->pieces = p->corrections + 1;
+      if ((e = cudaMalloc(&p->wacc32, sizeof(float) * size * C * p->pieces))) goto fail;
+      if ((e = cudaMalloc(&p->xpieces, sizeof(float) * np * C * p->pieces))) goto fail;
     }
     p->partial_len = size_t(C) * 8 * 4096;
     if ((e = cudaMalloc(&p->partial, sizeof(double) * p->partial_len))) goto fail;
@@ -244,6 +246,7 @@ void plan_free(Plan* p) {
   free_transforms(p->t64);
   free_transforms(p->t32);
   cudaFree(p->w); cudaFree(p->cells); cudaFree(p->cells32); cudaFree(p->w32); cudaFree(p->wacc32);
+  cudaFree(p->xpieces);
   cudaFree(p->partial); cudaFree(p->partial2); cudaFree(p->cg); cudaFree(p->checks); cudaFree(p->active); cudaFree(p->shift);
   cudaFree(p->errword);
   cudaFree(p->done_counter);
@@ -263,7 +266,8 @@ void plan_free(Plan* p) {
   if (p->evc) cudaEventDestroy(p->evc);
   p->evc = nullptr;
   p->w = p->cells = p->partial = p->partial2 = p->shift = nullptr;
-  p->cells32 = p->w32 = p->wacc32 = nullptr;
+  p->cells32 = p->w32 = p->wacc32 = p->xpieces = nullptr;
+  p->pieces = 0;
   p->cg = nullptr; p->checks = nullptr; p->active = p->errword = nullptr;
   p->h_cg = nullptr; p->h_checks = nullptr; p->h_active = p->h_err = nullptr;
   p->done = nullptr;

@@ -103,7 +103,12 @@ struct Plan {
   double* cells = nullptr;  // 6 cell-sized vectors per column: b x r z p q
   float* cells32 = nullptr; // float CG vectors (mixed path)
   float* w32 = nullptr;
-  float* wacc32 = nullptr;  // velocity of an FP32 inner solve, accumulated inside its CG (mixed path)
+  // mixed path: the velocity and pressure of each FP32 inner solve of a
+  // Stokes solve (velocity accumulated inside its CG), one piece per sweep,
+  // summed into the FP64 fields once at the end
+  float* wacc32 = nullptr;   // [pieces][maxcols][size]
+  float* xpieces = nullptr;  // [pieces][maxcols][np]
+  int pieces = 0;
   double* partial = nullptr;
   size_t partial_len = 0;
   CGScalars* cg = nullptr;

@@ -588,13 +588,103 @@ static void finish_pressure(Plan* P, const Exec& X, const T* x, double* pres, in
   P->launches += 3;
 }
 
+// Closing checks of an FP32-bulk solve (tensor_stokes.py:329-351, the same
+// key slots as k_stokes_check): the final defect m u + k K u - D^T p - f and
+// divergence D u of the FP64 fields are the defect pairs before the last
+// sweep minus what the last sweep's float solve (u, x) adds, formed as in
+// k_defect_update (double-float, about 48 bits; the fields' FP64 sums of the
+// pieces round at 1e-16 of their size, far below the 1e-9 gates), so the
+// check needs no FP64 arithmetic.  max|f|, max|u| and the finiteness of
+// f, u and p are read from the FP64 arrays themselves.  f_prev: the Stokes
+// right-hand side when the last sweep was the first solve, else null (the
+// pairs hold the defect).
+__global__ void __launch_bounds__(kThreads) k_stokes_check_df(GridDev g, const double* f_prev, const float* u,
+                                                              const float* x, const float* ru_hi, const float* ru_lo,
+                                                              const float* rd_hi, const float* rd_lo,
+                                                              const double* vel, const double* pres, const double* f,
+                                                              const double* shift, double* partial,
+                                                              CGFin<double> fin, unsigned int* done) {
+  pdl_wait();
+  const int c = blockIdx.y;
+  const df32 mass = d2df(shift[2 * c]), visc = d2df(shift[2 * c + 1]);
+  const df32 ihx = d2df(g.ihx), ihy = d2df(g.ihy), ihx2 = d2df(g.ihx2), ihy2 = d2df(g.ihy2);
+  const long long su = c * (long long)g.size, sp = c * (long long)g.np;
+  const float* uc = u + su;
+  const float* xc = x + sp;
+  unsigned long long m[6] = {0, 0, 0, 0, 0, 0};
+  constexpr unsigned long long kInf = 0x7ff0000000000000ull;
+  const int n = g.size > g.np ? g.size : g.np;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (i < g.size) {
+      const float cc = uc[i];
+      float l, r, s, nn;
+      df32 dt;
+      if (i < g.nu) {
+        const int w = g.nx - 1, j = i / w, q = i - j * w;
+        l = q > 0 ? uc[i - 1] : 0.0f;
+        r = q < w - 1 ? uc[i + 1] : 0.0f;
+        s = j > 0 ? uc[i - w] : -cc;
+        nn = j < g.ny - 1 ? uc[i + w] : -cc;
+        const int lc = j * g.nx + q;
+        dt = df_mul(df_two_sum(xc[lc], -xc[lc + 1]), ihx);
+      } else {
+        const int fi = i - g.nu, j = fi / g.nx, q = fi - j * g.nx;
+        l = q > 0 ? uc[i - 1] : -cc;
+        r = q < g.nx - 1 ? uc[i + 1] : -cc;
+        s = j > 0 ? uc[i - g.nx] : 0.0f;
+        nn = j < g.ny - 2 ? uc[i + g.nx] : 0.0f;
+        const int lc = j * g.nx + q;
+        dt = df_mul(df_two_sum(xc[lc], -xc[lc + g.nx]), ihy);
+      }
+      const df32 kx = df_mul(df_add(df_two_sum(cc, -l), df_two_sum(cc, -r)), ihx2);
+      const df32 ky = df_mul(df_add(df_two_sum(cc, -s), df_two_sum(cc, -nn)), ihy2);
+      const df32 op = df_sub(df_add(df_mul(mass, df32{cc, 0.0f}), df_mul(visc, df_add(kx, ky))), dt);
+      const long long k = su + i;
+      const df32 prev = f_prev ? d2df(f_prev[k]) : df32{ru_hi[k], ru_lo[k]};
+      const df32 d = df_sub(prev, op);  // f - (m u + k K u - D^T p)
+      const unsigned long long kf = abs_key(f[k]), ku = abs_key(vel[k]);
+      m[0] = max(m[0], abs_key(f2d_bits(d.hi)));
+      m[1] = max(m[1], kf);
+      m[2] = max(m[2], ku);
+      if (kf >= kInf) m[4] = 1;
+      if (ku >= kInf) m[5] = 1;
+    }
+    if (i < g.np) {
+      const int j = i / g.nx, q = i - j * g.nx;
+      const float ue = q < g.nx - 1 ? uc[j * (g.nx - 1) + q] : 0.0f, uw = q > 0 ? uc[j * (g.nx - 1) + q - 1] : 0.0f;
+      const float vn = j < g.ny - 1 ? uc[g.nu + j * g.nx + q] : 0.0f, vs = j > 0 ? uc[g.nu + (j - 1) * g.nx + q] : 0.0f;
+      const df32 du = df_add(df_mul(df_two_sum(ue, -uw), ihx), df_mul(df_two_sum(vn, -vs), ihy));
+      const long long k = sp + i;
+      const df32 prev = f_prev ? df32{0.0f, 0.0f} : df32{rd_hi[k], rd_lo[k]};  // -D of the earlier pieces
+      m[3] = max(m[3], abs_key(f2d_bits(df_sub(prev, du).hi)));
+      if (abs_key(pres[k]) >= kInf) m[5] = 1;
+    }
+  }
+  write_keys<6>(m, partial, 6, 0);
+  last_block_finish(fin, done);
+}
+
 static void closing_checks(Plan* P, const Exec& X, const double* f, const double* vel, const double* pres, int cols,
                            const double* shift) {
-  const long long n = P->g.size > P->g.np ? P->g.size : P->g.np;
+  const GridDev& g = P->g;
+  const long long n = g.size > g.np ? g.size : g.np;
   const int rb = red_blocks(n);
-  launch_k(k_stokes_check, dim3(rb, cols), kThreads, 0, X.s, P->g, vel, pres, f, P->g.size, P->g.np, shift,
-           X.partial ? X.partial : P->partial, make_fin<double>(P, X, OP_CHECKS, rb, 6, cols),
-           X.counter ? X.counter : P->done_counter);
+  double* part = X.partial ? X.partial : P->partial;
+  unsigned int* done = X.counter ? X.counter : P->done_counter;
+  if (P->precision == MACSAV_FP32_MIXED) {
+    // from the defect pairs and the last sweep's pieces (enqueue_solve_mixed)
+    const int last = P->corrections;
+    const long long sz = g.size, np = g.np;
+    const float* ru_hi = reinterpret_cast<const float*>(P->w);
+    const float* rd_hi = reinterpret_cast<const float*>(P->cells);
+    launch_k(k_stokes_check_df, dim3(rb, cols), kThreads, 0, X.s, g, last == 0 ? f : nullptr,
+             static_cast<const float*>(P->wacc32 + last * sz * cols),
+             static_cast<const float*>(P->xpieces + last * np * cols), ru_hi, ru_hi + sz * cols, rd_hi,
+             rd_hi + np * cols, vel, pres, f, shift, part, make_fin<double>(P, X, OP_CHECKS, rb, 6, cols), done);
+  } else {
+    launch_k(k_stokes_check, dim3(rb, cols), kThreads, 0, X.s, g, vel, pres, f, g.size, g.np, shift, part,
+             make_fin<double>(P, X, OP_CHECKS, rb, 6, cols), done);
+  }
   ++P->launches;
 }
 
@@ -714,27 +804,32 @@ __global__ void __launch_bounds__(kThreads) k_defect_update(GridDev g, const dou
   }
 }
 
-// vel (+)= double(u) over sz and pres (+)= double(x) over np elements per
-// column: the closing accumulation of an FP32 inner solve.
-__global__ void __launch_bounds__(kThreads) k_accumulate_sweep(const float* u, double* vel, long long sz, const float* x,
-                                                               double* pres, long long np, int add) {
+// vel = sum of the pieces' double(u) and pres = sum of double(x), in sweep
+// order (FP64 adds, the same rounding as adding each sweep's piece to the
+// FP64 fields as it comes): the closing accumulation of an FP32-bulk solve.
+__global__ void __launch_bounds__(kThreads) k_sum_pieces(const float* u, double* vel, long long sz, const float* x,
+                                                         double* pres, long long np, int cols, int pieces) {
   pdl_wait();
   const int c = blockIdx.y;
   const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long us = sz * cols, xs = np * cols;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < sz; i += stride) {
     const long long k = c * sz + i;
-    vel[k] = add ? vel[k] + double(u[k]) : double(u[k]);
+    double v = f2d_bits(u[k]);
+    for (int q = 1; q < pieces; ++q) v += f2d_bits(u[q * us + k]);
+    vel[k] = v;
   }
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += stride) {
     const long long k = c * np + i;
-    pres[k] = add ? pres[k] + double(x[k]) : double(x[k]);
+    double v = f2d_bits(x[k]);
+    for (int q = 1; q < pieces; ++q) v += f2d_bits(x[q * xs + k]);
+    pres[k] = v;
   }
 }
 
 // One FP32 Stokes solve of (f, 0) or of the defect (ru, rd): transforms,
-// stencils and Krylov vectors
-// in float, reductions in double.  Its velocity and pressure are added to
-// the FP64 `vel` and `pres` (set when add = 0).
+// stencils and Krylov vectors in float, reductions in double.  Its velocity
+// and pressure become the sweep's pieces (wacc32 and xpieces slot `sweep`).
 //
 // Plain PCG: the velocity is accumulated inside the CG, u = (mI+kK)^{-1} ru
 // + sum_k alpha_k (mI+kK)^{-1} D^T pdir_k, from the velocity each iteration
@@ -748,30 +843,26 @@ __global__ void __launch_bounds__(kThreads) k_accumulate_sweep(const float* u, d
 // sweeps solve for rounding-level defects), or in all of them with the
 // every-iteration placement.  A column that restarts from zero also takes its
 // accumulated velocity back to the start, kept in net_wacc0.
-static int inner_solve32(Plan* P, Exec& X, const double* f, const float* ru, const float* rd, int cols, double* vel,
-                         double* pres, int add) {
+static int inner_solve32(Plan* P, Exec& X, const double* f, const float* ru, const float* rd, int cols, int sweep) {
   const GridDev& g = P->g;
   Launcher<float> L{P->t32, X.s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
   const long long sz = g.size, np = g.np;
   float* w = P->w32;
-  const bool net = P->net != nullptr && (P->net_every || add == 0);
-  float* wacc = P->wacc32;
+  const bool net = P->net != nullptr && (P->net_every || sweep == 0);
+  float* wacc = P->wacc32 + sweep * sz * cols;
   if (f) velocity_inverse<float>(P, L, SrcPacked<float, double>{f, sz, g.nu, g.nx - 1, g.nx}, wacc, sz, cols, nullptr);
   else velocity_inverse<float>(P, L, SrcPacked<float, float>{ru, sz, g.nu, g.nx - 1, g.nx}, wacc, sz, cols, nullptr);
   if (net) cudaMemcpyAsync(P->net_wacc0, wacc, sizeof(float) * size_t(sz) * cols, cudaMemcpyDeviceToDevice, X.s);
   const double keep = X.ktol;
   const int keep_net = X.net;
-  X.ktol = (add == 0 && P->first_ktol > 0.0) ? P->first_ktol : P->inner_ktol;
+  X.ktol = (sweep == 0 && P->first_ktol > 0.0) ? P->first_ktol : P->inner_ktol;
   X.net = net ? 1 : 0;
   int rc = schur_pcg<float>(P, X, L, w, P->cells32, cols, rd, wacc);
   X.ktol = keep;
   X.net = keep_net;
   if (rc != MACSAV_OK) return rc;
   const float* x = P->cells32 + 1 * np * cols;
-  const int nb = red_blocks(sz);
-  launch_k(k_accumulate_sweep, dim3(nb, cols), kThreads, 0, X.s, static_cast<const float*>(wacc), vel, sz, x, pres, np,
-           add);
-  ++P->launches;
+  cudaMemcpyAsync(P->xpieces + sweep * np * cols, x, sizeof(float) * size_t(np) * cols, cudaMemcpyDeviceToDevice, X.s);
   return MACSAV_OK;
 }
 
@@ -791,14 +882,16 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
   for (int sweep = 0; sweep <= P->corrections; ++sweep) {
     if (sweep > 0) {
       launch_k(k_defect_update, dim3(nbm, cols), kThreads, 0, X.s, g, sweep == 1 ? f : nullptr,
-               static_cast<const float*>(P->wacc32), static_cast<const float*>(P->cells32 + np * cols), P->shift,
-               ru_hi, ru_lo, rd_hi, rd_lo);
+               static_cast<const float*>(P->wacc32 + (sweep - 1) * sz * cols),
+               static_cast<const float*>(P->xpieces + (sweep - 1) * np * cols), P->shift, ru_hi, ru_lo, rd_hi, rd_lo);
       ++P->launches;
     }
-    int rc = inner_solve32(P, X, sweep == 0 ? f : nullptr, ru_hi, sweep == 0 ? nullptr : rd_hi, cols, vel, pres,
-                           sweep > 0);
+    int rc = inner_solve32(P, X, sweep == 0 ? f : nullptr, ru_hi, sweep == 0 ? nullptr : rd_hi, cols, sweep);
     if (rc != MACSAV_OK) return rc;
   }
+  launch_k(k_sum_pieces, dim3(nbm, cols), kThreads, 0, X.s, static_cast<const float*>(P->wacc32), vel, sz,
+           static_cast<const float*>(P->xpieces), pres, np, cols, P->corrections + 1);
+  ++P->launches;
   // mean-zero pressure and the FP64 closing checks, as in the FP64 path
   if (close) {
     finish_pressure<double>(P, X, pres, pres, cols);
