@@ -443,8 +443,13 @@ static void cg_iteration(Plan* P, const Exec& X, const Launcher<T>& L, T* w, T* 
       }
       launch_k(k_fcg_z, dim3(rb, cols), kThreads, 0, s, g.np, z, add, r, r_old, np, P->cg, P->active, P->partial,
                                                   make_fin<float>(P, X, OP_FCG, rb, 5, cols), P->done_counter);
-      launch_k(k_fcg_center, dim3(rb, cols), kThreads, 0, s, g.np, z, np, P->cg, P->active);
-      P->launches += 2;
+      ++P->launches;
+      // the network's output is projected to mean zero; M r alone already is
+      // (the preconditioner's Poisson inverse drops the zero mode), as in plain PCG
+      if (eval_net) {
+        launch_k(k_fcg_center, dim3(rb, cols), kThreads, 0, s, g.np, z, np, P->cg, P->active);
+        ++P->launches;
+      }
     }
   }
   // q = S pdir = D (mI+kK)^{-1} D^T pdir,  pdir = z + beta p
