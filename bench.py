@@ -849,7 +849,8 @@ def profile_tgemm() -> None:
 
 def profile_pass(workload: str, pass_id: int) -> None:
     """Three launches of one transform pass (macsav_time_pass: 0 the FP32
-    velocity column pass, 3 the FP64 one) on the workload's grid, after one
+    velocity column pass, 1 and 2 the FP32 velocity row forward and inverse
+    passes, 3 the FP64 column pass) on the workload's grid, after one
     warm-up launch, for a DRAM-traffic capture of that kernel."""
     import torch
     import __graft_entry__
@@ -941,8 +942,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["learned1024", "cavity512", "ensemble256", "adaptive2048", "channel512"],
                     default="learned1024")
-    ap.add_argument("--profile", choices=["fp32", "fp64", "learned", "unet", "pass0", "pass3", "transform32",
-                                          "tgemm"],
+    ap.add_argument("--profile", choices=["fp32", "fp64", "learned", "unet", "pass0", "pass1", "pass2", "pass3",
+                                          "transform32", "tgemm"],
                     default=None,
                     help="run two eager steps of the workload (or launches of one transform pass) and exit, "
                          "for ncu captures")
@@ -959,7 +960,7 @@ def main() -> None:
     if args.profile == "tgemm":
         profile_tgemm()
         return
-    if args.profile in ("pass0", "pass3"):
+    if args.profile in ("pass0", "pass1", "pass2", "pass3"):
         profile_pass(args.workload, int(args.profile[-1]))
         return
     if args.profile:

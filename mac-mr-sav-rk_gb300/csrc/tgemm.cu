@@ -119,18 +119,11 @@ __global__ void __launch_bounds__(128) k_tgemm(const float* __restrict__ in, flo
     __nv_bfloat16* A = sm + buf * stage_elems;
     __nv_bfloat16* Bs = A + S * a_elems;
     const int k = c * kTgK + lane;
-    // A: each warp stages 32 rows, lanes along k (coalesced); all 32 loads
-    // are issued before the pieces are formed and stored
-    float xv[32];
-#pragma unroll
+    // A: each warp stages 32 rows, one row per step, lanes along k (coalesced)
     for (int rr = 0; rr < 32; ++rr) {
-      const int r = row0 + warp * 32 + rr;
-      xv[rr] = (r < rows && k < n) ? __ldg(in + (long long)r * n + k) : 0.0f;
-    }
-#pragma unroll
-    for (int rr = 0; rr < 32; ++rr) {
-      float x = xv[rr];
-      const int o = tg_off(warp * 32 + rr, lane, kTgM / 8);
+      const int row = warp * 32 + rr, r = row0 + row;
+      float x = (r < rows && k < n) ? __ldg(in + (long long)r * n + k) : 0.0f;
+      const int o = tg_off(row, lane, kTgM / 8);
 #pragma unroll
       for (int p = 0; p < S; ++p) {
         const __nv_bfloat16 h = __float2bfloat16_rn(x);
