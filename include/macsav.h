@@ -125,6 +125,20 @@ int macsav_transform32_autotune(macsav_plan* plan, int kind, int inverse, int ro
 int macsav_stokes_solve(macsav_plan* plan, const double* rhs, int columns, double mass, double viscosity,
                         double* velocity, double* pressure, macsav_stokes_info* info, void* stream);
 
+/* The two spectral operators of the Stokes solve, applied on their own in the
+ * plan's precision (FP32 transforms for MACSAV_FP32_MIXED plans, inputs and
+ * outputs FP64 either way); `columns` columns, at most the plan's maximum.
+ * macsav_velocity_inverse: out = (mass I + viscosity K)^{-1} values, packed
+ * velocities (TensorStokes._velocity_inverse, solver/mac/tensor_stokes.py:200-215).
+ * macsav_schur_precondition: out = mass (D D^T)^+ p + viscosity p on the
+ * mean-zero part of the cell columns p, mean zero (the preconditioner of the
+ * pressure Schur CG, tensor_stokes.py:217-243,281-287).
+ * Both return MACSAV_ERR_VALUE for invalid shifts or column counts. */
+int macsav_velocity_inverse(macsav_plan* plan, const double* values, double* out, int columns, double mass,
+                            double viscosity, void* stream);
+int macsav_schur_precondition(macsav_plan* plan, const double* pressure, double* out, int columns, double mass,
+                              double viscosity, void* stream);
+
 /* out = sum_k coeffs[k] * fields[k] accumulated in the order given
  * (MACNavierStokes.combine, solver/mac_ns.py:40-45).  coeffs is a HOST array,
  * fields a HOST array of device pointers, n elements each. */

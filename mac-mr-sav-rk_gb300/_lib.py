@@ -53,6 +53,8 @@ _SIGNATURES = {
     "macsav_convection": (_I, [_P, _P, _P, _I, _P]),
     "macsav_transform": (_I, [_P, _I, _I, _I, _I, _P, _P, _P]),
     "macsav_stokes_solve": (_I, [_P, _P, _I, _D, _D, _P, _P, C.POINTER(StokesInfo), _P]),
+    "macsav_velocity_inverse": (_I, [_P, _P, _P, _I, _D, _D, _P]),
+    "macsav_schur_precondition": (_I, [_P, _P, _P, _I, _D, _D, _P]),
     "macsav_combine": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_P), _P, _LL, _P]),
     "macsav_inner": (_I, [_P, _P, _P, _LL, C.POINTER(_D), _P]),
     "macsav_max_abs": (_I, [_P, _P, _LL, C.POINTER(_D), _P]),

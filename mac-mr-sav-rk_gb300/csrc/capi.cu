@@ -30,6 +30,8 @@ int op_diagnostics(Plan* P, const double* x, double r, double nu, const double* 
                    cudaStream_t s);
 int op_transform(Plan* P, int kind, int inverse, int rows, int n, const double* in, double* out, cudaStream_t s);
 int time_pass(Plan* P, int pass, int reps, cudaStream_t s, double* ms, double* bytes);
+int op_velocity_inverse(Plan* P, const double* in, double* out, int cols, cudaStream_t s);
+int op_schur_precondition(Plan* P, const double* in, double* out, int cols, cudaStream_t s);
 int op_transform32(Plan* P, int kind, int inverse, int rows, int n, int method, const float* in, float* out,
                    cudaStream_t s);
 int op_transform32_autotune(Plan* P, int kind, int inverse, int rows, int n, int* method, double* ms_fft,
@@ -164,6 +166,37 @@ int macsav_transform(macsav_plan* plan, int kind, int inverse, int rows, int n, 
                      void* stream) {
   if (!plan || !in || !out) return MACSAV_ERR_VALUE;
   return macsav::op_transform(&plan->p, kind, inverse, rows, n, in, out, static_cast<cudaStream_t>(stream));
+}
+
+static int spectral_op(macsav_plan* plan, int which, const double* in, double* out, int columns, double mass,
+                       double viscosity, void* stream) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // tensor_stokes.py:246-251
+  if (!std::isfinite(mass) || !std::isfinite(viscosity) || std::fmin(mass, viscosity) < 0 || mass + viscosity <= 0)
+    return fail(P, MACSAV_ERR_VALUE, "Require mass,viscosity >= 0 and nonzero total");
+  if (!in || !out || columns < 1 || columns > P->maxcols || columns > MACSAV_MAX_COLUMNS)
+    return fail(P, MACSAV_ERR_VALUE, "columns must be in 1..the plan's maximum");
+  double shift[2 * MACSAV_MAX_COLUMNS];
+  for (int c = 0; c < columns; ++c) {
+    shift[2 * c] = mass;
+    shift[2 * c + 1] = viscosity;
+  }
+  cudaMemcpyAsync(P->shift, shift, sizeof(double) * 2 * columns, cudaMemcpyHostToDevice, s);
+  const int rc = which == 0 ? macsav::op_velocity_inverse(P, in, out, columns, s)
+                            : macsav::op_schur_precondition(P, in, out, columns, s);
+  return rc == MACSAV_OK ? cuda_status(P) : rc;
+}
+
+int macsav_velocity_inverse(macsav_plan* plan, const double* values, double* out, int columns, double mass,
+                            double viscosity, void* stream) {
+  return spectral_op(plan, 0, values, out, columns, mass, viscosity, stream);
+}
+
+int macsav_schur_precondition(macsav_plan* plan, const double* pressure, double* out, int columns, double mass,
+                              double viscosity, void* stream) {
+  return spectral_op(plan, 1, pressure, out, columns, mass, viscosity, stream);
 }
 
 int macsav_stokes_solve(macsav_plan* plan, const double* rhs, int columns, double mass, double viscosity,

@@ -969,6 +969,39 @@ int time_pass(Plan* P, int pass, int reps, cudaStream_t user, double* ms, double
   return e == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
 }
 
+// (m I + k K)^{-1} of `cols` packed velocity columns in the plan's precision
+// (TensorStokes._velocity_inverse, solver/mac/tensor_stokes.py:200-215).
+int op_velocity_inverse(Plan* P, const double* in, double* out, int cols, cudaStream_t s) {
+  const GridDev& g = P->g;
+  if (P->precision == MACSAV_FP64) {
+    const Launcher<double> L{P->t64, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
+    velocity_inverse(P, L, SrcPacked<double, double>{in, g.size, g.nu, g.nx - 1, g.nx}, out, g.size, cols, nullptr);
+  } else {
+    const Launcher<float> L{P->t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
+    velocity_inverse(P, L, SrcPacked<float, double>{in, g.size, g.nu, g.nx - 1, g.nx}, out, g.size, cols, nullptr);
+  }
+  return MACSAV_OK;
+}
+
+// m (D D^T)^+ p + k p on the mean-zero part of `cols` cell columns, mean
+// zero out (the pressure Schur preconditioner, tensor_stokes.py:217-243,281-287).
+int op_schur_precondition(Plan* P, const double* in, double* out, int cols, cudaStream_t s) {
+  const GridDev& g = P->g;
+  const long long np = g.np;
+  if (P->precision == MACSAV_FP64) {
+    const Launcher<double> L{P->t64, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
+    L.row_forward_p(SrcCells<double, double>{in, np, g.nx}, cols, nullptr);
+    L.column_p(cols, nullptr, P->shift, P->pthr);
+    L.row_inverse_p(DstCells<double, double>{out, np, g.nx}, cols, nullptr, nullptr, NoFin{}, nullptr);
+  } else {
+    const Launcher<float> L{P->t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
+    L.row_forward_p(SrcCells<float, double>{in, np, g.nx}, cols, nullptr);
+    L.column_p(cols, nullptr, P->shift, float(P->pthr));
+    L.row_inverse_p(DstCells<float, double>{out, np, g.nx}, cols, nullptr, nullptr, NoFin{}, nullptr);
+  }
+  return MACSAV_OK;
+}
+
 int solve_mixed(Plan* P, const double* f, int cols, double mass, double visc, double* vel, double* pres,
                 cudaStream_t s, int* sweeps) {
   (void)mass;

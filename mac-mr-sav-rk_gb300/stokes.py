@@ -164,6 +164,29 @@ class TensorStokes:
         self.plan.check(code)
         return velocity, pressure, info
 
+    def _spectral(self, which: int, values, size: int, mass: float, viscosity: float):
+        f, two_d, is_torch = _as_device_columns(values, size)
+        if f.shape[0] > self.plan.max_columns:
+            raise ValueError(f"at most {self.plan.max_columns} columns per call")
+        out = torch.empty_like(f)
+        fn = self.plan.lib.macsav_velocity_inverse if which == 0 else self.plan.lib.macsav_schur_precondition
+        self.plan.check(fn(self.plan.handle, dptr(f), dptr(out), f.shape[0], float(mass), float(viscosity),
+                           stream_handle()))
+        res = out.T if two_d else out[0]
+        return res if is_torch else res.cpu().numpy().copy()
+
+    def velocity_inverse(self, values, mass: float, viscosity: float):
+        """(mass I + viscosity K)^{-1} of packed velocity columns in the
+        solver's precision (``TensorStokes._velocity_inverse`` with the shifts
+        mass + viscosity * eigenvalues, tensor_stokes.py:200-215)."""
+        return self._spectral(0, values, self.grid.size, mass, viscosity)
+
+    def precondition(self, pressure, mass: float, viscosity: float):
+        """The pressure Schur CG preconditioner mass (D D^T)^+ p + viscosity p
+        on the mean-zero part of cell columns, mean zero (the ``precondition``
+        closure of ``TensorStokes.solve``, tensor_stokes.py:217-243,281-287)."""
+        return self._spectral(1, pressure, self.grid.np, mass, viscosity)
+
     def solve(self, rhs, *, mass: float, viscosity: float) -> StokesResult:
         """``TensorStokes.solve`` (tensor_stokes.py:245-364)."""
         if not np.isfinite([mass, viscosity]).all() or min(mass, viscosity) < 0 or mass + viscosity <= 0:
