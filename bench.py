@@ -610,7 +610,7 @@ def run_headline(args) -> None:
     pkg = __graft_entry__.load_package()
     from importlib import import_module
     lib = import_module(pkg.__name__ + "._lib")
-    w = HEADLINE
+    w = dict(HEADLINE, restriction=args.restriction) if args.restriction else HEADLINE
     g = pkg.MACGrid(w["nx"], w["ny"], w["lx"], w["ly"])
     dev = torch.device("cuda", local)
     x0_host = pkg.fields.packed_curl_velocity(w["nx"], w["ny"], w["lx"], w["ly"], w["psi_modes"], w["seed"])
@@ -940,6 +940,9 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--restriction", type=int, choices=[2, 4, 8], default=None,
+                    help="headline: the learned preconditioner's restriction factor (the network sees "
+                         "(nx/f) x (ny/f) cell means); default the workload's own")
     ap.add_argument("--workload", choices=["learned1024", "cavity512", "ensemble256", "adaptive2048", "channel512"],
                     default="learned1024")
     ap.add_argument("--profile", choices=["fp32", "fp64", "learned", "unet", "pass0", "pass1", "pass2", "pass3",

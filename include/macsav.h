@@ -303,7 +303,7 @@ int macsav_plan_set_preconditioner(macsav_plan* plan, macsav_unet* net, int lear
  * each Stokes solve, i.e. it shapes the first search direction of the solve
  * of the stage's own right-hand side, and the remaining iterations are
  * flexible CG with the spectral preconditioner; 1: in every iteration of
- * every inner solve.  restriction f = 1, 2 or 4: the network sees the residual
+ * every inner solve.  restriction f = 1, 2, 4 or 8: the network sees the residual
  * averaged over f x f cells (nx / f, ny / f multiples of 8) and its output is
  * prolonged bilinearly to the cells, which makes one evaluation f^2 times
  * cheaper.  No reference counterpart (see macsav_unet above). */

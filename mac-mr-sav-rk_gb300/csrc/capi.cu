@@ -559,8 +559,8 @@ int macsav_plan_set_preconditioner(macsav_plan* plan, macsav_unet* net, int lear
 int macsav_plan_set_learned_placement(macsav_plan* plan, int every_iteration, int restriction) {
   if (!plan) return MACSAV_ERR_VALUE;
   Plan* P = &plan->p;
-  if (restriction != 1 && restriction != 2 && restriction != 4)
-    return fail(P, MACSAV_ERR_VALUE, "restriction must be 1, 2 or 4");
+  if (restriction != 1 && restriction != 2 && restriction != 4 && restriction != 8)
+    return fail(P, MACSAV_ERR_VALUE, "restriction must be 1, 2, 4 or 8");
   cudaDeviceSynchronize();
   for (auto& kv : P->st.graphs) cudaGraphExecDestroy(kv.exec);  // captured with the old placement
   P->st.graphs.clear();

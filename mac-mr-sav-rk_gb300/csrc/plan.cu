@@ -94,25 +94,12 @@ static cudaError_t build_block(TBlockDev<T>& B, int rows, int cols, int kx, int 
   for (int k = 0; k < rows; ++k) qy[k] = mk(T(std::cos(kPi * k / (2.0 * rows))), T(-std::sin(kPi * k / (2.0 * rows))));
   std::vector<double> ex = internal_eigenvalues(kx, cols, hx), ey = internal_eigenvalues(ky, rows, hy);
   std::vector<T> exT(ex.begin(), ex.end()), eyT(ey.begin(), ey.end());
-  // warp-line passes (FP32 lines of 512 or 1024 FFT points; DST-I lines of
-  // N points take an FFT of N + 1)
-  auto warp_table = [](int kind, int n, int& wl, std::vector<cplx<T>>& tw) {
-    const int Lw = kind == KIND_DST1 ? n + 1 : n;
-    wl = (sizeof(T) == 4 && warp_line_length(Lw)) ? Lw : 0;
-    tw.resize(wl);
-    for (int k2 = 0; k2 < wl / 32; ++k2)
-      for (int l = 0; l < 32; ++l)
-        tw[32 * k2 + l] = mk(T(std::cos(2 * kPi * l * k2 / Lw)), T(-std::sin(2 * kPi * l * k2 / Lw)));
-  };
-  std::vector<cplx<T>> twcx, twcy;
-  warp_table(kx, cols, B.wlx, twcx);
-  warp_table(ky, rows, B.wly, twcy);
   // every table starts on a 16-byte boundary (the kernels read the complex
-  // tables as 8- or 16-byte vectors)
+  // tables as 8- or 16-byte vectors, and an FP32 eigenvalue table of odd
+  // length would leave a following table 4 bytes off)
   auto up16 = [](size_t n) { return (n + 15) / 16 * 16; };
   const size_t bytes = up16(sizeof(cplx<T>) * Lx) + up16(sizeof(cplx<T>) * Ly) + up16(sizeof(cplx<T>) * cols) +
-                       up16(sizeof(cplx<T>) * rows) + up16(sizeof(T) * cols) + up16(sizeof(T) * rows) +
-                       up16(sizeof(cplx<T>) * B.wlx) + up16(sizeof(cplx<T>) * B.wly);
+                       up16(sizeof(cplx<T>) * rows) + up16(sizeof(T) * cols) + up16(sizeof(T) * rows);
   void* d = nullptr;
   cudaError_t e = cudaMalloc(&d, bytes);
   if (e != cudaSuccess) return e;
@@ -130,8 +117,6 @@ static cudaError_t build_block(TBlockDev<T>& B, int rows, int cols, int kx, int 
   B.qy = static_cast<const cplx<T>*>(put(qy.data(), sizeof(cplx<T>) * rows));
   B.eigx = static_cast<const T*>(put(exT.data(), sizeof(T) * cols));
   B.eigy = static_cast<const T*>(put(eyT.data(), sizeof(T) * rows));
-  B.twcx = B.wlx ? static_cast<const cplx<T>*>(put(twcx.data(), sizeof(cplx<T>) * B.wlx)) : nullptr;
-  B.twcy = B.wly ? static_cast<const cplx<T>*>(put(twcy.data(), sizeof(cplx<T>) * B.wly)) : nullptr;
   return cudaGetLastError();
 }
 

@@ -3,7 +3,6 @@
 #include <algorithm>
 
 #include "fftp.cuh"
-#include "wfft.cuh"
 #include "plan.cuh"
 
 namespace macsav {
@@ -404,7 +403,6 @@ struct Launcher {
 
   // number of CTAs along x of a row pass over one block
   int row_grid(const TBlockDev<T>& B) const {
-    if (B.wlx) return ((B.rows + 1) / 2 + kWRowLines - 1) / kWRowLines;  // warp-line rows: a pair per warp
     const int P = row_p2(B) ? p2_pairs(B) : B.px;
     return (B.rows + 2 * P - 1) / (2 * P);
   }
@@ -412,26 +410,6 @@ struct Launcher {
   // One specialised pass over block B (bk: 0 = u or the only block, 1 = v) on stream st.
   template <class Src>
   void row_forward_p2(const TBlockDev<T>& B, int bk, cudaStream_t st, Src src, int cols, const int* active) const {
-    if constexpr (std::is_same<T, float>::value) {
-      if (B.wlx) {
-        const size_t sm = wrow_smem(B.wlx);
-        const bool odd = B.kx == KIND_DST1;
-#define MACSAV_RW(RR, OD)                                                       \
-  {                                                                             \
-    auto k = k_row_forward_w<RR, OD, Src>;                                      \
-    set_smem(k, sm);                                                            \
-    launch_k(k, dim3(row_grid(B), cols), 32 * kWRowLines, sm, st, B, active, src, bk); \
-  }
-        if (B.wlx == 1024) {
-          if (odd) MACSAV_RW(32, true) else MACSAV_RW(32, false)
-        } else {
-          if (odd) MACSAV_RW(16, true) else MACSAV_RW(16, false)
-        }
-#undef MACSAV_RW
-        ++*counter;
-        return;
-      }
-    }
     const int P = p2_pairs(B), G = p2_threads_per_line<T>(B, B.fx.L, P);
     TBlockDev<T> Bl = B;
     Bl.tpl = G;
@@ -449,26 +427,6 @@ struct Launcher {
   template <class Dst, class Fin>
   void row_inverse_p2(const TBlockDev<T>& B, int bk, cudaStream_t st, Dst dst, int cols, const int* active,
                       double* partial, Fin fin, unsigned int* done) const {
-    if constexpr (std::is_same<T, float>::value) {
-      if (B.wlx) {
-        const size_t sm = wrow_smem(B.wlx);
-        const bool odd = B.kx == KIND_DST1;
-#define MACSAV_RW(RR, OD)                                                                          \
-  {                                                                                                \
-    auto k = k_row_inverse_w<RR, OD, Dst, Fin>;                                                    \
-    set_smem(k, sm);                                                                               \
-    launch_k(k, dim3(row_grid(B), cols), 32 * kWRowLines, sm, st, B, active, dst, bk, partial, fin, done); \
-  }
-        if (B.wlx == 1024) {
-          if (odd) MACSAV_RW(32, true) else MACSAV_RW(32, false)
-        } else {
-          if (odd) MACSAV_RW(16, true) else MACSAV_RW(16, false)
-        }
-#undef MACSAV_RW
-        ++*counter;
-        return;
-      }
-    }
     const int P = p2_pairs(B), G = p2_threads_per_line<T>(B, B.fx.L, P);
     TBlockDev<T> Bl = B;
     Bl.tpl = G;
@@ -485,12 +443,6 @@ struct Launcher {
   }
   void column_p2(const TBlockDev<T>& B, cudaStream_t st, int cols, const int* active, int mode, const double* shift,
                  T thr) const {
-    if constexpr (std::is_same<T, float>::value) {
-      if (B.wly) {
-        column_w(B, st, cols, active, mode, shift, thr);
-        return;
-      }
-    }
     const int NL = B.wy / 2, G = p2_threads_per_line<T>(B, B.fy.L, NL);
     TBlockDev<T> Bl = B;
     Bl.tpl = G;
@@ -504,27 +456,6 @@ struct Launcher {
   }
     MACSAV_P2_SWITCH(B.fy.L, MACSAV_CO)
 #undef MACSAV_CO
-    ++*counter;
-  }
-
-  // Warp-line column pass (wfft.cuh) of an FP32 block with B.wly = 512 or 1024.
-  void column_w(const TBlockDev<float>& B, cudaStream_t st, int cols, const int* active, int mode,
-                const double* shift, float thr) const {
-    const size_t sm = wline_smem(B.wly);
-    const dim3 grid((B.cols + 2 * kWLines - 1) / (2 * kWLines), cols);
-    const bool odd = B.ky == KIND_DST1;
-#define MACSAV_CW(RR, OD)                                                   \
-  {                                                                         \
-    auto k = k_column_w<RR, OD>;                                            \
-    set_smem(k, sm);                                                        \
-    launch_k(k, grid, kWThreads, sm, st, B, active, mode, shift, thr);      \
-  }
-    if (B.wly == 1024) {
-      if (odd) MACSAV_CW(32, true) else MACSAV_CW(32, false)
-    } else {
-      if (odd) MACSAV_CW(16, true) else MACSAV_CW(16, false)
-    }
-#undef MACSAV_CW
     ++*counter;
   }
 

@@ -35,12 +35,6 @@ struct TBlockDev {
   FFTPlan fx, fy;
   const cplx<T>* twx;  // exp(-2 pi i m / Lx)
   const cplx<T>* twy;
-  // warp-line passes (FP32, wfft.cuh): FFT length along x (rows) and y
-  // (columns), 0 where the block's lines take the shared-memory passes, and
-  // the twiddles tw[32 k2 + l] = exp(-2 pi i l k2 / length), k2 < length / 32
-  int wlx, wly;
-  const cplx<T>* twcx;
-  const cplx<T>* twcy;
   const cplx<T>* qx;   // exp(-i pi k / (2 N)) for DCT kinds
   const cplx<T>* qy;
   const T* eigx;       // eigenvalues in internal order
@@ -56,9 +50,6 @@ struct TBlockDev {
   FastDiv fcols, frows, fw, fvpr, fhalf;  // divisors of the element loops
   T sx, sy;            // inverse normalisation of the x / y transforms
 };
-
-// FP32 columns of 512 or 1024 FFT points take the warp-line column pass (wfft.cuh).
-inline bool warp_line_length(int L) { return L == 512 || L == 1024; }
 
 __device__ __forceinline__ int makhoul_pos(int n, int N) { return (n & 1) ? N - 1 - (n >> 1) : (n >> 1); }
 

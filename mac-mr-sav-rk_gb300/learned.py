@@ -286,7 +286,7 @@ def calibrate_gain(net: UNet, grid: MACGrid, rhs_columns, mass: float, viscosity
 def placement(backend, *, every_iteration: bool = False, restriction: int = 1) -> None:
     """Where the attached network runs: the first search direction of each
     Stokes solve (default) or every CG iteration; on the residual restricted
-    by f x f cell means (``restriction`` 1, 2 or 4)."""
+    by f x f cell means (``restriction`` 1, 2, 4 or 8)."""
     backend = getattr(backend, "backend", backend)
     plan = backend.plan
     plan.check(plan.lib.macsav_plan_set_learned_placement(plan.handle, 1 if every_iteration else 0,

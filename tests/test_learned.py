@@ -145,10 +145,10 @@ def _first_direction_net(env, grid, shift, restriction):
     return net
 
 
-@pytest.mark.parametrize("restriction", [1, 2])
+@pytest.mark.parametrize("restriction", [1, 2, 8])
 def test_first_direction_placement_keeps_answer(env, restriction):
     """The network shaping only the first search direction of each Stokes
-    solve (on the full or the 2x2-restricted residual): the answer is the
+    solve (on the full, the 2x2- or the 8x8-restricted residual): the answer is the
     plain solve's to the defect-corrected tolerance, the gates hold, and the
     network ran in the first inner solve only."""
     pkg, L, torch = env
