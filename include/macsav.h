@@ -331,6 +331,51 @@ int macsav_stokes_log(macsav_plan* plan, const double* rhs, double mass, double 
  * device round trip.  Reads host memory only. */
 int macsav_step_embedded_norms(macsav_plan* plan, double* out);
 
+/* Embedded-error step control of the device-resident adaptive run: the
+ * reference's IController / PIController (solver/adaptivity/controller.py:14-70)
+ * with its scaled error (controller.py:112-123).  proportional <= 0 selects
+ * the elementary (I) controller; the PI factor is
+ * safety err^(-proportional/order) err_prev^(integral/order). */
+typedef struct {
+  double atol, rtol, safety, min_factor, max_factor, min_step, max_step, error_floor;
+  double proportional, integral;
+  int order, max_rejections, max_steps, pad;
+} macsav_step_control;
+
+/* One attempt of the device-resident adaptive run.  reason: 0 accepted,
+ * 1 scaled error above 1, 2 non-finite error, 3 non-finite trial state,
+ * 4 a stage check failed (its status in stage_status). */
+typedef struct {
+  double t, step, error, factor;
+  int accepted, reason, stage_status, pad;
+} macsav_adaptive_attempt;
+
+/* Outcome: status 0 complete, 1 failed; reason (failed): the last
+ * attempt's reason after too many rejections or a step below min_step
+ * following a rejection, 5 the next step below min_step, 6 the maximum
+ * number of accepted steps reached.  next_step: the step the controller
+ * proposes after the last attempt. */
+typedef struct {
+  double t, r, next_step;
+  int status, reason, accepted_steps, attempted_steps;
+} macsav_adaptive_result;
+
+/* The adaptive integration of an autonomous cavity (no body force) from
+ * (t0, x0, r0) over a span T with first step dt0, entirely on the device:
+ * each attempt (one fused step with its embedded error), the accept/reject
+ * decision, the retry with a smaller step and the next step's proposal run
+ * inside one CUDA graph launch (a conditional WHILE node over attempts), and
+ * the host reads the outcome once at the end.  The reference's driver
+ * (integrate_adaptive, solver/adaptivity/controller.py:126-398) makes the same
+ * decisions on the host after every attempt.  x0, x_final: device packed
+ * velocities (may alias).  history: host array for up to history_cap
+ * attempts (may be NULL).  Single-cavity plans; schemes with an embedded
+ * velocity (sdirk2[_mrsav], sdirk3[_mrsav]).  Synchronises. */
+int macsav_integrate_adaptive(macsav_plan* plan, int scheme, double t0, double T, double dt0, double nu,
+                              double gamma, const double* x0, double r0, const macsav_step_control* control,
+                              double* x_final, macsav_adaptive_result* result, macsav_adaptive_attempt* history,
+                              int history_cap, void* stream);
+
 /* ---- channel MAC: periodic x, no-slip walls in y (solver/channel/*.py).
  * Packed free vector (grid.py:64-77): u faces (j, i), i < nx, then the v faces
  * of the interior rows; cells (j, i).  All arithmetic FP64, device pointers,

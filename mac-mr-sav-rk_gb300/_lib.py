@@ -28,6 +28,26 @@ class StokesInfo(C.Structure):
                 ("iterations", C.c_int * MAX_COLUMNS), ("refinements", C.c_int)]
 
 
+class StepControl(C.Structure):
+    """``macsav_step_control``."""
+    _fields_ = [("atol", C.c_double), ("rtol", C.c_double), ("safety", C.c_double), ("min_factor", C.c_double),
+                ("max_factor", C.c_double), ("min_step", C.c_double), ("max_step", C.c_double),
+                ("error_floor", C.c_double), ("proportional", C.c_double), ("integral", C.c_double),
+                ("order", C.c_int), ("max_rejections", C.c_int), ("max_steps", C.c_int), ("pad", C.c_int)]
+
+
+class AdaptiveAttempt(C.Structure):
+    """``macsav_adaptive_attempt``."""
+    _fields_ = [("t", C.c_double), ("step", C.c_double), ("error", C.c_double), ("factor", C.c_double),
+                ("accepted", C.c_int), ("reason", C.c_int), ("stage_status", C.c_int), ("pad", C.c_int)]
+
+
+class AdaptiveResult(C.Structure):
+    """``macsav_adaptive_result``."""
+    _fields_ = [("t", C.c_double), ("r", C.c_double), ("next_step", C.c_double), ("status", C.c_int),
+                ("reason", C.c_int), ("accepted_steps", C.c_int), ("attempted_steps", C.c_int)]
+
+
 class StageRecord(C.Structure):
     """``macsav_stage_record``."""
     _fields_ = [("r", C.c_double), ("residual", C.c_double), ("scalar_residual", C.c_double),
@@ -80,6 +100,8 @@ _SIGNATURES = {
     "macsav_plan_cg_counters": (_I, [_P, _I, _P, _P, _P]),
     "macsav_stokes_log": (_I, [_P, _P, _D, _D, _I, _P, _P, _P, C.POINTER(_I), _P]),
     "macsav_step_embedded_norms": (_I, [_P, C.POINTER(_D)]),
+    "macsav_integrate_adaptive": (_I, [_P, _I, _D, _D, _D, _D, _D, _P, _D, C.POINTER(StepControl), _P,
+                                       C.POINTER(AdaptiveResult), C.POINTER(AdaptiveAttempt), _I, _P]),
     "macsav_channel_create": (_I, [C.POINTER(_P), _I, _I, _D, _D, _D, _I]),
     "macsav_channel_destroy": (None, [_P]),
     "macsav_channel_error": (C.c_char_p, [_P]),

@@ -349,6 +349,32 @@ int macsav_step(macsav_plan* plan, int scheme, double t, double dt, double nu, d
   return stage_status_code(P, st);
 }
 
+int macsav_integrate_adaptive(macsav_plan* plan, int scheme, double t0, double T, double dt0, double nu,
+                              double gamma, const double* x0, double r0, const macsav_step_control* control,
+                              double* x_final, macsav_adaptive_result* result, macsav_adaptive_attempt* history,
+                              int history_cap, void* stream) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  Plan* P = &plan->p;
+  if (scheme < 0 || scheme > MACSAV_IMEX_EULER) return fail(P, MACSAV_ERR_VALUE, "Unknown scheme");
+  if (!control || !result || !x0 || !x_final || history_cap < 0 || P->maxcols < 2)
+    return fail(P, MACSAV_ERR_VALUE, "invalid adaptive-run arguments");
+  if (!std::isfinite(nu) || nu <= 0) return fail(P, MACSAV_ERR_VALUE, "nu must be positive and finite");
+  if (!std::isfinite(gamma) || gamma < 0) return fail(P, MACSAV_ERR_VALUE, "gamma must be finite and nonnegative");
+  if (!std::isfinite(t0) || !std::isfinite(T) || !std::isfinite(dt0) || T <= 0 || dt0 <= 0)
+    return fail(P, MACSAV_ERR_VALUE, "T and initial_step must be finite and positive");
+  const macsav_step_control& c = *control;
+  // controller.py:14-70 (validation)
+  if (!(c.atol >= 0 && c.rtol >= 0 && c.atol + c.rtol > 0) || !(c.safety > 0 && c.safety < 1) ||
+      !(c.min_factor > 0 && c.min_factor < 1 && c.max_factor > 1) || !(c.min_step > 0 && c.min_step <= c.max_step) ||
+      c.max_rejections < 0 || c.max_steps < 1 || c.order < 2 || !(c.error_floor > 0 && c.error_floor < 1) ||
+      (c.proportional > 0 && !(c.proportional > c.integral && c.integral >= 0)))
+    return fail(P, MACSAV_ERR_VALUE, "invalid step control");
+  if (dt0 < c.min_step) return fail(P, MACSAV_ERR_VALUE, "initial_step is below min_step");
+  const int st = macsav::run_adaptive_device(P, scheme, t0, T, dt0, nu, gamma, x0, r0, c, x_final, result, history,
+                                             history_cap, static_cast<cudaStream_t>(stream));
+  return st == MACSAV_ERR_CUDA ? cuda_status(P) : st;
+}
+
 int macsav_step_enqueue(macsav_plan* plan, int scheme, double t, double dt, double nu, double gamma,
                         const double* x0, double r0, const double* forces, double* x1, double* embedded,
                         double* pressures, void* stream) {

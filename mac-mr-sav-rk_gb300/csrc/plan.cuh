@@ -71,6 +71,8 @@ struct StepBuffers {
   double* enorm = nullptr;    // embedded-error inner products of the last step (device)
   double* h_enorm = nullptr;  // and their pinned host copy
   bool have_enorm = false;
+  void* adapt = nullptr;            // device-resident adaptive run: coefficient recipe, state, history
+  cudaStream_t loop = nullptr;      // capture stream of its attempt loop's body
 };
 
 template <typename T>

@@ -463,6 +463,127 @@ __global__ void k_clear_recs(StageRec* recs, int n) {
   }
 }
 
+// ---------------------------------------------- device-resident adaptive run ---
+// State of an adaptive run on the device: the accepted time, SAV scalar and
+// proposed step, the attempt in flight and the counters.  status: 0 running,
+// 1 complete, 2 failed.
+struct AdaptState {
+  double t, end, dt, r, prev_err;  // prev_err < 0: no accepted attempt yet
+  double h;                        // step of the attempt in flight
+  int last, copy, accepted, attempts, rejections, status, reason, hist_cap, max_attempts;
+};
+
+// Step-factor arithmetic of the reference's controllers (controller.py:14-70).
+__device__ double adapt_elementary(const macsav_step_control& c, double err) {
+  if (err == 0.0) return c.max_factor;
+  return fmin(fmax(c.safety * pow(err, -1.0 / c.order), c.min_factor), c.max_factor);
+}
+__device__ double adapt_grow(const macsav_step_control& c, double err, double prev) {
+  if (c.proportional <= 0.0 || prev < 0.0) return adapt_elementary(c, err);
+  const double f = c.safety * pow(fmax(err, c.error_floor), -c.proportional / c.order) *
+                   pow(fmax(prev, c.error_floor), c.integral / c.order);
+  return fmin(fmax(f, c.min_factor), c.max_factor);
+}
+
+// Head of an attempt: h = min(dt, end - t) and the step's coefficient table
+// for h (every slot is c0 + c1 h; the SAV scalar's slot is the accepted r).
+__global__ void k_adapt_begin(AdaptState* st, const double* c0, const double* c1, int ncoef, int r0_idx,
+                              double* coef) {
+  pdl_wait();
+  const double rem = st->end - st->t;
+  const double h = fmin(st->dt, rem);
+  for (int i = threadIdx.x; i < ncoef; i += blockDim.x) coef[i] = i == r0_idx ? st->r : c0[i] + c1[i] * h;
+  if (threadIdx.x == 0) {
+    st->h = h;
+    st->last = h == rem;
+  }
+}
+
+// Decision on the attempt (the reference driver's loop body,
+// controller.py:244-327): the scaled embedded error, accept or reject, the
+// next step, the history record, and the WHILE node's condition.
+__global__ void k_adapt_control(AdaptState* st, const macsav_step_control* ctl, const double* enorm,
+                                const StageRec* recs, int nstages, int sav, macsav_adaptive_attempt* hist,
+                                cudaGraphConditionalHandle cond) {
+  pdl_wait();
+  if (threadIdx.x != 0) return;
+  const macsav_step_control c = *ctl;
+  const double h = st->h;
+  int stage_status = 0;
+  for (int i = 0; i < nstages; ++i)
+    if (recs[i].status && !stage_status) stage_status = recs[i].status;
+  const double r1 = sav ? recs[nstages - 1].r : 0.0;
+  double err = INFINITY;
+  int reason = 0;
+  if (stage_status) {
+    reason = 4;
+  } else {
+    const double d = enorm[0], o = enorm[1], n = enorm[2];
+    if (enorm[3] != 0.0 || !isfinite(n) || !isfinite(r1)) {
+      reason = 3;
+    } else {
+      if (isfinite(d) && d >= 0.0 && isfinite(o) && o >= 0.0 && n >= 0.0)
+        err = sqrt(d) / (c.atol + c.rtol * fmax(sqrt(o), sqrt(n)));
+      reason = !isfinite(err) ? 2 : (err > 1.0 ? 1 : 0);
+    }
+  }
+  const double factor = reason ? fmin(adapt_elementary(c, err), 0.8) : adapt_grow(c, err, st->prev_err);
+  if (st->attempts < st->hist_cap) {
+    macsav_adaptive_attempt a;
+    a.t = st->t;
+    a.step = h;
+    a.error = err;
+    a.factor = factor;
+    a.accepted = reason == 0;
+    a.reason = reason;
+    a.stage_status = stage_status;
+    a.pad = 0;
+    hist[st->attempts] = a;
+  }
+  ++st->attempts;
+  st->copy = 0;
+  if (reason) {
+    ++st->rejections;
+    st->dt = h * factor;
+    if (st->rejections > c.max_rejections || st->dt < c.min_step) {
+      st->status = 2;
+      st->reason = reason;
+    }
+  } else {
+    st->rejections = 0;
+    st->prev_err = err;
+    st->t = st->last ? st->end : st->t + h;
+    st->r = r1;
+    ++st->accepted;
+    st->dt = fmin(h * factor, c.max_step);
+    st->copy = 1;
+    if (!(st->t < st->end)) st->status = 1;
+  }
+  if (st->status == 0) {  // the checks at the head of the reference's loop, for the next attempt
+    const double rem = st->end - st->t, hn = fmin(st->dt, rem);
+    if (st->accepted >= c.max_steps) {
+      st->status = 2;
+      st->reason = 6;
+    } else if (hn < c.min_step && hn != rem) {
+      st->status = 2;
+      st->reason = 5;
+    } else if (st->attempts >= st->max_attempts) {
+      st->status = 2;
+      st->reason = reason ? reason : 6;
+    }
+  }
+  cudaGraphSetConditional(cond, st->status == 0 ? 1u : 0u);
+}
+
+// An accepted attempt's velocity becomes the next attempt's start.
+__global__ void __launch_bounds__(kThreads) k_adapt_accept(const AdaptState* st, double* X, long long src,
+                                                           long long n) {
+  pdl_wait();
+  if (!st->copy) return;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    X[i] = X[src + i];
+}
+
 }  // namespace
 
 // --------------------------------------------------------------- host side ---
@@ -498,6 +619,7 @@ int step_buffers(Plan* P) {
   if (cudaMallocHost(&B.h_enorm, sizeof(double) * 4 * M) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (cudaStreamCreateWithFlags(&B.side, cudaStreamNonBlocking) != cudaSuccess) return MACSAV_ERR_CUDA;
+  if (cudaStreamCreateWithFlags(&B.loop, cudaStreamNonBlocking) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (cudaEventCreateWithFlags(&B.ev_in, cudaEventDisableTiming) != cudaSuccess) return MACSAV_ERR_CUDA;
   if (cudaEventCreateWithFlags(&B.ev_out, cudaEventDisableTiming) != cudaSuccess) return MACSAV_ERR_CUDA;
   return MACSAV_OK;
@@ -515,6 +637,8 @@ void step_free(Plan* P) {
   cudaFreeHost(B.h_enorm);
   if (B.stream) cudaStreamDestroy(B.stream);
   if (B.side) cudaStreamDestroy(B.side);
+  if (B.loop) cudaStreamDestroy(B.loop);
+  cudaFree(B.adapt);
   if (B.ev_in) cudaEventDestroy(B.ev_in);
   if (B.ev_out) cudaEventDestroy(B.ev_out);
   B = StepBuffers{};
@@ -890,6 +1014,131 @@ int enqueue_step_async(Plan* P, int scheme, double t, double dt, double nu, doub
 }
 
 int finish_step(Plan* P, macsav_stage_record* records, double* r1) { return finish_members(P, records, r1); }
+
+// Device-resident adaptive run (see macsav_integrate_adaptive).  The step
+// program is affine in dt, so its coefficient table is c0 + c1 dt with
+// (c0, c1) from two host builds; the attempt loop is one conditional WHILE
+// node whose body is [table for the attempt's step, the fused step with its
+// embedded-error inner products, the decision, the copy of an accepted
+// velocity], captured once per scheme.
+constexpr int kAdaptHistory = 65536;  // attempts kept on the device
+int run_adaptive_device(Plan* P, int scheme, double t0, double T, double dt0, double nu, double gamma,
+                        const double* x0, double r0, const macsav_step_control& ctl, double* x_final,
+                        macsav_adaptive_result* res, macsav_adaptive_attempt* hist, int hist_cap,
+                        cudaStream_t user) {
+  if (P->members != 1) {
+    P->err = "the device-resident adaptive run takes single-cavity plans";
+    return MACSAV_ERR_VALUE;
+  }
+  const int n = scheme_stages(scheme);
+  if (n < 2) {
+    P->err = "the scheme has no embedded velocity";
+    return MACSAV_ERR_VALUE;
+  }
+  int rc = step_buffers(P);
+  if (rc != MACSAV_OK) return rc;
+  StepBuffers& B = P->st;
+  const long long sz = P->g.size;
+  StageProgram G, G1;
+  std::vector<double> c(2 * kCoefStride, 0.0), one(kCoefStride, 0.0);
+  build_program(P, scheme, false, 0.0, nu, gamma, r0, G, c.data());
+  build_program(P, scheme, false, 1.0, nu, gamma, r0, G1, one.data());
+  for (int i = 0; i < kCoefStride; ++i) c[kCoefStride + i] = one[i] - c[i];
+  const size_t state_off = 2 * kCoefStride * sizeof(double);
+  const size_t hist_off = (state_off + sizeof(AdaptState) + sizeof(macsav_step_control) + 255) / 256 * 256;
+  if (!B.adapt && cudaMalloc(&B.adapt, hist_off + sizeof(macsav_adaptive_attempt) * kAdaptHistory) != cudaSuccess)
+    return MACSAV_ERR_CUDA;
+  char* base = static_cast<char*>(B.adapt);
+  double* dc0 = reinterpret_cast<double*>(base);
+  AdaptState* dst = reinterpret_cast<AdaptState*>(base + state_off);
+  macsav_step_control* dctl = reinterpret_cast<macsav_step_control*>(dst + 1);
+  macsav_adaptive_attempt* dh = reinterpret_cast<macsav_adaptive_attempt*>(base + hist_off);
+  AdaptState s0;
+  std::memset(&s0, 0, sizeof(s0));
+  s0.t = t0;
+  s0.end = t0 + T;
+  s0.dt = std::fmin(dt0, ctl.max_step);
+  s0.r = r0;
+  s0.prev_err = -1.0;
+  s0.hist_cap = kAdaptHistory;
+  const double cap_attempts = double(ctl.max_steps) * (double(ctl.max_rejections) + 1.0) + 1.0;
+  s0.max_attempts = cap_attempts > 2e9 ? 2000000000 : int(cap_attempts);
+  const cudaStream_t s = B.stream;
+  cudaEventRecord(B.ev_in, user);
+  cudaStreamWaitEvent(s, B.ev_in, 0);
+  cudaMemcpyAsync(dc0, c.data(), sizeof(double) * c.size(), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(dst, &s0, sizeof(s0), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(dctl, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(B.X, x0, sizeof(double) * sz, cudaMemcpyDeviceToDevice, s);
+  const int key = 1000 + scheme;
+  cudaGraphExec_t exec = nullptr;
+  for (auto& kv : B.graphs)
+    if (kv.key == key) exec = kv.exec;
+  if (!exec) {
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed) != cudaSuccess) return MACSAV_ERR_CUDA;
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cap;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cudaGraphConditionalHandle cond;
+    cudaGraphNodeParams cp = {};
+    cudaGraphNode_t node;
+    bool ok = cudaStreamGetCaptureInfo(s, &st, nullptr, &cap, &deps, nullptr, &ndeps) == cudaSuccess &&
+              cudaGraphConditionalHandleCreate(&cond, cap, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+    if (ok) {
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = cond;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      ok = cudaGraphAddNode(&node, cap, deps, nullptr, ndeps, &cp) == cudaSuccess &&
+           cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies) == cudaSuccess;
+    }
+    if (ok) {
+      ok = cudaStreamBeginCaptureToGraph(B.loop, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeRelaxed) == cudaSuccess;
+      if (ok) {
+        launch_k(k_adapt_begin, 1, kThreads, 0, B.loop, dst, static_cast<const double*>(dc0),
+                 static_cast<const double*>(dc0 + kCoefStride), kCoefStride, G.r0_idx, B.coef);
+        Exec X{B.loop, true, B.side, 0, 0.0};
+        rc = enqueue_step(P, X, scheme, G, true);
+        launch_k(k_adapt_control, 1, 32, 0, B.loop, dst, static_cast<const macsav_step_control*>(dctl),
+                 static_cast<const double*>(B.enorm),
+                 static_cast<const StageRec*>(B.recs), n, scheme_sav(scheme) ? 1 : 0, dh, cond);
+        launch_k(k_adapt_accept, red_nb(sz), kThreads, 0, B.loop, static_cast<const AdaptState*>(dst), B.X, n * sz, sz);
+        P->launches += 3;
+        cudaGraph_t body;
+        ok = cudaStreamEndCapture(B.loop, &body) == cudaSuccess && rc == MACSAV_OK;
+      }
+    }
+    const cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (!ok || e != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      P->err = "adaptive loop capture failed";
+      return rc != MACSAV_OK ? rc : MACSAV_ERR_CUDA;
+    }
+    cudaGraphDestroy(graph);
+    B.graphs.push_back(GraphEntry{key, exec});
+  }
+  if (cudaGraphLaunch(exec, s) != cudaSuccess) return MACSAV_ERR_CUDA;
+  cudaMemcpyAsync(x_final, B.X, sizeof(double) * sz, cudaMemcpyDeviceToDevice, s);
+  AdaptState out;
+  cudaMemcpyAsync(&out, dst, sizeof(out), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return MACSAV_ERR_CUDA;
+  const int nh = std::min(std::min(hist_cap, out.attempts), kAdaptHistory);
+  if (hist && nh > 0 && cudaMemcpy(hist, dh, sizeof(macsav_adaptive_attempt) * nh, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return MACSAV_ERR_CUDA;
+  cudaEventRecord(B.ev_out, s);
+  cudaStreamWaitEvent(user, B.ev_out, 0);
+  res->t = out.t;
+  res->r = out.r;
+  res->next_step = out.dt;
+  res->status = out.status == 1 ? 0 : 1;
+  res->reason = out.status == 1 ? 0 : out.reason;
+  res->accepted_steps = out.accepted;
+  res->attempted_steps = out.attempts;
+  return MACSAV_OK;
+}
 
 int run_step(Plan* P, int scheme, double t, double dt, double nu, double gamma, const double* x0, double r0,
              const double* forces, double* x1, double* embedded, double* pressures, macsav_stage_record* records,

@@ -42,5 +42,9 @@ int enqueue_members(Plan* P, int scheme, double t, double dt, const double* nus,
 int finish_members(Plan* P, macsav_stage_record* records, double* r1);
 int scheme_stages(int scheme);
 void step_free(Plan* P);
+int run_adaptive_device(Plan* P, int scheme, double t0, double T, double dt0, double nu, double gamma,
+                        const double* x0, double r0, const macsav_step_control& ctl, double* x_final,
+                        macsav_adaptive_result* res, macsav_adaptive_attempt* hist, int hist_cap,
+                        cudaStream_t user);
 
 }  // namespace macsav

@@ -246,6 +246,68 @@ def run_adaptive(model, scheme, initial, T: float, initial_step: float, control:
     return run
 
 
+_REASONS = {1: "error_exceeded", 2: "nonfinite_error", 3: "FloatingPointError: Nonfinite trial state",
+            5: "Step below min_step", 6: "Maximum accepted steps exceeded"}
+
+
+def _reason_text(code: int, stage_status: int = 0) -> str:
+    if code == 4:
+        return f"RuntimeError: stage check failed (status {stage_status})"
+    return _REASONS.get(code, "")
+
+
+def run_adaptive_device(model, scheme, initial, T: float, initial_step: float, control: Any = None, *,
+                        history: int = 4096) -> AdaptiveRun:
+    """``run_adaptive`` with the whole attempt loop on the device: every
+    attempt, its accept/reject decision, the retry with a smaller step and
+    the next step's proposal run inside one CUDA graph launch
+    (``macsav_integrate_adaptive``), so the host reads the outcome once.
+    The step control and the decisions are those of ``run_adaptive`` (the
+    reference's controllers, solver/adaptivity/controller.py:14-123,244-327).
+    Needs an autonomous model (no body force: the device cannot evaluate
+    the force's Python callable at the stage times of an attempt it chose);
+    ``history`` attempts are returned in ``attempts``."""
+    ctl = StepControl.of(control if control is not None else StepControl())
+    if scheme.info.estimator_order is None:
+        raise ValueError(f"{scheme.name} has no embedded velocity to control the step with")
+    if not getattr(model.force, "zero", False):
+        raise ValueError("the device-resident loop needs a model without body force; use run_adaptive")
+    if not (math.isfinite(T) and math.isfinite(initial_step) and math.isfinite(initial.t)) or T <= 0 \
+            or initial_step <= 0:
+        raise ValueError("T and initial_step must be finite and positive")
+    if initial_step < ctl.min_step:
+        raise ValueError("initial_step is below min_step")
+    lib = _lib.load()
+    c = _lib.StepControl(ctl.atol, ctl.rtol, ctl.safety, ctl.min_factor, ctl.max_factor, ctl.min_step,
+                         ctl.max_step, ctl.error_floor, ctl.pi[0] if ctl.pi else 0.0, ctl.pi[1] if ctl.pi else 0.0,
+                         ctl.order, ctl.max_rejections, ctl.max_steps, 0)
+    x0 = model.device_vector(initial).contiguous()
+    x1 = torch.empty_like(x0)
+    res = _lib.AdaptiveResult()
+    hist = (_lib.AdaptiveAttempt * max(int(history), 1))()
+    start = perf_counter()
+    lib.macsav_plan_set_graph(model.plan.handle, 1)
+    _lib.check(lib.macsav_integrate_adaptive(model.plan.handle, scheme._id, float(initial.t), float(T),
+                                             float(initial_step), float(model.nu), float(scheme.gamma),
+                                             C.c_void_p(x0.data_ptr()), float(initial.r), C.byref(c),
+                                             C.c_void_p(x1.data_ptr()), C.byref(res), hist, int(history),
+                                             C.c_void_p(torch.cuda.current_stream().cuda_stream)),
+               model.plan.handle)
+    run = AdaptiveRun(final=model.state(res.t, x1, res.r), accepted_steps=res.accepted_steps,
+                      attempted_steps=res.attempted_steps, seconds=perf_counter() - start)
+    if res.status != 0:
+        run.status, run.error = "failed", _reason_text(res.reason)
+    t = float(initial.t)
+    run.times = [t]
+    for a in hist[:min(res.attempted_steps, int(history))]:
+        run.attempts.append({"t": a.t, "step": a.step, "error": a.error, "accepted": bool(a.accepted),
+                             "reason": _reason_text(a.reason, a.stage_status), "factor": a.factor})
+    for a, nxt in zip(run.attempts, run.attempts[1:] + [None]):
+        if a["accepted"]:
+            run.times.append(nxt["t"] if nxt is not None else res.t)
+    return run
+
+
 @dataclass
 class FixedRun:
     """Outcome of ``run_fixed``: the final state, the accepted times, the last
