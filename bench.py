@@ -437,7 +437,7 @@ def train_first_direction(pkg, g, w) -> tuple:
     train_cols = stage_rhs_columns(pkg, g, w, range(1000, 1000 + w["train_fields"]), helper)
     rhs = [c[:, k] for c in train_cols for k in range(2)]
     pairs = L.collect_first_direction_pairs(g, rhs, mass, visc, restriction=w["restriction"])
-    net = L.UNet(seed=0)
+    net = L.UNet(channels=w.get("net_channels", L.DEFAULT_CHANNELS), seed=0)
     losses = L.train(net, pairs, steps=w["train_steps"], batch=8, lr=1e-3)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
@@ -593,7 +593,7 @@ def e2e_steps(pkg, model, w, x0_host, args, pageable: bool) -> float:
 HEADLINE = {"workload": "learned1024_sdirk3_mrsav", "nx": 1024, "ny": 1024, "lx": 1.0, "ly": 1.0, "nu": 1e-4,
             "dt": 1e-4, "psi_modes": 32, "seed": 20261204, "scheme": "sdirk3_mrsav", "stages_per_step": 4,
             "krylov_tolerance": 1e-10, "reference_krylov_tolerance": 1e-12, "restriction": 4,
-            "train_fields": 32, "train_steps": 400, "judge_fields": 3}
+            "net_channels": (16, 16, 16, 16), "train_fields": 32, "train_steps": 400, "judge_fields": 3}
 
 
 def oracle_step(w, x0, threads: int):
@@ -629,7 +629,11 @@ def run_headline(args) -> None:
     pkg = __graft_entry__.load_package()
     from importlib import import_module
     lib = import_module(pkg.__name__ + "._lib")
-    w = dict(HEADLINE, restriction=args.restriction) if args.restriction else HEADLINE
+    w = dict(HEADLINE)
+    if args.restriction:
+        w["restriction"] = args.restriction
+    if args.net_channels:
+        w["net_channels"] = tuple(int(c) for c in args.net_channels.split(","))
     g = pkg.MACGrid(w["nx"], w["ny"], w["lx"], w["ly"])
     dev = torch.device("cuda", local)
     x0_host = pkg.fields.packed_curl_velocity(w["nx"], w["ny"], w["lx"], w["ly"], w["psi_modes"], w["seed"])
@@ -808,7 +812,7 @@ def profile_steps(precision: str, workload: str) -> None:
                                 krylov_tolerance=ktol)
     if precision == "learned":
         L = import_module(pkg.__name__ + ".learned")
-        net = L.UNet(seed=0)
+        net = L.UNet(channels=w.get("net_channels", L.DEFAULT_CHANNELS), seed=0)
         L.attach(model, net)
         L.placement(model, every_iteration=False, restriction=w["restriction"])
     scheme = pkg.make_scheme(w["scheme"])
@@ -959,6 +963,9 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--net-channels", default=None,
+                    help="headline: the U-Net's channels per level, four comma-separated values "
+                         "(16, 32 or 64 each; default the workload's own)")
     ap.add_argument("--restriction", type=int, choices=[2, 4, 8], default=None,
                     help="headline: the learned preconditioner's restriction factor (the network sees "
                          "(nx/f) x (ny/f) cell means); default the workload's own")
