@@ -699,6 +699,10 @@ def run_headline(args) -> None:
         vs_oracle = {k: float(torch.linalg.vector_norm(v - ox) / torch.linalg.vector_norm(ox))
                      for k, v in first.items()}
     cav = quick_cavity512(pkg, dev, args, flush)
+    try:
+        ens = quick_ensemble(pkg, flush)
+    except Exception as exc:  # the headline stands on its own
+        ens = {"error": f"{type(exc).__name__}: {exc}"}
     autotune = transform_choices(pkg)
     line = {
         "metric": METRIC, "value": cells / (ms_l / 1e3), "unit": "cell-stage/s", "n_gpus": world,
@@ -708,8 +712,8 @@ def run_headline(args) -> None:
         "config": {"workload": w["workload"], **{k: w[k] for k in ("nx", "ny", "nu", "dt", "scheme", "psi_modes",
                                                                    "krylov_tolerance", "reference_krylov_tolerance")},
                    "parallelism": f"replicas{world}",
-                   "form": "fp32 transforms/stencils/Krylov + fp64 reductions + fp64 defect correction; "
-                           "flexible CG with the learned first direction",
+                   "form": "fp32 transforms/stencils/Krylov + fp64-accurate reductions + double-float defect "
+                           "correction; flexible CG with the learned first direction",
                    "learned_placement": f"first search direction of each Stokes solve, network on the "
                                         f"{w['restriction']}x{w['restriction']}-restricted residual",
                    "l2": "flushed (256 MiB write) before every timed step", "graph": "one CUDA graph per step"},
@@ -733,6 +737,7 @@ def run_headline(args) -> None:
         "roofline": roof,
         "roofline_fp64": roof64,
         "cavity512_sdirk3_mrsav": cav,
+        "ensemble256_sdirk2_mrsav": ens,
         "transform_autotune": autotune,
     }
     if oracle_sec is not None:
@@ -777,6 +782,40 @@ def quick_cavity512(pkg, dev, args, flush) -> dict:
             "fp64": {"value": cells / (sum(b["ms"]) / 1e3), "ms_per_step": sum(b["ms"]) / args.steps},
             "error_vs_fp64": float(torch.linalg.vector_norm(a["x"] - b["x"]) / torch.linalg.vector_norm(b["x"])),
             "unit": "cell-stage/s"}
+
+
+def quick_ensemble(pkg, flush, warmup: int = 3, steps: int = 5) -> dict:
+    """The mixed-size ensemble (256 cavities, sdirk2_mrsav, FP32 bulk) on a
+    few steps: throughput over all members and kernels per ensemble step."""
+    import torch
+    from importlib import import_module
+    E = import_module(pkg.__name__ + ".ensemble")
+    w = ENSEMBLE
+    members = E.ensemble_members(w["members"], seed=w["seed"])
+    ens = E.Ensemble(members, w["scheme"], precision="fp32")
+    ens.seed_fields(modes=w["psi_modes"])
+    for _ in range(warmup):
+        ens.step(w["dt"])
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    total = 0.0
+    for _ in range(steps):
+        flush.fill_(1.0)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ens.step(w["dt"])
+        b.record(stream)
+        b.synchronize()
+        total += a.elapsed_time(b)
+    eager = E.Ensemble(members, w["scheme"], precision="fp32", use_graph=False)
+    eager.seed_fields(modes=w["psi_modes"])
+    before = eager.launches()
+    eager.step(w["dt"])
+    launches = eager.launches() - before
+    cells = sum(m.cells for m in members) * w["stages_per_step"] * steps
+    return {"value": cells / (total / 1e3), "ms_per_step": total / steps, "unit": "cell-stage/s",
+            "members": len(members), "plans": len(ens.units), "kernels_per_step": launches,
+            "precision": "fp32 bulk", "steps": steps}
 
 
 def profile_unet() -> None:
