@@ -161,22 +161,69 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int np, T* x, T* r, T* p
   if (active[c]) {
     const bool first = cg[c].iters == 0;
     const T beta = cg_beta<T>(cg[c]), alpha = cg_alpha<T>(cg[c]), mq = cg_mean_q<T>(cg[c]);
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
-      const long long k = c * cs + idx;
-      const T pd = first ? z[k] : T(z[k] + beta * p[k]);
-      p[k] = pd;
-      x[k] = x[k] + alpha * pd;
-      const T ro = r[k];
-      if (r_old) r_old[k] = ro;
-      const T rv = ro - alpha * (q[k] - mq);
-      r[k] = rv;
-      acc[0].add(rv * rv);
+    const long long stride = (long long)gridDim.x * blockDim.x, t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    bool vec = false;
+    if constexpr (sizeof(T) == 4) {
+      // FP32: 16-byte vectors of four cells (the same arithmetic per cell),
+      // four times the bytes in flight per load of these streaming loops
+      vec = (np & 3) == 0 && (cs & 3) == 0;
+      if (vec) {
+        float4* x4 = reinterpret_cast<float4*>(x + c * cs);
+        float4* r4 = reinterpret_cast<float4*>(r + c * cs);
+        float4* p4 = reinterpret_cast<float4*>(p + c * cs);
+        const float4* z4 = reinterpret_cast<const float4*>(z + c * cs);
+        const float4* q4 = reinterpret_cast<const float4*>(q + c * cs);
+        float4* o4 = r_old ? reinterpret_cast<float4*>(r_old + c * cs) : nullptr;
+        for (long long i = t0; i < (np >> 2); i += stride) {
+          const float4 zz = z4[i], qq = q4[i], ro = r4[i], xx = x4[i];
+          float4 pd = zz;
+          if (!first) {
+            const float4 pp = p4[i];
+            pd = make_float4(zz.x + beta * pp.x, zz.y + beta * pp.y, zz.z + beta * pp.z, zz.w + beta * pp.w);
+          }
+          p4[i] = pd;
+          x4[i] = make_float4(xx.x + alpha * pd.x, xx.y + alpha * pd.y, xx.z + alpha * pd.z, xx.w + alpha * pd.w);
+          if (o4) o4[i] = ro;
+          const float4 rv = make_float4(ro.x - alpha * (qq.x - mq), ro.y - alpha * (qq.y - mq),
+                                        ro.z - alpha * (qq.z - mq), ro.w - alpha * (qq.w - mq));
+          r4[i] = rv;
+          acc[0].add(rv.x * rv.x);
+          acc[0].add(rv.y * rv.y);
+          acc[0].add(rv.z * rv.z);
+          acc[0].add(rv.w * rv.w);
+        }
+      }
+    }
+    if (!vec) {
+      for (long long idx = t0; idx < np; idx += stride) {
+        const long long k = c * cs + idx;
+        const T pd = first ? z[k] : T(z[k] + beta * p[k]);
+        p[k] = pd;
+        x[k] = x[k] + alpha * pd;
+        const T ro = r[k];
+        if (r_old) r_old[k] = ro;
+        const T rv = ro - alpha * (q[k] - mq);
+        r[k] = rv;
+        acc[0].add(rv * rv);
+      }
     }
     // the velocity follows x: wacc += alpha (mI+kK)^{-1} D^T pdir (wv holds
     // that velocity for this iteration's direction)
     if (wacc) {
-      for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vsz; i += (long long)gridDim.x * blockDim.x)
-        wacc[c * vsz + i] += alpha * wv[c * vsz + i];
+      if constexpr (sizeof(T) == 4) {
+        if ((vsz & 3) == 0) {
+          float4* a4 = reinterpret_cast<float4*>(wacc + c * vsz);
+          const float4* w4 = reinterpret_cast<const float4*>(wv + c * vsz);
+          for (long long i = t0; i < (vsz >> 2); i += stride) {
+            const float4 a = a4[i], w = w4[i];
+            a4[i] = make_float4(a.x + alpha * w.x, a.y + alpha * w.y, a.z + alpha * w.z, a.w + alpha * w.w);
+          }
+        } else {
+          for (long long i = t0; i < vsz; i += stride) wacc[c * vsz + i] += alpha * wv[c * vsz + i];
+        }
+      } else {
+        for (long long i = t0; i < vsz; i += stride) wacc[c * vsz + i] += alpha * wv[c * vsz + i];
+      }
     }
   }
   write_sums<T, 1>(acc, partial, 1);
