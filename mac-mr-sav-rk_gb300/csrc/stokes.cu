@@ -103,22 +103,85 @@ __global__ void __launch_bounds__(kThreads) k_pressure_rhs_start(GridDev g, cons
   Acc<T> acc[2];
   T mt = T(0);
   bool bad = false;
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < g.np; idx += gridDim.x * blockDim.x) {
-    const int j = idx / g.nx, i = idx - j * g.nx;
-    T v = -D_atT<T>(w + c * ws, g, j, i, ihx, ihy);
-    if (rd) v += load_as<T>(rd + c * (long long)g.np + idx);
-    b[c * cs + idx] = v;
-    x[c * cs + idx] = T(0);  // x0 = 0 (also the answer of a column that never starts)
+  auto take = [&](T v) {
     acc[0].add(v);
     acc[1].add(v * v);
     const T av = v < T(0) ? -v : v;
     bad |= !(av == av);
     mt = av > mt ? av : mt;
+  };
+  bool vec = false;
+  if constexpr (sizeof(T) == 4 && sizeof(WIn) == 4) {
+    // FP32: four cells of a row per thread (16-byte vectors of b, x, rd)
+    vec = (g.nx & 3) == 0 && (cs & 3) == 0;
+    if (vec) {
+      const long long stride = (long long)gridDim.x * blockDim.x;
+      float4* b4 = reinterpret_cast<float4*>(b + c * cs);
+      float4* x4 = reinterpret_cast<float4*>(x + c * cs);
+      const float4* r4 = rd ? reinterpret_cast<const float4*>(rd + c * (long long)g.np) : nullptr;
+      for (long long i4 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i4 < (g.np >> 2); i4 += stride) {
+        const int e = int(i4 << 2), j = e / g.nx, i0 = e - j * g.nx;
+        const float4 d = D_at4(w + c * ws, g, j, i0, ihx, ihy);
+        float4 v = make_float4(-d.x, -d.y, -d.z, -d.w);
+        if (r4) {
+          const float4 rr = r4[i4];
+          v = make_float4(v.x + rr.x, v.y + rr.y, v.z + rr.z, v.w + rr.w);
+        }
+        b4[i4] = v;
+        x4[i4] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // x0 = 0 (also the answer of a column that never starts)
+        take(v.x);
+        take(v.y);
+        take(v.z);
+        take(v.w);
+      }
+    }
+  }
+  if (!vec) {
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < g.np; idx += gridDim.x * blockDim.x) {
+      const int j = idx / g.nx, i = idx - j * g.nx;
+      T v = -D_atT<T>(w + c * ws, g, j, i, ihx, ihy);
+      if (rd) v += load_as<T>(rd + c * (long long)g.np + idx);
+      b[c * cs + idx] = v;
+      x[c * cs + idx] = T(0);  // x0 = 0 (also the answer of a column that never starts)
+      take(v);
+    }
   }
   unsigned long long key[1] = {bad ? 0x7ff8000000000000ull : abs_key_t<T>(mt)};
   write_sums<T, 2>(acc, partial, 3);
   write_keys<1>(key, partial, 3, 2);
   last_block_finish(fin, done);
+}
+
+// D w at the four cells (j, i0..i0+3) of one row (nx a multiple of 4), in the
+// operation order of D_atT: the five u faces and eight v faces they touch are
+// loaded together.
+__device__ __forceinline__ float4 D_at4(const float* w, const GridDev& g, int j, int i0, float ihx, float ihy) {
+  const float* u = w + (long long)j * (g.nx - 1);
+  const float* vn = w + g.nu + (long long)j * g.nx;
+  const float* vs = vn - g.nx;
+  float ul[5], n4[4], s4[4];
+#pragma unroll
+  for (int t = 0; t < 5; ++t) {
+    const int i = i0 - 1 + t;
+    ul[t] = (i >= 0 && i < g.nx - 1) ? u[i] : 0.0f;
+  }
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    n4[t] = j < g.ny - 1 ? vn[i0 + t] : 0.0f;
+    s4[t] = j > 0 ? vs[i0 + t] : 0.0f;
+  }
+  float r[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int i = i0 + t;
+    float v = 0.0f;
+    if (i < g.nx - 1) v += ul[t + 1] * ihx;
+    if (i > 0) v -= ul[t] * ihx;
+    if (j < g.ny - 1) v += n4[t] * ihy;
+    if (j > 0) v -= s4[t] * ihy;
+    r[t] = v;
+  }
+  return make_float4(r[0], r[1], r[2], r[3]);
 }
 
 // q = D w; last block: alpha from p.q, sum q, sum p (OP_ALPHA), p = z + beta p.
@@ -133,15 +196,51 @@ __global__ void __launch_bounds__(kThreads) k_div_q(GridDev g, const WIn* w, lon
     const bool first = cg[c].iters == 0;
     const T beta = cg_beta<T>(cg[c]);
     const T ihx = T(g.ihx), ihy = T(g.ihy);
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < g.np; idx += gridDim.x * blockDim.x) {
-      const int j = idx / g.nx, i = idx - j * g.nx;
-      const long long k = c * cs + idx;
-      const T qv = D_atT<T>(w + c * ws, g, j, i, ihx, ihy);
-      q[k] = qv;
-      const T pd = first ? z[k] : T(z[k] + beta * p[k]);
-      a[0].add(pd * qv);
-      a[1].add(qv);
-      a[2].add(pd);
+    bool vec = false;
+    if constexpr (sizeof(T) == 4 && sizeof(WIn) == 4) {
+      // FP32: four cells of a row per thread (16-byte vectors of q, z, p)
+      vec = (g.nx & 3) == 0 && (cs & 3) == 0;
+      if (vec) {
+        const long long stride = (long long)gridDim.x * blockDim.x;
+        float4* q4 = reinterpret_cast<float4*>(q + c * cs);
+        const float4* z4 = reinterpret_cast<const float4*>(z + c * cs);
+        const float4* p4 = reinterpret_cast<const float4*>(p + c * cs);
+        for (long long i4 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i4 < (g.np >> 2); i4 += stride) {
+          const int e = int(i4 << 2), j = e / g.nx, i0 = e - j * g.nx;
+          const float4 qv = D_at4(w + c * ws, g, j, i0, ihx, ihy);
+          q4[i4] = qv;
+          const float4 zz = z4[i4];
+          float4 pd = zz;
+          if (!first) {
+            const float4 pp = p4[i4];
+            pd = make_float4(zz.x + beta * pp.x, zz.y + beta * pp.y, zz.z + beta * pp.z, zz.w + beta * pp.w);
+          }
+          a[0].add(pd.x * qv.x);
+          a[1].add(qv.x);
+          a[2].add(pd.x);
+          a[0].add(pd.y * qv.y);
+          a[1].add(qv.y);
+          a[2].add(pd.y);
+          a[0].add(pd.z * qv.z);
+          a[1].add(qv.z);
+          a[2].add(pd.z);
+          a[0].add(pd.w * qv.w);
+          a[1].add(qv.w);
+          a[2].add(pd.w);
+        }
+      }
+    }
+    if (!vec) {
+      for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < g.np; idx += gridDim.x * blockDim.x) {
+        const int j = idx / g.nx, i = idx - j * g.nx;
+        const long long k = c * cs + idx;
+        const T qv = D_atT<T>(w + c * ws, g, j, i, ihx, ihy);
+        q[k] = qv;
+        const T pd = first ? z[k] : T(z[k] + beta * p[k]);
+        a[0].add(pd * qv);
+        a[1].add(qv);
+        a[2].add(pd);
+      }
     }
   }
   write_sums<T, 3>(a, partial, 3);
@@ -865,18 +964,36 @@ __global__ void __launch_bounds__(kThreads) k_sum_pieces(const float* u, double*
   const int c = blockIdx.y;
   const long long stride = (long long)gridDim.x * blockDim.x;
   const long long us = sz * cols, xs = np * cols;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < sz; i += stride) {
-    const long long k = c * sz + i;
-    double v = f2d_bits(u[k]);
-    for (int q = 1; q < pieces; ++q) v += f2d_bits(u[q * us + k]);
-    vel[k] = v;
-  }
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += stride) {
-    const long long k = c * np + i;
-    double v = f2d_bits(x[k]);
-    for (int q = 1; q < pieces; ++q) v += f2d_bits(x[q * xs + k]);
-    pres[k] = v;
-  }
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  // four elements per thread (16-byte float loads, two 16-byte double stores)
+  auto sum4 = [&](const float* src, long long ps, double* dst, long long n, long long base) {
+    const bool aligned = ((reinterpret_cast<unsigned long long>(src) | reinterpret_cast<unsigned long long>(dst)) & 15) == 0;
+    if (aligned && (n & 3) == 0 && (ps & 3) == 0) {
+      for (long long i4 = t0; i4 < (n >> 2); i4 += stride) {
+        const long long k = base + (i4 << 2);
+        float4 f = *reinterpret_cast<const float4*>(src + k);
+        double v0 = f2d_bits(f.x), v1 = f2d_bits(f.y), v2 = f2d_bits(f.z), v3 = f2d_bits(f.w);
+        for (int q = 1; q < pieces; ++q) {
+          f = *reinterpret_cast<const float4*>(src + q * ps + k);
+          v0 += f2d_bits(f.x);
+          v1 += f2d_bits(f.y);
+          v2 += f2d_bits(f.z);
+          v3 += f2d_bits(f.w);
+        }
+        reinterpret_cast<double2*>(dst + k)[0] = make_double2(v0, v1);
+        reinterpret_cast<double2*>(dst + k)[1] = make_double2(v2, v3);
+      }
+    } else {
+      for (long long i = t0; i < n; i += stride) {
+        const long long k = base + i;
+        double v = f2d_bits(src[k]);
+        for (int q = 1; q < pieces; ++q) v += f2d_bits(src[q * ps + k]);
+        dst[k] = v;
+      }
+    }
+  };
+  sum4(u, us, vel, sz, c * sz);
+  sum4(x, xs, pres, np, c * np);
 }
 
 // One FP32 Stokes solve of (f, 0) or of the defect (ru, rd): transforms,
