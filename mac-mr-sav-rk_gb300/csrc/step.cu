@@ -59,16 +59,48 @@ __global__ void __launch_bounds__(kThreads) k_combine2(CombineArgs a, const doub
   partial += mem * kPartStride;
   unsigned long long m[2] = {0ull, 0ull};  // abs_key maxima: integer pipe, NaN propagates
   double s[1] = {0.0};
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    for (int o = 0; o < a.nout; ++o) {
-      double acc = 0.0;
-      for (int t = 0; t < a.nterm[o]; ++t) {
-        const double* src = a.src[o][t];
-        if (src) acc += coef[a.idx[o][t]] * src[mem * a.sstr[o][t] + i];
+  // pairs of elements on 16-byte vectors when every array allows (the same
+  // arithmetic per element, twice the bytes per load of this streaming loop)
+  bool vec = (n & 1) == 0 && (a.ostr & 1) == 0;
+  for (int o = 0; o < a.nout && vec; ++o) {
+    vec = (reinterpret_cast<unsigned long long>(a.out[o]) & 15) == 0;
+    for (int t = 0; t < a.nterm[o]; ++t)
+      if (a.src[o][t]) vec = vec && (a.sstr[o][t] & 1) == 0 && (reinterpret_cast<unsigned long long>(a.src[o][t]) & 15) == 0;
+  }
+  const long long stride = (long long)gridDim.x * blockDim.x, t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (vec) {
+    for (long long i2 = t0; i2 < (n >> 1); i2 += stride) {
+      for (int o = 0; o < a.nout; ++o) {
+        double a0 = 0.0, a1 = 0.0;
+        for (int t = 0; t < a.nterm[o]; ++t) {
+          const double* src = a.src[o][t];
+          if (src) {
+            const double cf = coef[a.idx[o][t]];
+            const double2 v = reinterpret_cast<const double2*>(src + mem * a.sstr[o][t])[i2];
+            a0 += cf * v.x;
+            a1 += cf * v.y;
+          }
+        }
+        reinterpret_cast<double2*>(a.out[o] + mem * a.ostr)[i2] = make_double2(a0, a1);
+        m[o] = max(m[o], max(abs_key(a0), abs_key(a1)));
+        if (o == 1) {
+          s[0] += a0 * a0;
+          s[0] += a1 * a1;
+        }
       }
-      a.out[o][mem * a.ostr + i] = acc;
-      m[o] = max(m[o], abs_key(acc));
-      if (o == 1) s[0] += acc * acc;
+    }
+  } else {
+    for (long long i = t0; i < n; i += stride) {
+      for (int o = 0; o < a.nout; ++o) {
+        double acc = 0.0;
+        for (int t = 0; t < a.nterm[o]; ++t) {
+          const double* src = a.src[o][t];
+          if (src) acc += coef[a.idx[o][t]] * src[mem * a.sstr[o][t] + i];
+        }
+        a.out[o][mem * a.ostr + i] = acc;
+        m[o] = max(m[o], abs_key(acc));
+        if (o == 1) s[0] += acc * acc;
+      }
     }
   }
   block_max_key<2>(m, redk);
@@ -92,11 +124,28 @@ __global__ void __launch_bounds__(kThreads) k_dots3(const double* N, const doubl
   const double* W = V + n;
   partial += mem * kPartStride;
   double s[3] = {0, 0, 0};
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double nv = N[i], w = W[i];
-    s[0] += nv * V[i];
-    s[1] += nv * w;
-    s[2] += w * w;
+  const long long stride = (long long)gridDim.x * blockDim.x, t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const bool vec = (n & 1) == 0 && ((reinterpret_cast<unsigned long long>(N) | reinterpret_cast<unsigned long long>(V)) & 15) == 0;
+  if (vec) {  // pairs on 16-byte vectors
+    const double2* N2 = reinterpret_cast<const double2*>(N);
+    const double2* V2 = reinterpret_cast<const double2*>(V);
+    const double2* W2 = reinterpret_cast<const double2*>(W);
+    for (long long i = t0; i < (n >> 1); i += stride) {
+      const double2 nv = N2[i], v = V2[i], w = W2[i];
+      s[0] += nv.x * v.x;
+      s[1] += nv.x * w.x;
+      s[2] += w.x * w.x;
+      s[0] += nv.y * v.y;
+      s[1] += nv.y * w.y;
+      s[2] += w.y * w.y;
+    }
+  } else {
+    for (long long i = t0; i < n; i += stride) {
+      const double nv = N[i], w = W[i];
+      s[0] += nv * V[i];
+      s[1] += nv * w;
+      s[2] += w * w;
+    }
   }
   block_sum<3>(s, red);
   if (threadIdx.x == 0)
@@ -129,14 +178,48 @@ __global__ void __launch_bounds__(kThreads) k_recombine(GridDev g, const double*
   const double cpl = sav ? rec->coupling : 0.0;
   const double resp = dt * cpl;
   double s[1] = {0.0};
-  const int n = g.size > g.np ? g.size : g.np;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    if (i < g.size) {
-      const double u = sav ? VW[i] - resp * VW[g.size + i] : VW[i];
-      U[i] = u;
-      if (sav) s[0] += N[i] * u;
+  const long long stride = (long long)gridDim.x * blockDim.x, t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const unsigned long long ptrs = reinterpret_cast<unsigned long long>(VW) | reinterpret_cast<unsigned long long>(PI) |
+                                  reinterpret_cast<unsigned long long>(N) | reinterpret_cast<unsigned long long>(U) |
+                                  reinterpret_cast<unsigned long long>(pi);
+  if ((g.size & 1) == 0 && (g.np & 1) == 0 && (ptrs & 15) == 0) {  // pairs on 16-byte vectors
+    const double2* V2 = reinterpret_cast<const double2*>(VW);
+    const double2* W2 = reinterpret_cast<const double2*>(VW + g.size);
+    const double2* N2 = reinterpret_cast<const double2*>(N);
+    double2* U2 = reinterpret_cast<double2*>(U);
+    for (long long i = t0; i < (g.size >> 1); i += stride) {
+      const double2 v = V2[i];
+      double2 u = v;
+      if (sav) {
+        const double2 w = W2[i], nn = N2[i];
+        u = make_double2(v.x - resp * w.x, v.y - resp * w.y);
+        s[0] += nn.x * u.x;
+        s[0] += nn.y * u.y;
+      }
+      U2[i] = u;
     }
-    if (i < g.np) pi[i] = sav ? PI[i] / dt - cpl * PI[g.np + i] : PI[i] / dt;
+    const double2* P2 = reinterpret_cast<const double2*>(PI);
+    const double2* Q2 = reinterpret_cast<const double2*>(PI + g.np);
+    double2* pi2 = reinterpret_cast<double2*>(pi);
+    for (long long i = t0; i < (g.np >> 1); i += stride) {
+      const double2 a = P2[i];
+      if (sav) {
+        const double2 b = Q2[i];
+        pi2[i] = make_double2(a.x / dt - cpl * b.x, a.y / dt - cpl * b.y);
+      } else {
+        pi2[i] = make_double2(a.x / dt, a.y / dt);
+      }
+    }
+  } else {
+    const int n = g.size > g.np ? g.size : g.np;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      if (i < g.size) {
+        const double u = sav ? VW[i] - resp * VW[g.size + i] : VW[i];
+        U[i] = u;
+        if (sav) s[0] += N[i] * u;
+      }
+      if (i < g.np) pi[i] = sav ? PI[i] / dt - cpl * PI[g.np + i] : PI[i] / dt;
+    }
   }
   block_sum<1>(s, red);
   if (threadIdx.x == 0) partial[blockIdx.x] = s[0];

@@ -28,6 +28,12 @@ inline int red_blocks(long long n) {
   long long b = (n + kThreads - 1) / kThreads;
   return int(b < 1 ? 1 : (b > g_red_cap ? g_red_cap : b));
 }
+// Light kernels without a block reduction take one element (or one 16-byte
+// vector) per thread: the whole range in flight at once, up to full occupancy.
+inline int flat_blocks(long long n) {
+  long long b = (n + kThreads - 1) / kThreads;
+  return int(b < 1 ? 1 : (b > 65535 ? 65535 : b));
+}
 #ifndef MACSAV_RED_PER_SM
 #define MACSAV_RED_PER_SM 2
 #endif
@@ -735,7 +741,7 @@ static void finish_pressure(Plan* P, const Exec& X, const T* x, double* pres, in
                                                         make_fin<double>(P, X, OP_MEAN_X, rb, 1, cols), done);
   launch_k(k_center_cells<T>, dim3(rb, cols), kThreads, 0, s, P->g.np, x, np, pres, np, P->cg, 1, part,
                                                         make_fin<double>(P, X, OP_MEAN_X, rb, 1, cols), done);
-  launch_k(k_shift_cells, dim3(rb, cols), kThreads, 0, s, P->g.np, pres, np, P->cg);
+  launch_k(k_shift_cells, dim3(flat_blocks(np), cols), kThreads, 0, s, P->g.np, pres, np, P->cg);
   P->launches += 3;
 }
 
@@ -1047,10 +1053,10 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
   float* ru_lo = ru_hi + sz * cols;
   float* rd_hi = reinterpret_cast<float*>(P->cells);
   float* rd_lo = rd_hi + np * cols;
-  const int nbm = red_blocks(sz > np ? sz : np);
   for (int sweep = 0; sweep <= P->corrections; ++sweep) {
     if (sweep > 0) {
-      launch_k(k_defect_update, dim3(nbm, cols), kThreads, 0, X.s, g, sweep == 1 ? f : nullptr,
+      launch_k(k_defect_update, dim3(red_blocks(sz > np ? sz : np), cols), kThreads, 0, X.s, g,
+               sweep == 1 ? f : nullptr,
                static_cast<const float*>(P->wacc32 + (sweep - 1) * sz * cols),
                static_cast<const float*>(P->xpieces + (sweep - 1) * np * cols), P->shift, ru_hi, ru_lo, rd_hi, rd_lo);
       ++P->launches;
@@ -1058,7 +1064,8 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
     int rc = inner_solve32(P, X, sweep == 0 ? f : nullptr, ru_hi, sweep == 0 ? nullptr : rd_hi, cols, sweep);
     if (rc != MACSAV_OK) return rc;
   }
-  launch_k(k_sum_pieces, dim3(nbm, cols), kThreads, 0, X.s, static_cast<const float*>(P->wacc32), vel, sz,
+  launch_k(k_sum_pieces, dim3(flat_blocks(sz / 4 + 1), cols), kThreads, 0, X.s, static_cast<const float*>(P->wacc32),
+           vel, sz,
            static_cast<const float*>(P->xpieces), pres, np, cols, P->corrections + 1);
   ++P->launches;
   // mean-zero pressure and the FP64 closing checks, as in the FP64 path
