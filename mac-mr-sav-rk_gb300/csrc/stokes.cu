@@ -1055,8 +1055,10 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
   float* rd_lo = rd_hi + np * cols;
   for (int sweep = 0; sweep <= P->corrections; ++sweep) {
     if (sweep > 0) {
-      launch_k(k_defect_update, dim3(red_blocks(sz > np ? sz : np), cols), kThreads, 0, X.s, g,
-               sweep == 1 ? f : nullptr,
+      // no block reduction: four times the reduction kernels' blocks fill the
+      // SMs (a few elements per thread keep its set-up amortised)
+      launch_k(k_defect_update, dim3(std::min(4 * red_blocks(sz > np ? sz : np), flat_blocks(sz > np ? sz : np)), cols),
+               kThreads, 0, X.s, g, sweep == 1 ? f : nullptr,
                static_cast<const float*>(P->wacc32 + (sweep - 1) * sz * cols),
                static_cast<const float*>(P->xpieces + (sweep - 1) * np * cols), P->shift, ru_hi, ru_lo, rd_hi, rd_lo);
       ++P->launches;
