@@ -380,17 +380,40 @@ __global__ void __launch_bounds__(kThreads) k_fcg_z(int np, float* z, const floa
   pdl_wait();
   const int c = blockIdx.y;
   Acc<float> a[5];
+  auto take = [&](float zn, float rv, float ro) {
+    a[0].add(zn);
+    a[1].add(rv * zn);
+    a[2].add(ro * zn);
+    a[3].add(rv);
+    a[4].add(ro);
+  };
   if (active[c]) {
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
-      const long long k = c * cs + idx;
-      const float zn = add ? z[k] + add[k] : z[k];
-      z[k] = zn;
-      const float rv = r[k], ro = r_old[k];
-      a[0].add(zn);
-      a[1].add(rv * zn);
-      a[2].add(ro * zn);
-      a[3].add(rv);
-      a[4].add(ro);
+    const long long stride = (long long)gridDim.x * blockDim.x, t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if ((np & 3) == 0 && (cs & 3) == 0) {  // 16-byte vectors of four cells
+      float4* z4 = reinterpret_cast<float4*>(z + c * cs);
+      const float4* a4 = add ? reinterpret_cast<const float4*>(add + c * cs) : nullptr;
+      const float4* r4 = reinterpret_cast<const float4*>(r + c * cs);
+      const float4* o4 = reinterpret_cast<const float4*>(r_old + c * cs);
+      for (long long i = t0; i < (np >> 2); i += stride) {
+        float4 zn = z4[i];
+        if (a4) {
+          const float4 ad = a4[i];
+          zn = make_float4(zn.x + ad.x, zn.y + ad.y, zn.z + ad.z, zn.w + ad.w);
+          z4[i] = zn;
+        }
+        const float4 rv = r4[i], ro = o4[i];
+        take(zn.x, rv.x, ro.x);
+        take(zn.y, rv.y, ro.y);
+        take(zn.z, rv.z, ro.z);
+        take(zn.w, rv.w, ro.w);
+      }
+    } else {
+      for (long long idx = t0; idx < np; idx += stride) {
+        const long long k = c * cs + idx;
+        const float zn = add ? z[k] + add[k] : z[k];
+        z[k] = zn;
+        take(zn, r[k], r_old[k]);
+      }
     }
   }
   write_sums<float, 5>(a, partial, 5);
@@ -473,10 +496,29 @@ __global__ void __launch_bounds__(kThreads) k_center_cells(int np, const T* x, l
   const int c = blockIdx.y;
   const double mean = center ? cg[c].mean_q : 0.0;
   Acc<double> acc[1];
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
-    const double v = double(x[c * xs + idx]) - mean;
-    if (out) out[c * os + idx] = v;
-    acc[0].add(v);
+  const long long stride = (long long)gridDim.x * blockDim.x, t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  bool vec = false;
+  if constexpr (sizeof(T) == 8) {  // pairs on 16-byte vectors
+    vec = (np & 1) == 0 && (xs & 1) == 0 && (os & 1) == 0 &&
+          ((reinterpret_cast<unsigned long long>(x) | reinterpret_cast<unsigned long long>(out)) & 15) == 0;
+    if (vec) {
+      const double2* x2 = reinterpret_cast<const double2*>(x + c * xs);
+      double2* o2 = out ? reinterpret_cast<double2*>(out + c * os) : nullptr;
+      for (long long i = t0; i < (np >> 1); i += stride) {
+        const double2 xv = x2[i];
+        const double2 v = make_double2(xv.x - mean, xv.y - mean);
+        if (o2) o2[i] = v;
+        acc[0].add(v.x);
+        acc[0].add(v.y);
+      }
+    }
+  }
+  if (!vec) {
+    for (long long idx = t0; idx < np; idx += stride) {
+      const double v = double(x[c * xs + idx]) - mean;
+      if (out) out[c * os + idx] = v;
+      acc[0].add(v);
+    }
   }
   write_sums<double, 1>(acc, partial, 1);
   last_block_finish(fin, done);
