@@ -928,7 +928,8 @@ def profile_pass(workload: str, pass_id: int) -> None:
     model.plan.check(lib.load().macsav_time_pass(model.plan.handle, pass_id, 3, C.byref(ms_k), C.byref(bytes_k),
                                                  stokes.stream_handle()))
     torch.cuda.synchronize()
-    print(json.dumps({"profile": "pass", "pass": pass_id, "workload": w["workload"], "bytes": bytes_k.value}))
+    print(json.dumps({"profile": "pass", "pass": pass_id, "workload": w["workload"], "bytes": bytes_k.value,
+                      "ms_per_launch": ms_k.value}))
 
 
 CHANNEL = {"workload": "channel512_fft_stokes", "nx": 512, "ny": 512, "lx": 6.283185307179586, "ly": 1.0,

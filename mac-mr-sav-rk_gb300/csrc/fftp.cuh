@@ -50,9 +50,22 @@ inline size_t p2_smem(int L, int lines) {
 // ones).  XOR-ing bits 0-2 with bits 3-5 and bit 3 with bit 6 makes every
 // pass's loads and stores conflict-free (16 threads of 8 bytes or 8 threads
 // of 16 bytes per shared-memory wavefront).
+// Bits 3-6 of i XOR-ed into bits 0-3: a GF(2)-linear map, so for bit-disjoint
+// a and b (a + b = a ^ b) swz(a + b) = swz(a) ^ swz(b), and swz(b) = b when b
+// is a multiple of 128.  The Stockham passes use this to fold the compile-time
+// part of every shared address into a constant (an immediate offset where the
+// constant is a multiple of 128, one XOR otherwise).
+__host__ __device__ constexpr int swz(int i) { return i ^ ((i >> 3) & 15); }
 struct SwIx {
-  __device__ __forceinline__ int operator()(int i) const { return i ^ ((i >> 3) & 7) ^ (((i >> 6) & 1) << 3); }
+  __device__ __forceinline__ int operator()(int i) const { return swz(i); }
 };
+
+// swz(b + C) for b bit-disjoint from the constant C (C's lowest set bit above b).
+template <int STEP>
+__device__ __forceinline__ int swz_plus(int sb, int c) {
+  if constexpr (STEP % 128 == 0) return sb + c;
+  else return sb ^ swz(c);
+}
 
 template <typename T, int SIGN>
 __device__ __forceinline__ cplx<T> tw_at(const cplx<T>* __restrict__ tw, int m) {
@@ -122,10 +135,12 @@ __device__ __forceinline__ void fft_p2(cplx<T>* z, int t, const cplx<T>* __restr
   if (own) {
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
+      // j < STRIDE and r * STRIDE share no bits, so swz(j + r STRIDE) folds
       const int j = t + q * G;
       const int k = j & (NS - 1);
+      const int sj = ix(j);
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[q][r] = z[ix(j + r * STRIDE)];
+      for (int r = 0; r < R; ++r) v[q][r] = z[swz_plus<STRIDE>(sj, r * STRIDE)];
       if constexpr (NS > 1) {
 #pragma unroll
         for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], tw_at<T, SIGN>(tw, r * k * TWS));
@@ -139,9 +154,10 @@ __device__ __forceinline__ void fft_p2(cplx<T>* z, int t, const cplx<T>* __restr
     for (int q = 0; q < NB; ++q) {
       const int j = t + q * G;
       const int k = j & (NS - 1);
-      const int base = (j - k) * R + k;
+      // (j - k) R is a multiple of NS R and k < NS: r * NS shares no bits
+      const int sb = ix((j - k) * R + k);
 #pragma unroll
-      for (int r = 0; r < R; ++r) z[ix(base + r * NS)] = v[q][r];
+      for (int r = 0; r < R; ++r) z[swz_plus<NS>(sb, r * NS)] = v[q][r];
     }
   }
   __syncthreads();
@@ -329,10 +345,13 @@ __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const
       if (e < totv) {
         const int n = B.fvpr.div(e), jv = e - n * vpr;
         const T* comp = reinterpret_cast<const T*>(&v[u]);
+        // columns (2h, 2h + 1) of the vector are the real and imaginary parts of one line
 #pragma unroll
-        for (int k = 0; k < V; ++k) {
-          const int j = jv * V + k;
-          if (j < 2 * nl) put_real(z + (j >> 1) * L, kind, N, n, j & 1, j < ncols ? comp[k] : T(0), SwIx{});
+        for (int h = 0; h < V / 2; ++h) {
+          const int j = jv * V + 2 * h;
+          if (j < 2 * nl)
+            put_pair(z + (j >> 1) * L, kind, N, n, j < ncols ? comp[2 * h] : T(0),
+                     j + 1 < ncols ? comp[2 * h + 1] : T(0), SwIx{});
         }
       }
     }
