@@ -909,11 +909,13 @@ def profile_tgemm() -> None:
     print(json.dumps({"profile": "tgemm", "n": 512, "rows": 1024}))
 
 
-def profile_pass(workload: str, pass_id: int) -> None:
-    """Three launches of one transform pass (macsav_time_pass: 0 the FP32
+def profile_pass(workload: str, pass_id: int, reps: int = 3) -> None:
+    """``reps`` launches of one transform pass (macsav_time_pass: 0 the FP32
     velocity column pass, 1 and 2 the FP32 velocity row forward and inverse
-    passes, 3 the FP64 column pass) on the workload's grid, after one
-    warm-up launch, for a DRAM-traffic capture of that kernel."""
+    passes, 3 the FP64 column pass, 4-6 passes 0-2 with each block's launch
+    shape inverted) on the
+    workload's grid, after one warm-up launch, for a capture of that kernel
+    and its average time per launch (graph replay)."""
     import torch
     import __graft_entry__
     from importlib import import_module
@@ -925,7 +927,7 @@ def profile_pass(workload: str, pass_id: int) -> None:
     g = pkg.MACGrid(w["nx"], w["ny"], w["lx"], w["ly"])
     model = pkg.MACNavierStokes(g, w["nu"], precision="fp64" if pass_id == 3 else "fp32")
     ms_k, bytes_k = C.c_double(), C.c_double()
-    model.plan.check(lib.load().macsav_time_pass(model.plan.handle, pass_id, 3, C.byref(ms_k), C.byref(bytes_k),
+    model.plan.check(lib.load().macsav_time_pass(model.plan.handle, pass_id, reps, C.byref(ms_k), C.byref(bytes_k),
                                                  stokes.stream_handle()))
     torch.cuda.synchronize()
     print(json.dumps({"profile": "pass", "pass": pass_id, "workload": w["workload"], "bytes": bytes_k.value,
@@ -1012,7 +1014,7 @@ def main() -> None:
     ap.add_argument("--workload", choices=["learned1024", "cavity512", "ensemble256", "adaptive2048", "channel512"],
                     default="learned1024")
     ap.add_argument("--profile", choices=["fp32", "fp64", "learned", "unet", "pass0", "pass1", "pass2", "pass3",
-                                          "transform32", "tgemm"],
+                                          "pass4", "pass5", "pass6", "transform32", "tgemm"],
                     default=None,
                     help="run two eager steps of the workload (or launches of one transform pass) and exit, "
                          "for ncu captures")
@@ -1029,8 +1031,8 @@ def main() -> None:
     if args.profile == "tgemm":
         profile_tgemm()
         return
-    if args.profile in ("pass0", "pass1", "pass2", "pass3"):
-        profile_pass(args.workload, int(args.profile[-1]))
+    if args.profile in ("pass0", "pass1", "pass2", "pass3", "pass4", "pass5", "pass6"):
+        profile_pass(args.workload, int(args.profile[-1]), args.steps if args.steps > 0 else 3)
         return
     if args.profile:
         profile_steps(args.profile, args.workload)

@@ -442,7 +442,10 @@ int macsav_set_programmatic_launch(int enable);
  * back-to-back launches of one transform pass over the velocity blocks with two
  * right-hand sides, and the pass's algorithmic bytes per launch.
  * pass 0: FP32 column pass, 1: FP32 forward row pass, 2: FP32 inverse row pass
- * (these need a MACSAV_FP32_MIXED plan), 3: FP64 column pass.  Synchronises. */
+ * (these need a MACSAV_FP32_MIXED plan), 3: FP64 column pass, 4, 5, 6: passes
+ * 0, 1, 2 with each block's launch shape inverted (the split launch, half the
+ * threads per line with two butterflies per thread and pass, where the plan
+ * does not use it, and the plain one where it does).  Synchronises. */
 int macsav_time_pass(macsav_plan* plan, int pass, int reps, double* ms, double* bytes, void* stream);
 
 /* FP32_MIXED only (no reference counterpart: the reference solves in FP64):

@@ -36,6 +36,20 @@ inline int p2_threads_per_line(const TBlockDev<T>& B, int L, int lines) {
   return twice ? 2 * G : G;
 }
 
+// Split launch of a pass of length L: L/16 threads per line, each owning two
+// radix-8 butterflies per Stockham pass (FP32, L from 1024 to 4096; the flag
+// is the block's choice for that direction).  Measured on GB300 (1024^2,
+// two right-hand sides): the DST-I column pass of the v block (L = 2048) takes
+// 32.5 us split against 39.7 us with L/8 threads (two waves of 512-thread CTAs
+// at 44 registers become one of 256-thread CTAs), the DST-II column pass of
+// the u block (L = 1024, already one wave) 27.2 against 26.4 us, and at
+// 512^2 the split L = 1024 pass is twice as slow (a quarter of the doubled
+// threads); so blocks choose it for L >= 2048.
+template <typename T>
+inline bool p2_split(int flag, int L) {
+  return flag && sizeof(T) == 4 && L >= 1024 && L <= 4096;
+}
+
 // Shared bytes of a CTA holding `lines` lines of length L.
 template <typename T>
 inline size_t p2_smem(int L, int lines) {
@@ -118,16 +132,18 @@ __device__ __forceinline__ void dftR(cplx<T> (&v)[R]) {
   }
 }
 
-// Stockham passes on one (swizzled) line z by its first G = L/8 threads;
-// thread t < G owns butterflies j = t + q G, threads t >= G (doubled
+// Stockham passes on one (swizzled) line z by its first G threads (L/8, or
+// L/16 for the split launches, whose threads own two radix-8 butterflies per
+// pass); thread t < G owns butterflies j = t + q G, threads t >= G (doubled
 // launches) only join the barriers.  Every thread of the CTA must call this
-// (two block barriers per pass).
-template <typename T, int L, int NS, int SIGN>
+// (two block barriers per pass).  Which thread computes a butterfly does not
+// change its arithmetic, so every G gives the same bits.
+template <typename T, int L, int NS, int SIGN, int G = L / kE>
 __device__ __forceinline__ void fft_p2(cplx<T>* z, int t, const cplx<T>* __restrict__ tw) {
   constexpr int R = (L / NS >= kE) ? kE : L / NS;
-  constexpr int G = L / kE;
-  constexpr int NB = kE / R;
+  constexpr int NB = (L / R) / G;
   constexpr int STRIDE = L / R;
+  static_assert(NB * G == L / R, "threads per line must divide the butterflies of every pass");
   constexpr int TWS = L / (NS * R);
   const SwIx ix;
   cplx<T> v[NB][R];
@@ -161,12 +177,12 @@ __device__ __forceinline__ void fft_p2(cplx<T>* z, int t, const cplx<T>* __restr
     }
   }
   __syncthreads();
-  if constexpr (NS * R < L) fft_p2<T, L, NS * R, SIGN>(z, t, tw);
+  if constexpr (NS * R < L) fft_p2<T, L, NS * R, SIGN, G>(z, t, tw);
 }
 
 // ------------------------------------------------------------ row passes ---
 // One block (u, v or p) per launch; NL = blockDim.x / B.tpl line pairs per CTA.
-template <typename T, int L, class Src>
+template <typename T, int L, class Src, int GT = L / kE>
 __global__ void __launch_bounds__(kFFTThreads) k_row_forward_p2(TBlockDev<T> B, const int* active, Src src, int bk) {
   pdl_wait();
   const int c = blockIdx.y;
@@ -205,7 +221,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_forward_p2(TBlockDev<T> B, 
   if (kind == KIND_DST1)
     for (int q = threadIdx.x; q < npairs; q += blockDim.x) zero_dst1_ends(z + q * L, N, SwIx{});
   __syncthreads();
-  fft_p2<T, L, 1, -1>(z + (threadIdx.x / TPL) * L, threadIdx.x % TPL, tw);
+  fft_p2<T, L, 1, -1, GT>(z + (threadIdx.x / TPL) * L, threadIdx.x % TPL, tw);
   T* H = B.H + c * B.hstride;
   for (int e = threadIdx.x; e < total; e += blockDim.x) {
     const int q = B.fcols.div(e), k = e - q * N;
@@ -217,7 +233,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_forward_p2(TBlockDev<T> B, 
   }
 }
 
-template <typename T, int L, class Dst, class Fin>
+template <typename T, int L, class Dst, class Fin, int GT = L / kE>
 __global__ void __launch_bounds__(kFFTThreads) k_row_inverse_p2(TBlockDev<T> B, const int* active, Dst dst, int bk,
                                                                 double* partial, Fin fin, unsigned int* counter) {
   pdl_wait();
@@ -268,8 +284,8 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_inverse_p2(TBlockDev<T> B, 
       for (int q = threadIdx.x; q < npairs; q += blockDim.x) zero_dst1_ends(z + q * L, N, SwIx{});
       __syncthreads();
     cplx<T>* za = z + (threadIdx.x / TPL) * L;
-    if (kind == KIND_DST1) fft_p2<T, L, 1, -1>(za, threadIdx.x % TPL, tw);
-    else fft_p2<T, L, 1, 1>(za, threadIdx.x % TPL, tw);
+    if (kind == KIND_DST1) fft_p2<T, L, 1, -1, GT>(za, threadIdx.x % TPL, tw);
+    else fft_p2<T, L, 1, 1, GT>(za, threadIdx.x % TPL, tw);
       for (int base = threadIdx.x; base < total; base += kStage * blockDim.x) {
       typename Dst::aux_t xa[kStage], xb[kStage];
 #pragma unroll
@@ -299,8 +315,9 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_inverse_p2(TBlockDev<T> B, 
 }
 
 // ----------------------------------------------------------- column pass ---
-// NL = blockDim.x / (L/8) complex lines = W = 2 NL columns per CTA.
-template <typename T, int L>
+// NL = blockDim.x / B.tpl complex lines = W = 2 NL columns per CTA; GT
+// threads per line compute the FFTs (L/8, or L/16 for the split launch).
+template <typename T, int L, int GT = L / kE>
 __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const int* active, int mode,
                                                           const double* shift, T thr) {
   pdl_wait();
@@ -360,7 +377,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const
     for (int q = threadIdx.x; q < nl; q += blockDim.x) zero_dst1_ends(z + q * L, N, SwIx{});
   __syncthreads();
   const int line = threadIdx.x / TPL, t = threadIdx.x % TPL;
-  fft_p2<T, L, 1, -1>(z + line * L, t, tw);
+  fft_p2<T, L, 1, -1, GT>(z + line * L, t, tw);
   if (kind == KIND_DST1) {
     for (int e = threadIdx.x; e < nl * N; e += blockDim.x) {
       const int q = B.frows.div(e), k = e - q * N;
@@ -405,8 +422,8 @@ __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const
     }
   }
   __syncthreads();
-  if (kind == KIND_DST1) fft_p2<T, L, 1, -1>(z + line * L, t, tw);
-  else fft_p2<T, L, 1, 1>(z + line * L, t, tw);
+  if (kind == KIND_DST1) fft_p2<T, L, 1, -1, GT>(z + line * L, t, tw);
+  else fft_p2<T, L, 1, 1, GT>(z + line * L, t, tw);
   if (vec && ncols == W) {
     for (int e = threadIdx.x; e < totv; e += blockDim.x) {
       const int n = B.fvpr.div(e), jv = e - n * vpr;
@@ -440,6 +457,17 @@ inline bool is_p2_length(int L) { return L >= 64 && L <= 4096 && (L & (L - 1)) =
     case 2048: CALL(2048); break; \
     case 4096: CALL(4096); break; \
     default: break;               \
+  }
+
+// The split launches (p2_split), FP32 only: CALL(L, threads per line).
+#define MACSAV_SPLIT_SWITCH(L, CALL)                 \
+  if constexpr (sizeof(T) == 4) {                    \
+    switch (L) {                                     \
+      case 1024: CALL(1024, 64); break;              \
+      case 2048: CALL(2048, 128); break;             \
+      case 4096: CALL(4096, 256); break;             \
+      default: break;                                \
+    }                                                \
   }
 
 }  // namespace macsav

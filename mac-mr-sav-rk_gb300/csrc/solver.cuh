@@ -410,51 +410,75 @@ struct Launcher {
   // One specialised pass over block B (bk: 0 = u or the only block, 1 = v) on stream st.
   template <class Src>
   void row_forward_p2(const TBlockDev<T>& B, int bk, cudaStream_t st, Src src, int cols, const int* active) const {
-    const int P = p2_pairs(B), G = p2_threads_per_line<T>(B, B.fx.L, P);
+    const int P = p2_pairs(B);
+    const bool split = p2_split<T>(B.splitx, B.fx.L);
+    const int G = split ? B.fx.L / 16 : p2_threads_per_line<T>(B, B.fx.L, P);
     TBlockDev<T> Bl = B;
     Bl.tpl = G;
     const size_t sm = p2_smem<T>(B.fx.L, P);
-#define MACSAV_RF(LL)                                                          \
+#define MACSAV_RF(LL, GG)                                                      \
   {                                                                            \
-    auto k = k_row_forward_p2<T, LL, Src>;                                     \
+    auto k = k_row_forward_p2<T, LL, Src, GG>;                                 \
     set_smem(k, sm);                                                           \
     launch_k(k, dim3(row_grid(B), cols), P * G, sm, st, Bl, active, src, bk);  \
   }
-    MACSAV_P2_SWITCH(B.fx.L, MACSAV_RF)
+#define MACSAV_RF1(LL) MACSAV_RF(LL, LL / kE)
+    if (!split) {
+      MACSAV_P2_SWITCH(B.fx.L, MACSAV_RF1)
+    } else {
+      MACSAV_SPLIT_SWITCH(B.fx.L, MACSAV_RF)
+    }
+#undef MACSAV_RF1
 #undef MACSAV_RF
     ++*counter;
   }
   template <class Dst, class Fin>
   void row_inverse_p2(const TBlockDev<T>& B, int bk, cudaStream_t st, Dst dst, int cols, const int* active,
                       double* partial, Fin fin, unsigned int* done) const {
-    const int P = p2_pairs(B), G = p2_threads_per_line<T>(B, B.fx.L, P);
+    const int P = p2_pairs(B);
+    const bool split = p2_split<T>(B.splitx, B.fx.L);
+    const int G = split ? B.fx.L / 16 : p2_threads_per_line<T>(B, B.fx.L, P);
     TBlockDev<T> Bl = B;
     Bl.tpl = G;
     const size_t sm = p2_smem<T>(B.fx.L, P);
-#define MACSAV_RI(LL)                                                                                \
+#define MACSAV_RI(LL, GG)                                                                            \
   {                                                                                                  \
-    auto k = k_row_inverse_p2<T, LL, Dst, Fin>;                                                      \
+    auto k = k_row_inverse_p2<T, LL, Dst, Fin, GG>;                                                  \
     set_smem(k, sm);                                                                                 \
     launch_k(k, dim3(row_grid(B), cols), P * G, sm, st, Bl, active, dst, bk, partial, fin, done);  \
   }
-    MACSAV_P2_SWITCH(B.fx.L, MACSAV_RI)
+#define MACSAV_RI1(LL) MACSAV_RI(LL, LL / kE)
+    if (!split) {
+      MACSAV_P2_SWITCH(B.fx.L, MACSAV_RI1)
+    } else {
+      MACSAV_SPLIT_SWITCH(B.fx.L, MACSAV_RI)
+    }
+#undef MACSAV_RI1
 #undef MACSAV_RI
     ++*counter;
   }
   void column_p2(const TBlockDev<T>& B, cudaStream_t st, int cols, const int* active, int mode, const double* shift,
                  T thr) const {
-    const int NL = B.wy / 2, G = p2_threads_per_line<T>(B, B.fy.L, NL);
+    const int NL = B.wy / 2;
+    const bool split = p2_split<T>(B.splity, B.fy.L);
+    const int G = split ? B.fy.L / 16 : p2_threads_per_line<T>(B, B.fy.L, NL);
     TBlockDev<T> Bl = B;
     Bl.tpl = G;
     const size_t sm = p2_smem<T>(B.fy.L, NL);
     const int grid = (B.cols + B.wy - 1) / B.wy;
-#define MACSAV_CO(LL)                                                                  \
+#define MACSAV_CO(LL, GG)                                                              \
   {                                                                                    \
-    auto k = k_column_p2<T, LL>;                                                       \
+    auto k = k_column_p2<T, LL, GG>;                                                   \
     set_smem(k, sm);                                                                   \
     launch_k(k, dim3(grid, cols), NL * G, sm, st, Bl, active, mode, shift, thr);      \
   }
-    MACSAV_P2_SWITCH(B.fy.L, MACSAV_CO)
+#define MACSAV_CO1(LL) MACSAV_CO(LL, LL / kE)
+    if (!split) {
+      MACSAV_P2_SWITCH(B.fy.L, MACSAV_CO1)
+    } else {
+      MACSAV_SPLIT_SWITCH(B.fy.L, MACSAV_CO)
+    }
+#undef MACSAV_CO1
 #undef MACSAV_CO
     ++*counter;
   }

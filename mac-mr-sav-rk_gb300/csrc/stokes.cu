@@ -1125,12 +1125,21 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
 // a captured graph, with its algorithmic bytes per launch (each element of the
 // pass's input read once and output written once).
 //   pass 0: FP32 column pass; 1: FP32 forward row pass (FP64 packed input);
-//   2: FP32 inverse row pass; 3: FP64 column pass.
+//   2: FP32 inverse row pass; 3: FP64 column pass; 4, 5, 6: passes 0, 1, 2
+//   with each block's split-launch choice (p2_split) inverted.
 int time_pass(Plan* P, int pass, int reps, cudaStream_t user, double* ms, double* bytes) {
   const GridDev& g = P->g;
   const int cols = 2;
-  if (P->maxcols < 2 || reps < 1 || pass < 0 || pass > 3) return MACSAV_ERR_VALUE;
-  if (pass < 3 && P->precision != MACSAV_FP32_MIXED) return MACSAV_ERR_VALUE;
+  if (P->maxcols < 2 || reps < 1 || pass < 0 || pass > 6) return MACSAV_ERR_VALUE;
+  if (pass != 3 && P->precision != MACSAV_FP32_MIXED) return MACSAV_ERR_VALUE;
+  Transforms<float> t32 = P->t32;
+  if (pass >= 4) {
+    for (TBlockDev<float>* B : {&t32.u, &t32.v}) {
+      B->splitx ^= 1;
+      B->splity ^= 1;
+    }
+    pass -= 4;
+  }
   // a capturable stream of our own (the caller's may be the legacy stream),
   // ordered after the caller's work
   cudaStream_t s;
@@ -1144,12 +1153,13 @@ int time_pass(Plan* P, int pass, int reps, cudaStream_t user, double* ms, double
   cudaMemcpyAsync(P->shift, shift, sizeof shift, cudaMemcpyHostToDevice, s);
   const double n = double(g.size) * cols;
   auto run = [&]() {
-    if (pass == 0) Launcher<float>{P->t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.column_uv(cols, nullptr, P->shift);
+    if (pass == 0)
+      Launcher<float>{t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.column_uv(cols, nullptr, P->shift);
     else if (pass == 1)
-      Launcher<float>{P->t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.row_forward_uv(SrcPacked<float, double>{P->w, g.size, g.nu, g.nx - 1,
+      Launcher<float>{t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.row_forward_uv(SrcPacked<float, double>{P->w, g.size, g.nu, g.nx - 1,
                                                                                         g.nx}, cols, nullptr);
     else if (pass == 2)
-      Launcher<float>{P->t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.row_inverse_uv(DstPacked<float, float>{P->w32, g.size, g.nu,
+      Launcher<float>{t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.row_inverse_uv(DstPacked<float, float>{P->w32, g.size, g.nu,
                                                                                       g.nx - 1, g.nx}, cols, nullptr);
     else Launcher<double>{P->t64, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.column_uv(cols, nullptr, P->shift);
   };
