@@ -912,8 +912,8 @@ def profile_tgemm() -> None:
 def profile_pass(workload: str, pass_id: int, reps: int = 3) -> None:
     """``reps`` launches of one transform pass (macsav_time_pass: 0 the FP32
     velocity column pass, 1 and 2 the FP32 velocity row forward and inverse
-    passes, 3 the FP64 column pass, 4-6 passes 0-2 with each block's launch
-    shape inverted) on the
+    passes, 3 the FP64 column pass, 4-6 the FP32 pressure column, forward
+    and inverse row passes; pass // 10 forces a launch shape) on the
     workload's grid, after one warm-up launch, for a capture of that kernel
     and its average time per launch (graph replay)."""
     import torch
@@ -1014,10 +1014,12 @@ def main() -> None:
     ap.add_argument("--workload", choices=["learned1024", "cavity512", "ensemble256", "adaptive2048", "channel512"],
                     default="learned1024")
     ap.add_argument("--profile", choices=["fp32", "fp64", "learned", "unet", "pass0", "pass1", "pass2", "pass3",
-                                          "pass4", "pass5", "pass6", "transform32", "tgemm"],
+                                          "pass", "transform32", "tgemm"],
                     default=None,
                     help="run two eager steps of the workload (or launches of one transform pass) and exit, "
                          "for ncu captures")
+    ap.add_argument("--pass-id", type=int, default=0,
+                    help="--profile pass: macsav_time_pass's pass (pass %% 10) and launch shape (pass // 10)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -1031,8 +1033,9 @@ def main() -> None:
     if args.profile == "tgemm":
         profile_tgemm()
         return
-    if args.profile in ("pass0", "pass1", "pass2", "pass3", "pass4", "pass5", "pass6"):
-        profile_pass(args.workload, int(args.profile[-1]), args.steps if args.steps > 0 else 3)
+    if args.profile in ("pass0", "pass1", "pass2", "pass3", "pass"):
+        pass_id = args.pass_id if args.profile == "pass" else int(args.profile[-1])
+        profile_pass(args.workload, pass_id, args.steps if args.steps > 0 else 3)
         return
     if args.profile:
         profile_steps(args.profile, args.workload)

@@ -442,10 +442,12 @@ int macsav_set_programmatic_launch(int enable);
  * back-to-back launches of one transform pass over the velocity blocks with two
  * right-hand sides, and the pass's algorithmic bytes per launch.
  * pass 0: FP32 column pass, 1: FP32 forward row pass, 2: FP32 inverse row pass
- * (these need a MACSAV_FP32_MIXED plan), 3: FP64 column pass, 4, 5, 6: passes
- * 0, 1, 2 with each block's launch shape inverted (the split launch, half the
- * threads per line with two butterflies per thread and pass, where the plan
- * does not use it, and the plain one where it does).  Synchronises. */
+ * (these need a MACSAV_FP32_MIXED plan), 3: FP64 column pass, 4, 5, 6: the
+ * FP32 pressure-block column, forward row and inverse row passes (the Schur
+ * preconditioner's); pass + 10 s forces launch shape s on every block: 1 one
+ * radix-8 butterfly per thread and pass, 2 twice the threads per line, 3 half
+ * the threads per line with two butterflies each (0: the plan's own choice;
+ * FP32 passes only).  Synchronises. */
 int macsav_time_pass(macsav_plan* plan, int pass, int reps, double* ms, double* bytes, void* stream);
 
 /* FP32_MIXED only (no reference counterpart: the reference solves in FP64):
@@ -460,6 +462,13 @@ int macsav_plan_set_refinement(macsav_plan* plan, int corrections, double inner_
  * first solve leaves a smaller defect, so fewer sweeps reach the gates; like
  * the sweep count, a bad choice surfaces as the Stokes-gate error. */
 int macsav_plan_set_first_solve_tolerance(macsav_plan* plan, double first_krylov_tolerance);
+/* Launch shape of the plan's FP32 power-of-two transform passes (no reference
+ * counterpart: a tuning control): 0 each pass's own choice (the default),
+ * 1 one radix-8 butterfly per thread and Stockham pass, 2 twice the threads
+ * per line, 3 half the threads per line with two butterflies each (lengths
+ * 1024 to 4096; others fall back to 1).  Every shape computes the same bits;
+ * only the time differs.  Affects launches and captures after the call. */
+int macsav_plan_set_launch_shape(macsav_plan* plan, int shape);
 
 /* Run macsav_step as one captured CUDA graph per (scheme, force, embedded)
  * (the pressure CG loop becomes a conditional WHILE node).  Default: off. */

@@ -697,6 +697,14 @@ int macsav_plan_set_first_solve_tolerance(macsav_plan* plan, double first_krylov
   return MACSAV_OK;
 }
 
+int macsav_plan_set_launch_shape(macsav_plan* plan, int shape) {
+  if (!plan || shape < 0 || shape > 3) return MACSAV_ERR_VALUE;
+  for (macsav::TBlockDev<float>* B : {&plan->p.t32.u, &plan->p.t32.v, &plan->p.t32.p}) B->shapex = B->shapey = shape;
+  for (auto& kv : plan->p.st.graphs) cudaGraphExecDestroy(kv.exec);  // captured with the old shapes
+  plan->p.st.graphs.clear();
+  return MACSAV_OK;
+}
+
 int macsav_plan_set_graph(macsav_plan* plan, int enable) {
   if (!plan) return MACSAV_ERR_VALUE;
   plan->p.use_graph = enable ? 1 : 0;

@@ -9,17 +9,12 @@
 // and the post/pre-processing are the same as in the generic kernels
 // (transforms.cuh).
 //
-// Shared lines are stored bank-swizzled (SwIx below).  Small blocks (at most
-// 512 x 512, FP32) launch 2G threads per line: the packing and unpacking
-// loops, the longer dependent chains of these latency-bound passes, then run
-// on twice as many warps, while the extra threads only join the FFT
-// barriers (TBlockDev::tpl carries the launch's threads per line).
-// Measured on GB300 (512^2 sdirk3_mrsav step): the swizzle and the doubled
-// threads take the FP32 step from 4.74 to 4.63 ms and the swizzle the FP64
-// step from 11.54 to 11.13 ms; doubled threads slow the 1024^2 and 2048^2
-// passes (throughput-bound), so larger blocks keep G.  A ping-pong buffer
-// pair (one barrier per pass) and a shared copy of the twiddle table gave
-// nothing on top and are not used.
+// Shared lines are stored bank-swizzled (SwIx below).  Each launch picks a
+// shape (threads per line, p2_shape below; TBlockDev::tpl carries it).
+// Measured on GB300 (512^2 sdirk3_mrsav step): the swizzle takes the FP64
+// step from 11.54 to 11.13 ms.  A ping-pong buffer pair (one barrier per
+// pass) and a shared copy of the twiddle table gave nothing on top and are
+// not used.
 #pragma once
 #include "transforms.cuh"
 
@@ -27,27 +22,44 @@ namespace macsav {
 
 constexpr int kE = 8;  // elements per thread per line
 
-// Threads per line (pair) for a launch over block B with `lines` lines per
-// CTA: 2G for small FP32 blocks while the CTA stays within kFFTThreads.
+// Launch shape of a pass of length L over `lines` lines per CTA:
+//   P2_PLAIN    G = L/8 threads per line, one radix-8 butterfly per pass;
+//   P2_DOUBLED  2G threads per line; the packing and unpacking loops, the
+//               longer dependent chains of these latency-bound passes, run on
+//               twice the warps while the extra threads only join the FFT
+//               barriers (the CTA stays within kFFTThreads);
+//   P2_SPLIT    G/2 threads per line, two radix-8 butterflies per thread and
+//               pass (FP32, L from 1024 to 4096).
+// P2_AUTO picks by block: split for FP32 L >= 2048, doubled for FP32 blocks
+// of at most 512 x 512, plain otherwise.  Measured on GB300 (two right-hand
+// sides, u and v concurrently): at 1024^2 the split DST-I column pass of the
+// v block (L = 2048) takes 32.5 us against 39.7 us plain (two waves of
+// 512-thread CTAs at 44 registers become one of 256-thread CTAs), and the
+// velocity row-inverse pair 22.3 against 25.9 us; the split L = 1024 column
+// pass of the u block, already one wave, 27.2 against 26.4 us; at 512^2 the
+// doubled threads took the FP32 step from 4.74 to 4.63 ms (with the
+// swizzle) and the split L = 1024 column pass is twice as slow.  Which
+// thread computes a butterfly does not change its arithmetic: every shape
+// gives the same bits.
+enum P2Shape : int { P2_AUTO = 0, P2_PLAIN = 1, P2_DOUBLED = 2, P2_SPLIT = 3 };
+
 template <typename T>
-inline int p2_threads_per_line(const TBlockDev<T>& B, int L, int lines) {
+inline int p2_shape(const TBlockDev<T>& B, int L, int lines, int shape) {
   const int G = L / kE;
-  const bool twice = sizeof(T) == 4 && (long long)B.rows * B.cols <= 512LL * 512 && 2 * G * lines <= kFFTThreads;
-  return twice ? 2 * G : G;
+  const bool can_split = sizeof(T) == 4 && L >= 1024 && L <= 4096;
+  const bool can_double = 2 * G * lines <= kFFTThreads;
+  if (shape == P2_AUTO) {
+    if (can_split && L >= 2048) return P2_SPLIT;
+    if (sizeof(T) == 4 && (long long)B.rows * B.cols <= 512LL * 512 && can_double) return P2_DOUBLED;
+    return P2_PLAIN;
+  }
+  if ((shape == P2_SPLIT && !can_split) || (shape == P2_DOUBLED && !can_double)) return P2_PLAIN;
+  return shape;
 }
 
-// Split launch of a pass of length L: L/16 threads per line, each owning two
-// radix-8 butterflies per Stockham pass (FP32, L from 1024 to 4096; the flag
-// is the block's choice for that direction).  Measured on GB300 (1024^2,
-// two right-hand sides): the DST-I column pass of the v block (L = 2048) takes
-// 32.5 us split against 39.7 us with L/8 threads (two waves of 512-thread CTAs
-// at 44 registers become one of 256-thread CTAs), the DST-II column pass of
-// the u block (L = 1024, already one wave) 27.2 against 26.4 us, and at
-// 512^2 the split L = 1024 pass is twice as slow (a quarter of the doubled
-// threads); so blocks choose it for L >= 2048.
-template <typename T>
-inline bool p2_split(int flag, int L) {
-  return flag && sizeof(T) == 4 && L >= 1024 && L <= 4096;
+// Threads per line of a resolved shape.
+inline int p2_tpl(int L, int shape) {
+  return shape == P2_SPLIT ? L / 16 : (shape == P2_DOUBLED ? L / 4 : L / 8);
 }
 
 // Shared bytes of a CTA holding `lines` lines of length L.

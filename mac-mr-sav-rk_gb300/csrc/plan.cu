@@ -79,8 +79,7 @@ static cudaError_t build_block(TBlockDev<T>& B, int rows, int cols, int kx, int 
   B.px = pick_pairs(Lx, rows, sms);
   B.wy = pick_strip(Ly, cols, sms, int(sizeof(T)));
   B.tpl = Lx / 8;  // each specialised launch sets its own
-  B.splitx = Lx >= 2048 ? 1 : 0;  // p2_split: faster from L = 2048 on (FP32 only)
-  B.splity = Ly >= 2048 ? 1 : 0;
+  B.shapex = B.shapey = 0;  // P2_AUTO: each pass picks its launch shape
   B.fcols = FastDiv(cols);
   B.frows = FastDiv(rows);
   B.fw = FastDiv(B.wy);

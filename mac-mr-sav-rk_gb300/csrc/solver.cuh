@@ -411,8 +411,9 @@ struct Launcher {
   template <class Src>
   void row_forward_p2(const TBlockDev<T>& B, int bk, cudaStream_t st, Src src, int cols, const int* active) const {
     const int P = p2_pairs(B);
-    const bool split = p2_split<T>(B.splitx, B.fx.L);
-    const int G = split ? B.fx.L / 16 : p2_threads_per_line<T>(B, B.fx.L, P);
+    const int shape = p2_shape<T>(B, B.fx.L, P, B.shapex);
+    const bool split = shape == P2_SPLIT;
+    const int G = p2_tpl(B.fx.L, shape);
     TBlockDev<T> Bl = B;
     Bl.tpl = G;
     const size_t sm = p2_smem<T>(B.fx.L, P);
@@ -436,8 +437,9 @@ struct Launcher {
   void row_inverse_p2(const TBlockDev<T>& B, int bk, cudaStream_t st, Dst dst, int cols, const int* active,
                       double* partial, Fin fin, unsigned int* done) const {
     const int P = p2_pairs(B);
-    const bool split = p2_split<T>(B.splitx, B.fx.L);
-    const int G = split ? B.fx.L / 16 : p2_threads_per_line<T>(B, B.fx.L, P);
+    const int shape = p2_shape<T>(B, B.fx.L, P, B.shapex);
+    const bool split = shape == P2_SPLIT;
+    const int G = p2_tpl(B.fx.L, shape);
     TBlockDev<T> Bl = B;
     Bl.tpl = G;
     const size_t sm = p2_smem<T>(B.fx.L, P);
@@ -460,8 +462,9 @@ struct Launcher {
   void column_p2(const TBlockDev<T>& B, cudaStream_t st, int cols, const int* active, int mode, const double* shift,
                  T thr) const {
     const int NL = B.wy / 2;
-    const bool split = p2_split<T>(B.splity, B.fy.L);
-    const int G = split ? B.fy.L / 16 : p2_threads_per_line<T>(B, B.fy.L, NL);
+    const int shape = p2_shape<T>(B, B.fy.L, NL, B.shapey);
+    const bool split = shape == P2_SPLIT;
+    const int G = p2_tpl(B.fy.L, shape);
     TBlockDev<T> Bl = B;
     Bl.tpl = G;
     const size_t sm = p2_smem<T>(B.fy.L, NL);

@@ -787,6 +787,185 @@ static void finish_pressure(Plan* P, const Exec& X, const T* x, double* pres, in
   P->launches += 3;
 }
 
+// ------------------------------------------- double-float defect groups ---
+// The defect kernels below walk the packed velocity and the cells in groups
+// of four consecutive elements per thread (16-byte loads and stores of the
+// float pieces and pairs where the arrays allow it, one division per group,
+// the left and right neighbours of a face from the group's registers).
+//
+// Double-float coefficients of m u + k K u - D^T p and of D: m, k/hx^2,
+// k/hy^2, 1/hx, 1/hy (FP64 products rounded to double-float), formed once
+// per block.
+struct OpCoef {
+  df32 m, kx, ky, gx, gy;
+};
+__device__ __forceinline__ OpCoef op_coef(const GridDev& g, const double* shift, int c) {
+  __shared__ OpCoef sc;
+  if (threadIdx.x == 0) {
+    const double m = shift[2 * c], k = shift[2 * c + 1];
+    sc = OpCoef{d2df(m), d2df(k * g.ihx2), d2df(k * g.ihy2), d2df(g.ihx), d2df(g.ihy)};
+  }
+  __syncthreads();
+  return sc;
+}
+
+// s + c: a running double-float sum.  Each product of double-floats enters
+// as p = a.hi b.hi and its low part (the FMA error of p plus the cross terms,
+// rounded once: about 2^-48 of the product), the sum of p into s by an
+// error-free two-sum whose error joins c.  Each term then carries an error
+// of about 2^-48 of its own size, as a chain of double-float operations.
+struct DFSum {
+  float s, c;
+  __device__ __forceinline__ void add(float p, float pe) {
+    const df32 t = df_two_sum(s, p);
+    s = t.hi;
+    c += t.lo + pe;
+  }
+  __device__ __forceinline__ void add_mul(df32 a, df32 b) {
+    const float p = a.hi * b.hi;
+    add(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p))));
+  }
+  __device__ __forceinline__ void add_mul(df32 a, float b) {
+    const float p = a.hi * b;
+    add(p, fmaf(a.lo, b, fmaf(a.hi, b, -p)));
+  }
+  __device__ __forceinline__ df32 value() const {
+    const float h = s + c;
+    return {h, c - (h - s)};
+  }
+};
+
+// prev - (m u + k K u - D^T p) at one face: l, r, s, n its neighbours in x
+// and y (wall values already applied), xa - xb the pressure difference across
+// it.  The stencil differences are exact two-sums, so the error is relative
+// to the terms m u, k K u and D^T p, not to the neighbours.
+__device__ __forceinline__ df32 face_defect(const OpCoef& C, df32 prev, float cc, float l, float r, float s,
+                                            float n, float xa, float xb, bool ublk) {
+  const df32 ex = df_add(df_two_sum(cc, -l), df_two_sum(cc, -r));
+  const df32 ey = df_add(df_two_sum(cc, -s), df_two_sum(cc, -n));
+  DFSum a{prev.hi, prev.lo};
+  a.add_mul(df_neg(C.m), cc);
+  a.add_mul(df_neg(C.kx), ex);
+  a.add_mul(df_neg(C.ky), ey);
+  a.add_mul(ublk ? C.gx : C.gy, df_two_sum(xa, -xb));
+  return a.value();
+}
+
+// prev - D u at one cell from its four faces.
+__device__ __forceinline__ df32 cell_defect(const OpCoef& C, df32 prev, float ue, float uw, float vn, float vs) {
+  DFSum a{prev.hi, prev.lo};
+  a.add_mul(df_neg(C.gx), df_two_sum(ue, -uw));
+  a.add_mul(df_neg(C.gy), df_two_sum(vn, -vs));
+  return a.value();
+}
+
+// Four consecutive floats from p[i..i+3] (cnt of them valid, the rest 0):
+// one 16-byte load when vec and the group is whole.
+__device__ __forceinline__ void load4(const float* p, long long i, int cnt, bool vec, float (&v)[4]) {
+  if (vec && cnt == 4) {
+    const float4 t = *reinterpret_cast<const float4*>(p + i);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  } else {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) v[e] = e < cnt ? p[i + e] : 0.0f;
+  }
+}
+__device__ __forceinline__ void store4(float* p, long long i, int cnt, bool vec, const float (&v)[4]) {
+  if (vec && cnt == 4) {
+    *reinterpret_cast<float4*>(p + i) = make_float4(v[0], v[1], v[2], v[3]);
+  } else {
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (e < cnt) p[i + e] = v[e];
+  }
+}
+__device__ __forceinline__ void load4d(const double* p, long long i, int cnt, bool vec, double (&v)[4]) {
+  if (vec && cnt == 4) {
+    const double2 a = *reinterpret_cast<const double2*>(p + i), b = *reinterpret_cast<const double2*>(p + i + 2);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  } else {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) v[e] = e < cnt ? p[i + e] : 0.0;
+  }
+}
+
+// The defects of faces i0 .. i0 + cnt - 1 of one column (uc: its velocity
+// piece, xc: its pressure piece, prev: the defect before the piece).
+__device__ __forceinline__ void face_group(const GridDev& g, const OpCoef& C, const float* uc, const float* xc,
+                                           int i0, int cnt, bool vec, const df32 (&prev)[4], df32 (&out)[4]) {
+  float u[4];
+  load4(uc, i0, cnt, vec, u);
+  const float left = i0 > 0 ? uc[i0 - 1] : 0.0f;
+  const float right = i0 + 4 < g.size ? uc[i0 + 4] : 0.0f;
+  bool isu = i0 < g.nu;
+  int j, q;
+  if (isu) {
+    j = i0 / (g.nx - 1);
+    q = i0 - j * (g.nx - 1);
+  } else {
+    j = (i0 - g.nu) / g.nx;
+    q = i0 - g.nu - j * g.nx;
+  }
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int i = i0 + e;
+    if (e > 0) {
+      if (i == g.nu) {
+        isu = false;
+        j = 0;
+        q = 0;
+      } else if (++q == (isu ? g.nx - 1 : g.nx)) {
+        q = 0;
+        ++j;
+      }
+    }
+    if (e < cnt) {
+      const float cc = u[e];
+      const float lv = e > 0 ? u[e - 1] : left, rv = e < 3 ? u[e + 1] : right;
+      float l, r, s, n, xa, xb;
+      const int lc = j * g.nx + q;
+      if (isu) {
+        // K_at's wall rows: beyond a normal wall 0, beyond a tangential wall -u
+        const int w = g.nx - 1;
+        l = q > 0 ? lv : 0.0f;
+        r = q < w - 1 ? rv : 0.0f;
+        s = j > 0 ? uc[i - w] : -cc;
+        n = j < g.ny - 1 ? uc[i + w] : -cc;
+        xa = xc[lc];
+        xb = xc[lc + 1];
+      } else {
+        l = q > 0 ? lv : -cc;
+        r = q < g.nx - 1 ? rv : -cc;
+        s = j > 0 ? uc[i - g.nx] : 0.0f;
+        n = j < g.ny - 2 ? uc[i + g.nx] : 0.0f;
+        xa = xc[lc];
+        xb = xc[lc + g.nx];
+      }
+      out[e] = face_defect(C, prev[e], cc, l, r, s, n, xa, xb, isu);
+    }
+  }
+}
+
+// The divergence defects of cells i0 .. i0 + cnt - 1 of one column.
+__device__ __forceinline__ void cell_group(const GridDev& g, const OpCoef& C, const float* uc, int i0, int cnt,
+                                           const df32 (&prev)[4], df32 (&out)[4]) {
+  int j = i0 / g.nx, q = i0 - j * g.nx;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    if (e > 0 && ++q == g.nx) {
+      q = 0;
+      ++j;
+    }
+    if (e < cnt) {
+      const float* ur = uc + j * (g.nx - 1);
+      const float ue = q < g.nx - 1 ? ur[q] : 0.0f, uw = q > 0 ? ur[q - 1] : 0.0f;
+      const float vn = j < g.ny - 1 ? uc[g.nu + j * g.nx + q] : 0.0f;
+      const float vs = j > 0 ? uc[g.nu + (j - 1) * g.nx + q] : 0.0f;
+      out[e] = cell_defect(C, prev[e], ue, uw, vn, vs);
+    }
+  }
+}
+
 // Closing checks of an FP32-bulk solve (tensor_stokes.py:329-351, the same
 // key slots as k_stokes_check): the final defect m u + k K u - D^T p - f and
 // divergence D u of the FP64 fields are the defect pairs before the last
@@ -797,70 +976,92 @@ static void finish_pressure(Plan* P, const Exec& X, const T* x, double* pres, in
 // f, u and p are read from the FP64 arrays themselves.  f_prev: the Stokes
 // right-hand side when the last sweep was the first solve, else null (the
 // pairs hold the defect).
-__global__ void __launch_bounds__(kThreads) k_stokes_check_df(GridDev g, const double* f_prev, const float* u,
+__global__ void __launch_bounds__(kThreads, 4) k_stokes_check_df(GridDev g, const double* f_prev, const float* u,
                                                               const float* x, const float* ru_hi, const float* ru_lo,
                                                               const float* rd_hi, const float* rd_lo,
                                                               const double* vel, const double* pres, const double* f,
-                                                              const double* shift, double* partial,
+                                                              const double* shift, int vec, double* partial,
                                                               CGFin<double> fin, unsigned int* done) {
   pdl_wait();
   const int c = blockIdx.y;
-  const df32 mass = d2df(shift[2 * c]), visc = d2df(shift[2 * c + 1]);
-  const df32 ihx = d2df(g.ihx), ihy = d2df(g.ihy), ihx2 = d2df(g.ihx2), ihy2 = d2df(g.ihy2);
+  const OpCoef C = op_coef(g, shift, c);
   const long long su = c * (long long)g.size, sp = c * (long long)g.np;
   const float* uc = u + su;
   const float* xc = x + sp;
+  const bool first = f_prev != nullptr;  // then f_prev is f
   unsigned long long m[6] = {0, 0, 0, 0, 0, 0};
   constexpr unsigned long long kInf = 0x7ff0000000000000ull;
-  const int n = g.size > g.np ? g.size : g.np;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    if (i < g.size) {
-      const float cc = uc[i];
-      float l, r, s, nn;
-      df32 dt;
-      if (i < g.nu) {
-        const int w = g.nx - 1, j = i / w, q = i - j * w;
-        l = q > 0 ? uc[i - 1] : 0.0f;
-        r = q < w - 1 ? uc[i + 1] : 0.0f;
-        s = j > 0 ? uc[i - w] : -cc;
-        nn = j < g.ny - 1 ? uc[i + w] : -cc;
-        const int lc = j * g.nx + q;
-        dt = df_mul(df_two_sum(xc[lc], -xc[lc + 1]), ihx);
-      } else {
-        const int fi = i - g.nu, j = fi / g.nx, q = fi - j * g.nx;
-        l = q > 0 ? uc[i - 1] : -cc;
-        r = q < g.nx - 1 ? uc[i + 1] : -cc;
-        s = j > 0 ? uc[i - g.nx] : 0.0f;
-        nn = j < g.ny - 2 ? uc[i + g.nx] : 0.0f;
-        const int lc = j * g.nx + q;
-        dt = df_mul(df_two_sum(xc[lc], -xc[lc + g.nx]), ihy);
+  const int ngf = (g.size + 3) / 4, ngc = (g.np + 3) / 4, ng = ngf > ngc ? ngf : ngc;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ng; t += gridDim.x * blockDim.x) {
+    if (t < ngf) {
+      const int i0 = 4 * t, cnt = min(4, g.size - i0);
+      df32 prev[4], d[4];
+      {
+        // the FP64 fields' maxima and finiteness first, so that their values
+        // are dead before the defect arithmetic
+        double fv[4], vv[4];
+        load4d(f + su, i0, cnt, vec, fv);
+        load4d(vel + su, i0, cnt, vec, vv);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (e < cnt) {
+            const unsigned long long kf = abs_key(fv[e]), ku = abs_key(vv[e]);
+            m[1] = max(m[1], kf);
+            m[2] = max(m[2], ku);
+            if (kf >= kInf) m[4] = 1;
+            if (ku >= kInf) m[5] = 1;
+          }
+          if (first) prev[e] = d2df(fv[e]);
+        }
       }
-      const df32 kx = df_mul(df_add(df_two_sum(cc, -l), df_two_sum(cc, -r)), ihx2);
-      const df32 ky = df_mul(df_add(df_two_sum(cc, -s), df_two_sum(cc, -nn)), ihy2);
-      const df32 op = df_sub(df_add(df_mul(mass, df32{cc, 0.0f}), df_mul(visc, df_add(kx, ky))), dt);
-      const long long k = su + i;
-      const df32 prev = f_prev ? d2df(f_prev[k]) : df32{ru_hi[k], ru_lo[k]};
-      const df32 d = df_sub(prev, op);  // f - (m u + k K u - D^T p)
-      const unsigned long long kf = abs_key(f[k]), ku = abs_key(vel[k]);
-      m[0] = max(m[0], abs_key(f2d_bits(d.hi)));
-      m[1] = max(m[1], kf);
-      m[2] = max(m[2], ku);
-      if (kf >= kInf) m[4] = 1;
-      if (ku >= kInf) m[5] = 1;
+      if (!first) {
+        float hi[4], lo[4];
+        load4(ru_hi + su, i0, cnt, vec, hi);
+        load4(ru_lo + su, i0, cnt, vec, lo);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) prev[e] = df32{hi[e], lo[e]};
+      }
+      face_group(g, C, uc, xc, i0, cnt, vec, prev, d);
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (e < cnt) m[0] = max(m[0], abs_key(f2d_bits(d[e].hi)));
     }
-    if (i < g.np) {
-      const int j = i / g.nx, q = i - j * g.nx;
-      const float ue = q < g.nx - 1 ? uc[j * (g.nx - 1) + q] : 0.0f, uw = q > 0 ? uc[j * (g.nx - 1) + q - 1] : 0.0f;
-      const float vn = j < g.ny - 1 ? uc[g.nu + j * g.nx + q] : 0.0f, vs = j > 0 ? uc[g.nu + (j - 1) * g.nx + q] : 0.0f;
-      const df32 du = df_add(df_mul(df_two_sum(ue, -uw), ihx), df_mul(df_two_sum(vn, -vs), ihy));
-      const long long k = sp + i;
-      const df32 prev = f_prev ? df32{0.0f, 0.0f} : df32{rd_hi[k], rd_lo[k]};  // -D of the earlier pieces
-      m[3] = max(m[3], abs_key(f2d_bits(df_sub(prev, du).hi)));
-      if (abs_key(pres[k]) >= kInf) m[5] = 1;
+    if (t < ngc) {
+      const int i0 = 4 * t, cnt = min(4, g.np - i0);
+      double pv[4];
+      load4d(pres + sp, i0, cnt, vec, pv);
+      df32 prev[4], d[4];
+      if (first) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) prev[e] = df32{0.0f, 0.0f};
+      } else {
+        float hi[4], lo[4];
+        load4(rd_hi + sp, i0, cnt, vec, hi);
+        load4(rd_lo + sp, i0, cnt, vec, lo);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) prev[e] = df32{hi[e], lo[e]};
+      }
+      cell_group(g, C, uc, i0, cnt, prev, d);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if (e < cnt) {
+          m[3] = max(m[3], abs_key(f2d_bits(d[e].hi)));
+          if (abs_key(pv[e]) >= kInf) m[5] = 1;
+        }
+      }
     }
   }
   write_keys<6>(m, partial, 6, 0);
   last_block_finish(fin, done);
+}
+
+// 16-byte group loads in the defect kernels: every column's face and cell
+// ranges start on a 16-byte boundary (sizes multiples of four, aligned bases).
+static int defect_vec(const GridDev& g, std::initializer_list<const void*> ptrs) {
+  if (g.size % 4 || g.np % 4) return 0;
+  for (const void* p : ptrs)
+    if (reinterpret_cast<uintptr_t>(p) % 16) return 0;
+  return 1;
 }
 
 static void closing_checks(Plan* P, const Exec& X, const double* f, const double* vel, const double* pres, int cols,
@@ -876,10 +1077,14 @@ static void closing_checks(Plan* P, const Exec& X, const double* f, const double
     const long long sz = g.size, np = g.np;
     const float* ru_hi = reinterpret_cast<const float*>(P->w);
     const float* rd_hi = reinterpret_cast<const float*>(P->cells);
-    launch_k(k_stokes_check_df, dim3(rb, cols), kThreads, 0, X.s, g, last == 0 ? f : nullptr,
-             static_cast<const float*>(P->wacc32 + last * sz * cols),
-             static_cast<const float*>(P->xpieces + last * np * cols), ru_hi, ru_hi + sz * cols, rd_hi,
-             rd_hi + np * cols, vel, pres, f, shift, part, make_fin<double>(P, X, OP_CHECKS, rb, 6, cols), done);
+    const float* u = static_cast<const float*>(P->wacc32 + last * sz * cols);
+    const float* x = static_cast<const float*>(P->xpieces + last * np * cols);
+    const int vec = defect_vec(g, {u, x, ru_hi, rd_hi, f, vel, pres});
+    // four times the reduction blocks: the groups' loads in flight fill the SMs
+    const int nb = std::min(4 * rb, flat_blocks((n + 3) / 4));
+    launch_k(k_stokes_check_df, dim3(nb, cols), kThreads, 0, X.s, g, last == 0 ? f : nullptr, u, x, ru_hi,
+             ru_hi + sz * cols, rd_hi, rd_hi + np * cols, vel, pres, f, shift, vec, part,
+             make_fin<double>(P, X, OP_CHECKS, nb, 6, cols), done);
   } else {
     launch_k(k_stokes_check, dim3(rb, cols), kThreads, 0, X.s, g, vel, pres, f, g.size, g.np, shift, part,
              make_fin<double>(P, X, OP_CHECKS, rb, 6, cols), done);
@@ -944,61 +1149,64 @@ int solve_fp64(Plan* P, const double* f, int cols, double mass, double visc, dou
 // operations per face.
 //   f: the Stokes right-hand side (first sweep) or null (the pairs hold the
 //   previous defect); u, x: the last solve's velocity and pressure (float).
-__global__ void __launch_bounds__(kThreads) k_defect_update(GridDev g, const double* f, const float* u,
-                                                            const float* x, const double* shift, float* ru_hi,
-                                                            float* ru_lo, float* rd_hi, float* rd_lo) {
+__global__ void __launch_bounds__(kThreads, 4) k_defect_update(GridDev g, const double* f, const float* u,
+                                                            const float* x, const double* shift, int vec,
+                                                            float* ru_hi, float* ru_lo, float* rd_hi, float* rd_lo) {
   pdl_wait();
   const int c = blockIdx.y;
-  const df32 mass = d2df(shift[2 * c]), visc = d2df(shift[2 * c + 1]);
-  const df32 ihx = d2df(g.ihx), ihy = d2df(g.ihy), ihx2 = d2df(g.ihx2), ihy2 = d2df(g.ihy2);
+  const OpCoef C = op_coef(g, shift, c);
   const long long su = c * (long long)g.size, sp = c * (long long)g.np;
   const float* uc = u + su;
   const float* xc = x + sp;
-  const int n = g.size > g.np ? g.size : g.np;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    if (i < g.size) {
-      // K u_k with the wall rows of K_at: neighbours beyond a normal wall are
-      // 0, beyond a tangential wall -u (diagonal 3/h^2)
-      const float cc = uc[i];
-      float l, r, s, nn;
-      df32 dt;
-      if (i < g.nu) {
-        const int w = g.nx - 1, j = i / w, q = i - j * w;
-        l = q > 0 ? uc[i - 1] : 0.0f;
-        r = q < w - 1 ? uc[i + 1] : 0.0f;
-        s = j > 0 ? uc[i - w] : -cc;
-        nn = j < g.ny - 1 ? uc[i + w] : -cc;
-        const int lc = j * g.nx + q;
-        dt = df_mul(df_two_sum(xc[lc], -xc[lc + 1]), ihx);
+  const int ngf = (g.size + 3) / 4, ngc = (g.np + 3) / 4, ng = ngf > ngc ? ngf : ngc;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ng; t += gridDim.x * blockDim.x) {
+    if (t < ngf) {
+      const int i0 = 4 * t, cnt = min(4, g.size - i0);
+      df32 prev[4], d[4];
+      if (f) {
+        double fv[4];
+        load4d(f + su, i0, cnt, vec, fv);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) prev[e] = d2df(fv[e]);
       } else {
-        const int fi = i - g.nu, j = fi / g.nx, q = fi - j * g.nx;
-        l = q > 0 ? uc[i - 1] : -cc;
-        r = q < g.nx - 1 ? uc[i + 1] : -cc;
-        s = j > 0 ? uc[i - g.nx] : 0.0f;
-        nn = j < g.ny - 2 ? uc[i + g.nx] : 0.0f;
-        const int lc = j * g.nx + q;
-        dt = df_mul(df_two_sum(xc[lc], -xc[lc + g.nx]), ihy);
+        float hi[4], lo[4];
+        load4(ru_hi + su, i0, cnt, vec, hi);
+        load4(ru_lo + su, i0, cnt, vec, lo);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) prev[e] = df32{hi[e], lo[e]};
       }
-      const df32 kx = df_mul(df_add(df_two_sum(cc, -l), df_two_sum(cc, -r)), ihx2);
-      const df32 ky = df_mul(df_add(df_two_sum(cc, -s), df_two_sum(cc, -nn)), ihy2);
-      const df32 op = df_sub(df_add(df_mul(mass, df32{cc, 0.0f}), df_mul(visc, df_add(kx, ky))), dt);
-      const long long k = su + i;
-      const df32 prev = f ? d2df(f[k]) : df32{ru_hi[k], ru_lo[k]};
-      const df32 now = df_sub(prev, op);
-      ru_hi[k] = now.hi;
-      ru_lo[k] = now.lo;
+      face_group(g, C, uc, xc, i0, cnt, vec, prev, d);
+      float hi[4], lo[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        hi[e] = d[e].hi;
+        lo[e] = d[e].lo;
+      }
+      store4(ru_hi + su, i0, cnt, vec, hi);
+      store4(ru_lo + su, i0, cnt, vec, lo);
     }
-    if (i < g.np) {
-      const int j = i / g.nx, q = i - j * g.nx;
-      df32 d{0.0f, 0.0f};
-      const float ue = q < g.nx - 1 ? uc[j * (g.nx - 1) + q] : 0.0f, uw = q > 0 ? uc[j * (g.nx - 1) + q - 1] : 0.0f;
-      const float vn = j < g.ny - 1 ? uc[g.nu + j * g.nx + q] : 0.0f, vs = j > 0 ? uc[g.nu + (j - 1) * g.nx + q] : 0.0f;
-      d = df_add(df_mul(df_two_sum(ue, -uw), ihx), df_mul(df_two_sum(vn, -vs), ihy));
-      const long long k = sp + i;
-      const df32 prev = f ? df32{0.0f, 0.0f} : df32{rd_hi[k], rd_lo[k]};
-      const df32 now = df_sub(prev, d);
-      rd_hi[k] = now.hi;
-      rd_lo[k] = now.lo;
+    if (t < ngc) {
+      const int i0 = 4 * t, cnt = min(4, g.np - i0);
+      df32 prev[4], d[4];
+      if (f) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) prev[e] = df32{0.0f, 0.0f};
+      } else {
+        float hi[4], lo[4];
+        load4(rd_hi + sp, i0, cnt, vec, hi);
+        load4(rd_lo + sp, i0, cnt, vec, lo);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) prev[e] = df32{hi[e], lo[e]};
+      }
+      cell_group(g, C, uc, i0, cnt, prev, d);
+      float hi[4], lo[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        hi[e] = d[e].hi;
+        lo[e] = d[e].lo;
+      }
+      store4(rd_hi + sp, i0, cnt, vec, hi);
+      store4(rd_lo + sp, i0, cnt, vec, lo);
     }
   }
 }
@@ -1099,10 +1307,12 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
     if (sweep > 0) {
       // no block reduction: four times the reduction kernels' blocks fill the
       // SMs (a few elements per thread keep its set-up amortised)
-      launch_k(k_defect_update, dim3(std::min(4 * red_blocks(sz > np ? sz : np), flat_blocks(sz > np ? sz : np)), cols),
-               kThreads, 0, X.s, g, sweep == 1 ? f : nullptr,
-               static_cast<const float*>(P->wacc32 + (sweep - 1) * sz * cols),
-               static_cast<const float*>(P->xpieces + (sweep - 1) * np * cols), P->shift, ru_hi, ru_lo, rd_hi, rd_lo);
+      const float* u = static_cast<const float*>(P->wacc32 + (sweep - 1) * sz * cols);
+      const float* x = static_cast<const float*>(P->xpieces + (sweep - 1) * np * cols);
+      const long long n4 = ((sz > np ? sz : np) + 3) / 4;
+      launch_k(k_defect_update, dim3(std::min(4 * red_blocks(4 * n4), flat_blocks(n4)), cols), kThreads, 0, X.s, g,
+               sweep == 1 ? f : nullptr, u, x, P->shift, defect_vec(g, {u, x, ru_hi, rd_hi, f}), ru_hi, ru_lo, rd_hi,
+               rd_lo);
       ++P->launches;
     }
     int rc = inner_solve32(P, X, sweep == 0 ? f : nullptr, ru_hi, sweep == 0 ? nullptr : rd_hi, cols, sweep);
@@ -1120,26 +1330,26 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
   return MACSAV_OK;
 }
 
-// Average device time of `reps` launches of one transform pass over the
-// velocity blocks (two right-hand sides, u and v concurrently), replayed from
-// a captured graph, with its algorithmic bytes per launch (each element of the
-// pass's input read once and output written once).
-//   pass 0: FP32 column pass; 1: FP32 forward row pass (FP64 packed input);
-//   2: FP32 inverse row pass; 3: FP64 column pass; 4, 5, 6: passes 0, 1, 2
-//   with each block's split-launch choice (p2_split) inverted.
+// Average device time of `reps` launches of one transform pass (two
+// right-hand sides; the velocity passes over the u and v blocks
+// concurrently), replayed from a captured graph, with its algorithmic bytes
+// per launch (each element of the pass's input read once and output written
+// once).  pass % 10 selects the pass:
+//   0: FP32 velocity column pass; 1: FP32 velocity forward row pass (FP64
+//   packed input); 2: FP32 velocity inverse row pass; 3: FP64 velocity column
+//   pass; 4: FP32 pressure column pass; 5: FP32 pressure forward row pass
+//   (FP64 cells in); 6: FP32 pressure inverse row pass (FP64 cells out);
+// pass / 10 the launch shape of every block: 0 the plan's own (P2_AUTO),
+// 1 plain, 2 doubled, 3 split (P2Shape, where the pass allows it).
 int time_pass(Plan* P, int pass, int reps, cudaStream_t user, double* ms, double* bytes) {
   const GridDev& g = P->g;
   const int cols = 2;
-  if (P->maxcols < 2 || reps < 1 || pass < 0 || pass > 6) return MACSAV_ERR_VALUE;
-  if (pass != 3 && P->precision != MACSAV_FP32_MIXED) return MACSAV_ERR_VALUE;
+  const int base = pass % 10, shape = pass / 10;
+  if (P->maxcols < 2 || reps < 1 || pass < 0 || base > 6 || shape > 3) return MACSAV_ERR_VALUE;
+  if (base != 3 && P->precision != MACSAV_FP32_MIXED) return MACSAV_ERR_VALUE;
+  if (base == 3 && shape != 0) return MACSAV_ERR_VALUE;
   Transforms<float> t32 = P->t32;
-  if (pass >= 4) {
-    for (TBlockDev<float>* B : {&t32.u, &t32.v}) {
-      B->splitx ^= 1;
-      B->splity ^= 1;
-    }
-    pass -= 4;
-  }
+  for (TBlockDev<float>* B : {&t32.u, &t32.v, &t32.p}) B->shapex = B->shapey = shape;
   // a capturable stream of our own (the caller's may be the legacy stream),
   // ordered after the caller's work
   cudaStream_t s;
@@ -1151,17 +1361,18 @@ int time_pass(Plan* P, int pass, int reps, cudaStream_t user, double* ms, double
   cudaStreamWaitEvent(s, a, 0);
   const double shift[4] = {1.0, 1e-6, 1.0, 1e-6};
   cudaMemcpyAsync(P->shift, shift, sizeof shift, cudaMemcpyHostToDevice, s);
-  const double n = double(g.size) * cols;
+  const double n = double(base >= 4 ? g.np : g.size) * cols;
+  const long long np = g.np;
   auto run = [&]() {
-    if (pass == 0)
-      Launcher<float>{t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.column_uv(cols, nullptr, P->shift);
-    else if (pass == 1)
-      Launcher<float>{t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.row_forward_uv(SrcPacked<float, double>{P->w, g.size, g.nu, g.nx - 1,
-                                                                                        g.nx}, cols, nullptr);
-    else if (pass == 2)
-      Launcher<float>{t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.row_inverse_uv(DstPacked<float, float>{P->w32, g.size, g.nu,
-                                                                                      g.nx - 1, g.nx}, cols, nullptr);
-    else Launcher<double>{P->t64, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.column_uv(cols, nullptr, P->shift);
+    const Launcher<float> L{t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
+    if (base == 0) L.column_uv(cols, nullptr, P->shift);
+    else if (base == 1) L.row_forward_uv(SrcPacked<float, double>{P->w, g.size, g.nu, g.nx - 1, g.nx}, cols, nullptr);
+    else if (base == 2) L.row_inverse_uv(DstPacked<float, float>{P->w32, g.size, g.nu, g.nx - 1, g.nx}, cols, nullptr);
+    else if (base == 3)
+      Launcher<double>{P->t64, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]}.column_uv(cols, nullptr, P->shift);
+    else if (base == 4) L.column_p(cols, nullptr, P->shift, float(P->pthr));
+    else if (base == 5) L.row_forward_p(SrcCells<float, double>{P->w, np, g.nx}, cols, nullptr);
+    else L.row_inverse_p(DstCells<float, double>{P->w, np, g.nx}, cols, nullptr, nullptr, NoFin{}, nullptr);
   };
   run();  // warm-up
   // the reps are captured into one graph and replayed, as the pass runs
@@ -1190,7 +1401,8 @@ int time_pass(Plan* P, int pass, int reps, cudaStream_t user, double* ms, double
   cudaEventDestroy(b);
   cudaStreamDestroy(s);
   *ms = double(t) / reps;
-  *bytes = pass == 0 ? 2 * 4 * n : (pass == 1 ? (8 + 4) * n : (pass == 2 ? (4 + 4) * n : 2 * 8 * n));
+  const double per[7] = {2 * 4, 8 + 4, 4 + 4, 2 * 8, 2 * 4, 8 + 4, 4 + 8};
+  *bytes = per[base] * n;
   return e == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
 }
 

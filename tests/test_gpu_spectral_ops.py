@@ -86,3 +86,31 @@ def test_spectral_ops_reject_bad_shifts_and_columns(pkg):
         solver.precondition(np.ones((g.np, 5)), 1.0, 0.0)
     with pytest.raises(ValueError):
         solver.velocity_inverse(np.ones(g.size + 1), 1.0, 0.0)
+
+
+@pytest.mark.parametrize("shape", [(512, 512, 1.0, 1.0), (1024, 1024, 1.0, 1.0), (2048, 1024, 2.0, 1.0)],
+                         ids=lambda s: f"{s[0]}x{s[1]}")
+def test_launch_shapes_give_the_same_bits(pkg, shape):
+    """Every launch shape of the FP32 transform passes (one butterfly per
+    thread, doubled threads, split lines: macsav_plan_set_launch_shape)
+    computes each butterfly with the same arithmetic, so the operators and a
+    whole FP32-bulk Stokes solve are bitwise equal across shapes."""
+    nx, ny, lx, ly = shape
+    og = O.Grid(nx, ny, lx, ly)
+    g = pkg.MACGrid(nx, ny, lx, ly)
+    from importlib import import_module
+    stokes = import_module(pkg.__name__ + ".stokes")
+    vel_in = _fields(pkg, og, nx, ny, lx, ly, og.size, 3)
+    p_in = _fields(pkg, og, nx, ny, lx, ly, og.np, 4)
+    solver = stokes.TensorStokes(g, precision="fp32")
+    outs = []
+    for s in (0, 1, 2, 3):
+        solver.plan.check(solver.plan.lib.macsav_plan_set_launch_shape(solver.plan.handle, s))
+        res = solver.solve(vel_in, mass=1.0, viscosity=1e-4 * 0.25)
+        outs.append((solver.velocity_inverse(vel_in, 1.0, 2.5e-9), solver.precondition(p_in, 1.0, 2.5e-9),
+                     res.velocity, res.pressure, solver.last_iterations))
+    for s in (1, 2, 3):
+        for a, b in zip(outs[0], outs[s]):
+            np.testing.assert_array_equal(np.asarray(a), np.asarray(b))
+    with pytest.raises(Exception):
+        solver.plan.check(solver.plan.lib.macsav_plan_set_launch_shape(solver.plan.handle, 4))
