@@ -176,16 +176,38 @@ struct CGFin {
       const int c = pr / K, k = pr - c * K;
       if (gated && !active[c]) continue;  // uniform across the warp
       const double* o = partial + size_t(c) * nb * K + k;
+      // the lane's partials are loaded kFold at a time before they are
+      // combined (in the same order as one by one, so the same bits): the
+      // last block then waits for one L2 round trip per kFold partials, not
+      // per partial
+      constexpr int kFold = 8;
       if ((mm >> k) & 1) {
         unsigned long long m = 0ull;
-        for (int b = lane; b < nb; b += 32)
+        int b = lane;
+        for (; b + (kFold - 1) * 32 < nb; b += kFold * 32) {
+          unsigned long long t[kFold];
+#pragma unroll
+          for (int u = 0; u < kFold; ++u)
+            t[u] = (unsigned long long)__ldcg(reinterpret_cast<const long long*>(o + size_t(b + 32 * u) * K));
+#pragma unroll
+          for (int u = 0; u < kFold; ++u) m = max(m, t[u]);
+        }
+        for (; b < nb; b += 32)
           m = max(m, (unsigned long long)__ldcg(reinterpret_cast<const long long*>(o + size_t(b) * K)));
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, off));
         if (lane == 0) vals[c][k] = key_value(m);
       } else {
         typename R::P v = R::zero();
-        for (int b = lane; b < nb; b += 32) v = R::add(v, R::load(o + size_t(b) * K));
+        int b = lane;
+        for (; b + (kFold - 1) * 32 < nb; b += kFold * 32) {
+          typename R::P t[kFold];
+#pragma unroll
+          for (int u = 0; u < kFold; ++u) t[u] = R::load(o + size_t(b + 32 * u) * K);
+#pragma unroll
+          for (int u = 0; u < kFold; ++u) v = R::add(v, t[u]);
+        }
+        for (; b < nb; b += 32) v = R::add(v, R::load(o + size_t(b) * K));
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) v = R::add(v, R::shfl_down(v, off));
         if (lane == 0) vals[c][k] = R::value(v);
