@@ -677,7 +677,7 @@ def run_headline(args) -> None:
         peaks = json.loads(pk.read_text())
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     roof = column_roofline(pkg, plain["model"], 0, 50, hbm, pk.exists(), "column_pass_traffic_1024.json")
-    roof["kernel"] = "k_column_p2<float,1024> (velocity blocks, 2 RHS)"
+    roof["kernel"] = "k_column_p2<float,1024,128> (u) + k_column_p2<float,2048,128> (v, split) (velocity blocks, 2 RHS)"
     roof64 = fp64_roofline(pkg, g, fp64["model"], dev, hbm)
 
     # the first step of each GPU form against the CPU oracle's first step
