@@ -150,13 +150,14 @@ __device__ __forceinline__ void dftR(cplx<T> (&v)[R]) {
 // launches) only join the barriers.  Every thread of the CTA must call this
 // (two block barriers per pass).  Which thread computes a butterfly does not
 // change its arithmetic, so every G gives the same bits.
-template <typename T, int L, int NS, int SIGN, int G = L / kE>
+// tw: the twiddles in pass order (TBlockDev::twpx / twpy, plan.cu's
+// pass_twiddles); OFF is this pass's offset in that table.
+template <typename T, int L, int NS, int SIGN, int G = L / kE, int OFF = 0>
 __device__ __forceinline__ void fft_p2(cplx<T>* z, int t, const cplx<T>* __restrict__ tw) {
   constexpr int R = (L / NS >= kE) ? kE : L / NS;
   constexpr int NB = (L / R) / G;
   constexpr int STRIDE = L / R;
   static_assert(NB * G == L / R, "threads per line must divide the butterflies of every pass");
-  constexpr int TWS = L / (NS * R);
   const SwIx ix;
   cplx<T> v[NB][R];
   const bool own = t < G;
@@ -170,8 +171,9 @@ __device__ __forceinline__ void fft_p2(cplx<T>* z, int t, const cplx<T>* __restr
 #pragma unroll
       for (int r = 0; r < R; ++r) v[q][r] = z[swz_plus<STRIDE>(sj, r * STRIDE)];
       if constexpr (NS > 1) {
+        const cplx<T>* twk = tw + OFF + k;  // row r - 1 of this pass's table at (r - 1) NS
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], tw_at<T, SIGN>(tw, r * k * TWS));
+        for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], tw_at<T, SIGN>(twk, (r - 1) * NS));
       }
       dftR<T, R, SIGN>(v[q]);
     }
@@ -189,7 +191,7 @@ __device__ __forceinline__ void fft_p2(cplx<T>* z, int t, const cplx<T>* __restr
     }
   }
   __syncthreads();
-  if constexpr (NS * R < L) fft_p2<T, L, NS * R, SIGN, G>(z, t, tw);
+  if constexpr (NS * R < L) fft_p2<T, L, NS * R, SIGN, G, OFF + (NS > 1 ? (R - 1) * NS : 0)>(z, t, tw);
 }
 
 // ------------------------------------------------------------ row passes ---
@@ -203,7 +205,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_forward_p2(TBlockDev<T> B, 
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T>* z = reinterpret_cast<cplx<T>*>(smraw);
   const int NL = blockDim.x / TPL;
-  const cplx<T>* tw = B.twx;
+  const cplx<T>* tw = B.twpx;
   const int N = B.cols, rows = B.rows, kind = B.kx;
   const int row0 = blockIdx.x * 2 * NL;
   const int npairs = min(NL, (rows - row0 + 1) / 2);
@@ -257,7 +259,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_row_inverse_p2(TBlockDev<T> B, 
   cplx<T>* z = reinterpret_cast<cplx<T>*>(smraw);
   if (live) {
     const int NL = blockDim.x / TPL;
-    const cplx<T>* tw = B.twx;
+    const cplx<T>* tw = B.twpx;
     const int N = B.cols, rows = B.rows, kind = B.kx;
     const int row0 = blockIdx.x * 2 * NL;
     const int npairs = min(NL, (rows - row0 + 1) / 2);
@@ -341,7 +343,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const
   using vec_t = typename Vec16<T>::type;
   constexpr int V = Vec16<T>::n;
   const int NL = blockDim.x / TPL;
-  const cplx<T>* tw = B.twy;
+  const cplx<T>* tw = B.twpy;
   const int W = 2 * NL;
   const int N = B.rows, kind = B.ky;
   const int col0 = blockIdx.x * W;

@@ -63,6 +63,28 @@ static int pick_strip(int L, int cols, int sms, int elem_bytes) {
   return W;
 }
 
+// The twiddles of a power-of-two length L = tw.size() in the order the
+// Stockham passes of fft_p2 read them: for each pass with NS > 1 (radix R,
+// TWS = L / (NS R)), rows r = 1 .. R-1 of NS entries tw[r k TWS], k = 0 ..
+// NS-1.  A butterfly's seven twiddles are then one per-thread base plus
+// compile-time offsets, and a warp's loads of one r are consecutive.  The
+// values are the table's own, so the transforms' bits do not change.  Empty
+// for other lengths (the generic passes read tw itself).
+template <typename T>
+static std::vector<cplx<T>> pass_twiddles(const std::vector<cplx<T>>& tw) {
+  const int L = int(tw.size());
+  std::vector<cplx<T>> out;
+  if (L < 64 || L > 4096 || (L & (L - 1))) return out;  // the power-of-two passes' lengths
+  for (int NS = 1; NS < L;) {
+    const int R = L / NS >= 8 ? 8 : L / NS, TWS = L / (NS * R);
+    if (NS > 1)
+      for (int r = 1; r < R; ++r)
+        for (int k = 0; k < NS; ++k) out.push_back(tw[size_t(r) * k * TWS]);
+    NS *= R;
+  }
+  return out;
+}
+
 template <typename T>
 static cudaError_t build_block(TBlockDev<T>& B, int rows, int cols, int kx, int ky, double hx, double hy,
                                int sms, std::vector<void*>& allocs) {
@@ -91,6 +113,7 @@ static cudaError_t build_block(TBlockDev<T>& B, int rows, int cols, int kx, int 
   std::vector<cplx<T>> twx(Lx), twy(Ly), qx(cols), qy(rows);
   for (int m = 0; m < Lx; ++m) twx[m] = mk(T(std::cos(2 * kPi * m / Lx)), T(-std::sin(2 * kPi * m / Lx)));
   for (int m = 0; m < Ly; ++m) twy[m] = mk(T(std::cos(2 * kPi * m / Ly)), T(-std::sin(2 * kPi * m / Ly)));
+  const std::vector<cplx<T>> twpx = pass_twiddles(twx), twpy = pass_twiddles(twy);
   for (int k = 0; k < cols; ++k) qx[k] = mk(T(std::cos(kPi * k / (2.0 * cols))), T(-std::sin(kPi * k / (2.0 * cols))));
   for (int k = 0; k < rows; ++k) qy[k] = mk(T(std::cos(kPi * k / (2.0 * rows))), T(-std::sin(kPi * k / (2.0 * rows))));
   std::vector<double> ex = internal_eigenvalues(kx, cols, hx), ey = internal_eigenvalues(ky, rows, hy);
@@ -100,7 +123,8 @@ static cudaError_t build_block(TBlockDev<T>& B, int rows, int cols, int kx, int 
   // length would leave a following table 4 bytes off)
   auto up16 = [](size_t n) { return (n + 15) / 16 * 16; };
   const size_t bytes = up16(sizeof(cplx<T>) * Lx) + up16(sizeof(cplx<T>) * Ly) + up16(sizeof(cplx<T>) * cols) +
-                       up16(sizeof(cplx<T>) * rows) + up16(sizeof(T) * cols) + up16(sizeof(T) * rows);
+                       up16(sizeof(cplx<T>) * rows) + up16(sizeof(T) * cols) + up16(sizeof(T) * rows) +
+                       up16(sizeof(cplx<T>) * twpx.size()) + up16(sizeof(cplx<T>) * twpy.size());
   void* d = nullptr;
   cudaError_t e = cudaMalloc(&d, bytes);
   if (e != cudaSuccess) return e;
@@ -118,6 +142,8 @@ static cudaError_t build_block(TBlockDev<T>& B, int rows, int cols, int kx, int 
   B.qy = static_cast<const cplx<T>*>(put(qy.data(), sizeof(cplx<T>) * rows));
   B.eigx = static_cast<const T*>(put(exT.data(), sizeof(T) * cols));
   B.eigy = static_cast<const T*>(put(eyT.data(), sizeof(T) * rows));
+  B.twpx = twpx.empty() ? nullptr : static_cast<const cplx<T>*>(put(twpx.data(), sizeof(cplx<T>) * twpx.size()));
+  B.twpy = twpy.empty() ? nullptr : static_cast<const cplx<T>*>(put(twpy.data(), sizeof(cplx<T>) * twpy.size()));
   return cudaGetLastError();
 }
 

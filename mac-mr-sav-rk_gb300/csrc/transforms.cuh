@@ -35,6 +35,8 @@ struct TBlockDev {
   FFTPlan fx, fy;
   const cplx<T>* twx;  // exp(-2 pi i m / Lx)
   const cplx<T>* twy;
+  const cplx<T>* twpx;  // the same twiddles in Stockham-pass order (power-of-two Lx, fftp.cuh)
+  const cplx<T>* twpy;
   const cplx<T>* qx;   // exp(-i pi k / (2 N)) for DCT kinds
   const cplx<T>* qy;
   const T* eigx;       // eigenvalues in internal order
