@@ -739,6 +739,7 @@ def run_headline(args) -> None:
         "cavity512_sdirk3_mrsav": cav,
         "ensemble256_sdirk2_mrsav": ens,
         "transform_autotune": autotune,
+        "launch_shapes": {"learned": learned["model"].plan.launch_shapes, "plain_fp32": plain["model"].plan.launch_shapes},
     }
     if oracle_sec is not None:
         line["cpu_baseline"] = {"value": w["nx"] * w["ny"] * w["stages_per_step"] / oracle_sec,

@@ -469,6 +469,15 @@ int macsav_plan_set_first_solve_tolerance(macsav_plan* plan, double first_krylov
  * 1024 to 4096; others fall back to 1).  Every shape computes the same bits;
  * only the time differs.  Affects launches and captures after the call. */
 int macsav_plan_set_launch_shape(macsav_plan* plan, int shape);
+/* Launch-shape autotuner (no reference counterpart; FP32_MIXED plans): for
+ * each of six pass kinds (velocity forward rows, columns, inverse rows, then
+ * the pressure block's) times the plan's rule and the three shapes above,
+ * `reps` launches each from a captured graph on `stream`'s device, and keeps
+ * the fastest (another shape replaces the rule only when 2 % faster).
+ * chosen (6 ints, or NULL) receives the kept shapes in that order
+ * (0 = the rule).  Results do not change; graphs captured before are
+ * dropped.  Synchronises. */
+int macsav_plan_autotune_launch_shapes(macsav_plan* plan, int reps, int* chosen, void* stream);
 
 /* Run macsav_step as one captured CUDA graph per (scheme, force, embedded)
  * (the pressure CG loop becomes a conditional WHILE node).  Default: off. */

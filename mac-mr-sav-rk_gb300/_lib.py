@@ -96,6 +96,7 @@ _SIGNATURES = {
     "macsav_plan_set_learned_placement": (_I, [_P, _I, _I]),
     "macsav_plan_set_first_solve_tolerance": (_I, [_P, _D]),
     "macsav_plan_set_launch_shape": (_I, [_P, _I]),
+    "macsav_plan_autotune_launch_shapes": (_I, [_P, _I, C.POINTER(C.c_int), _P]),
     "macsav_transform32": (_I, [_P, _I, _I, _I, _I, _I, _P, _P, _P]),
     "macsav_transform32_autotune": (_I, [_P, _I, _I, _I, _I, C.POINTER(_I), C.POINTER(_D), C.POINTER(_D), _P]),
     "macsav_plan_cg_counters": (_I, [_P, _I, _P, _P, _P]),

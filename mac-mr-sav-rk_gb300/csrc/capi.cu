@@ -30,6 +30,7 @@ int op_diagnostics(Plan* P, const double* x, double r, double nu, const double* 
                    cudaStream_t s);
 int op_transform(Plan* P, int kind, int inverse, int rows, int n, const double* in, double* out, cudaStream_t s);
 int time_pass(Plan* P, int pass, int reps, cudaStream_t s, double* ms, double* bytes);
+int autotune_shapes(Plan* P, int reps, cudaStream_t user, int* chosen);
 int op_velocity_inverse(Plan* P, const double* in, double* out, int cols, cudaStream_t s);
 int op_schur_precondition(Plan* P, const double* in, double* out, int cols, cudaStream_t s);
 int op_transform32(Plan* P, int kind, int inverse, int rows, int n, int method, const float* in, float* out,
@@ -697,9 +698,20 @@ int macsav_plan_set_first_solve_tolerance(macsav_plan* plan, double first_krylov
   return MACSAV_OK;
 }
 
+int macsav_plan_autotune_launch_shapes(macsav_plan* plan, int reps, int* chosen, void* stream) {
+  if (!plan) return MACSAV_ERR_VALUE;
+  if (plan->p.precision != MACSAV_FP32_MIXED || reps < 1 || reps > 1000)
+    return fail(&plan->p, MACSAV_ERR_VALUE, "autotune: an FP32_MIXED plan and 1 <= reps <= 1000");
+  const int rc = macsav::autotune_shapes(&plan->p, reps, static_cast<cudaStream_t>(stream), chosen);
+  for (auto& kv : plan->p.st.graphs) cudaGraphExecDestroy(kv.exec);  // captured with the old shapes
+  plan->p.st.graphs.clear();
+  return rc == MACSAV_ERR_CUDA ? cuda_status(&plan->p) : rc;
+}
+
 int macsav_plan_set_launch_shape(macsav_plan* plan, int shape) {
   if (!plan || shape < 0 || shape > 3) return MACSAV_ERR_VALUE;
-  for (macsav::TBlockDev<float>* B : {&plan->p.t32.u, &plan->p.t32.v, &plan->p.t32.p}) B->shapex = B->shapey = shape;
+  for (macsav::TBlockDev<float>* B : {&plan->p.t32.u, &plan->p.t32.v, &plan->p.t32.p})
+    B->shape[0] = B->shape[1] = B->shape[2] = shape;
   for (auto& kv : plan->p.st.graphs) cudaGraphExecDestroy(kv.exec);  // captured with the old shapes
   plan->p.st.graphs.clear();
   return MACSAV_OK;

@@ -101,7 +101,7 @@ static cudaError_t build_block(TBlockDev<T>& B, int rows, int cols, int kx, int 
   B.px = pick_pairs(Lx, rows, sms);
   B.wy = pick_strip(Ly, cols, sms, int(sizeof(T)));
   B.tpl = Lx / 8;  // each specialised launch sets its own
-  B.shapex = B.shapey = 0;  // P2_AUTO: each pass picks its launch shape
+  B.shape[0] = B.shape[1] = B.shape[2] = 0;  // P2_AUTO: each pass picks its launch shape
   B.fcols = FastDiv(cols);
   B.frows = FastDiv(rows);
   B.fw = FastDiv(B.wy);

@@ -433,7 +433,7 @@ struct Launcher {
   template <class Src>
   void row_forward_p2(const TBlockDev<T>& B, int bk, cudaStream_t st, Src src, int cols, const int* active) const {
     const int P = p2_pairs(B);
-    const int shape = p2_shape<T>(B, B.fx.L, P, B.shapex);
+    const int shape = p2_shape<T>(B, B.fx.L, P, B.shape[0]);
     const bool split = shape == P2_SPLIT;
     const int G = p2_tpl(B.fx.L, shape);
     TBlockDev<T> Bl = B;
@@ -459,7 +459,7 @@ struct Launcher {
   void row_inverse_p2(const TBlockDev<T>& B, int bk, cudaStream_t st, Dst dst, int cols, const int* active,
                       double* partial, Fin fin, unsigned int* done) const {
     const int P = p2_pairs(B);
-    const int shape = p2_shape<T>(B, B.fx.L, P, B.shapex);
+    const int shape = p2_shape<T>(B, B.fx.L, P, B.shape[2]);
     const bool split = shape == P2_SPLIT;
     const int G = p2_tpl(B.fx.L, shape);
     TBlockDev<T> Bl = B;
@@ -484,7 +484,7 @@ struct Launcher {
   void column_p2(const TBlockDev<T>& B, cudaStream_t st, int cols, const int* active, int mode, const double* shift,
                  T thr) const {
     const int NL = B.wy / 2;
-    const int shape = p2_shape<T>(B, B.fy.L, NL, B.shapey);
+    const int shape = p2_shape<T>(B, B.fy.L, NL, B.shape[1]);
     const bool split = shape == P2_SPLIT;
     const int G = p2_tpl(B.fy.L, shape);
     TBlockDev<T> Bl = B;

@@ -1330,28 +1330,18 @@ int enqueue_solve_mixed(Plan* P, Exec& X, const double* f, int cols, double* vel
   return MACSAV_OK;
 }
 
-// Average device time of `reps` launches of one transform pass (two
-// right-hand sides; the velocity passes over the u and v blocks
-// concurrently), replayed from a captured graph, with its algorithmic bytes
-// per launch (each element of the pass's input read once and output written
-// once).  pass % 10 selects the pass:
+// Average device milliseconds of `reps` launches of transform pass `base`
+// (two right-hand sides; the velocity passes over the u and v blocks
+// concurrently), replayed from a captured graph on a stream of its own
+// ordered after `user`, with the FP32 transforms t32 (the plan's, or a copy
+// with other launch shapes):
 //   0: FP32 velocity column pass; 1: FP32 velocity forward row pass (FP64
 //   packed input); 2: FP32 velocity inverse row pass; 3: FP64 velocity column
 //   pass; 4: FP32 pressure column pass; 5: FP32 pressure forward row pass
-//   (FP64 cells in); 6: FP32 pressure inverse row pass (FP64 cells out);
-// pass / 10 the launch shape of every block: 0 the plan's own (P2_AUTO),
-// 1 plain, 2 doubled, 3 split (P2Shape, where the pass allows it).
-int time_pass(Plan* P, int pass, int reps, cudaStream_t user, double* ms, double* bytes) {
+//   (FP64 cells in); 6: FP32 pressure inverse row pass (FP64 cells out).
+static int time_pass_t(Plan* P, const Transforms<float>& t32, int base, int reps, cudaStream_t user, double* ms) {
   const GridDev& g = P->g;
   const int cols = 2;
-  const int base = pass % 10, shape = pass / 10;
-  if (P->maxcols < 2 || reps < 1 || pass < 0 || base > 6 || shape > 3) return MACSAV_ERR_VALUE;
-  if (base != 3 && P->precision != MACSAV_FP32_MIXED) return MACSAV_ERR_VALUE;
-  if (base == 3 && shape != 0) return MACSAV_ERR_VALUE;
-  Transforms<float> t32 = P->t32;
-  for (TBlockDev<float>* B : {&t32.u, &t32.v, &t32.p}) B->shapex = B->shapey = shape;
-  // a capturable stream of our own (the caller's may be the legacy stream),
-  // ordered after the caller's work
   cudaStream_t s;
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return MACSAV_ERR_CUDA;
   cudaEvent_t a, b;
@@ -1361,7 +1351,6 @@ int time_pass(Plan* P, int pass, int reps, cudaStream_t user, double* ms, double
   cudaStreamWaitEvent(s, a, 0);
   const double shift[4] = {1.0, 1e-6, 1.0, 1e-6};
   cudaMemcpyAsync(P->shift, shift, sizeof shift, cudaMemcpyHostToDevice, s);
-  const double n = double(base >= 4 ? g.np : g.size) * cols;
   const long long np = g.np;
   auto run = [&]() {
     const Launcher<float> L{t32, s, &P->launches, P->aux[0], P->evf[0], P->evj[0]};
@@ -1401,9 +1390,74 @@ int time_pass(Plan* P, int pass, int reps, cudaStream_t user, double* ms, double
   cudaEventDestroy(b);
   cudaStreamDestroy(s);
   *ms = double(t) / reps;
+  return e == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
+}
+
+// macsav_time_pass: pass % 10 is the pass of time_pass_t, pass / 10 the
+// launch shape forced on every block (0 the plan's own, 1 plain, 2 doubled,
+// 3 split: P2Shape, where the pass allows it); also the pass's algorithmic
+// bytes per launch (each element of its input read once and output written
+// once).
+int time_pass(Plan* P, int pass, int reps, cudaStream_t user, double* ms, double* bytes) {
+  const int base = pass % 10, shape = pass / 10;
+  if (P->maxcols < 2 || reps < 1 || pass < 0 || base > 6 || shape > 3) return MACSAV_ERR_VALUE;
+  if (base != 3 && P->precision != MACSAV_FP32_MIXED) return MACSAV_ERR_VALUE;
+  if (base == 3 && shape != 0) return MACSAV_ERR_VALUE;
+  Transforms<float> t32 = P->t32;
+  if (shape)
+    for (TBlockDev<float>* B : {&t32.u, &t32.v, &t32.p}) B->shape[0] = B->shape[1] = B->shape[2] = shape;
+  const int rc = time_pass_t(P, t32, base, reps, user, ms);
+  const double n = double(base >= 4 ? P->g.np : P->g.size) * 2;
   const double per[7] = {2 * 4, 8 + 4, 4 + 4, 2 * 8, 2 * 4, 8 + 4, 4 + 8};
   *bytes = per[base] * n;
-  return e == cudaSuccess ? MACSAV_OK : MACSAV_ERR_CUDA;
+  return rc;
+}
+
+// Launch-shape autotuner of the FP32 power-of-two passes.  For each of the
+// six pass kinds (velocity forward rows, columns, inverse rows; the same for
+// the pressure block) it times the block's rule (P2_AUTO) and the plain,
+// doubled and split shapes on every block of that kind, `reps` launches each
+// from a captured graph, and keeps the fastest; another shape replaces the
+// rule only when at least 2 % faster, so timing noise does not flip it.
+// Every shape computes the same bits, so the choice changes time only.
+// chosen[k] (if not null): the kept shape per kind, in the order above.
+int autotune_shapes(Plan* P, int reps, cudaStream_t user, int* chosen) {
+  if (P->precision != MACSAV_FP32_MIXED || P->maxcols < 2 || reps < 1) return MACSAV_ERR_VALUE;
+  struct Kind {
+    int base, idx;
+    bool vel;
+  };
+  const Kind kinds[6] = {{1, 0, true}, {0, 1, true}, {2, 2, true}, {5, 0, false}, {4, 1, false}, {6, 2, false}};
+  for (int k = 0; k < 6; ++k) {
+    const Kind& K = kinds[k];
+    double best = 0.0;
+    int keep = P2_AUTO;
+    for (int sh = P2_AUTO; sh <= P2_SPLIT; ++sh) {
+      Transforms<float> t = P->t32;
+      if (K.vel) {
+        t.u.shape[K.idx] = sh;
+        t.v.shape[K.idx] = sh;
+      } else {
+        t.p.shape[K.idx] = sh;
+      }
+      double ms = 0.0;
+      const int rc = time_pass_t(P, t, K.base, reps, user, &ms);
+      if (rc != MACSAV_OK) return rc;
+      if (sh == P2_AUTO) best = ms;
+      else if (ms < 0.98 * best) {
+        best = ms;
+        keep = sh;
+      }
+    }
+    if (K.vel) {
+      P->t32.u.shape[K.idx] = keep;
+      P->t32.v.shape[K.idx] = keep;
+    } else {
+      P->t32.p.shape[K.idx] = keep;
+    }
+    if (chosen) chosen[k] = keep;
+  }
+  return MACSAV_OK;
 }
 
 // (m I + k K)^{-1} of `cols` packed velocity columns in the plan's precision

@@ -49,7 +49,7 @@ struct TBlockDev {
   int wy;              // columns per CTA in the column pass (even)
   int groups;          // CTAs of this block in the current pass
   int tpl;             // threads per line of a specialised pass (set per launch)
-  int shapex, shapey;  // launch shape of the row / column passes (P2Shape, fftp.cuh)
+  int shape[3];        // launch shapes of the forward row, column and inverse row passes (P2Shape, fftp.cuh)
   FastDiv fcols, frows, fw, fvpr, fhalf;  // divisors of the element loops
   T sx, sy;            // inverse normalisation of the x / y transforms
 };

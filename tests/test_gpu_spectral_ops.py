@@ -114,3 +114,30 @@ def test_launch_shapes_give_the_same_bits(pkg, shape):
             np.testing.assert_array_equal(np.asarray(a), np.asarray(b))
     with pytest.raises(Exception):
         solver.plan.check(solver.plan.lib.macsav_plan_set_launch_shape(solver.plan.handle, 4))
+
+
+def test_launch_shape_autotuner_keeps_the_bits(pkg):
+    """The autotuner (macsav_plan_autotune_launch_shapes) only picks among
+    shapes that compute the same bits: a solve before and after it agrees
+    bitwise; plans tune only when asked."""
+    nx = ny = 512
+    og = O.Grid(nx, ny, 1.0, 1.0)
+    g = pkg.MACGrid(nx, ny, 1.0, 1.0)
+    from importlib import import_module
+    stokes = import_module(pkg.__name__ + ".stokes")
+    rhs = _fields(pkg, og, nx, ny, 1.0, 1.0, og.size, 5)
+    plain = stokes.TensorStokes(g, precision="fp32")
+    assert plain.plan.launch_shapes is None
+    tuned = stokes.TensorStokes(g, precision="fp32", autotune_launch_shapes=True)
+    assert set(tuned.plan.launch_shapes) == set(stokes.SHAPE_KINDS)
+    assert set(tuned.plan.launch_shapes.values()) <= set(stokes.SHAPE_NAMES)
+    a = plain.solve(rhs, mass=1.0, viscosity=2.5e-5)
+    b = tuned.solve(rhs, mass=1.0, viscosity=2.5e-5)
+    np.testing.assert_array_equal(a.velocity, b.velocity)
+    np.testing.assert_array_equal(a.pressure, b.pressure)
+    assert plain.last_iterations == tuned.last_iterations
+    again = tuned.plan.autotune_launch_shapes(reps=5)
+    assert set(again) == set(stokes.SHAPE_KINDS)
+    np.testing.assert_array_equal(tuned.solve(rhs, mass=1.0, viscosity=2.5e-5).velocity, a.velocity)
+    with pytest.raises(Exception):
+        stokes.TensorStokes(pkg.MACGrid(64, 64), precision="fp64").plan.autotune_launch_shapes()
