@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "unet.cuh"
+#include "common.cuh"
 #include "../../include/macsav.h"
 
 namespace macsav {
@@ -44,6 +45,7 @@ struct ConvArgs {
 // BWD: gx[i](p) = sum_o sum_k w[o][i][k] dy[o](p - d_k)   (d_k: tap offset)
 template <int KS, bool BWD>
 __global__ void __launch_bounds__(256) k_conv(ConvArgs q) {
+  pdl_wait();
   constexpr int R = KS / 2, KK = KS * KS, SW = kTile + 2 * R;
   __shared__ float xs[kCI][SW][SW];
   __shared__ __align__(16) float wsh[kCI][KK][kCT];
@@ -176,6 +178,7 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
 }
 
 __global__ void __launch_bounds__(128, 5) k_conv3_tc(ConvArgs q, int* err) {
+  pdl_wait();
   extern __shared__ __align__(1024) unsigned char tcsm[];
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ uint32_t tmem_slot;
@@ -383,6 +386,7 @@ __global__ void __launch_bounds__(256) k_conv_wgrad(ConvArgs q, int tiles_x, int
 }
 
 __global__ void k_to_bf16(const float* in, const float* scale, long long hw, int batch, __nv_bfloat16* out) {
+  pdl_wait();
   const long long n = hw * batch;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
     const int b = int(e / hw);
@@ -392,6 +396,7 @@ __global__ void k_to_bf16(const float* in, const float* scale, long long hw, int
 
 // 2x2 average pool of [planes][H][W] to [planes][H/2][W/2]
 __global__ void k_pool(const __nv_bfloat16* x, __nv_bfloat16* y, long long planes, int H, int W) {
+  pdl_wait();
   const int h = H / 2, w = W / 2;
   const long long n = planes * h * w;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
@@ -413,6 +418,7 @@ __global__ void k_pool_bwd(const float* gy, float* gx, long long planes, int H, 
 }
 // nearest 2x upsample of [planes][h][w] to [planes][2h][2w]
 __global__ void k_up(const __nv_bfloat16* x, __nv_bfloat16* y, long long planes, int H, int W) {
+  pdl_wait();
   const long long n = planes * H * W;
   const int h = H / 2, w = W / 2;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
@@ -575,13 +581,13 @@ void conv_fwd(UNet* N, int li, const __nv_bfloat16* xa, const __nv_bfloat16* xb,
     const int cin = L.ca + L.cb, nchunks = (cin + kTcC - 1) / kTcC;
     const int per_chunk = int(kTcSmemHalo) + 9 * (L.co / 8) * int(kTcBSBO);
     q.tc_group = std::max(1, std::min(nchunks, smem_max / per_chunk));
-    k_conv3_tc<<<tgrid, 128, size_t(q.tc_group) * per_chunk, s>>>(q, N->tc_err);
+    launch_k(k_conv3_tc, tgrid, 128, size_t(q.tc_group) * per_chunk, s, q, N->tc_err);
     ++N->launches;
     return;
   }
   const dim3 grid((W + kTile - 1) / kTile, (H + kTile - 1) / kTile, B * ((L.co + kCT - 1) / kCT));
-  if (L.ks == 3) k_conv<3, false><<<grid, 256, 0, s>>>(q);
-  else k_conv<1, false><<<grid, 256, 0, s>>>(q);
+  if (L.ks == 3) launch_k(k_conv<3, false>, grid, 256, 0, s, q);
+  else launch_k(k_conv<1, false>, grid, 256, 0, s, q);
   ++N->launches;
 }
 
@@ -628,7 +634,7 @@ void forward_into(UNet* N, const Bufs& b, const float* in, const float* in_scale
     W[l] = nx >> l;
   }
   const long long hw0 = (long long)ny * nx;
-  k_to_bf16<<<grid1(hw0 * B), 256, 0, s>>>(in, in_scale, hw0, B, b.x0);
+  launch_k(k_to_bf16, grid1(hw0 * B), 256, 0, s, in, in_scale, hw0, B, b.x0);
   ++N->launches;
   // encoder and bottom: layers 2l (from x0 or the pooled level above) and 2l+1
   for (int l = 0; l < kNetLevels; ++l) {
@@ -637,7 +643,7 @@ void forward_into(UNet* N, const Bufs& b, const float* in, const float* in_scale
     conv_fwd(N, 2 * l + 1, b.a[l], nullptr, b.e[l], nullptr, nullptr, B, H[l], W[l], s);
     if (l + 1 < kNetLevels) {
       const long long planes = (long long)B * c[l];
-      k_pool<<<grid1(planes * H[l + 1] * W[l + 1]), 256, 0, s>>>(b.e[l], b.p[l], planes, H[l], W[l]);
+      launch_k(k_pool, grid1(planes * H[l + 1] * W[l + 1]), 256, 0, s, b.e[l], b.p[l], planes, H[l], W[l]);
       ++N->launches;
     }
   }
@@ -646,7 +652,7 @@ void forward_into(UNet* N, const Bufs& b, const float* in, const float* in_scale
     const __nv_bfloat16* below = l == kNetLevels - 2 ? b.e[kNetLevels - 1] : b.d[l + 1];
     const int cbelow = l == kNetLevels - 2 ? c[kNetLevels - 1] : c[l + 1];
     const long long planes = (long long)B * cbelow;
-    k_up<<<grid1(planes * H[l] * W[l]), 256, 0, s>>>(below, b.u[l], planes, H[l], W[l]);
+    launch_k(k_up, grid1(planes * H[l] * W[l]), 256, 0, s, below, b.u[l], planes, H[l], W[l]);
     ++N->launches;
     conv_fwd(N, 2 * kNetLevels + (kNetLevels - 2 - l), b.u[l], b.e[l], b.d[l], nullptr, nullptr, B, H[l], W[l], s);
   }
