@@ -35,7 +35,9 @@ reference's own path, all host threads) on the same workload.
 from __future__ import annotations
 
 import argparse
+import contextlib
 import ctypes as C
+import gc
 import json
 import os
 import pathlib
@@ -489,16 +491,17 @@ def timed_steps(pkg, g, w, x0_host, dev, args, precision, ktol, net=None, flush=
     torch.cuda.synchronize()
     before = L.cg_counters(model, 2) if precision == "fp32" else None
     events = []
-    for _ in range(args.steps):
-        if flush is not None:
-            flush.fill_(1.0)
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        y, r, _, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
-        b.record(stream)
-        events.append((a, b))
-        x, y, t = y, x, t + w["dt"]
-    torch.cuda.synchronize()
+    with quiet_host():
+        for _ in range(args.steps):
+            if flush is not None:
+                flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            y, r, _, _, _ = scheme.step_device(model, x, t, r, w["dt"], x1=y, pres=pres, want_embedded=False)
+            b.record(stream)
+            events.append((a, b))
+            x, y, t = y, x, t + w["dt"]
+        torch.cuda.synchronize()
     ms = [a.elapsed_time(b) for a, b in events]
     iters = None
     if before is not None:
@@ -564,6 +567,21 @@ def fp64_roofline(pkg, g, model64, dev, hbm):
             "ms_per_launch": ms_k64.value, "bytes": {"achieved": gbs, "unit": "GB/s", "frac_of_hbm": gbs / hbm}}
 
 
+@contextlib.contextmanager
+def quiet_host():
+    """A timed region without Python garbage collection: collected once
+    before (with the device idle), none during, so no collector pause or
+    allocator free lands between a step's launch and its events."""
+    import torch
+    gc.collect()
+    torch.cuda.synchronize()
+    gc.disable()
+    try:
+        yield
+    finally:
+        gc.enable()
+
+
 def e2e_steps(pkg, model, w, x0_host, args, pageable: bool) -> float:
     """Seconds for K steps through the public API, ``scheme.step(model,
     state, dt)``, with host states: every step its velocity goes host ->
@@ -583,11 +601,12 @@ def e2e_steps(pkg, model, w, x0_host, args, pageable: bool) -> float:
     for _ in range(args.warmup):
         st = scheme.step(model, fresh(st), w["dt"]).state
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        st = scheme.step(model, fresh(st), w["dt"]).state
-    torch.cuda.synchronize()
-    return time.perf_counter() - t0
+    with quiet_host():
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            st = scheme.step(model, fresh(st), w["dt"]).state
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
 
 
 HEADLINE = {"workload": "learned1024_sdirk3_mrsav", "nx": 1024, "ny": 1024, "lx": 1.0, "ly": 1.0, "nu": 1e-4,
