@@ -745,6 +745,8 @@ def run_headline(args) -> None:
         "fp64": {"value": cells / (ms_64 / 1e3), "ms_per_step": ms_64 / args.steps, "unit": "cell-stage/s",
                  "krylov_tolerance": w["reference_krylov_tolerance"]},
         "learned_vs_plain_fp32": ms_p / ms_l,
+        "step_ms": {k: {"min": min(v["ms"]), "median": statistics.median(v["ms"]), "max": max(v["ms"])}
+                    for k, v in (("learned", learned), ("plain_fp32", plain), ("fp64", fp64))},
         "network": network_info(net), "training": training,
         "clocks": clk.summary(),
         "e2e": {"value": cells / float(et[0]), "unit": "cell-stage/s", "h2d_bytes_per_step": face_bytes,

@@ -41,7 +41,7 @@ constexpr int kE = 8;  // elements per thread per line
 // swizzle) and the split L = 1024 column pass is twice as slow.  Which
 // thread computes a butterfly does not change its arithmetic: every shape
 // gives the same bits.
-enum P2Shape : int { P2_AUTO = 0, P2_PLAIN = 1, P2_DOUBLED = 2, P2_SPLIT = 3 };
+// (P2Shape: transforms.cuh, beside TBlockDev::shape)
 
 template <typename T>
 inline int p2_shape(const TBlockDev<T>& B, int L, int lines, int shape) {

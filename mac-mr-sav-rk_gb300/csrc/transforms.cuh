@@ -27,6 +27,8 @@ namespace macsav {
 
 enum Kind : int { KIND_DCT2 = 0, KIND_DST2 = 1, KIND_DST1 = 2 };
 enum WeightMode : int { W_HELMHOLTZ = 0, W_POISSON = 1 };
+// Launch shape of a power-of-two transform pass (p2_shape, fftp.cuh).
+enum P2Shape : int { P2_AUTO = 0, P2_PLAIN = 1, P2_DOUBLED = 2, P2_SPLIT = 3 };
 
 template <typename T>
 struct TBlockDev {
