@@ -47,3 +47,15 @@ def test_host_mapped_rejects_bad_arguments_and_pageable_memory():
     # ordinary (pageable) host memory is never reported as mapped pinned memory
     ok.value = 7
     assert so.macsav_host_mapped(a.ctypes.data, a.nbytes, ctypes.byref(ok)) == lib.OK and ok.value == 0
+
+
+def test_tuning_controls_reject_a_missing_plan_without_gpu():
+    """The launch-shape controls and the pass timer validate their plan
+    before touching the device."""
+    lib = _lib_module()
+    so = lib.load()
+    ms, nbytes = ctypes.c_double(), ctypes.c_double()
+    chosen = (ctypes.c_int * 6)()
+    assert so.macsav_plan_set_launch_shape(None, 0) == lib.ERR_VALUE
+    assert so.macsav_plan_autotune_launch_shapes(None, 10, chosen, None) == lib.ERR_VALUE
+    assert so.macsav_time_pass(None, 0, 3, ctypes.byref(ms), ctypes.byref(nbytes), None) == lib.ERR_VALUE
