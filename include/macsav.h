@@ -376,7 +376,7 @@ int macsav_integrate_adaptive(macsav_plan* plan, int scheme, double t0, double T
                               double* x_final, macsav_adaptive_result* result, macsav_adaptive_attempt* history,
                               int history_cap, void* stream);
 
-/* ---- channel MAC: periodic x, no-slip walls in y (solver/channel/*.py).
+/* ---- channel MAC: periodic x, no-slip walls in y (the reference's solver/channel/ package).
  * Packed free vector (grid.py:64-77): u faces (j, i), i < nx, then the v faces
  * of the interior rows; cells (j, i).  All arithmetic FP64, device pointers,
  * column-blocked multi-RHS data as for the cavity. */

@@ -12,8 +12,7 @@ namespace macsav {
 static const double kPi = 3.14159265358979323846264338327950288;
 
 FFTPlan make_fft_plan(int L) {
-  FFTPlan f;
-  std::memset(&f, 0, sizeof(f));
+  FFTPlan f{};
   f.L = L;
   int m = L, ns = 0;
   while (m % 4 == 0 && ns < kMaxStages) { f.radix[ns++] = 4; m /= 4; }

@@ -32,7 +32,6 @@ const double kD3[4][4] = {{1. / 4, 0, 0, 0}, {3. / 10, 1. / 4, 0, 0}, {-31. / 22
                           {31. / 198, 5. / 132, -4. / 9, 1. / 4}};                       // sdirk3.py:8-9
 const double kDH3[4][4] = {{1. / 4, 0, 0, 0}, {-33. / 50, 121. / 100, 0, 0}, {239. / 400, -71. / 100, 5. / 16, 0},
                            {-1. / 48, -17. / 66, 235. / 528, -1. / 6}};                  // sdirk3.py:10-12
-const double kC3[5] = {0., 1. / 4, 4. / 5, 1., 1.};                                      // sdirk3.py:13
 
 // ------------------------------------------------------------- kernels ---
 // Every kernel serves all M members of the plan at once (an ensemble of
