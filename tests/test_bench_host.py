@@ -1,5 +1,6 @@
 """Host logic of bench.py that needs no GPU: the clock record's decoding of
-NVML clock-event reasons and of nvidia-smi lines (fake samples, no NVML)."""
+NVML clock-event reasons and of nvidia-smi lines (fake samples, no NVML),
+and the reference arm's JSON line (the CPU oracle, one step)."""
 import bench
 
 
@@ -34,3 +35,27 @@ def test_sampler_enters_and_exits_on_any_host():
     out = s.summary()
     assert {"sm_mhz", "sm_max_mhz", "reasons", "samples"} <= set(out)
     assert out["samples"] <= len(s.samples) + len(s.lines)
+
+
+def test_reference_arm_prints_one_contract_line():
+    """`bench.py --impl reference` (the CPU oracle on the host's threads, no
+    GPU) prints one JSON line with the reference arm's keys: its own value as
+    the CPU baseline and an e2e record without device copies."""
+    import json
+    import pathlib
+    import subprocess
+    import sys
+    root = pathlib.Path(bench.__file__).resolve().parent
+    out = subprocess.run([sys.executable, str(root / "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "0"], cwd=root, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, out.stdout[-2000:]
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC
+    assert d["value"] > 0 and d["unit"] == "cell-stage/s" and d["higher_is_better"] is True
+    assert d["steps"] == 1 and d["n_gpus"] == 1
+    assert d["config"]["workload"] == bench.HEADLINE["workload"]
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["cores"] >= 1 and cb["kind"] in ("port", "reference") and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
