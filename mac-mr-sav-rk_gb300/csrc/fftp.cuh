@@ -392,46 +392,51 @@ __global__ void __launch_bounds__(kFFTThreads) k_column_p2(TBlockDev<T> B, const
   __syncthreads();
   const int line = threadIdx.x / TPL, t = threadIdx.x % TPL;
   fft_p2<T, L, 1, -1, GT>(z + line * L, t, tw);
+  // spectral weights: a thread takes one wavenumber k for every line of the
+  // CTA (the y tables read once per k, the lines' x eigenvalues broadcast)
   if (kind == KIND_DST1) {
-    for (int e = threadIdx.x; e < nl * N; e += blockDim.x) {
-      const int q = B.frows.div(e), k = e - q * N;
-      cplx<T>* y = z + q * L;
-      const int ca = col0 + 2 * q, cb = min(ca + 1, B.cols - 1);
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {
       const T ey = B.eigy[k];
-      const T wa = spectral_weight<T>(mode, mass, visc, thr, ey, B.eigx[ca]);
-      const T wb = spectral_weight<T>(mode, mass, visc, thr, ey, B.eigx[cb]);
-      const SwIx ix;
-      const cplx<T> Z = y[ix(k + 1)];
-      const T sa = -Z.y * T(0.5) * wa, sb = Z.x * T(0.5) * wb;
-      y[ix(k + 1)] = mk(sa, sb);
-      y[ix(2 * (N + 1) - 1 - k)] = mk(-sa, -sb);
-      if (k == 0) {
-        y[ix(0)] = mk(T(0), T(0));
-        y[ix(N + 1)] = mk(T(0), T(0));
+      for (int q = 0; q < nl; ++q) {
+        cplx<T>* y = z + q * L;
+        const int ca = col0 + 2 * q, cb = min(ca + 1, B.cols - 1);
+        const T wa = spectral_weight<T>(mode, mass, visc, thr, ey, B.eigx[ca]);
+        const T wb = spectral_weight<T>(mode, mass, visc, thr, ey, B.eigx[cb]);
+        const SwIx ix;
+        const cplx<T> Z = y[ix(k + 1)];
+        const T sa = -Z.y * T(0.5) * wa, sb = Z.x * T(0.5) * wb;
+        y[ix(k + 1)] = mk(sa, sb);
+        y[ix(2 * (N + 1) - 1 - k)] = mk(-sa, -sb);
+        if (k == 0) {
+          y[ix(0)] = mk(T(0), T(0));
+          y[ix(N + 1)] = mk(T(0), T(0));
+        }
       }
     }
   } else {
     const int half = N / 2 + 1;
-    for (int e = threadIdx.x; e < nl * half; e += blockDim.x) {
-      const int q = B.fhalf.div(e), k = e - q * half;
+    for (int k = threadIdx.x; k < half; k += blockDim.x) {
       const int m = k == 0 ? 0 : N - k;
-      const int ca = col0 + 2 * q, cb = min(ca + 1, B.cols - 1);
-      cplx<T>* y = z + q * L;
-      const SwIx ix;
-      const cplx<T> Zk = y[ix(k)], Zm = y[ix(m)];
       const cplx<T> qk = B.qy[k], qm = B.qy[m];
-      T yak = cmul(qk, Zk + conjg(Zm)).x, ybk = cmul(qk, Zk - conjg(Zm)).y;
-      T yam = cmul(qm, Zm + conjg(Zk)).x, ybm = cmul(qm, Zm - conjg(Zk)).y;
-      const T eyk = B.eigy[k], eym = B.eigy[m], exa = B.eigx[ca], exb = B.eigx[cb];
-      yak *= spectral_weight<T>(mode, mass, visc, thr, eyk, exa);
-      ybk *= spectral_weight<T>(mode, mass, visc, thr, eyk, exb);
-      yam *= spectral_weight<T>(mode, mass, visc, thr, eym, exa);
-      ybm *= spectral_weight<T>(mode, mass, visc, thr, eym, exb);
-      if (k == 0) {
-        y[ix(0)] = pre_inverse(yak, T(0), ybk, T(0), qk);
-      } else {
-        y[ix(k)] = pre_inverse(yak, yam, ybk, ybm, qk);
-        if (m != k) y[ix(m)] = pre_inverse(yam, yak, ybm, ybk, qm);
+      const T eyk = B.eigy[k], eym = B.eigy[m];
+      for (int q = 0; q < nl; ++q) {
+        const int ca = col0 + 2 * q, cb = min(ca + 1, B.cols - 1);
+        cplx<T>* y = z + q * L;
+        const SwIx ix;
+        const cplx<T> Zk = y[ix(k)], Zm = y[ix(m)];
+        T yak = cmul(qk, Zk + conjg(Zm)).x, ybk = cmul(qk, Zk - conjg(Zm)).y;
+        T yam = cmul(qm, Zm + conjg(Zk)).x, ybm = cmul(qm, Zm - conjg(Zk)).y;
+        const T exa = B.eigx[ca], exb = B.eigx[cb];
+        yak *= spectral_weight<T>(mode, mass, visc, thr, eyk, exa);
+        ybk *= spectral_weight<T>(mode, mass, visc, thr, eyk, exb);
+        yam *= spectral_weight<T>(mode, mass, visc, thr, eym, exa);
+        ybm *= spectral_weight<T>(mode, mass, visc, thr, eym, exb);
+        if (k == 0) {
+          y[ix(0)] = pre_inverse(yak, T(0), ybk, T(0), qk);
+        } else {
+          y[ix(k)] = pre_inverse(yak, yam, ybk, ybm, qk);
+          if (m != k) y[ix(m)] = pre_inverse(yam, yak, ybm, ybk, qm);
+        }
       }
     }
   }
