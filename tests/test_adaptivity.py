@@ -102,3 +102,25 @@ def test_step_control_reads_reference_controllers_and_validates():
     for bad in (dict(atol=0.0, rtol=0.0), dict(safety=1.5), dict(min_step=0.0), dict(order=1), dict(pi=(0.2, 0.4))):
         with pytest.raises(ValueError):
             D.StepControl(**bad)
+
+
+def test_step_control_factors_equal_the_controllers_over_a_seeded_sweep():
+    """Over seeded errors from 1e-20 to 1e6 (and exact zeros), the package's
+    step factors equal the reference controllers' bit for bit: accepted
+    (I and PI, with and without a previous error) and rejected (the I factor
+    capped at 0.8, controller.py:276 in the driver)."""
+    pkg = load_package()
+    from importlib import import_module
+    D = import_module(pkg.__name__ + ".drive")
+    rng = np.random.default_rng(11)
+    errs = np.concatenate([[0.0, 1.0, 1e-14, 1e-15], 10.0 ** rng.uniform(-20, 6, 2000)])
+    prevs = np.concatenate([[0.0, 1.0, 1e-15, 1e-14], 10.0 ** rng.uniform(-20, 6, 2000)])
+    for ref in (A.IController(atol=1e-10, rtol=1e-6, max_step=0.01), A.PIController(rtol=1e-5, atol=1e-8),
+                A.PIController(rtol=1e-4, atol=0.0, proportional=0.6, integral=0.2, safety=0.8, min_factor=0.1,
+                               max_factor=5.0, estimator_order=2)):
+        ctl = D.StepControl.of(ref)
+        for e, p in zip(errs, prevs):
+            e, p = float(e), float(p)
+            assert ctl.grow(e, None) == ref.accepted_factor(e, None)
+            assert ctl.grow(e, p) == ref.accepted_factor(e, p)
+            assert ctl.shrink(e) == min(A.IController.accepted_factor(ref, e, None), 0.8)
